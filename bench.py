@@ -1,0 +1,359 @@
+"""Benchmark of the GB300 hair step: point-steps/s of the batched step (many
+assets, one persistent launch in a CUDA graph) vs the plain step (one launch
+sequence per asset), with p50/p99 step latency.
+
+Workload ("batched"): 256 seeded synthetic heads, strands log-uniform in
+[512, 65536], points per strand in {8,16,24,32}, lengths U(0.2,1.0), grids
+32^3..64^3 (int64 sums), 0-4 ellipsoids + the head sphere, friction 0.05,
+repulsion 0.02, wind with gusts.  Inputs (~3.6 GB of Strand records) exceed
+L2 (129 MB), so no flush is needed between steps.
+
+  value : device time of the batched launches (CUDA events on the launching
+          stream), inputs resident in HBM.
+  e2e   : the same step through the C ABI with host data every step: frame
+          parameters from pinned host memory (H2D) and every curve point's
+          position back to host memory (D2H), all inside the timed region.
+  --impl reference : the oracle's OpenMP C++ restatement of the reference
+          shader on the host cores (the reference itself is a Vulkan shader
+          and has no CPU implementation), on a bounded sample of the workload.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun (N>1) assets are sharded across ranks (no collective on the
+data path); timing is max over ranks after a barrier.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "realtime-vulkan-hair_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "point-steps/s batched+served vs plain on 1 GB300 @1e-3 err; p50/p99 step ms"
+BYTES_PER_POINT = 80        # read x,v (32 B) + write x,v,corr (48 B) per point-step
+BYTES_PER_CELL = 16         # one clear/flush pass per grid cell-step
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = os.environ.get("RVH_DIST_BACKEND", "nccl")
+        dist.init_process_group(backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(specs, rank, world):
+    """Asset i goes to rank i % world: weak scaling, no data-path collective."""
+    return [s for i, s in enumerate(specs) if i % world == rank]
+
+
+def make_assets(ctx, specs):
+    from rvh import api
+    assets = []
+    for s in specs:
+        a = api.Asset(ctx, s.records, s.n_points, rest=s.rest, strand_wind=s.strand_wind)
+        a.set_params(s.params)
+        a.set_colliders(s.colliders_at(0))
+        assets.append(a)
+    return assets
+
+
+def algorithmic_bytes(specs):
+    pts = sum(s.n_total_points for s in specs)
+    cells = sum(int(np.prod(list(s.params.grid_dims))) for s in specs if s.params.grid_enabled)
+    return pts * BYTES_PER_POINT + cells * BYTES_PER_CELL, pts, cells
+
+
+def cpu_sample(specs, budget_points=3_000_000):
+    """A bounded sample of the workload for the CPU leg: whole assets taken in
+    order until ~budget_points points."""
+    out, pts = [], 0
+    for s in specs:
+        out.append(s)
+        pts += s.n_total_points
+        if pts >= budget_points:
+            break
+    return out, pts
+
+
+def time_cpu(specs, steps, threads):
+    from oracle import oracle_ctypes as O
+    states = [s.records.copy() for s in specs]
+    pts = sum(s.n_total_points for s in specs)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        for st, s in zip(states, specs):
+            O.run(st, s.n_points, s.rest, s.params, [s.frame(k)], s.colliders, 1, threads=threads)
+    dt = time.perf_counter() - t0
+    return pts * steps / dt, dt
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle's OpenMP restatement on the host cores."""
+    if rank != 0:
+        return
+    import __graft_entry__
+    __graft_entry__.build()   # the scene generator (host C++) makes the inputs
+    from oracle import oracle_ctypes as O
+    from rvh import configs
+    specs = configs.batched()
+    sample, pts = cpu_sample(specs, 1_500_000)
+    threads = O.max_threads()
+    time_cpu(sample, 1, threads)  # warm-up
+    per_step = []
+    for k in range(args.steps):
+        v, dt = time_cpu(sample, 1, threads)
+        per_step.append(dt)
+    value = pts * len(per_step) / sum(per_step)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(per_step),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "batched: 256 heads, strands log-uniform 512..65536, 8..32 points, "
+                                   "32^3..64^3 grids", "sample_points": pts},
+            "cpu_baseline": {"value": value, "unit": "point-steps/s", "cores": threads, "kind": "port",
+                             "sample": "first %d assets (%d points) of the batched workload, %d steps, FP32 "
+                                       "OpenMP over strands" % (len(sample), pts, args.steps)},
+            "e2e": {"value": value, "unit": "point-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--assets", type=int, default=256)
+    ap.add_argument("--lanes", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from rvh import api, configs
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    all_specs = configs.batched(n_assets=args.assets)
+    specs = shard(all_specs, rank, world)
+    ctx = api.Context(device=dev, math=api.MATH_FAST)
+    assets = make_assets(ctx, specs)
+    batch = api.Batch(ctx, assets, lanes=args.lanes)
+    info = batch.info()
+    alg_bytes, pts, cells = algorithmic_bytes(specs)
+    frames = [[s.frame(k) for s in specs] for k in range(args.warmup + args.steps)]
+
+    # ---- batched step, device time ----
+    for k in range(args.warmup):
+        batch.step(frames[k])
+    ctx.synchronize()
+    batch.check()
+    barrier(world)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    batch.timing(True)
+    batch.read_timing()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        batch.step(frames[args.warmup + k])
+    ctx.synchronize()
+    host_s = time.perf_counter() - t0
+    dev_ms, launches = batch.read_timing()
+    batch.timing(False)
+    clk = clocks.stop()
+    batch.check()
+    step_ms = dev_ms / max(1, launches)
+    step_ms = max_over_ranks(step_ms, world)
+    total_pts = int(max_over_ranks(pts, world)) * world if world > 1 else pts  # weak scaling: ~equal shards
+    value = total_pts / (step_ms * 1e-3)
+
+    # per-step latency distribution (each launch timed separately)
+    lat = []
+    batch.timing(True)
+    for k in range(min(args.steps, 20)):
+        batch.step(frames[k % len(frames)])
+        ms, _ = batch.read_timing()
+        lat.append(ms)
+    batch.timing(False)
+
+    # ---- plain step: one launch sequence per asset, no graph ----
+    plain_value, plain_ms = None, None
+    if not args.no_plain:
+        for k in range(2):
+            for a, s in zip(assets, specs):
+                a.step(s.frame(k))
+        ctx.synchronize()
+        nplain = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for k in range(nplain):
+            for a, s in zip(assets, specs):
+                a.step(s.frame(k))
+        ctx.synchronize()
+        plain_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / nplain, world)
+        plain_value = total_pts / (plain_ms * 1e-3)
+
+    # ---- e2e through the C ABI with host buffers ----
+    pos_bufs = [np.empty((s.n_strands, s.n_points, 4), np.float32) for s in specs]
+    import ctypes as C
+    from rvh._lib import check as _check
+    lib = ctx.lib
+    pin = []
+    try:
+        import torch
+        pin = [torch.empty(b.nbytes, dtype=torch.uint8).pin_memory() for b in pos_bufs]
+        ptrs = [p.data_ptr() for p in pin]
+    except Exception:
+        ptrs = [b.ctypes.data for b in pos_bufs]
+    d2h = sum(b.nbytes for b in pos_bufs)
+    h2d = batch.h2d_bytes_per_step()
+    ne2e = max(3, min(args.steps, 10))
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(ne2e):
+        batch.step(frames[k])
+        for a, p, b in zip(assets, ptrs, pos_bufs):
+            _check(lib.rvh_asset_read_positions_async(a.h, C.c_void_p(p), b.nbytes, None))
+    ctx.synchronize()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / ne2e, world)
+    e2e_value = total_pts / (e2e_ms * 1e-3)
+
+    # ---- CPU baseline on a bounded sample (rank 0, N=1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import oracle_ctypes as O
+        sample, spts = cpu_sample(specs, 1_500_000)
+        threads = O.max_threads()
+        v, dt = time_cpu(sample, 3, threads)
+        cpu = {"value": v, "unit": "point-steps/s", "cores": threads, "kind": "port",
+               "sample": "first %d assets (%d points) of the workload, 3 steps, FP32 OpenMP restatement "
+                         "of the reference shader" % (len(sample), spts)}
+
+    peak, peak_kind = load_peaks()
+    achieved = alg_bytes / (step_ms * 1e-3) / 1e9
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        line = {
+            "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators, no dataset)",
+            "config": {"workload": "batched: %d heads, strands log-uniform 512..65536, points {8,16,24,32}, "
+                                   "lengths U(0.2,1), grids 32^3..64^3, 0-4 ellipsoids" % args.assets,
+                       "points_per_step": total_pts, "grid_cells": cells, "lanes_per_strand": info["lanes"],
+                       "work_items": info["items"], "ctas": info["ctas"],
+                       "l2": "inputs (%.1f GB) larger than L2; no flush" % (pts * 48 / 1e9),
+                       "math": "fast"},
+            "p50_step_ms": lat_sorted[len(lat_sorted) // 2], "p99_step_ms": lat_sorted[-1],
+            "plain": {"value": plain_value, "ms_per_step": plain_ms,
+                      "speedup_batched_vs_plain": (value / plain_value) if plain_value else None},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                         "fallback 6.8 TB/s"},
+            "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+    for a in assets:
+        a.close()
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

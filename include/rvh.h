@@ -1,0 +1,139 @@
+/*
+ * rvh.h — C ABI of the GB300 hair-physics step.
+ *
+ * A drop-in for the hair simulation of clach/Realtime-Vulkan-Hair: the
+ * reference runs it as one Vulkan compute shader (src/shaders/compute.comp)
+ * over a `Strand[]` storage buffer, recorded once and submitted every frame.
+ * Here the same buffer layout (float4 curvePoints[n], curveVels[n],
+ * correctionVecs[n] per strand, src/Strand.h:11-15) lives in HBM and each
+ * call below replaces one piece of that Vulkan plumbing (cited per entry).
+ *
+ * Conventions: every call returns rvh_status (RVH_OK = 0); no C++ exception
+ * crosses the ABI; rvh_last_error() gives a message for the calling thread.
+ * Stream arguments are cudaStream_t passed as void* (NULL = the context's own
+ * stream).  Work is asynchronous on its stream unless stated otherwise.
+ * One GPU per context.
+ */
+#ifndef RVH_H
+#define RVH_H
+
+#include "rvh_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rvh_context rvh_context;
+typedef struct rvh_asset rvh_asset;
+typedef struct rvh_batch rvh_batch;
+typedef struct rvh_server rvh_server;
+
+enum { RVH_MATH_FAST = 0, RVH_MATH_EXACT = 1 };
+
+typedef struct rvh_context_desc {
+    int32_t device;               /* CUDA device ordinal */
+    int32_t math;                 /* RVH_MATH_FAST, or RVH_MATH_EXACT: separately rounded IEEE ops in
+                                     the oracle's order (bit-identical to the FP32 restatement) */
+    uint64_t hbm_budget_bytes;    /* admission budget for everything the context allocates; 0 = 90% of free */
+} rvh_context_desc;
+
+typedef struct rvh_asset_desc {
+    int32_t n_strands;
+    int32_t n_points;             /* curve points per strand, 2..32 (reference NUM_CURVE_POINTS = 10) */
+    const void* strands;          /* n_strands Strand records, 48*n_points bytes each */
+    int32_t strands_location;     /* RVH_MEM_HOST / RVH_MEM_DEVICE / RVH_MEM_DEVICE_BORROWED */
+    float uniform_rest_length;    /* used when rest_lengths is NULL (reference 2.5/(n-1), compute.comp:139-140) */
+    const float* rest_lengths;    /* optional host array: rest segment length per strand */
+    const float* strand_wind;     /* optional host array: wind acceleration per strand (3 floats) */
+    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1,2,4,8,16,32 (strands per warp = 32/lanes) */
+    int32_t reserved;
+} rvh_asset_desc;
+
+/* ---- context --------------------------------------------------------------
+ * Replaces the Instance / Device / queue set-up (src/main.cpp:164-184,
+ * src/Device.h:13-17) for the compute half. */
+rvh_status rvh_context_create(const rvh_context_desc* desc, rvh_context** out);
+rvh_status rvh_context_destroy(rvh_context* ctx);
+rvh_status rvh_context_synchronize(rvh_context* ctx);
+/* bytes the context has admitted against its budget, and the budget */
+rvh_status rvh_context_memory(rvh_context* ctx, uint64_t* used, uint64_t* budget);
+const char* rvh_last_error(void);
+const char* rvh_status_string(rvh_status s);
+int32_t rvh_abi_version(void);
+
+/* ---- parameter helpers ------------------------------------------------------ */
+/* The constants compute.comp hard-codes (lines cited in rvh_types.h). */
+rvh_status rvh_sim_params_reference(rvh_sim_params* out);
+/* Collider(trans, rot, scale) of src/Scene.h:28-39: transform = T*Rz*Ry*Rx*S
+ * (rotation in degrees), inv, invTrans; kind/radius as given. */
+rvh_status rvh_collider_from_trs(const float trans[3], const float rot_deg[3], const float scale[3],
+                                 int32_t kind, float radius, rvh_collider* out);
+/* Scene::translateSphere (src/Scene.cpp:110-120): transform = transform *
+ * translate(delta); inv and invTrans recomputed. */
+rvh_status rvh_collider_translate(rvh_collider* c, const float delta[3]);
+/* Initial straight strands as Hair::Hair builds them (src/Strand.cpp:157-175):
+ * point j = root + j*seg*(normal + dir_offset), velocity (0,0,-1), correction 0.
+ * The reference uses seg = 2.5/9 and dir_offset = (0.05, 5, -2). */
+rvh_status rvh_init_strands_reference(const float* roots, const float* normals, int32_t n_strands,
+                                      int32_t n_points, float seg, const float dir_offset[3], void* out_records);
+
+/* ---- assets -----------------------------------------------------------------
+ * Replaces Hair::Hair's buffer creation (src/Strand.cpp:186-191,
+ * BufferUtils::CreateBufferFromData, src/BufferUtils.cpp:68-94) and the
+ * per-asset descriptor set 4 (src/Renderer.cpp:836-997). */
+rvh_status rvh_asset_create(rvh_context* ctx, const rvh_asset_desc* desc, rvh_asset** out);
+rvh_status rvh_asset_destroy(rvh_asset* a);
+/* Time/Collider/Grid uniforms of sets 1-3 (compute.comp:20-42, Scene.cpp:4-20). */
+rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p);
+rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t n);
+/* Device pointer of the Strand records (the VkBuffer Hair::GetStrandsBuffer(), Strand.cpp:195). */
+rvh_status rvh_asset_device_ptr(rvh_asset* a, void** out);
+/* Device pointer of the StrandDrawIndirect record the step writes (Strand.cpp:199, compute.comp:302). */
+rvh_status rvh_asset_draw_indirect(rvh_asset* a, void** out);
+rvh_status rvh_asset_strand_count(rvh_asset* a, int32_t* n_strands, int32_t* n_points);
+/* Copy records to / from host memory (synchronous). */
+rvh_status rvh_asset_read(rvh_asset* a, void* host_dst, size_t bytes);
+rvh_status rvh_asset_write(rvh_asset* a, const void* host_src, size_t bytes);
+/* Positions only (float4 per point, the curvePoints the renderer reads, hair.vert:9,15),
+ * gathered on the device and copied to host memory asynchronously on `stream`. */
+rvh_status rvh_asset_read_positions_async(rvh_asset* a, void* host_dst, size_t bytes, void* stream);
+/* Copy of the StrandDrawIndirect record (synchronous). */
+rvh_status rvh_asset_read_draw(rvh_asset* a, rvh_draw_indirect* out);
+/* Last grid sums (4 int64 per cell {vx,vy,vz,density}); synchronous; for tests. */
+rvh_status rvh_asset_read_grid(rvh_asset* a, int64_t* host_dst, size_t bytes);
+
+/* ---- the step ---------------------------------------------------------------
+ * One Renderer::Frame() compute submit (src/Renderer.cpp:2309-2319) for one
+ * asset: clear its grid (vkCmdFillBuffer, Renderer.cpp:2063), phase A
+ * (compute.comp:144-253), phase B (:257-298); writes vertexCount (:302).
+ * Plain path: one launch sequence per call, no graph. */
+rvh_status rvh_step(rvh_asset* a, const rvh_frame* frame, void* stream);
+
+/* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
+typedef struct rvh_batch_desc {
+    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 4, 8, 16, 32 */
+    int32_t strands_per_tile;     /* phase-A tile size; 0 = tuner's choice */
+    int32_t ctas_per_sm;          /* 0 = occupancy limit */
+    int32_t use_graph;            /* 1 = capture the launch in a CUDA graph (default) */
+} rvh_batch_desc;
+rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t n, const rvh_batch_desc* desc,
+                            rvh_batch** out);
+rvh_status rvh_batch_destroy(rvh_batch* b);
+/* One step of every asset; frames[i] belongs to assets[i]. */
+rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream);
+/* Nonzero device-side status of the last finished batch launch (RVH_ERR_TIMEOUT if a bounded wait gave up). */
+rvh_status rvh_batch_check(rvh_batch* b);
+rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_t* n_ctas, int64_t* n_points);
+/* Kernel timing: while enabled, every rvh_batch_step records CUDA events on
+ * its stream around the persistent launch.  rvh_batch_timing_read waits for
+ * them and returns the summed device time and the launch count since the
+ * last read (then resets). */
+/* Bytes rvh_batch_step copies host->device per step (per-asset frame and collider tables). */
+rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
+rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);
+rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RVH_H */

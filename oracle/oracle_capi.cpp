@@ -1,0 +1,86 @@
+/*
+ * oracle_capi.cpp — TEST INFRASTRUCTURE ONLY.
+ *
+ * extern "C" entry points over hair_oracle.hpp for the Python tests (ctypes),
+ * __graft_entry__.smoke() and bench.py's CPU legs.  Built by oracle/build.py
+ * into oracle/_build/liboracle.so.  Nothing in the product links this.
+ */
+#include <omp.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "hair_adjoint.hpp"
+#include "hair_oracle.hpp"
+
+namespace {
+
+template <class T>
+int run(T* state, int ns, int n, const float* rest, const float* strand_wind, const rvh_sim_params* P,
+        const rvh_frame* frames, const rvh_collider* cols, int ncol, int n_steps, int threads,
+        int64_t* grid_out) {
+    if (!state || !rest || !P || !frames || ns < 0 || n < RVH_MIN_POINTS || n > RVH_MAX_POINTS ||
+        ncol < 0 || ncol > RVH_MAX_COLLIDERS || n_steps < 0 || (ncol > 0 && !cols))
+        return 1;
+    if (threads < 1) threads = 1;
+    oracle::Grid G;
+    for (int s = 0; s < n_steps; ++s)
+        oracle::step_asset<T>(state, ns, n, rest, strand_wind, *P, frames[s], cols + size_t(s) * ncol, ncol,
+                              G, threads);
+    if (grid_out && P->grid_enabled && !G.cells.empty())
+        std::copy(G.cells.begin(), G.cells.end(), grid_out);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Advance n_steps steps in FP64.  state = ns*12*n doubles (Strand records);
+ * cols = n_steps*ncol colliders (one set per step); grid_out (nullable) gets the
+ * last step's 4*nx*ny*nz int64 sums. */
+int oracle_run_f64(double* state, int ns, int n, const float* rest, const float* strand_wind,
+                   const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                   int n_steps, int threads, int64_t* grid_out) {
+    return run<double>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out);
+}
+
+/* The FP32 twin: same operation order, float state. */
+int oracle_run_f32(float* state, int ns, int n, const float* rest, const float* strand_wind,
+                   const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                   int n_steps, int threads, int64_t* grid_out) {
+    return run<float>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out);
+}
+
+/* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */
+int oracle_adjoint_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,
+                       const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                       int n_steps, const double* targets, int threads, double* loss, double* d_wind,
+                       double* d_rest, double* d_v0) {
+    if (!state0 || !rest || !P || !frames || !targets || !loss || ns < 1 || n < RVH_MIN_POINTS ||
+        n > RVH_MAX_POINTS || ncol < 0 || ncol > RVH_MAX_COLLIDERS || n_steps < 1 || (ncol > 0 && !cols))
+        return 1;
+    if (P->grid_enabled) return 7;
+    if (threads < 1) threads = 1;
+    oracle::adjoint_asset(state0, ns, n, rest, strand_wind, *P, frames, cols, ncol, n_steps, targets,
+                          threads, loss, d_wind, d_rest, d_v0);
+    return 0;
+}
+
+/* Loss alone (forward only), for central finite differences in FP64. */
+int oracle_loss_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,
+                    const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                    int n_steps, const double* targets, int threads, double* loss) {
+    if (!state0 || !rest || !P || !frames || !targets || !loss || ns < 1 || n < RVH_MIN_POINTS ||
+        n > RVH_MAX_POINTS || n_steps < 1 || (ncol > 0 && !cols))
+        return 1;
+    if (P->grid_enabled) return 7;
+    if (threads < 1) threads = 1;
+    *loss = oracle::forward_loss(state0, ns, n, rest, strand_wind, *P, frames, cols, ncol, n_steps, targets,
+                                 threads);
+    return 0;
+}
+
+int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"

@@ -1,0 +1,192 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU legs import this.
+It exposes the FP64 oracle, its FP32 twin, the FP64 adjoint, and (where the
+reference checkout exists) the reference's own shader compiled as C++.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.join(HERE, "..", "realtime-vulkan-hair_gb300")
+if _PKG not in sys.path:
+    sys.path.insert(0, _PKG)
+
+from rvh import types as T  # noqa: E402  (layouts only)
+
+from . import build as _build  # noqa: E402
+from . import build_ref as _build_ref  # noqa: E402
+
+_lib = None
+_ref = None
+
+_P = C.POINTER
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        l = C.CDLL(path)
+        common = [C.c_int, C.c_int, _P(C.c_float), _P(C.c_float), _P(T.SimParams), _P(T.Frame), _P(T.Collider),
+                  C.c_int, C.c_int, C.c_int, _P(C.c_int64)]
+        l.oracle_run_f64.argtypes = [_P(C.c_double)] + common
+        l.oracle_run_f32.argtypes = [_P(C.c_float)] + common
+        adj = [_P(C.c_double), C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(T.SimParams), _P(T.Frame),
+               _P(T.Collider), C.c_int, C.c_int, _P(C.c_double), C.c_int, _P(C.c_double)]
+        l.oracle_adjoint_f64.argtypes = adj + [_P(C.c_double), _P(C.c_double), _P(C.c_double)]
+        l.oracle_loss_f64.argtypes = adj
+        for f in (l.oracle_run_f64, l.oracle_run_f32, l.oracle_adjoint_f64, l.oracle_loss_f64):
+            f.restype = C.c_int
+        l.oracle_max_threads.restype = C.c_int
+        _lib = l
+    return _lib
+
+
+def _fptr(a, ct):
+    return None if a is None else a.ctypes.data_as(_P(ct))
+
+
+def _cols(colliders, n_steps):
+    """colliders: list of Collider (same every step) or list (per step) of lists."""
+    if colliders and isinstance(colliders[0], (list, tuple)):
+        rows = list(colliders)
+        assert len(rows) == n_steps
+    else:
+        rows = [list(colliders)] * n_steps
+    ncol = len(rows[0]) if rows else 0
+    return T.colliders_array(rows), ncol
+
+
+def _frames(frames, n_steps):
+    if isinstance(frames, T.Frame):
+        frames = [frames] * n_steps
+    assert len(frames) == n_steps
+    return T.frames_array(frames)
+
+
+def run(state, n_points, rest, params, frames, colliders, n_steps, strand_wind=None, threads=1,
+        want_grid=False):
+    """Advance `state` (float64 -> FP64 oracle, float32 -> FP32 twin) in place.
+
+    state: (ns, 3*n_points, 4) array in the Strand record layout.
+    Returns the last step's grid (nx*ny*nz, 4) int64 when want_grid."""
+    assert state.flags.c_contiguous
+    ns = state.shape[0]
+    rest = np.ascontiguousarray(rest, np.float32)
+    wind = None if strand_wind is None else np.ascontiguousarray(strand_wind, np.float32)
+    fr = _frames(frames, n_steps)
+    cols, ncol = _cols(colliders, n_steps)
+    grid = None
+    if want_grid and params.grid_enabled:
+        d = params.grid_dims
+        grid = np.zeros((d[0] * d[1] * d[2], 4), np.int64)
+    if state.dtype == np.float64:
+        fn, ptr = lib().oracle_run_f64, _fptr(state, C.c_double)
+    elif state.dtype == np.float32:
+        fn, ptr = lib().oracle_run_f32, _fptr(state, C.c_float)
+    else:
+        raise TypeError(state.dtype)
+    rc = fn(ptr, ns, n_points, _fptr(rest, C.c_float), _fptr(wind, C.c_float), C.byref(params), fr, cols, ncol,
+            n_steps, threads, _fptr(grid, C.c_int64))
+    if rc != 0:
+        raise RuntimeError("oracle_run failed: %d" % rc)
+    return grid
+
+
+def adjoint(state0, n_points, rest, params, frames, colliders, n_steps, targets, strand_wind=None, threads=1):
+    """FP64 adjoint: returns (loss, d_wind (ns,3), d_rest (ns,), d_v0 (ns,n,3))."""
+    ns = state0.shape[0]
+    s0 = np.ascontiguousarray(state0, np.float64)
+    rest = np.ascontiguousarray(rest, np.float64)
+    wind = np.zeros((ns, 3)) if strand_wind is None else np.ascontiguousarray(strand_wind, np.float64)
+    tg = np.ascontiguousarray(targets, np.float64)
+    fr = _frames(frames, n_steps)
+    cols, ncol = _cols(colliders, n_steps)
+    loss = np.zeros(1)
+    dw = np.zeros((ns, 3))
+    dr = np.zeros(ns)
+    dv = np.zeros((ns, n_points, 3))
+    rc = lib().oracle_adjoint_f64(_fptr(s0, C.c_double), ns, n_points, _fptr(rest, C.c_double),
+                                  _fptr(wind, C.c_double), C.byref(params), fr, cols, ncol, n_steps,
+                                  _fptr(tg, C.c_double), threads, _fptr(loss, C.c_double), _fptr(dw, C.c_double),
+                                  _fptr(dr, C.c_double), _fptr(dv, C.c_double))
+    if rc != 0:
+        raise RuntimeError("oracle_adjoint failed: %d" % rc)
+    return loss[0], dw, dr, dv
+
+
+def loss(state0, n_points, rest, params, frames, colliders, n_steps, targets, strand_wind=None, threads=1):
+    ns = state0.shape[0]
+    s0 = np.ascontiguousarray(state0, np.float64)
+    rest = np.ascontiguousarray(rest, np.float64)
+    wind = np.zeros((ns, 3)) if strand_wind is None else np.ascontiguousarray(strand_wind, np.float64)
+    tg = np.ascontiguousarray(targets, np.float64)
+    fr = _frames(frames, n_steps)
+    cols, ncol = _cols(colliders, n_steps)
+    out = np.zeros(1)
+    rc = lib().oracle_loss_f64(_fptr(s0, C.c_double), ns, n_points, _fptr(rest, C.c_double),
+                               _fptr(wind, C.c_double), C.byref(params), fr, cols, ncol, n_steps,
+                               _fptr(tg, C.c_double), threads, _fptr(out, C.c_double))
+    if rc != 0:
+        raise RuntimeError("oracle_loss failed: %d" % rc)
+    return out[0]
+
+
+def max_threads():
+    return lib().oracle_max_threads()
+
+
+# ---- the reference's own shader compiled as C++ (only where the checkout exists) ----
+
+def ref_available():
+    return _build_ref.available()
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        path = _build_ref.build()
+        if path is None:
+            return None
+        l = C.CDLL(path)
+        l.ref_run.argtypes = [_P(C.c_float), C.c_int, _P(C.c_float), _P(C.c_float), C.c_int, _P(C.c_int32),
+                              _P(C.c_uint32)]
+        l.ref_run.restype = C.c_int
+        l.ref_collider.argtypes = [_P(C.c_float)] * 4
+        l.ref_translate.argtypes = [_P(C.c_float)] * 2
+        _ref = l
+    return _ref
+
+
+def ref_collider(trans, rot_deg, scale):
+    out = np.zeros(48, np.float32)
+    a = [np.ascontiguousarray(x, np.float32) for x in (trans, rot_deg, scale)]
+    ref_lib().ref_collider(*[_fptr(x, C.c_float) for x in a], _fptr(out, C.c_float))
+    return out
+
+
+def ref_translate(flat48, delta):
+    out = np.ascontiguousarray(flat48, np.float32).copy()
+    d = np.ascontiguousarray(delta, np.float32)
+    ref_lib().ref_translate(_fptr(out, C.c_float), _fptr(d, C.c_float))
+    return out
+
+
+def ref_run(strands, colliders_steps, times, want_grid=False):
+    """strands: (ns, 30, 4) float32, advanced in place; colliders_steps: (steps, 6, 48);
+    times: (steps, 2).  Returns (grid int32 (64^3,4) or None, draw uint32[4])."""
+    assert strands.dtype == np.float32 and strands.flags.c_contiguous
+    cs = np.ascontiguousarray(colliders_steps, np.float32)
+    tm = np.ascontiguousarray(times, np.float32)
+    steps = tm.shape[0]
+    grid = np.zeros((64 ** 3, 4), np.int32) if want_grid else None
+    draw = np.zeros(4, np.uint32)
+    rc = ref_lib().ref_run(_fptr(strands, C.c_float), strands.shape[0], _fptr(cs, C.c_float), _fptr(tm, C.c_float),
+                           steps, _fptr(grid, C.c_int32), _fptr(draw, C.c_uint32))
+    if rc != 0:
+        raise RuntimeError("ref_run failed")
+    return grid, draw

@@ -1,0 +1,448 @@
+// rvh_device.cuh — device-side data layout and the per-strand / per-point step
+// functions of the GB300 hair step.  Every kernel (plain per-asset launches,
+// the batched persistent launch) calls these, so they compute identical bits.
+//
+// Reference: clach/Realtime-Vulkan-Hair src/shaders/compute.comp:124-303.
+//   loop 1 (:144-202)  predict + penalty collisions + FTL     -> phase A
+//   loop 2 (:211-253)  DFTL velocity correction + grid splat  -> phase A
+//   loop 3 (:257-298)  grid gather + friction (+ repulsion)   -> phase B
+// Phase B of an asset starts only after every phase-A tile of that asset has
+// splatted (a global phase split; the shader's barrier() is workgroup-only).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rvh_types.h"
+
+namespace rvh {
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies.
+//   Exact: every + - * / sqrt is a separately rounded IEEE operation in the
+//          order the oracle writes it (no FMA contraction), so a step is
+//          bit-identical to the oracle's FP32 twin.
+//   Fast:  FMA contraction and approximate reciprocal / rsqrt; results stay
+//          within the FP64 tolerances, at fewer instructions.
+// ---------------------------------------------------------------------------
+struct ExactMath {
+    static constexpr bool kExact = true;
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+    static __device__ __forceinline__ float rsqrt(float a) { return __fdiv_rn(1.0f, __fsqrt_rn(a)); }
+    static __device__ __forceinline__ float rcp(float a) { return __fdiv_rn(1.0f, a); }
+    // a*b + c written as two roundings, as the oracle does
+    static __device__ __forceinline__ float madd(float a, float b, float c) { return __fadd_rn(__fmul_rn(a, b), c); }
+};
+
+struct FastMath {
+    static constexpr bool kExact = false;
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+    static __device__ __forceinline__ float rsqrt(float a) { return rsqrtf(a); }
+    static __device__ __forceinline__ float rcp(float a) { return __frcp_rn(a); }
+    static __device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+};
+
+// ---------------------------------------------------------------------------
+// Device layout.
+// ---------------------------------------------------------------------------
+
+// One collider, repacked from rvh_collider (three column-major mat4,
+// src/Scene.h:23-27) into the 3x4 / 3x3 blocks the shader reads.
+struct DevCollider {
+    int32_t kind;
+    float radius;
+    float c[3];      // sphere centre: transform[3].xyz (compute.comp:162)
+    float inv[12];   // inv, columns 0..3, rows xyz: local = inv * (p, 1) (compute.comp:65)
+    float itr[9];    // invTrans, columns 0..2, rows xyz: n = invTrans * (q, 0) (compute.comp:72)
+    float xf[12];    // transform, columns 0..3, rows xyz (compute.comp:78)
+};
+
+// Everything one step of one asset reads besides its buffers' contents.
+struct DevAsset {
+    float4* strands;             // n_strands records of 3*n float4 (Strand.h:11-15), updated in place
+    const float* rest;           // per-strand rest segment length (compute.comp:139-140)
+    const float4* strand_wind;   // optional per-strand wind (xyz), or null
+    unsigned long long* grid;    // 4 x int64 per cell {vx, vy, vz, density} for this step
+    unsigned long long* grid_next;  // the other grid buffer (cleared during a batched step)
+    rvh_draw_indirect* draw;     // StrandDrawIndirect (Strand.h:53-58), or null
+    int32_t n_strands;
+    int32_t n_points;
+    // constants (rvh_sim_params)
+    float gravity[3];
+    float damping, dftl, vmax, k_penalty, friction, repulsion, scale;
+    int32_t grid_enabled, wrap32;
+    float origin[3];
+    float h;
+    int32_t nx, ny, nz;
+    // frame (rvh_frame)
+    float dt;
+    float t;
+    float wind[3];
+    int32_t n_colliders;
+    DevCollider col[RVH_MAX_COLLIDERS];
+};
+
+struct f3 {
+    float x, y, z;
+};
+
+template <class M> __device__ __forceinline__ f3 v_add(f3 a, f3 b) { return {M::add(a.x, b.x), M::add(a.y, b.y), M::add(a.z, b.z)}; }
+template <class M> __device__ __forceinline__ f3 v_sub(f3 a, f3 b) { return {M::sub(a.x, b.x), M::sub(a.y, b.y), M::sub(a.z, b.z)}; }
+template <class M> __device__ __forceinline__ f3 v_scale(float s, f3 a) { return {M::mul(s, a.x), M::mul(s, a.y), M::mul(s, a.z)}; }
+template <class M> __device__ __forceinline__ f3 v_div(f3 a, float s) { return {M::div(a.x, s), M::div(a.y, s), M::div(a.z, s)}; }
+// a + s*b
+template <class M> __device__ __forceinline__ f3 v_axpy(f3 a, float s, f3 b) {
+    return {M::madd(s, b.x, a.x), M::madd(s, b.y, a.y), M::madd(s, b.z, a.z)};
+}
+template <class M> __device__ __forceinline__ float v_dot(f3 a, f3 b) {
+    return M::add(M::add(M::mul(a.x, b.x), M::mul(a.y, b.y)), M::mul(a.z, b.z));
+}
+template <class M> __device__ __forceinline__ float v_len(f3 a) { return M::sqrt(v_dot<M>(a, a)); }
+// GLSL normalize: x * inversesqrt(dot(x, x))
+template <class M> __device__ __forceinline__ f3 v_normalize(f3 a) { return v_scale<M>(M::rsqrt(v_dot<M>(a, a)), a); }
+
+// xyz of m * (p, 1) for a 3x4 column block: (c0 x + c1 y) + (c2 z + c3)
+template <class M> __device__ __forceinline__ f3 mat_p1(const float* m, f3 p) {
+    return {M::add(M::add(M::mul(m[0], p.x), M::mul(m[3], p.y)), M::add(M::mul(m[6], p.z), m[9])),
+            M::add(M::add(M::mul(m[1], p.x), M::mul(m[4], p.y)), M::add(M::mul(m[7], p.z), m[10])),
+            M::add(M::add(M::mul(m[2], p.x), M::mul(m[5], p.y)), M::add(M::mul(m[8], p.z), m[11]))};
+}
+// xyz of m * (q, 0) for a 3x3 column block: (c0 x + c1 y) + c2 z
+template <class M> __device__ __forceinline__ f3 mat_q0(const float* m, f3 q) {
+    return {M::add(M::add(M::mul(m[0], q.x), M::mul(m[3], q.y)), M::mul(m[6], q.z)),
+            M::add(M::add(M::mul(m[1], q.x), M::mul(m[4], q.y)), M::mul(m[7], q.z)),
+            M::add(M::add(M::mul(m[2], q.x), M::mul(m[5], q.y)), M::mul(m[8], q.z))};
+}
+
+__device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
+
+// Streaming 16-B load that skips L1: data written by other CTAs in the same
+// launch (phase A output, grid sums) must not be served from a stale L1 line.
+__device__ __forceinline__ float4 ld_cg(const float4* p) { return __ldcg(p); }
+__device__ __forceinline__ void st_f4(float4* p, f3 a, float w) { *p = make_float4(a.x, a.y, a.z, w); }
+
+// ---------------------------------------------------------------------------
+// Penalty collisions for one point (compute.comp:155-184).  Returns the force.
+// ---------------------------------------------------------------------------
+template <class M>
+__device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
+    const float k = A.k_penalty;
+    f3 added = {0.f, 0.f, 0.f};
+    int cnt = 0;
+    const int nc = A.n_colliders;
+    for (int j = 0; j < nc; ++j) {
+        const DevCollider& c = A.col[j];
+        if (c.kind == RVH_COLLIDER_SPHERE) {
+            const f3 e = v_sub<M>(x, f3{c.c[0], c.c[1], c.c[2]});
+            const float dist = v_len<M>(e);
+            if (dist < c.radius) {
+                const float d = M::sub(c.radius, dist);
+                const f3 nrm = v_normalize<M>(e);
+                added = v_add<M>(added, v_scale<M>(M::mul(k, d), nrm));
+                ++cnt;
+            }
+        } else {
+            const f3 q = mat_p1<M>(c.inv, x);
+            const float lq = v_len<M>(q);
+            if (lq <= 1.0f) {
+                const f3 surf = mat_p1<M>(c.xf, v_normalize<M>(q));
+                const float d = v_len<M>(v_sub<M>(surf, x));
+                const f3 nrm = v_normalize<M>(v_normalize<M>(mat_q0<M>(c.itr, q)));
+                added = v_add<M>(added, v_scale<M>(M::mul(k, d), nrm));
+                ++cnt;
+            }
+        }
+    }
+    if (cnt > 0) force = v_add<M>(force, v_div<M>(added, (float)cnt));
+    return force;
+}
+
+// ---------------------------------------------------------------------------
+// Grid helpers (compute.comp:217-252 splat, :258-293 gather).
+// ---------------------------------------------------------------------------
+struct Corners {
+    float g[3];    // grid-space coordinates
+    int lo[3];     // first corner per axis
+    int cnt[3];    // 0, 1 or 2 corners per axis
+};
+
+template <class M>
+__device__ __forceinline__ Corners corners_of(const DevAsset& A, f3 p) {
+    Corners C;
+    const float pv[3] = {p.x, p.y, p.z};
+    const int dim[3] = {A.nx, A.ny, A.nz};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const float g = M::div(M::sub(pv[ax], A.origin[ax]), A.h);
+        float f = floorf(g);
+        f = fminf(fmaxf(f, -2.0f), (float)dim[ax]);   // same corner set, defined conversion
+        const int fi = (int)f;
+        const int lo = max(fi, 0);
+        const int hi = min(fi + 1, dim[ax] - 1);
+        C.g[ax] = g;
+        C.lo[ax] = lo;
+        C.cnt[ax] = max(hi - lo + 1, 0);
+    }
+    return C;
+}
+
+template <class M>
+__device__ __forceinline__ float tri_w(float g, int a) {  // clamp(1 - abs(g - a), 0, 1)
+    return fminf(fmaxf(M::sub(1.0f, fabsf(M::sub(g, (float)a))), 0.0f), 1.0f);
+}
+
+__device__ __forceinline__ long long fixed_of(float scale_times_x) {
+    return (long long)__float2int_rz(scale_times_x);
+}
+
+__device__ __forceinline__ void red_add_s64(unsigned long long* p, long long v) {
+    if (v != 0) atomicAdd(p, (unsigned long long)v);
+}
+
+// Splat one point: 4 x int64 atomics per touched corner, sums wrap-free.
+template <class M>
+__device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel) {
+    const Corners C = corners_of<M>(A, pos);
+    const int nxny = A.nx * A.ny;
+#pragma unroll
+    for (int da = 0; da < 2; ++da) {
+        if (da >= C.cnt[0]) continue;
+        const int a = C.lo[0] + da;
+        const float wx = tri_w<M>(C.g[0], a);
+#pragma unroll
+        for (int db = 0; db < 2; ++db) {
+            if (db >= C.cnt[1]) continue;
+            const int b = C.lo[1] + db;
+            const float wy = tri_w<M>(C.g[1], b);
+            const float wxy = M::mul(wx, wy);
+#pragma unroll
+            for (int dc = 0; dc < 2; ++dc) {
+                if (dc >= C.cnt[2]) continue;
+                const int c = C.lo[2] + dc;
+                const float w = M::mul(wxy, tri_w<M>(C.g[2], c));
+                unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + c * nxny);
+                red_add_s64(cell + 0, fixed_of(M::mul(A.scale, M::mul(w, vel.x))));
+                red_add_s64(cell + 1, fixed_of(M::mul(A.scale, M::mul(w, vel.y))));
+                red_add_s64(cell + 2, fixed_of(M::mul(A.scale, M::mul(w, vel.z))));
+                red_add_s64(cell + 3, fixed_of(M::mul(A.scale, w)));
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ long long grid_val(unsigned long long raw, bool wrap32) {
+    return wrap32 ? (long long)(int)(unsigned)(raw & 0xffffffffull) : (long long)raw;
+}
+
+// Gather + friction (+ repulsion) for one point; returns the new velocity.
+template <class M>
+__device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel) {
+    const Corners C = corners_of<M>(A, pos);
+    const int nxny = A.nx * A.ny;
+    const bool wrap = A.wrap32 != 0;
+    const bool rep = A.repulsion != 0.0f;
+    f3 gv = {0.f, 0.f, 0.f};
+    float rho = 0.f;
+    f3 grad = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int da = 0; da < 2; ++da) {
+        if (da >= C.cnt[0]) continue;
+        const int a = C.lo[0] + da;
+#pragma unroll
+        for (int db = 0; db < 2; ++db) {
+            if (db >= C.cnt[1]) continue;
+            const int b = C.lo[1] + db;
+#pragma unroll
+            for (int dc = 0; dc < 2; ++dc) {
+                if (dc >= C.cnt[2]) continue;
+                const int c = C.lo[2] + dc;
+                const ulonglong2* cell =
+                    reinterpret_cast<const ulonglong2*>(A.grid + 4ull * (unsigned)(a + b * A.nx + c * nxny));
+                const ulonglong2 zw = __ldcg(cell + 1);
+                const long long dens = grid_val(zw.y, wrap);
+                if (dens > 0) {
+                    const ulonglong2 xy = __ldcg(cell);
+                    const float wx = tri_w<M>(C.g[0], a), wy = tri_w<M>(C.g[1], b), wz = tri_w<M>(C.g[2], c);
+                    const float w = M::mul(M::mul(wx, wy), wz);
+                    const float fd = (float)dens;
+                    const float s = M::mul(w, M::rcp(fd));
+                    const f3 cv = {(float)grid_val(xy.x, wrap), (float)grid_val(xy.y, wrap), (float)grid_val(zw.x, wrap)};
+                    gv = v_add<M>(gv, v_scale<M>(s, cv));
+                    if (rep) {
+                        const float rc = M::div(fd, A.scale);
+                        const float ga = M::sub(C.g[0], (float)a), gb = M::sub(C.g[1], (float)b), gc = M::sub(C.g[2], (float)c);
+                        const float dx = fabsf(ga) < 1.0f ? (ga >= 0.0f ? -1.0f : 1.0f) : 0.0f;
+                        const float dy = fabsf(gb) < 1.0f ? (gb >= 0.0f ? -1.0f : 1.0f) : 0.0f;
+                        const float dz = fabsf(gc) < 1.0f ? (gc >= 0.0f ? -1.0f : 1.0f) : 0.0f;
+                        rho = M::add(rho, M::mul(w, rc));
+                        const f3 dw = {M::mul(M::mul(dx, wy), wz), M::mul(M::mul(wx, dy), wz), M::mul(M::mul(wx, wy), dz)};
+                        grad = v_add<M>(grad, v_scale<M>(rc, dw));
+                    }
+                }
+            }
+        }
+    }
+    const float fr = A.friction;
+    f3 out = v_add<M>(v_scale<M>(M::sub(1.0f, fr), vel), v_scale<M>(fr, gv));
+    if (rep) {
+        const float coef = M::div(M::mul(A.repulsion, M::div(A.h, A.dt)), fmaxf(rho, 1.0f));
+        out = v_sub<M>(out, v_scale<M>(coef, grad));
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Phase A for one strand group.
+//   A warp holds S = 32/L strands; the L lanes of a strand hold its points in
+//   an interleaved order (lane l holds points l, l+L, l+2L, ...), so each
+//   16-B load/store instruction covers 16*L contiguous bytes per strand.
+//   The FTL chain (sequential along the strand) runs redundantly in every lane
+//   of the strand with the predicted points broadcast by shuffles; each lane
+//   keeps the results for its own points.
+//   NFIX > 0 fixes the point count at compile time; NFIX == 0 reads it from
+//   the asset (any n <= RVH_MAX_POINTS).
+// All lanes of the warp must call this (shuffles); `valid` masks the work.
+// ---------------------------------------------------------------------------
+template <int NFIX, int L, class M>
+__device__ __forceinline__ void strand_phase_a(const DevAsset& A, int strand, bool valid) {
+    constexpr int NMAX = NFIX > 0 ? NFIX : RVH_MAX_POINTS;
+    constexpr int K = (NMAX + L - 1) / L;
+    const int n = NFIX > 0 ? NFIX : A.n_points;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int l = lane % L;
+    const int base = lane - l;
+    float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+
+    f3 x[K], p[K], xn[K];
+    float4 vin[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = k * L + l;
+        if (valid && i < n) {
+            const float4 a = ld_cg(rec + i);
+            x[k] = xyz(a);
+            vin[k] = ld_cg(rec + n + i);
+        } else {
+            x[k] = f3{0.f, 0.f, 0.f};
+            vin[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        xn[k] = x[k];  // the root (i == 0) keeps its position
+    }
+    const float dt = A.dt;
+    const float r = valid ? A.rest[strand] : 0.f;
+    f3 f0 = v_add<M>(f3{A.gravity[0], A.gravity[1], A.gravity[2]}, f3{A.wind[0], A.wind[1], A.wind[2]});
+    if (A.strand_wind != nullptr && valid) f0 = v_add<M>(f0, xyz(A.strand_wind[strand]));
+    const float dt2 = M::mul(dt, dt);
+
+    // loop 1, independent part: force and predicted position of each point
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = k * L + l;
+        f3 force = f0;
+        if (valid && i >= 1 && i < n) force = collide_force<M>(A, x[k], force);
+        const f3 v = xyz(vin[k]);
+        // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
+        p[k] = v_add<M>(v_add<M>(x[k], v_scale<M>(dt, v)), v_scale<M>(dt2, force));
+    }
+
+    // loop 1, sequential part: FTL, newPos = parent + radius * normalize(pred - parent)
+    f3 par;
+    if (L == 1) {
+        par = x[0];
+    } else {
+        par.x = __shfl_sync(FULL, x[0].x, base);
+        par.y = __shfl_sync(FULL, x[0].y, base);
+        par.z = __shfl_sync(FULL, x[0].z, base);
+    }
+#pragma unroll
+    for (int i = 1; i < NMAX; ++i) {
+        if (NFIX == 0 && i >= n) break;  // n is uniform across the warp
+        const int k = i / L, own = i % L;
+        f3 pi;
+        if (L == 1) {
+            pi = p[k];
+        } else {
+            pi.x = __shfl_sync(FULL, p[k].x, base + own);
+            pi.y = __shfl_sync(FULL, p[k].y, base + own);
+            pi.z = __shfl_sync(FULL, p[k].z, base + own);
+        }
+        const f3 dir = v_normalize<M>(v_sub<M>(pi, par));
+        par = v_add<M>(par, v_scale<M>(r, dir));
+        if (L == 1 || l == own) xn[k] = par;
+    }
+
+    // velocity, clamp and correction vector (compute.comp:195-201)
+    f3 vel[K], cor[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const f3 newVel = v_div<M>(v_sub<M>(xn[k], x[k]), dt);
+        f3 v = v_scale<M>(A.damping, newVel);
+        if (v_len<M>(v) > A.vmax) v = v_scale<M>(A.vmax, v_normalize<M>(v));
+        vel[k] = v;
+        cor[k] = v_scale<M>(A.dftl, v_sub<M>(xn[k], p[k]));
+    }
+
+    // loop 2: v_i -= corr_{i+1} / dt for i < n-1 (compute.comp:213-215)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        f3 cn;
+        if (L == 1) {
+            cn = (k + 1 < K) ? cor[k + 1] : f3{0.f, 0.f, 0.f};
+        } else {
+            f3 same, wrap;
+            same.x = __shfl_sync(FULL, cor[k].x, (lane + 1) & 31);
+            same.y = __shfl_sync(FULL, cor[k].y, (lane + 1) & 31);
+            same.z = __shfl_sync(FULL, cor[k].z, (lane + 1) & 31);
+            const f3 nxt = (k + 1 < K) ? cor[k + 1] : f3{0.f, 0.f, 0.f};
+            wrap.x = __shfl_sync(FULL, nxt.x, base);
+            wrap.y = __shfl_sync(FULL, nxt.y, base);
+            wrap.z = __shfl_sync(FULL, nxt.z, base);
+            cn = (l + 1 < L) ? same : wrap;
+        }
+        const int i = k * L + l;
+        if (i >= 1 && i < n - 1) vel[k] = v_sub<M>(vel[k], v_div<M>(cn, dt));
+    }
+
+    // store x', v, corr for points 1..n-1 (the root is never written)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = k * L + l;
+        if (valid && i >= 1 && i < n) {
+            st_f4(rec + i, xn[k], 1.0f);
+            st_f4(rec + n + i, vel[k], 0.0f);
+            st_f4(rec + 2 * n + i, cor[k], 0.0f);
+        }
+    }
+    if (A.grid_enabled) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int i = k * L + l;
+            if (valid && i >= 1 && i < n) splat_point<M>(A, xn[k], vel[k]);
+        }
+    }
+}
+
+// Phase B for one point (loop 3): p = flat point index within the asset.
+template <class M>
+__device__ __forceinline__ void point_phase_b(const DevAsset& A, long long p) {
+    const int n = A.n_points;
+    const long long s = p / n;
+    const int i = (int)(p - s * n);
+    if (i == 0) return;
+    float4* rec = A.strands + (size_t)s * (3 * n);
+    const f3 x = xyz(ld_cg(rec + i));
+    const f3 v = xyz(ld_cg(rec + n + i));
+    const f3 out = gather_point<M>(A, x, v);
+    st_f4(rec + n + i, out, 0.0f);
+}
+
+}  // namespace rvh

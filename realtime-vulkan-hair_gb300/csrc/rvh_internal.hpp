@@ -1,0 +1,106 @@
+// rvh_internal.hpp — host-side objects behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/rvh.h"
+#include "rvh_kernels.cuh"
+
+namespace rvh {
+
+// ---- errors -------------------------------------------------------------------
+void set_error(const std::string& msg);
+rvh_status fail(rvh_status s, const std::string& msg);
+rvh_status cuda_fail(cudaError_t e, const char* what);
+#define RVH_CUDA(call)                                              \
+    do {                                                            \
+        cudaError_t e_ = (call);                                    \
+        if (e_ != cudaSuccess) return ::rvh::cuda_fail(e_, #call);  \
+    } while (0)
+
+// ---- HBM admission accounting --------------------------------------------------
+// Every device allocation a context makes is admitted against its budget
+// first; a request that would exceed it fails with RVH_ERR_BUDGET and
+// allocates nothing.
+class Budget {
+public:
+    void init(uint64_t budget) { budget_ = budget; }
+    bool reserve(uint64_t bytes) {
+        uint64_t cur = used_.load();
+        do {
+            if (cur + bytes > budget_) return false;
+        } while (!used_.compare_exchange_weak(cur, cur + bytes));
+        return true;
+    }
+    void release(uint64_t bytes) { used_.fetch_sub(bytes); }
+    uint64_t used() const { return used_.load(); }
+    uint64_t budget() const { return budget_; }
+
+private:
+    uint64_t budget_ = 0;
+    std::atomic<uint64_t> used_{0};
+};
+
+struct Context;
+
+// A device allocation charged to a context's budget.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    Context* owner = nullptr;
+    bool owned = true;
+};
+
+struct Context {
+    int device = 0;
+    int math = RVH_MATH_FAST;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    Budget budget;
+    std::mutex mu;
+
+    rvh_status alloc(DevBuf& b, size_t bytes);
+    void free(DevBuf& b);
+};
+
+struct Asset {
+    Context* ctx = nullptr;
+    int n_strands = 0;
+    int n_points = 0;
+    int lanes = 0;
+    DevBuf strands;   // borrowed when created with RVH_MEM_DEVICE_BORROWED
+    DevBuf rest;
+    DevBuf wind;      // float4 per strand, or empty
+    DevBuf grid[2];   // 4 x int64 per cell, two buffers (a batched step clears the other one)
+    DevBuf draw;
+    DevBuf positions; // scratch for rvh_asset_read_positions_async
+    int parity = 0;             // grid buffer the next step uses
+    bool grid_dirty[2] = {false, false};
+    size_t grid_cells = 0;
+    rvh_sim_params params{};
+    std::vector<rvh_collider> colliders;
+    bool has_wind = false;
+
+    size_t record_bytes() const { return size_t(n_strands) * 48u * size_t(n_points); }
+    size_t grid_bytes() const { return grid_cells * 32u; }
+    // DevAsset for one step with frame f on grid buffer `which`.
+    DevAsset device_view(const rvh_frame& f, int which) const;
+};
+
+rvh_status validate_params(const rvh_sim_params& p);
+rvh_status validate_frame(const rvh_frame& f);
+DevCollider pack_collider(const rvh_collider& c);
+int default_lanes(int n_points);
+rvh_status ensure_grid(Asset* a);
+rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s);
+
+}  // namespace rvh
+
+struct rvh_context : rvh::Context {};
+struct rvh_asset : rvh::Asset {};

@@ -1,0 +1,16 @@
+// rvh_registry.h — lookup of the compiled step kernels by shape.
+#pragma once
+
+namespace rvh {
+
+// Lanes per strand the plain phase-A kernel is compiled for, given n points
+// (strands per warp = 32 / lanes).  Returns false when (n, lanes) has no
+// kernel; n values without a fixed-size kernel use the generic one.
+bool plain_a_supported(int n, int lanes);
+const void* plain_a_kernel(int n, int lanes, bool exact);
+const void* plain_b_kernel(bool exact);
+// Persistent batch kernel; lanes in {4, 8, 16, 32}.
+const void* batch_kernel(int lanes, bool exact);
+bool batch_supported(int lanes);
+
+}  // namespace rvh

@@ -1,0 +1,268 @@
+"""Python host-side mirror of the C ABI: Context, Asset (the reference's Hair),
+Batch, and the scene helpers.  Every call goes through librvh.so."""
+import ctypes as C
+
+import numpy as np
+
+from . import types as T
+from ._lib import check, load
+
+_P = C.POINTER
+
+
+class ContextDesc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("math", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class AssetDesc(C.Structure):
+    _fields_ = [("n_strands", C.c_int32), ("n_points", C.c_int32), ("strands", C.c_void_p),
+                ("strands_location", C.c_int32), ("uniform_rest_length", C.c_float),
+                ("rest_lengths", _P(C.c_float)), ("strand_wind", _P(C.c_float)),
+                ("lanes_per_strand", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("lanes_per_strand", C.c_int32), ("strands_per_tile", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("use_graph", C.c_int32)]
+
+
+class HeadDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_strands", C.c_int32), ("n_points", C.c_int32),
+                ("head_radius", C.c_float), ("head_center", C.c_float * 3), ("root_sampling", C.c_int32),
+                ("sort_roots", C.c_int32), ("length_min", C.c_float), ("length_max", C.c_float),
+                ("head_collider", C.c_int32), ("n_ellipsoids", C.c_int32), ("axis_min", C.c_float),
+                ("axis_max", C.c_float), ("grid_res", C.c_int32), ("friction", C.c_float),
+                ("repulsion", C.c_float), ("dftl_damping", C.c_float)]
+
+
+class WindDesc(C.Structure):
+    _fields_ = [("amplitude", C.c_float), ("omega", C.c_float), ("dir", C.c_float * 3), ("gust_sigma", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+class Orbit(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("orbit_radius", C.c_float), ("omega", C.c_float),
+                ("phase", C.c_float), ("sphere_radius", C.c_float)]
+
+
+MATH_FAST = 0
+MATH_EXACT = 1
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(_P(C.c_float))
+
+
+class Context:
+    def __init__(self, device=0, math=MATH_FAST, hbm_budget_bytes=0):
+        self.lib = load()
+        d = ContextDesc(device, math, hbm_budget_bytes)
+        h = C.c_void_p()
+        check(self.lib.rvh_context_create(C.byref(d), C.byref(h)))
+        self.h = h
+        self.math = math
+
+    def close(self):
+        if self.h:
+            self.lib.rvh_context_destroy(self.h)
+            self.h = None
+
+    def synchronize(self):
+        check(self.lib.rvh_context_synchronize(self.h))
+
+    def memory(self):
+        u, b = C.c_uint64(), C.c_uint64()
+        check(self.lib.rvh_context_memory(self.h, C.byref(u), C.byref(b)))
+        return u.value, b.value
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Asset:
+    """One hair asset: the reference's Hair buffers (Strand.h:61-80) on the GPU."""
+
+    def __init__(self, ctx, records, n_points, rest=None, uniform_rest=0.0, strand_wind=None, lanes=0,
+                 location=T.MEM_HOST, device_ptr=None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        if device_ptr is not None:
+            n_strands = int(records)
+            src = C.c_void_p(device_ptr)
+        else:
+            rec = _f32(records).reshape(-1)
+            n_strands = rec.size // (12 * n_points)
+            assert n_strands * 12 * n_points == rec.size
+            src = rec.ctypes.data_as(C.c_void_p)
+            self._keep = rec
+        self.n_strands, self.n_points = n_strands, n_points
+        rest_a = None if rest is None else _f32(rest)
+        wind_a = None if strand_wind is None else _f32(strand_wind).reshape(-1)
+        d = AssetDesc(n_strands, n_points, src, location, uniform_rest, _fp(rest_a), _fp(wind_a), lanes, 0)
+        h = C.c_void_p()
+        check(self.lib.rvh_asset_create(ctx.h, C.byref(d), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.rvh_asset_destroy(self.h)
+            self.h = None
+
+    def set_params(self, p):
+        check(self.lib.rvh_asset_set_params(self.h, C.byref(p)))
+
+    def set_colliders(self, cols):
+        arr = (T.Collider * max(1, len(cols)))(*cols)
+        check(self.lib.rvh_asset_set_colliders(self.h, arr, len(cols)))
+
+    def step(self, frame, stream=None):
+        check(self.lib.rvh_step(self.h, C.byref(frame), stream))
+
+    def read(self):
+        out = np.empty((self.n_strands, 3 * self.n_points, 4), np.float32)
+        check(self.lib.rvh_asset_read(self.h, out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def write(self, records):
+        rec = _f32(records)
+        check(self.lib.rvh_asset_write(self.h, rec.ctypes.data_as(C.c_void_p), rec.nbytes))
+
+    def read_grid(self, cells):
+        out = np.empty((cells, 4), np.int64)
+        check(self.lib.rvh_asset_read_grid(self.h, out.ctypes.data_as(_P(C.c_int64)), out.nbytes))
+        return out
+
+    def read_draw(self):
+        d = T.DrawIndirect()
+        check(self.lib.rvh_asset_read_draw(self.h, C.byref(d)))
+        return (d.vertex_count, d.instance_count, d.first_vertex, d.first_instance)
+
+    def read_positions(self, stream=None):
+        out = np.empty((self.n_strands, self.n_points, 4), np.float32)
+        check(self.lib.rvh_asset_read_positions_async(self.h, out.ctypes.data_as(C.c_void_p), out.nbytes, stream))
+        self.ctx.synchronize()
+        return out
+
+    def device_ptr(self):
+        p = C.c_void_p()
+        check(self.lib.rvh_asset_device_ptr(self.h, C.byref(p)))
+        return p.value
+
+    def draw_indirect_ptr(self):
+        p = C.c_void_p()
+        check(self.lib.rvh_asset_draw_indirect(self.h, C.byref(p)))
+        return p.value
+
+
+class Batch:
+    def __init__(self, ctx, assets, lanes=0, strands_per_tile=0, ctas_per_sm=0, use_graph=True):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.assets = list(assets)
+        arr = (C.c_void_p * max(1, len(self.assets)))(*[a.h.value for a in self.assets])
+        d = BatchDesc(lanes, strands_per_tile, ctas_per_sm, 1 if use_graph else 0)
+        h = C.c_void_p()
+        check(self.lib.rvh_batch_create(ctx.h, arr, len(self.assets), C.byref(d), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.rvh_batch_destroy(self.h)
+            self.h = None
+
+    def step(self, frames, stream=None):
+        arr = (T.Frame * max(1, len(frames)))(*frames)
+        check(self.lib.rvh_batch_step(self.h, arr, stream))
+
+    def check(self):
+        check(self.lib.rvh_batch_check(self.h))
+
+    def h2d_bytes_per_step(self):
+        b = C.c_uint64()
+        check(self.lib.rvh_batch_h2d_bytes(self.h, C.byref(b)))
+        return b.value
+
+    def timing(self, on=True):
+        check(self.lib.rvh_batch_timing_enable(self.h, 1 if on else 0))
+
+    def read_timing(self):
+        ms, n = C.c_double(), C.c_int32()
+        check(self.lib.rvh_batch_timing_read(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def info(self):
+        l, it, ct, pts = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
+        check(self.lib.rvh_batch_info(self.h, C.byref(l), C.byref(it), C.byref(ct), C.byref(pts)))
+        return {"lanes": l.value, "items": it.value, "ctas": ct.value, "points": pts.value}
+
+
+# ---- scene helpers -------------------------------------------------------------
+
+def reference_params():
+    p = T.SimParams()
+    check(load().rvh_sim_params_reference(C.byref(p)))
+    return p
+
+
+def collider_from_trs(trans, rot_deg, scale, kind=T.COLLIDER_ELLIPSOID, radius=1.0):
+    c = T.Collider()
+    t, r, s = _f32(trans), _f32(rot_deg), _f32(scale)
+    check(load().rvh_collider_from_trs(_fp(t), _fp(r), _fp(s), kind, radius, C.byref(c)))
+    return c
+
+
+def collider_translate(c, delta):
+    out = T.Collider()
+    C.memmove(C.byref(out), C.byref(c), C.sizeof(T.Collider))
+    d = _f32(delta)
+    check(load().rvh_collider_translate(C.byref(out), _fp(d)))
+    return out
+
+
+def init_strands_reference(roots, normals, n_points, seg, dir_offset=(0.05, 5.0, -2.0)):
+    roots, normals, off = _f32(roots), _f32(normals), _f32(dir_offset)
+    ns = roots.shape[0]
+    out = np.empty((ns, 3 * n_points, 4), np.float32)
+    check(load().rvh_init_strands_reference(_fp(roots), _fp(normals), ns, n_points, seg, _fp(off),
+                                            out.ctypes.data_as(C.c_void_p)))
+    return out
+
+
+def generate_head(**kw):
+    """Returns (records (ns, 3n, 4) f32, rest (ns,), SimParams, [Collider])."""
+    d = HeadDesc()
+    d.head_radius = 1.0
+    d.dftl_damping = 0.0
+    for k, v in kw.items():
+        if k == "head_center":
+            d.head_center[:] = v
+        else:
+            setattr(d, k, v)
+    ns, n = d.n_strands, d.n_points
+    rec = np.empty((ns, 3 * n, 4), np.float32)
+    rest = np.empty(max(ns, 1), np.float32)
+    p = T.SimParams()
+    cols = (T.Collider * T.MAX_COLLIDERS)()
+    nc = C.c_int32()
+    check(load().rvh_generate_head(C.byref(d), rec.ctypes.data_as(C.c_void_p), _fp(rest), C.byref(p), cols,
+                                   C.byref(nc)))
+    return rec, rest[:ns], p, [cols[i] for i in range(nc.value)]
+
+
+def wind_at(desc, step, t):
+    out = (C.c_float * 3)()
+    check(load().rvh_wind_at(C.byref(desc), step, t, out))
+    return tuple(out)
+
+
+def sphere_on_orbit(orbit, t):
+    c = T.Collider()
+    check(load().rvh_sphere_on_orbit(C.byref(orbit), t, C.byref(c)))
+    return c
