@@ -86,6 +86,11 @@ rvh_status rvh_asset_destroy(rvh_asset* a);
 /* Time/Collider/Grid uniforms of sets 1-3 (compute.comp:20-42, Scene.cpp:4-20). */
 rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p);
 rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t n);
+/* Per-strand rest segment lengths (host array, n_strands floats; the
+ * reference's strandLength/(n-1), compute.comp:139-140) and per-strand wind
+ * (host array, 3 floats per strand, or NULL to remove it). */
+rvh_status rvh_asset_set_rest_lengths(rvh_asset* a, const float* rest);
+rvh_status rvh_asset_set_strand_wind(rvh_asset* a, const float* wind3);
 /* Device pointer of the Strand records (the VkBuffer Hair::GetStrandsBuffer(), Strand.cpp:195). */
 rvh_status rvh_asset_device_ptr(rvh_asset* a, void** out);
 /* Device pointer of the StrandDrawIndirect record the step writes (Strand.cpp:199, compute.comp:302). */
@@ -132,6 +137,18 @@ rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_
 rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
 rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);
 rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launches);
+
+/* ---- differentiation --------------------------------------------------------
+ * Reverse-mode derivative of n_steps steps from the asset's current state,
+ * through penalty collisions, PBD predict, FTL, the velocity clamp and the
+ * DFTL correction (compute.comp:144-216); the hair-hair grid must be off.
+ * Loss = 1/ns * sum_s |x_tip,s - target_s|^2 after the last step.  Gradients
+ * with respect to the per-strand wind (3 floats per strand), the rest segment
+ * lengths (1 per strand) and the initial velocities (3 per point); any output
+ * may be NULL.  Checkpoints every `checkpoint_every` steps (0 = 10) and
+ * recomputes each segment.  The asset's state is not modified.  Synchronous. */
+rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, int32_t checkpoint_every,
+                       const float* targets, double* loss, float* d_wind, float* d_rest, float* d_v0);
 
 #ifdef __cplusplus
 }

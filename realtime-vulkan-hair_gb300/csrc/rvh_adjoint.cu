@@ -1,0 +1,355 @@
+// rvh_adjoint.cu — reverse-mode derivative of the hair step without the
+// hair-hair grid (loops 1-2 of compute.comp:144-216: penalty collisions, PBD
+// predict, FTL, velocity damping/clamp, DFTL correction), with checkpointed
+// recomputation.
+//
+// One thread owns one strand for the whole run (strands are independent when
+// the grid is off).  The forward keeps (x, v) every C steps; the reverse walks
+// the checkpoints backwards, recomputes each segment's step inputs into a
+// per-strand tape, then back-propagates through those steps tip-to-root.
+//
+// Loss: L = 1/ns * sum_s |x_tip,s(T) - target_s|^2.  Outputs dL/d(strand
+// wind), dL/d(rest segment length), dL/d(initial velocity).  The contact set
+// and the |v| > vmax branch are held fixed (their derivative is zero almost
+// everywhere), as in the FP64 CPU adjoint the tests compare against.
+#include <algorithm>
+#include <vector>
+
+#include "rvh_internal.hpp"
+
+namespace rvh {
+
+constexpr int kAdjThreads = 64;
+
+struct AdjDev {
+    DevAsset A;                 // asset view: params, colliders, strands (initial state), rest, wind
+    const rvh_frame* frames;    // per step dt / wind
+    int32_t n_steps;
+    int32_t ckpt;               // checkpoint interval
+    int32_t n_ckpt;
+    const float4* targets;      // per strand
+    float4* ck;                 // n_ckpt * ns * 2n float4 (x then v)
+    float4* tape;               // ckpt * ns * 2n float4
+    double* loss_parts;         // per strand |tip - target|^2
+    float4* d_wind;             // per strand (xyz)
+    float* d_rest;              // per strand
+    float4* d_v0;               // per point (xyz)
+};
+
+template <class M>
+__device__ void fwd_local(f3* X, f3* V, int n, float r, f3 f0, const DevAsset& A, float dt) {
+    f3 P[RVH_MAX_POINTS], XN[RVH_MAX_POINTS];
+    const float dt2 = M::mul(dt, dt);
+    for (int i = 1; i < n; ++i) {
+        const f3 force = collide_force<M>(A, X[i], f0);
+        P[i] = v_add<M>(v_add<M>(X[i], v_scale<M>(dt, V[i])), v_scale<M>(dt2, force));
+    }
+    f3 par = X[0];
+    XN[0] = X[0];
+    for (int i = 1; i < n; ++i) {
+        const f3 dir = v_normalize<M>(v_sub<M>(P[i], par));
+        par = v_add<M>(par, v_scale<M>(r, dir));
+        XN[i] = par;
+    }
+    f3 cor[RVH_MAX_POINTS];
+    for (int i = 1; i < n; ++i) {
+        const f3 newVel = v_div<M>(v_sub<M>(XN[i], X[i]), dt);
+        f3 v = v_scale<M>(A.damping, newVel);
+        if (v_len<M>(v) > A.vmax) v = v_scale<M>(A.vmax, v_normalize<M>(v));
+        V[i] = v;
+        cor[i] = v_scale<M>(A.dftl, v_sub<M>(XN[i], P[i]));
+    }
+    for (int i = 1; i < n - 1; ++i) V[i] = v_sub<M>(V[i], v_div<M>(cor[i + 1], dt));
+    for (int i = 1; i < n; ++i) X[i] = XN[i];
+}
+
+// plain IEEE float helpers for the reverse sweep
+__device__ __forceinline__ f3 a3(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 s3(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 m3(float s, f3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float d3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float l3(f3 a) { return sqrtf(d3(a, a)); }
+// VJP of y = a/|a|: (ybar - y (y.ybar)) / |a|
+__device__ __forceinline__ f3 nvjp(f3 a, f3 yb) {
+    const float len = l3(a);
+    const f3 y = m3(1.0f / len, a);
+    return m3(1.0f / len, s3(yb, m3(d3(y, yb), y)));
+}
+// A^T v for a 3x4 / 3x3 column block (rows xyz)
+__device__ __forceinline__ f3 matT(const float* m, f3 v) {
+    return {m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+            m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+
+// Reverse of one step: X, V = step inputs; Xb, Vb in: adjoints of the outputs,
+// out: adjoints of the inputs.
+template <class M>
+__device__ void rev_local(const f3* X, const f3* V, f3* Xb, f3* Vb, int n, float r, f3 f0, const DevAsset& A,
+                          float dt, float& rest_bar, f3& wind_bar) {
+    const float k = A.k_penalty, damp = A.damping, s = A.dftl, vmax = A.vmax;
+    f3 P[RVH_MAX_POINTS], XN[RVH_MAX_POINTS], U[RVH_MAX_POINTS];
+    int cnt[RVH_MAX_POINTS];
+    const float dt2 = M::mul(dt, dt);
+    for (int i = 1; i < n; ++i) {
+        int c_n = 0;
+        const int nc = A.n_colliders;
+        for (int j = 0; j < nc; ++j) {
+            const DevCollider& c = A.col[j];
+            if (c.kind == RVH_COLLIDER_SPHERE) {
+                if (v_len<M>(v_sub<M>(X[i], f3{c.c[0], c.c[1], c.c[2]})) < c.radius) ++c_n;
+            } else {
+                if (v_len<M>(mat_p1<M>(c.inv, X[i])) <= 1.0f) ++c_n;
+            }
+        }
+        cnt[i] = c_n;
+        const f3 force = collide_force<M>(A, X[i], f0);
+        P[i] = v_add<M>(v_add<M>(X[i], v_scale<M>(dt, V[i])), v_scale<M>(dt2, force));
+    }
+    f3 par = X[0];
+    XN[0] = X[0];
+    for (int i = 1; i < n; ++i) {
+        par = v_add<M>(par, v_scale<M>(r, v_normalize<M>(v_sub<M>(P[i], par))));
+        XN[i] = par;
+        U[i] = v_scale<M>(damp, v_div<M>(v_sub<M>(XN[i], X[i]), dt));
+    }
+    f3 xnb[RVH_MAX_POINTS], cb[RVH_MAX_POINTS], xb[RVH_MAX_POINTS], vb[RVH_MAX_POINTS], pb[RVH_MAX_POINTS];
+    const f3 z = {0.f, 0.f, 0.f};
+    for (int i = 0; i < n; ++i) {
+        xnb[i] = Xb[i];
+        cb[i] = xb[i] = vb[i] = pb[i] = z;
+    }
+    for (int i = 1; i < n; ++i) {
+        const f3 vob = Vb[i];
+        if (i != n - 1) cb[i + 1] = s3(cb[i + 1], m3(1.0f / dt, vob));
+        f3 ub = vob;
+        const float ul = l3(U[i]);
+        if (ul > vmax) {
+            const f3 uh = m3(1.0f / ul, U[i]);
+            ub = m3(vmax / ul, s3(vob, m3(d3(uh, vob), uh)));
+        }
+        xnb[i] = a3(xnb[i], m3(damp / dt, ub));
+        xb[i] = s3(xb[i], m3(damp / dt, ub));
+    }
+    for (int i = 1; i < n; ++i) {
+        xnb[i] = a3(xnb[i], m3(s, cb[i]));
+        pb[i] = s3(pb[i], m3(s, cb[i]));
+    }
+    for (int i = n - 1; i >= 1; --i) {
+        const f3 dv = s3(P[i], XN[i - 1]);
+        const f3 nh = m3(1.0f / l3(dv), dv);
+        rest_bar += d3(xnb[i], nh);
+        const f3 db = nvjp(dv, m3(r, xnb[i]));
+        xnb[i - 1] = s3(a3(xnb[i - 1], xnb[i]), db);
+        pb[i] = a3(pb[i], db);
+    }
+    for (int i = 1; i < n; ++i) {
+        xb[i] = a3(xb[i], pb[i]);
+        vb[i] = a3(vb[i], m3(dt, pb[i]));
+        const f3 fb = m3(dt * dt, pb[i]);
+        wind_bar = a3(wind_bar, fb);
+        if (cnt[i] == 0) continue;
+        const f3 g = m3(1.0f / (float)cnt[i], fb);
+        const f3 x = X[i];
+        const int nc = A.n_colliders;
+        for (int j = 0; j < nc; ++j) {
+            const DevCollider& c = A.col[j];
+            if (c.kind == RVH_COLLIDER_SPHERE) {
+                const f3 e0 = s3(x, f3{c.c[0], c.c[1], c.c[2]});
+                const float rho = l3(e0);
+                if (!(v_len<M>(v_sub<M>(x, f3{c.c[0], c.c[1], c.c[2]})) < c.radius)) continue;
+                const f3 e = m3(1.0f / rho, e0);
+                const float eg = d3(e, g);
+                xb[i] = a3(xb[i], m3(k, a3(m3(-eg, e), m3((c.radius - rho) / rho, s3(g, m3(eg, e))))));
+            } else {
+                const f3 q = mat_p1<M>(c.inv, x);
+                if (!(v_len<M>(q) <= 1.0f)) continue;
+                const f3 uh = m3(1.0f / l3(q), q);
+                const f3 surf = mat_p1<M>(c.xf, uh);
+                const f3 e = s3(surf, x);
+                const float d = l3(e);
+                const f3 m = mat_q0<M>(c.itr, q);
+                const f3 nt = m3(1.0f / l3(m), m);
+                const float dbar = k * d3(nt, g);
+                const f3 ntb = m3(k * d, g);
+                f3 qb = z;
+                if (d > 0.f) {
+                    const f3 eb = m3(dbar / d, e);
+                    xb[i] = s3(xb[i], eb);
+                    qb = a3(qb, nvjp(q, matT(c.xf, eb)));
+                }
+                qb = a3(qb, matT(c.itr, nvjp(m, ntb)));
+                xb[i] = a3(xb[i], matT(c.inv, qb));
+            }
+        }
+    }
+    Xb[0] = z;
+    Vb[0] = z;
+    for (int i = 1; i < n; ++i) {
+        Xb[i] = xb[i];
+        Vb[i] = vb[i];
+    }
+}
+
+__device__ __forceinline__ f3 strand_f0(const DevAsset& A, const rvh_frame& F, int s) {
+    f3 f0 = {__fadd_rn(A.gravity[0], F.wind[0]), __fadd_rn(A.gravity[1], F.wind[1]), __fadd_rn(A.gravity[2], F.wind[2])};
+    if (A.strand_wind) {
+        const float4 w = A.strand_wind[s];
+        f0 = {__fadd_rn(f0.x, w.x), __fadd_rn(f0.y, w.y), __fadd_rn(f0.z, w.z)};
+    }
+    return f0;
+}
+
+template <class M>
+__global__ void __launch_bounds__(kAdjThreads) k_adjoint(const __grid_constant__ AdjDev D) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevAsset& A = D.A;
+    if (s >= A.n_strands) return;
+    const int n = A.n_points;
+    const float r = A.rest[s];
+    f3 X[RVH_MAX_POINTS], V[RVH_MAX_POINTS];
+    const float4* rec = A.strands + (size_t)s * 3 * n;
+    for (int i = 0; i < n; ++i) {
+        X[i] = xyz(rec[i]);
+        V[i] = xyz(rec[n + i]);
+    }
+    const size_t stride = (size_t)2 * n;  // float4 per strand per saved state
+    auto save = [&](float4* base, int slot) {
+        float4* p = base + ((size_t)slot * A.n_strands + s) * stride;
+        for (int i = 0; i < n; ++i) {
+            p[i] = make_float4(X[i].x, X[i].y, X[i].z, 0.f);
+            p[n + i] = make_float4(V[i].x, V[i].y, V[i].z, 0.f);
+        }
+    };
+    auto load = [&](const float4* base, int slot, f3* Xo, f3* Vo) {
+        const float4* p = base + ((size_t)slot * A.n_strands + s) * stride;
+        for (int i = 0; i < n; ++i) {
+            Xo[i] = xyz(p[i]);
+            Vo[i] = xyz(p[n + i]);
+        }
+    };
+    for (int t = 0; t < D.n_steps; ++t) {
+        if (t % D.ckpt == 0) save(D.ck, t / D.ckpt);
+        fwd_local<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
+    }
+    const float4 tg = D.targets[s];
+    const f3 e = {X[n - 1].x - tg.x, X[n - 1].y - tg.y, X[n - 1].z - tg.z};
+    D.loss_parts[s] = (double)e.x * e.x + (double)e.y * e.y + (double)e.z * e.z;
+    f3 Xb[RVH_MAX_POINTS], Vb[RVH_MAX_POINTS];
+    for (int i = 0; i < n; ++i) Xb[i] = Vb[i] = f3{0.f, 0.f, 0.f};
+    const float g2 = 2.0f / (float)A.n_strands;
+    Xb[n - 1] = {g2 * e.x, g2 * e.y, g2 * e.z};
+    float rest_bar = 0.f;
+    f3 wind_bar = {0.f, 0.f, 0.f};
+    for (int k = D.n_ckpt - 1; k >= 0; --k) {
+        const int t0 = k * D.ckpt, t1 = min(D.n_steps, t0 + D.ckpt);
+        load(D.ck, k, X, V);
+        for (int t = t0; t < t1; ++t) {
+            save(D.tape, t - t0);
+            if (t + 1 < t1) fwd_local<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
+        }
+        for (int t = t1 - 1; t >= t0; --t) {
+            f3 Xi[RVH_MAX_POINTS], Vi[RVH_MAX_POINTS];
+            load(D.tape, t - t0, Xi, Vi);
+            rev_local<M>(Xi, Vi, Xb, Vb, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt, rest_bar, wind_bar);
+        }
+    }
+    D.d_rest[s] = rest_bar;
+    D.d_wind[s] = make_float4(wind_bar.x, wind_bar.y, wind_bar.z, 0.f);
+    for (int i = 0; i < n; ++i) D.d_v0[(size_t)s * n + i] = make_float4(Vb[i].x, Vb[i].y, Vb[i].z, 0.f);
+}
+
+}  // namespace rvh
+
+using namespace rvh;
+
+extern "C" {
+
+rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, int32_t checkpoint_every,
+                       const float* targets, double* loss, float* d_wind, float* d_rest, float* d_v0) {
+    if (!a || !frames || !targets || !loss) return fail(RVH_ERR_INVALID_ARG, "adjoint: NULL argument");
+    if (n_steps < 1) return fail(RVH_ERR_INVALID_ARG, "adjoint: n_steps must be >= 1");
+    if (checkpoint_every < 1) checkpoint_every = 10;
+    if (a->params.grid_enabled)
+        return fail(RVH_ERR_UNSUPPORTED, "adjoint: the hair-hair grid must be disabled (FTL+DFTL+collisions only)");
+    for (int t = 0; t < n_steps; ++t) {
+        rvh_status st = validate_frame(frames[t]);
+        if (st != RVH_OK) return st;
+    }
+    Context* ctx = a->ctx;
+    cudaSetDevice(ctx->device);
+    const int ns = a->n_strands, n = a->n_points;
+    if (ns == 0) {
+        *loss = 0.0;
+        return RVH_OK;
+    }
+    const int C = std::min(checkpoint_every, n_steps);
+    const int n_ckpt = (n_steps + C - 1) / C;
+    DevBuf fr, tg, ck, tape, lp, dw, dr, dv;
+    auto cleanup = [&]() {
+        for (DevBuf* b : {&fr, &tg, &ck, &tape, &lp, &dw, &dr, &dv}) ctx->free(*b);
+    };
+    rvh_status st;
+    const size_t state = size_t(ns) * 2 * n * sizeof(float4);
+    if ((st = ctx->alloc(fr, sizeof(rvh_frame) * n_steps)) || (st = ctx->alloc(tg, sizeof(float4) * ns)) ||
+        (st = ctx->alloc(ck, state * n_ckpt)) || (st = ctx->alloc(tape, state * C)) ||
+        (st = ctx->alloc(lp, sizeof(double) * ns)) || (st = ctx->alloc(dw, sizeof(float4) * ns)) ||
+        (st = ctx->alloc(dr, sizeof(float) * ns)) || (st = ctx->alloc(dv, sizeof(float4) * size_t(ns) * n))) {
+        cleanup();
+        return st;
+    }
+    std::vector<float4> t4(ns);
+    for (int s = 0; s < ns; ++s) t4[s] = make_float4(targets[3 * s], targets[3 * s + 1], targets[3 * s + 2], 0.f);
+    cudaError_t e = cudaMemcpy(fr.ptr, frames, sizeof(rvh_frame) * n_steps, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(tg.ptr, t4.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "adjoint upload");
+    }
+    AdjDev D{};
+    D.A = a->device_view(frames[0], a->parity);
+    D.frames = static_cast<const rvh_frame*>(fr.ptr);
+    D.n_steps = n_steps;
+    D.ckpt = C;
+    D.n_ckpt = n_ckpt;
+    D.targets = static_cast<const float4*>(tg.ptr);
+    D.ck = static_cast<float4*>(ck.ptr);
+    D.tape = static_cast<float4*>(tape.ptr);
+    D.loss_parts = static_cast<double*>(lp.ptr);
+    D.d_wind = static_cast<float4*>(dw.ptr);
+    D.d_rest = static_cast<float*>(dr.ptr);
+    D.d_v0 = static_cast<float4*>(dv.ptr);
+    void* args[] = {&D};
+    const void* kern = ctx->math == RVH_MATH_EXACT ? reinterpret_cast<const void*>(&k_adjoint<ExactMath>)
+                                                   : reinterpret_cast<const void*>(&k_adjoint<FastMath>);
+    e = cudaLaunchKernel(kern, dim3(unsigned((ns + kAdjThreads - 1) / kAdjThreads)), dim3(kAdjThreads), args, 0,
+                         ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    std::vector<double> parts(ns);
+    std::vector<float4> w4(ns), v4(size_t(ns) * n);
+    std::vector<float> r1(ns);
+    if (e == cudaSuccess) e = cudaMemcpy(parts.data(), lp.ptr, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(w4.data(), dw.ptr, sizeof(float4) * ns, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(r1.data(), dr.ptr, sizeof(float) * ns, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(v4.data(), dv.ptr, sizeof(float4) * v4.size(), cudaMemcpyDeviceToHost);
+    cleanup();
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint");
+    double sum = 0.0;
+    for (double p : parts) sum += p;
+    *loss = sum / double(ns);
+    if (d_wind)
+        for (int s = 0; s < ns; ++s) {
+            d_wind[3 * s] = w4[s].x;
+            d_wind[3 * s + 1] = w4[s].y;
+            d_wind[3 * s + 2] = w4[s].z;
+        }
+    if (d_rest) std::copy(r1.begin(), r1.end(), d_rest);
+    if (d_v0)
+        for (size_t p = 0; p < v4.size(); ++p) {
+            d_v0[3 * p] = v4[p].x;
+            d_v0[3 * p + 1] = v4[p].y;
+            d_v0[3 * p + 2] = v4[p].z;
+        }
+    return RVH_OK;
+}
+
+}  // extern "C"

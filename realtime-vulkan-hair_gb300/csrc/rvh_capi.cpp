@@ -527,6 +527,40 @@ rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t 
     return RVH_OK;
 }
 
+rvh_status rvh_asset_set_rest_lengths(rvh_asset* a, const float* rest) {
+    if (!a || (!rest && a->n_strands)) return fail(RVH_ERR_INVALID_ARG, "set_rest_lengths: NULL argument");
+    for (int i = 0; i < a->n_strands; ++i)
+        if (!std::isfinite(rest[i]) || rest[i] < 0.f) return fail(RVH_ERR_INVALID_ARG, "set_rest_lengths: bad value");
+    if (!a->n_strands) return RVH_OK;
+    DeviceGuard g(a->ctx->device);
+    RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
+    RVH_CUDA(cudaMemcpy(a->rest.ptr, rest, sizeof(float) * a->n_strands, cudaMemcpyHostToDevice));
+    return RVH_OK;
+}
+
+rvh_status rvh_asset_set_strand_wind(rvh_asset* a, const float* wind3) {
+    if (!a) return fail(RVH_ERR_INVALID_ARG, "set_strand_wind: NULL asset");
+    DeviceGuard g(a->ctx->device);
+    RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
+    if (!wind3 || !a->n_strands) {
+        a->has_wind = false;
+        return RVH_OK;
+    }
+    std::vector<float> w(size_t(a->n_strands) * 4, 0.f);
+    for (int i = 0; i < a->n_strands; ++i)
+        for (int q = 0; q < 3; ++q) {
+            if (!std::isfinite(wind3[3 * i + q])) return fail(RVH_ERR_INVALID_ARG, "set_strand_wind: non-finite");
+            w[4 * i + q] = wind3[3 * i + q];
+        }
+    if (!a->wind.ptr) {
+        rvh_status s = a->ctx->alloc(a->wind, w.size() * 4);
+        if (s != RVH_OK) return s;
+    }
+    RVH_CUDA(cudaMemcpy(a->wind.ptr, w.data(), w.size() * 4, cudaMemcpyHostToDevice));
+    a->has_wind = true;
+    return RVH_OK;
+}
+
 rvh_status rvh_asset_device_ptr(rvh_asset* a, void** out) {
     if (!a || !out) return fail(RVH_ERR_INVALID_ARG, "device_ptr: NULL argument");
     *out = a->strands.ptr;

@@ -35,6 +35,8 @@ PROTOTYPES = [
     ("rvh_asset_destroy", _st, [_vp]),
     ("rvh_asset_set_params", _st, [_vp, _P(T.SimParams)]),
     ("rvh_asset_set_colliders", _st, [_vp, _P(T.Collider), C.c_int32]),
+    ("rvh_asset_set_rest_lengths", _st, [_vp, _P(C.c_float)]),
+    ("rvh_asset_set_strand_wind", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_device_ptr", _st, [_vp, _P(_vp)]),
     ("rvh_asset_draw_indirect", _st, [_vp, _P(_vp)]),
     ("rvh_asset_strand_count", _st, [_vp, _P(C.c_int32), _P(C.c_int32)]),
@@ -52,6 +54,8 @@ PROTOTYPES = [
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_batch_timing_enable", _st, [_vp, C.c_int32]),
     ("rvh_batch_timing_read", _st, [_vp, _P(C.c_double), _P(C.c_int32)]),
+    ("rvh_adjoint", _st, [_vp, _P(T.Frame), C.c_int32, C.c_int32, _P(C.c_float), _P(C.c_double),
+                          _P(C.c_float), _P(C.c_float), _P(C.c_float)]),
     ("rvh_generate_head", _st, [_vp, _vp, _P(C.c_float), _P(T.SimParams), _P(T.Collider), _P(C.c_int32)]),
     ("rvh_wind_at", _st, [_vp, C.c_int64, C.c_float, _P(C.c_float)]),
     ("rvh_sphere_on_orbit", _st, [_vp, C.c_float, _P(T.Collider)]),

@@ -139,6 +139,26 @@ class Asset:
         check(self.lib.rvh_asset_read_grid(self.h, out.ctypes.data_as(_P(C.c_int64)), out.nbytes))
         return out
 
+    def set_rest_lengths(self, rest):
+        r = _f32(rest)
+        check(self.lib.rvh_asset_set_rest_lengths(self.h, _fp(r)))
+
+    def set_strand_wind(self, wind):
+        w = None if wind is None else _f32(wind).reshape(-1)
+        check(self.lib.rvh_asset_set_strand_wind(self.h, _fp(w)))
+
+    def adjoint(self, frames, targets, checkpoint_every=10):
+        """Returns (loss, d_wind (ns,3), d_rest (ns,), d_v0 (ns,n,3)) of the tip loss."""
+        fr = (T.Frame * len(frames))(*frames)
+        tg = _f32(targets).reshape(-1)
+        loss = C.c_double()
+        dw = np.zeros((self.n_strands, 3), np.float32)
+        dr = np.zeros(self.n_strands, np.float32)
+        dv = np.zeros((self.n_strands, self.n_points, 3), np.float32)
+        check(self.lib.rvh_adjoint(self.h, fr, len(frames), checkpoint_every, _fp(tg), C.byref(loss), _fp(dw),
+                                   _fp(dr), _fp(dv)))
+        return loss.value, dw, dr, dv
+
     def read_draw(self):
         d = T.DrawIndirect()
         check(self.lib.rvh_asset_read_draw(self.h, C.byref(d)))

@@ -117,12 +117,18 @@ def batched(n_assets=256, seed=2, scale=1.0, smin=512, smax=65536):
     return specs
 
 
-def adjoint_case(n_strands=4096, n_points=32, seed=4, n_ellipsoids=2):
-    rec, rest, p, cols = api.generate_head(seed=seed, n_strands=n_strands, n_points=n_points,
+def adjoint_case(n_strands=4096, n_points=32, seed=4, n_ellipsoids=2, max_root_height=0.85):
+    """Roots above `max_root_height` (near the crown, where a strand starts
+    pointing straight up like an inverted pendulum) are skipped: there the
+    loss is so nonlinear that central differences at h = 1e-4 do not converge."""
+    rec, rest, p, cols = api.generate_head(seed=seed, n_strands=2 * n_strands, n_points=n_points,
                                            root_sampling=0, sort_roots=1, length_min=0.4, length_max=0.8,
                                            head_collider=1, n_ellipsoids=n_ellipsoids, axis_min=0.2,
                                            axis_max=0.5, grid_res=0, friction=0.0, repulsion=0.0,
                                            dftl_damping=0.9)
+    keep = np.nonzero(rec[:, 0, 1] < max_root_height)[0][:n_strands]
+    rec, rest = np.ascontiguousarray(rec[keep]), np.ascontiguousarray(rest[keep])
+    n_strands = rec.shape[0]
     rng = np.random.default_rng(seed)
     tips = rec[:, n_points - 1, :3].astype(np.float64)
     targets = tips + rng.normal(0.0, 0.05, size=tips.shape)

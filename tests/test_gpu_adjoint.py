@@ -1,0 +1,158 @@
+"""GPU adjoint (C ABI rvh_adjoint) wrapped in a torch.autograd.Function —
+a test-only harness — checked against the FP64 CPU adjoint and against
+central finite differences (h = 1e-4, 64 random parameters) evaluated in
+FP64 on the oracle.  Workload: 4,096 strands x 32 points, 60 steps, no grid,
+head sphere + 2 ellipsoids; loss = mean |tip - target|^2 with targets the
+initial tips displaced by N(0, 0.05^2)."""
+import numpy as np
+import pytest
+
+from rvh import api, configs
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 60
+
+
+class HairTipLoss:
+    """torch.autograd.Function over the GPU forward + adjoint (test harness only)."""
+
+    @staticmethod
+    def make():
+        import torch
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, v0, wind, rest, asset, base_records, frames, targets):
+                n = asset.n_points
+                rec = base_records.copy()
+                rec[:, n:2 * n, :3] = v0.detach().cpu().numpy().astype(np.float32)
+                asset.write(rec)
+                asset.set_strand_wind(wind.detach().cpu().numpy())
+                asset.set_rest_lengths(rest.detach().cpu().numpy())
+                loss, dw, dr, dv = asset.adjoint(frames, targets)
+                ctx.save_for_backward(torch.from_numpy(dv).double(), torch.from_numpy(dw).double(),
+                                      torch.from_numpy(dr).double())
+                return torch.tensor(loss, dtype=torch.float64)
+
+            @staticmethod
+            def backward(ctx, g):
+                dv, dw, dr = ctx.saved_tensors
+                return g * dv, g * dw, g * dr, None, None, None, None
+
+        return _Fn
+
+
+@pytest.fixture(scope="module")
+def case():
+    return configs.adjoint_case(n_strands=4096, n_points=32)
+
+
+@pytest.fixture(scope="module")
+def gpu_grads(gpu_ctx_fast, case):
+    import torch
+    spec, targets = case
+    n = spec.n_points
+    a = api.Asset(gpu_ctx_fast, spec.records, n, rest=spec.rest, strand_wind=spec.strand_wind)
+    a.set_params(spec.params)
+    a.set_colliders(spec.colliders)
+    frames = [spec.frame(k) for k in range(STEPS)]
+    v0 = torch.tensor(spec.records[:, n:2 * n, :3].astype(np.float64), requires_grad=True)
+    wind = torch.tensor(spec.strand_wind.astype(np.float64), requires_grad=True)
+    rest = torch.tensor(spec.rest.astype(np.float64), requires_grad=True)
+    fn = HairTipLoss.make()
+    loss = fn.apply(v0, wind, rest, a, spec.records, frames, targets)
+    loss.backward()
+    out = (float(loss), wind.grad.numpy(), rest.grad.numpy(), v0.grad.numpy(), a.read())
+    a.close()
+    return out
+
+
+def test_gpu_adjoint_matches_fp64_cpu_adjoint(case, gpu_grads, oracle):
+    spec, targets = case
+    loss_g, dw_g, dr_g, dv_g, _ = gpu_grads
+    frames = [spec.frame(k) for k in range(STEPS)]
+    loss_c, dw_c, dr_c, dv_c = oracle.adjoint(spec.records.astype(np.float64), spec.n_points,
+                                              spec.rest.astype(np.float64), spec.params, frames, spec.colliders,
+                                              STEPS, targets, strand_wind=spec.strand_wind.astype(np.float64),
+                                              threads=16)
+    assert abs(loss_g - loss_c) <= 1e-4 * abs(loss_c), (loss_g, loss_c)
+    for name, g, c in (("wind", dw_g, dw_c), ("rest", dr_g, dr_c), ("v0", dv_g, dv_c)):
+        rel = np.linalg.norm(g - c) / np.linalg.norm(c)
+        print("%s gradient: relative L2 error vs FP64 adjoint %.3g" % (name, rel))
+        assert rel < 2e-3, (name, rel)
+
+
+def test_gpu_adjoint_matches_central_fd_fp64(case, gpu_grads, oracle):
+    spec, targets = case
+    _, dw_g, dr_g, dv_g, _ = gpu_grads
+    n = spec.n_points
+    frames = [spec.frame(k) for k in range(STEPS)]
+    st0 = spec.records.astype(np.float64)
+    rest = spec.rest.astype(np.float64)
+    wind = spec.strand_wind.astype(np.float64)
+
+    def L(st=st0, r=rest, w=wind):
+        return oracle.loss(st, n, r, spec.params, frames, spec.colliders, STEPS, targets, strand_wind=w,
+                           threads=16)
+
+    rng = np.random.default_rng(64)
+    h = 1e-4
+    rows = []
+    for j in range(64):
+        kind = j % 3
+        s = int(rng.integers(0, spec.n_strands))
+        if kind == 0:
+            q = int(rng.integers(0, 3))
+            wp, wm = wind.copy(), wind.copy()
+            wp[s, q] += h
+            wm[s, q] -= h
+            fd, ad = (L(w=wp) - L(w=wm)) / (2 * h), dw_g[s, q]
+        elif kind == 1:
+            rp, rm = rest.copy(), rest.copy()
+            rp[s] += h
+            rm[s] -= h
+            fd, ad = (L(r=rp) - L(r=rm)) / (2 * h), dr_g[s]
+        else:
+            i, q = int(rng.integers(1, n)), int(rng.integers(0, 3))
+            sp, sm = st0.copy(), st0.copy()
+            sp[s, n + i, q] += h
+            sm[s, n + i, q] -= h
+            fd, ad = (L(st=sp) - L(st=sm)) / (2 * h), dv_g[s, i, q]
+        rows.append((kind, fd, ad))
+    rows = np.array(rows)
+    scale = np.abs(rows[:, 1]).max()
+    err = np.abs(rows[:, 1] - rows[:, 2])
+    ok = err <= 2e-2 * np.abs(rows[:, 1]) + 1e-3 * scale
+    print("FD h=1e-4: %d/64 within tolerance; median rel err %.3g" % (ok.sum(), np.median(err / np.maximum(np.abs(rows[:, 1]), 1e-12))))
+    assert ok.sum() >= 62, rows[~ok]
+
+
+def test_adjoint_forward_equals_the_step_kernel(gpu_ctx, case):
+    """Exact mode: the adjoint's own forward replay reproduces the step kernel's
+    positions bit for bit, so its loss equals the loss of 60 rvh_step calls."""
+    spec, targets = case
+    n = spec.n_points
+    sub = slice(0, 512)
+    rec = np.ascontiguousarray(spec.records[sub])
+    a = api.Asset(gpu_ctx, rec, n, rest=spec.rest[sub], strand_wind=spec.strand_wind[sub])
+    a.set_params(spec.params)
+    a.set_colliders(spec.colliders)
+    frames = [spec.frame(k) for k in range(STEPS)]
+    loss_adj = a.adjoint(frames, targets[sub])[0]
+    for f in frames:
+        a.step(f)
+    tips = a.read()[:, n - 1, :3].astype(np.float64)
+    loss_fwd = float(np.mean(np.sum((tips - targets[sub]) ** 2, axis=1)))
+    assert abs(loss_adj - loss_fwd) <= 1e-12 * abs(loss_fwd)
+    a.close()
+
+
+def test_adjoint_rejects_grid(gpu_ctx_fast):
+    from rvh._lib import RvhError
+    spec = configs.full_head(n_strands=64, n_points=8, grid_res=16)
+    a = api.Asset(gpu_ctx_fast, spec.records, 8, rest=spec.rest)
+    a.set_params(spec.params)
+    with pytest.raises(RvhError):
+        a.adjoint([spec.frame(0)], np.zeros((64, 3), np.float32))
+    a.close()
