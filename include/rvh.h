@@ -133,6 +133,10 @@ rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_
  * its stream around the persistent launch.  rvh_batch_timing_read waits for
  * them and returns the summed device time and the launch count since the
  * last read (then resets). */
+/* Counters since the last call (then reset): phase-A rounds splatted through
+ * the shared-memory box, rounds splatted with direct global atomics, phase-B
+ * tiles gathered from the box, tiles gathered from the global grid. */
+rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]);
 /* Bytes rvh_batch_step copies host->device per step (per-asset frame and collider tables). */
 rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
 rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);

@@ -26,7 +26,7 @@ struct Batch {
     int64_t n_points = 0;
     std::vector<WorkItem> items;
     std::vector<unsigned> need_a;
-    DevBuf d_assets, d_items, d_need, d_done, d_head, d_error;
+    DevBuf d_assets, d_items, d_need, d_done, d_head, d_error, d_stats;
     DevAsset* h_stage[2] = {nullptr, nullptr};
     cudaEvent_t staged[2] = {nullptr, nullptr};
     int slot = 0;
@@ -42,7 +42,7 @@ struct Batch {
 namespace {
 
 constexpr int kTargetPointsA = 4096;   // points per phase-A item
-constexpr int kTargetPointsB = 8192;   // points per phase-B item
+constexpr int kTargetPointsB = kTileB;  // points per phase-B item (one shared-memory box)
 constexpr int kClearChunk = 1 << 16;   // 16-B units per clear item (1 MiB)
 constexpr uint32_t kSpinLimit = 1u << 22;  // ~1 s of 256-ns sleeps before a wait gives up
 
@@ -114,6 +114,7 @@ void destroy(Batch* b) {
         b->ctx->free(b->d_done);
         b->ctx->free(b->d_head);
         b->ctx->free(b->d_error);
+        b->ctx->free(b->d_stats);
     }
     delete b;
 }
@@ -122,7 +123,7 @@ rvh_status enqueue_launch(Batch* b, cudaStream_t s) {
     RVH_CUDA(cudaMemsetAsync(b->d_head.ptr, 0, sizeof(unsigned), s));
     RVH_CUDA(cudaMemsetAsync(b->d_done.ptr, 0, sizeof(unsigned) * b->assets.size(), s));
     void* args[] = {&b->dev};
-    RVH_CUDA(cudaLaunchKernel(b->kernel, dim3(unsigned(b->n_ctas)), dim3(kThreads), args, 0, s));
+    RVH_CUDA(cudaLaunchKernel(b->kernel, dim3(unsigned(b->n_ctas)), dim3(kThreads), args, kSmemBytes, s));
     return RVH_OK;
 }
 
@@ -165,8 +166,12 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
         b->n_points += int64_t(assets[i]->n_strands) * assets[i]->n_points;
     }
     b->kernel = batch_kernel(lanes, b->exact);
+    if (!prepare_kernel(b->kernel)) {
+        destroy(b);
+        return fail(RVH_ERR_CUDA, "cannot opt the batch kernel into shared memory");
+    }
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kernel, kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->kernel, kThreads, kSmemBytes);
     if (e != cudaSuccess) {
         destroy(b);
         return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -186,6 +191,9 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
     if ((s = ctx->alloc(b->d_done, sizeof(unsigned) * na)) != RVH_OK) return bail(s);
     if ((s = ctx->alloc(b->d_head, sizeof(unsigned))) != RVH_OK) return bail(s);
     if ((s = ctx->alloc(b->d_error, sizeof(int))) != RVH_OK) return bail(s);
+    if ((s = ctx->alloc(b->d_stats, 4 * sizeof(unsigned))) != RVH_OK) return bail(s);
+    e = cudaMemset(b->d_stats.ptr, 0, 4 * sizeof(unsigned));
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemset stats"));
     if (!b->items.empty()) {
         e = cudaMemcpy(b->d_items.ptr, b->items.data(), sizeof(WorkItem) * b->items.size(), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMemcpy items"));
@@ -210,6 +218,7 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
     b->dev.done_a = static_cast<unsigned*>(b->d_done.ptr);
     b->dev.need_a = static_cast<const unsigned*>(b->d_need.ptr);
     b->dev.error = static_cast<int*>(b->d_error.ptr);
+    b->dev.stats = static_cast<unsigned*>(b->d_stats.ptr);
     if (b->use_graph && !b->items.empty()) {
         cudaStream_t cs = ctx->stream;
         e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
@@ -325,6 +334,15 @@ rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launch
     if (launches) *launches = int32_t(b->ev_pairs.size());
     if (total_ms) *total_ms = sum;
     b->ev_pairs.clear();
+    return RVH_OK;
+}
+
+rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]) {
+    if (!b || !out) return fail(RVH_ERR_INVALID_ARG, "batch_box_stats: NULL");
+    cudaSetDevice(b->ctx->device);
+    RVH_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    RVH_CUDA(cudaMemcpy(out, b->d_stats.ptr, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    RVH_CUDA(cudaMemset(b->d_stats.ptr, 0, 4 * sizeof(unsigned)));
     return RVH_OK;
 }
 

@@ -158,20 +158,22 @@ rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s) {
     const bool exact = a->ctx->math == RVH_MATH_EXACT;
     const void* ka = plain_a_kernel(a->n_points, a->lanes, exact);
     if (!ka) return fail(RVH_ERR_UNSUPPORTED, "no phase-A kernel for this (n_points, lanes_per_strand)");
+    const void* kb = plain_b_kernel(exact);
+    if (!prepare_kernel(ka) || !prepare_kernel(kb)) return fail(RVH_ERR_CUDA, "cannot opt the step kernels into shared memory");
     const int which = a->parity;
     DevAsset A = a->device_view(f, which);
     if (a->params.grid_enabled) RVH_CUDA(cudaMemsetAsync(A.grid, 0, a->grid_bytes(), s));
     const int per_cta = kWarps * (32 / a->lanes);
     const unsigned blocks_a = unsigned((a->n_strands + per_cta - 1) / per_cta);
     void* args[] = {&A};
-    if (blocks_a > 0) RVH_CUDA(cudaLaunchKernel(ka, dim3(blocks_a), dim3(kThreads), args, 0, s));
+    if (blocks_a > 0) RVH_CUDA(cudaLaunchKernel(ka, dim3(blocks_a), dim3(kThreads), args, kSmemBytes, s));
     if (a->params.grid_enabled) {
         const long long pts = (long long)a->n_strands * a->n_points;
-        long long blocks = (pts + kThreads - 1) / kThreads;
-        const long long cap = (long long)a->ctx->sm_count * 8;
+        long long blocks = (pts + kTileB - 1) / kTileB;
+        const long long cap = (long long)a->ctx->sm_count * 2 * 8;
         if (blocks > cap) blocks = cap;
         if (blocks < 1) blocks = 1;
-        RVH_CUDA(cudaLaunchKernel(plain_b_kernel(exact), dim3(unsigned(blocks)), dim3(kThreads), args, 0, s));
+        RVH_CUDA(cudaLaunchKernel(kb, dim3(unsigned(blocks)), dim3(kThreads), args, kSmemBytes, s));
         a->grid_dirty[which] = true;
     }
     return RVH_OK;

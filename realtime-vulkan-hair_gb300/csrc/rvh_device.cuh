@@ -242,12 +242,38 @@ __device__ __forceinline__ long long grid_val(unsigned long long raw, bool wrap3
     return wrap32 ? (long long)(int)(unsigned)(raw & 0xffffffffull) : (long long)raw;
 }
 
-// Gather + friction (+ repulsion) for one point; returns the new velocity.
+// One grid cell as the gather reads it: velocity sums as floats, the density
+// as a float (fd > 0 exactly when the integer density is > 0) and 1/fd.
+struct CellF {
+    float vx, vy, vz, fd, rcp;
+};
+
 template <class M>
-__device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel) {
-    const Corners C = corners_of<M>(A, pos);
-    const int nxny = A.nx * A.ny;
+__device__ __forceinline__ CellF cell_from_sums(long long vx, long long vy, long long vz, long long dens) {
+    CellF c;
+    c.vx = (float)vx;
+    c.vy = (float)vy;
+    c.vz = (float)vz;
+    c.fd = (float)dens;
+    c.rcp = dens > 0 ? M::rcp(c.fd) : 0.0f;
+    return c;
+}
+
+template <class M>
+__device__ __forceinline__ CellF cell_from_global(const DevAsset& A, unsigned idx) {
+    const ulonglong2* cell = reinterpret_cast<const ulonglong2*>(A.grid + 4ull * idx);
     const bool wrap = A.wrap32 != 0;
+    const ulonglong2 zw = __ldcg(cell + 1);
+    const long long dens = grid_val(zw.y, wrap);
+    if (dens <= 0) return CellF{0.f, 0.f, 0.f, 0.f, 0.f};
+    const ulonglong2 xy = __ldcg(cell);
+    return cell_from_sums<M>(grid_val(xy.x, wrap), grid_val(xy.y, wrap), grid_val(zw.x, wrap), dens);
+}
+
+// Gather + friction (+ repulsion) for one point (compute.comp:258-297);
+// cell(a, b, c) returns the CellF of corner (a, b, c).
+template <class M, class CellFn>
+__device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel, const Corners& C, CellFn cell) {
     const bool rep = A.repulsion != 0.0f;
     f3 gv = {0.f, 0.f, 0.f};
     float rho = 0.f;
@@ -264,20 +290,14 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel) {
             for (int dc = 0; dc < 2; ++dc) {
                 if (dc >= C.cnt[2]) continue;
                 const int c = C.lo[2] + dc;
-                const ulonglong2* cell =
-                    reinterpret_cast<const ulonglong2*>(A.grid + 4ull * (unsigned)(a + b * A.nx + c * nxny));
-                const ulonglong2 zw = __ldcg(cell + 1);
-                const long long dens = grid_val(zw.y, wrap);
-                if (dens > 0) {
-                    const ulonglong2 xy = __ldcg(cell);
+                const CellF cf = cell(a, b, c);
+                if (cf.fd > 0.0f) {
                     const float wx = tri_w<M>(C.g[0], a), wy = tri_w<M>(C.g[1], b), wz = tri_w<M>(C.g[2], c);
                     const float w = M::mul(M::mul(wx, wy), wz);
-                    const float fd = (float)dens;
-                    const float s = M::mul(w, M::rcp(fd));
-                    const f3 cv = {(float)grid_val(xy.x, wrap), (float)grid_val(xy.y, wrap), (float)grid_val(zw.x, wrap)};
-                    gv = v_add<M>(gv, v_scale<M>(s, cv));
+                    const float s = M::mul(w, cf.rcp);
+                    gv = v_add<M>(gv, v_scale<M>(s, f3{cf.vx, cf.vy, cf.vz}));
                     if (rep) {
-                        const float rc = M::div(fd, A.scale);
+                        const float rc = M::div(cf.fd, A.scale);
                         const float ga = M::sub(C.g[0], (float)a), gb = M::sub(C.g[1], (float)b), gc = M::sub(C.g[2], (float)c);
                         const float dx = fabsf(ga) < 1.0f ? (ga >= 0.0f ? -1.0f : 1.0f) : 0.0f;
                         const float dy = fabsf(gb) < 1.0f ? (gb >= 0.0f ? -1.0f : 1.0f) : 0.0f;
@@ -311,10 +331,20 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel) {
 //   the asset (any n <= RVH_MAX_POINTS).
 // All lanes of the warp must call this (shuffles); `valid` masks the work.
 // ---------------------------------------------------------------------------
+template <int NFIX, int L>
+struct PhaseA {
+    static constexpr int NMAX = NFIX > 0 ? NFIX : RVH_MAX_POINTS;
+    static constexpr int K = (NMAX + L - 1) / L;
+};
+
+// Computes loops 1-2 for the lane's points, stores x', v, corr, and returns
+// the splat inputs: xo/vo for the lane's points, bit k of the result set
+// when point k is splatted (valid strand, 1 <= i < n).
 template <int NFIX, int L, class M>
-__device__ __forceinline__ void strand_phase_a(const DevAsset& A, int strand, bool valid) {
-    constexpr int NMAX = NFIX > 0 ? NFIX : RVH_MAX_POINTS;
-    constexpr int K = (NMAX + L - 1) / L;
+__device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand, bool valid,
+                                                   f3 (&xo)[PhaseA<NFIX, L>::K], f3 (&vo)[PhaseA<NFIX, L>::K]) {
+    constexpr int NMAX = PhaseA<NFIX, L>::NMAX;
+    constexpr int K = PhaseA<NFIX, L>::K;
     const int n = NFIX > 0 ? NFIX : A.n_points;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -413,6 +443,7 @@ __device__ __forceinline__ void strand_phase_a(const DevAsset& A, int strand, bo
     }
 
     // store x', v, corr for points 1..n-1 (the root is never written)
+    unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int i = k * L + l;
@@ -420,29 +451,12 @@ __device__ __forceinline__ void strand_phase_a(const DevAsset& A, int strand, bo
             st_f4(rec + i, xn[k], 1.0f);
             st_f4(rec + n + i, vel[k], 0.0f);
             st_f4(rec + 2 * n + i, cor[k], 0.0f);
+            mask |= 1u << k;
         }
+        xo[k] = xn[k];
+        vo[k] = vel[k];
     }
-    if (A.grid_enabled) {
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            const int i = k * L + l;
-            if (valid && i >= 1 && i < n) splat_point<M>(A, xn[k], vel[k]);
-        }
-    }
-}
-
-// Phase B for one point (loop 3): p = flat point index within the asset.
-template <class M>
-__device__ __forceinline__ void point_phase_b(const DevAsset& A, long long p) {
-    const int n = A.n_points;
-    const long long s = p / n;
-    const int i = (int)(p - s * n);
-    if (i == 0) return;
-    float4* rec = A.strands + (size_t)s * (3 * n);
-    const f3 x = xyz(ld_cg(rec + i));
-    const f3 v = xyz(ld_cg(rec + n + i));
-    const f3 out = gather_point<M>(A, x, v);
-    st_f4(rec + n + i, out, 0.0f);
+    return mask;
 }
 
 }  // namespace rvh

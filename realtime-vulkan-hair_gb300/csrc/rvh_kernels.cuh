@@ -19,13 +19,18 @@ namespace rvh {
 
 constexpr int kThreads = 256;          // CTA size of every step kernel
 constexpr int kWarps = kThreads / 32;
+constexpr int kSmemBytes = 96 * 1024;  // dynamic shared memory per CTA (grid boxes)
+constexpr int kBoxCellsA = kSmemBytes / 16;   // phase A: 4 x int32 partial sums per cell
+constexpr int kBoxCellsB = kSmemBytes / 20;   // phase B: CellF without padding (float4 + rcp)
+constexpr int kTileB = 2048;           // points per phase-B tile
+constexpr int kPtsB = kTileB / kThreads;
 
 enum : int32_t { ITEM_CLEAR = 0, ITEM_A = 1, ITEM_B = 2 };
 
 struct WorkItem {
     int32_t kind;
     int32_t asset;
-    int32_t begin;   // strands (A), points (B) or 16-B grid chunks (CLEAR)
+    int32_t begin;   // strands (A, B) or 16-B grid chunks (CLEAR)
     int32_t end;
 };
 
@@ -38,6 +43,8 @@ struct BatchDev {
     unsigned* done_a;           // per asset: finished phase-A tiles (reset before every launch)
     const unsigned* need_a;     // per asset: phase-A tiles in this launch
     int* error;                 // nonzero: a wait gave up (RVH_ERR_TIMEOUT)
+    unsigned* stats;            // [0] phase-A rounds splatted through the shared box, [1] directly;
+                                // [2] phase-B tiles gathered from the box, [3] directly
 };
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
@@ -46,32 +53,267 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     return v;
 }
 
-// Strands [begin, end) of one asset, S = 32/L strands per warp per round.
+// ---- shared-memory grid boxes ----------------------------------------------------
+// A CTA's points touch a compact block of grid cells.  Phase A accumulates its
+// splat in that box with shared-memory int32 atomics and flushes each touched
+// cell once with int64 global atomics; phase B copies its box once from the
+// grid and gathers from shared memory.  Integer sums are order independent, so
+// both give exactly the bits of the direct global-atomic path.
+struct BoxShared {
+    int lo[3];
+    int hi[3];
+    unsigned vabs;   // max |v| component of the round's points (float bits)
+    int npts;        // points with at least one corner
+};
+
+__device__ __forceinline__ void box_reset(BoxShared& S) {
+    if (threadIdx.x == 0) {
+        for (int a = 0; a < 3; ++a) {
+            S.lo[a] = 0x7fffffff;
+            S.hi[a] = -0x7fffffff - 1;
+        }
+        S.vabs = 0u;
+        S.npts = 0;
+    }
+}
+
+__device__ __forceinline__ void box_reduce(BoxShared& S, const int (&lmin)[3], const int (&lmax)[3], unsigned vabs,
+                                           int np) {
+    const unsigned FULL = 0xffffffffu;
+    int mn[3], mx[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = __reduce_min_sync(FULL, lmin[a]);
+        mx[a] = __reduce_max_sync(FULL, lmax[a]);
+    }
+    const unsigned va = __reduce_max_sync(FULL, vabs);
+    const int n = (int)__reduce_add_sync(FULL, (unsigned)np);
+    if ((threadIdx.x & 31) == 0 && n > 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&S.lo[a], mn[a]);
+            atomicMax(&S.hi[a], mx[a]);
+        }
+        atomicMax(&S.vabs, va);
+        atomicAdd(&S.npts, n);
+    }
+}
+
+__device__ __forceinline__ void bounds_add(const Corners& C, int (&lmin)[3], int (&lmax)[3]) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lmin[a] = min(lmin[a], C.lo[a]);
+        lmax[a] = max(lmax[a], C.lo[a] + C.cnt[a] - 1);
+    }
+}
+
+__device__ __forceinline__ bool has_corners(const Corners& C) { return C.cnt[0] > 0 && C.cnt[1] > 0 && C.cnt[2] > 0; }
+
+// Splat one point into the shared box (int32 partial sums).
+template <class M>
+__device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const int (&lo)[3],
+                                                int bw, int bh) {
+#pragma unroll
+    for (int da = 0; da < 2; ++da) {
+        if (da >= C.cnt[0]) continue;
+        const int a = C.lo[0] + da;
+        const float wx = tri_w<M>(C.g[0], a);
+#pragma unroll
+        for (int db = 0; db < 2; ++db) {
+            if (db >= C.cnt[1]) continue;
+            const int b = C.lo[1] + db;
+            const float wxy = M::mul(wx, tri_w<M>(C.g[1], b));
+#pragma unroll
+            for (int dc = 0; dc < 2; ++dc) {
+                if (dc >= C.cnt[2]) continue;
+                const int c = C.lo[2] + dc;
+                const float w = M::mul(wxy, tri_w<M>(C.g[2], c));
+                int* cell = box + 4 * ((a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2])));
+                const int q0 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.x)));
+                const int q1 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.y)));
+                const int q2 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.z)));
+                const int q3 = __float2int_rz(M::mul(A.scale, w));
+                if (q0) atomicAdd(cell + 0, q0);
+                if (q1) atomicAdd(cell + 1, q1);
+                if (q2) atomicAdd(cell + 2, q2);
+                if (q3) atomicAdd(cell + 3, q3);
+            }
+        }
+    }
+}
+
+// Splat the round's points: one call per CTA round, every thread calls it.
+// Falls back to direct global atomics when the box does not fit, or when the
+// int32 partial sums cannot be proven free of overflow (|partial| <=
+// vmax * (density + npts) since |int(s w v)| <= vmax * (int(s w) + 1)).
+template <int K, class M>
+__device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K], const f3 (&vo)[K], unsigned mask,
+                                            int* box, BoxShared& S, unsigned* stats) {
+    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+    float vab = 0.f;
+    int np = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const Corners C = corners_of<M>(A, xo[k]);
+        if (!has_corners(C)) continue;
+        bounds_add(C, lmin, lmax);
+        vab = fmaxf(vab, fmaxf(fabsf(vo[k].x), fmaxf(fabsf(vo[k].y), fabsf(vo[k].z))));
+        ++np;
+    }
+    box_reset(S);
+    __syncthreads();
+    box_reduce(S, lmin, lmax, __float_as_uint(vab), np);
+    __syncthreads();
+    const int npts = S.npts;
+    if (npts > 0) {
+        const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
+        const long long vol = (long long)bw * bh * bd;
+        bool use = vol <= kBoxCellsA && (float)npts * A.scale < 2.0e9f;
+        if (use) {
+            const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
+            int4* b4 = reinterpret_cast<int4*>(box);
+            for (int c = threadIdx.x; c < (int)vol; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (!((mask >> k) & 1u)) continue;
+                const Corners C = corners_of<M>(A, xo[k]);
+                splat_point_box<M>(A, C, vo[k], box, lo, bw, bh);
+            }
+            __syncthreads();
+            const float vmax = __uint_as_float(S.vabs);
+            bool ok = true;
+            for (int c = threadIdx.x; c < (int)vol; c += kThreads)
+                ok = ok && vmax * ((float)box[4 * c + 3] + (float)npts) < 2.0e9f;
+            use = __syncthreads_and(ok);
+            if (use) {
+                const int nxny = A.nx * A.ny;
+                for (int c = threadIdx.x; c < (int)vol; c += kThreads) {
+                    const int4 v = b4[c];
+                    if (!(v.x | v.y | v.z | v.w)) continue;
+                    const int a = lo[0] + c % bw, b = lo[1] + (c / bw) % bh, cc = lo[2] + c / (bw * bh);
+                    unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + cc * nxny);
+                    red_add_s64(cell + 0, v.x);
+                    red_add_s64(cell + 1, v.y);
+                    red_add_s64(cell + 2, v.z);
+                    red_add_s64(cell + 3, v.w);
+                }
+            }
+        }
+        if (!use) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if ((mask >> k) & 1u) splat_point<M>(A, xo[k], vo[k]);
+        }
+        if (stats && threadIdx.x == 0) atomicAdd(stats + (use ? 0 : 1), 1u);
+    }
+    __syncthreads();  // every read of S and of the box is done before the next round resets them
+}
+
+// Strands [begin, end) of one asset in rounds of kWarps * (32/L) strands; the
+// round count is the same for every warp (the box splat synchronises the CTA).
 template <int NFIX, int L, class M>
-__device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end) {
-    constexpr int S = 32 / L;
+__device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, int* box, BoxShared& S,
+                                       unsigned* stats) {
+    constexpr int SPW = 32 / L;
+    constexpr int K = PhaseA<NFIX, L>::K;
     const int warp = threadIdx.x >> 5;
     const int g = (threadIdx.x & 31) / L;
-    for (int s0 = begin + warp * S; s0 < end; s0 += kWarps * S) {
-        const int strand = s0 + g;
-        strand_phase_a<NFIX, L, M>(A, strand, g < S && strand < end);
+    const int per_round = kWarps * SPW;
+    const int rounds = (end - begin + per_round - 1) / per_round;
+    for (int r = 0; r < rounds; ++r) {
+        const int strand = begin + r * per_round + warp * SPW + g;
+        const bool valid = g < SPW && strand < end;
+        f3 xo[K], vo[K];
+        const unsigned mask = strand_phase_a<NFIX, L, M>(A, strand, valid, xo, vo);
+        if (A.grid_enabled) splat_round<K, M>(A, xo, vo, mask, box, S, stats);
     }
 }
 
 template <int L, class M>
-__device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end) {
+__device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end, int* box, BoxShared& S,
+                                           unsigned* stats) {
     switch (A.n_points) {
-        case 8: tile_a<8, L, M>(A, begin, end); break;
-        case 16: tile_a<16, L, M>(A, begin, end); break;
-        case 24: tile_a<24, L, M>(A, begin, end); break;
-        case 32: tile_a<32, L, M>(A, begin, end); break;
-        default: tile_a<0, L, M>(A, begin, end); break;
+        case 8: tile_a<8, L, M>(A, begin, end, box, S, stats); break;
+        case 16: tile_a<16, L, M>(A, begin, end, box, S, stats); break;
+        case 24: tile_a<24, L, M>(A, begin, end, box, S, stats); break;
+        case 32: tile_a<32, L, M>(A, begin, end, box, S, stats); break;
+        default: tile_a<0, L, M>(A, begin, end, box, S, stats); break;
     }
 }
 
+// Phase B (loop 3) for points [pbeg, pend) of one asset, at most kTileB points.
 template <class M>
-__device__ __forceinline__ void tile_b(const DevAsset& A, long long begin, long long end) {
-    for (long long p = begin + threadIdx.x; p < end; p += kThreads) point_phase_b<M>(A, p);
+__device__ __forceinline__ void tile_b(const DevAsset& A, long long pbeg, long long pend, unsigned char* smem,
+                                       BoxShared& S, unsigned* stats) {
+    const int n = A.n_points;
+    f3 x[kPtsB];
+    unsigned m = 0u;
+    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+    int np = 0;
+#pragma unroll
+    for (int j = 0; j < kPtsB; ++j) {
+        const long long p = pbeg + threadIdx.x + (long long)j * kThreads;
+        x[j] = f3{0.f, 0.f, 0.f};
+        if (p >= pend) continue;
+        const long long s = p / n;
+        const int i = (int)(p - s * n);
+        if (i == 0) continue;
+        x[j] = xyz(ld_cg(A.strands + (size_t)s * (3 * n) + i));
+        m |= 1u << j;
+        const Corners C = corners_of<M>(A, x[j]);
+        if (!has_corners(C)) continue;
+        bounds_add(C, lmin, lmax);
+        ++np;
+    }
+    box_reset(S);
+    __syncthreads();
+    box_reduce(S, lmin, lmax, 0u, np);
+    __syncthreads();
+    const int npts = S.npts;
+    const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
+    const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
+    const bool use = npts > 0 && (long long)bw * bh * bd <= kBoxCellsB;
+    float4* bf = reinterpret_cast<float4*>(smem);
+    float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
+    if (use) {
+        const int vol = bw * bh * bd;
+        const int nxny = A.nx * A.ny;
+        for (int c = threadIdx.x; c < vol; c += kThreads) {
+            const int a = lo[0] + c % bw, b = lo[1] + (c / bw) % bh, cc = lo[2] + c / (bw * bh);
+            const CellF cf = cell_from_global<M>(A, (unsigned)(a + b * A.nx + cc * nxny));
+            bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
+            br[c] = cf.rcp;
+        }
+        __syncthreads();
+    }
+    if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+#pragma unroll
+    for (int j = 0; j < kPtsB; ++j) {
+        if (!((m >> j) & 1u)) continue;
+        const long long p = pbeg + threadIdx.x + (long long)j * kThreads;
+        const long long s = p / n;
+        const int i = (int)(p - s * n);
+        float4* rec = A.strands + (size_t)s * (3 * n);
+        const f3 v = xyz(ld_cg(rec + n + i));
+        const Corners C = corners_of<M>(A, x[j]);
+        f3 out;
+        if (use) {
+            out = gather_point<M>(A, x[j], v, C, [&](int a, int b, int c) {
+                const int li = (a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2]));
+                const float4 q = bf[li];
+                return CellF{q.x, q.y, q.z, q.w, br[li]};
+            });
+        } else {
+            const int nxny = A.nx * A.ny;
+            out = gather_point<M>(A, x[j], v, C, [&](int a, int b, int c) {
+                return cell_from_global<M>(A, (unsigned)(a + b * A.nx + c * nxny));
+            });
+        }
+        st_f4(rec + n + i, out, 0.0f);
+    }
+    __syncthreads();  // every read of S and of the box is done before the next tile resets them
 }
 
 __device__ __forceinline__ void write_draw(const DevAsset& A) {
@@ -87,19 +329,22 @@ __device__ __forceinline__ void write_draw(const DevAsset& A) {
 
 template <int NFIX, int L, class M>
 __global__ void __launch_bounds__(kThreads) k_plain_a(const __grid_constant__ DevAsset A) {
-    constexpr int S = 32 / L;
-    const int begin = blockIdx.x * kWarps * S;
-    const int end = min(begin + kWarps * S, A.n_strands);
-    tile_a<NFIX, L, M>(A, begin, end);
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ BoxShared S;
+    constexpr int SPW = 32 / L;
+    const int begin = blockIdx.x * kWarps * SPW;
+    const int end = min(begin + kWarps * SPW, A.n_strands);
+    tile_a<NFIX, L, M>(A, begin, end, reinterpret_cast<int*>(dsm), S, nullptr);
     if (!A.grid_enabled && blockIdx.x == 0 && threadIdx.x == 0) write_draw(A);
 }
 
 template <class M>
 __global__ void __launch_bounds__(kThreads) k_plain_b(const __grid_constant__ DevAsset A) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ BoxShared S;
     const long long total = (long long)A.n_strands * A.n_points;
-    for (long long p = (long long)blockIdx.x * kThreads + threadIdx.x; p < total;
-         p += (long long)gridDim.x * kThreads)
-        point_phase_b<M>(A, p);
+    for (long long t = (long long)blockIdx.x * kTileB; t < total; t += (long long)gridDim.x * kTileB)
+        tile_b<M>(A, t, min(total, t + kTileB), dsm, S, nullptr);
     if (blockIdx.x == 0 && threadIdx.x == 0) write_draw(A);
 }
 
@@ -107,6 +352,8 @@ __global__ void __launch_bounds__(kThreads) k_plain_b(const __grid_constant__ De
 
 template <int L, class M>
 __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ BatchDev B) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ BoxShared S;
     __shared__ int s_item;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(B.head, 1u);
@@ -116,7 +363,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ Batc
         const WorkItem w = B.items[it];
         const DevAsset& A = B.assets[w.asset];
         if (w.kind == ITEM_A) {
-            tile_a_any<L, M>(A, w.begin, w.end);
+            tile_a_any<L, M>(A, w.begin, w.end, reinterpret_cast<int*>(dsm), S, B.stats);
             if (!A.grid_enabled && w.begin == 0 && threadIdx.x == 0) write_draw(A);
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -136,7 +383,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ Batc
                 }
             }
             __syncthreads();
-            tile_b<M>(A, (long long)w.begin * A.n_points, (long long)w.end * A.n_points);
+            tile_b<M>(A, (long long)w.begin * A.n_points, (long long)w.end * A.n_points, dsm, S, B.stats);
             if (w.begin == 0 && threadIdx.x == 0) write_draw(A);
         } else {
             uint4* g = reinterpret_cast<uint4*>(A.grid_next);

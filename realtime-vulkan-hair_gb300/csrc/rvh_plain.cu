@@ -1,4 +1,7 @@
 // rvh_plain.cu — instantiations of the per-asset phase-A / phase-B kernels.
+#include <mutex>
+#include <set>
+
 #include "rvh_kernels.cuh"
 #include "rvh_registry.h"
 
@@ -32,6 +35,18 @@ const void* pick_n(int n, int lanes) {
     }
 }
 }  // namespace
+
+bool prepare_kernel(const void* fn) {
+    static std::mutex mu;
+    static std::set<const void*> done;
+    std::lock_guard<std::mutex> g(mu);
+    if (!fn) return false;
+    if (done.count(fn)) return true;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) != cudaSuccess)
+        return false;
+    done.insert(fn);
+    return true;
+}
 
 const void* plain_a_kernel(int n, int lanes, bool exact) {
     return exact ? pick_n<ExactMath>(n, lanes) : pick_n<FastMath>(n, lanes);

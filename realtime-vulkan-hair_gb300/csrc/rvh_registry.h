@@ -12,5 +12,7 @@ const void* plain_b_kernel(bool exact);
 // Persistent batch kernel; lanes in {4, 8, 16, 32}.
 const void* batch_kernel(int lanes, bool exact);
 bool batch_supported(int lanes);
+// Opts a kernel into kSmemBytes of dynamic shared memory (once per kernel).
+bool prepare_kernel(const void* fn);
 
 }  // namespace rvh

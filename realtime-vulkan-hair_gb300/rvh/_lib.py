@@ -51,6 +51,7 @@ PROTOTYPES = [
     ("rvh_batch_step", _st, [_vp, _P(T.Frame), _vp]),
     ("rvh_batch_check", _st, [_vp]),
     ("rvh_batch_info", _st, [_vp, _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_int64)]),
+    ("rvh_batch_box_stats", _st, [_vp, _P(C.c_uint32)]),
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_batch_timing_enable", _st, [_vp, C.c_int32]),
     ("rvh_batch_timing_read", _st, [_vp, _P(C.c_double), _P(C.c_int32)]),

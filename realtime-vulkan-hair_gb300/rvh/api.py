@@ -204,6 +204,11 @@ class Batch:
     def check(self):
         check(self.lib.rvh_batch_check(self.h))
 
+    def box_stats(self):
+        out = (C.c_uint32 * 4)()
+        check(self.lib.rvh_batch_box_stats(self.h, out))
+        return {"a_box": out[0], "a_direct": out[1], "b_box": out[2], "b_direct": out[3]}
+
     def h2d_bytes_per_step(self):
         b = C.c_uint64()
         check(self.lib.rvh_batch_h2d_bytes(self.h, C.byref(b)))
