@@ -177,6 +177,37 @@ def time_cpu(specs, steps, threads):
     return pts * steps / dt, dt
 
 
+def run_served(ctx, args, rank):
+    """1,000 resident characters sized as the batched workload; Poisson arrivals
+    at 20k req/s, 1-8 steps each; continuous batching at 1, 4 and 16 requests
+    per launch.  Returns {concurrency: stats}."""
+    from rvh import api, configs
+    n_chars = args.characters
+    specs = configs.batched(n_assets=n_chars, seed=3)
+    assets, out = [], {}
+    for s in specs:
+        a = api.Asset(ctx, s.records, s.n_points, rest=s.rest)
+        a.set_params(s.params)
+        a.set_colliders(s.colliders)
+        assets.append(a)
+    pts = sum(s.n_total_points for s in specs)
+    rng = np.random.default_rng(77)
+    for conc in (1, 4, 16):
+        srv = api.Server(ctx, max_active=conc, pipeline_depth=2, scratch_budget_bytes=24 << 30)
+        ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
+        t = np.cumsum(rng.exponential(1.0 / 20000.0, size=args.requests))
+        reqs = [(ids[int(rng.integers(0, n_chars))], int(rng.integers(1, 9)), float(ti)) for ti in t]
+        st, res, stats = srv.run(reqs)
+        d = stats.as_dict()
+        d["status"] = st
+        d["offered_point_steps_per_s"] = 20000.0 * 4.5 * pts / n_chars
+        out[str(conc)] = d
+        srv.close()
+    for a in assets:
+        a.close()
+    return out, pts
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle's OpenMP restatement on the host cores."""
     if rank != 0:
@@ -217,6 +248,9 @@ def main():
     ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--characters", type=int, default=1000)
+    ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world = dist_init()
@@ -323,6 +357,14 @@ def main():
                "sample": "first %d assets (%d points) of the workload, 3 steps, FP32 OpenMP restatement "
                          "of the reference shader" % (len(sample), spts)}
 
+    served, served_pts = None, None
+    if not args.no_served and world == 1:
+        batch.close()
+        for a in assets:
+            a.close()
+        assets, batch = [], None
+        served, served_pts = run_served(ctx, args, rank)
+
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (step_ms * 1e-3) / 1e9
     if rank == 0:
@@ -347,9 +389,15 @@ def main():
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+            "served": None if served is None else {
+                "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
+                            "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (
+                                args.characters, served_pts, args.requests),
+                "by_concurrency": served},
         }
         print(json.dumps(line), flush=True)
-    batch.close()
+    if batch is not None:
+        batch.close()
     for a in assets:
         a.close()
     ctx.close()

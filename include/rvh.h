@@ -17,6 +17,7 @@
 #ifndef RVH_H
 #define RVH_H
 
+#include "rvh_scene.h"
 #include "rvh_types.h"
 
 #ifdef __cplusplus
@@ -141,6 +142,54 @@ rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]);
 rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
 rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);
 rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launches);
+
+/* ---- serving: continuous batching of step requests for resident characters ----
+ * The server replays the reference's per-frame loop (src/main.cpp:257-285)
+ * for many characters at once: each launch advances every admitted request
+ * by one step; requests are admitted in arrival order as slots free up and
+ * their grid scratch fits the server's HBM budget; their work shares launches
+ * on the device. */
+typedef struct rvh_server_desc {
+    int32_t max_active;           /* requests co-scheduled per launch (default 16) */
+    int32_t lanes_per_strand;     /* batch kernel shape: 4, 8, 16, 32 (default 4) */
+    int32_t pipeline_depth;       /* launches in flight (default 2) */
+    int32_t reserved;
+    uint64_t scratch_budget_bytes;/* HBM for the grids of admitted requests; charged to the context */
+} rvh_server_desc;
+typedef struct rvh_request {
+    int32_t character;            /* id from rvh_server_add_character */
+    int32_t n_steps;
+    double arrival_s;             /* seconds after rvh_server_run starts */
+} rvh_request;
+typedef struct rvh_request_result {
+    double admit_s;
+    double done_s;
+    float max_step_ms;            /* device time of the slowest launch that carried one of its steps */
+    int32_t steps_done;
+    int32_t status;
+    int32_t reserved;
+} rvh_request_result;
+typedef struct rvh_server_stats {
+    int64_t requests, steps, point_steps;
+    int32_t launches, max_active;
+    double wall_s, point_steps_per_s;
+    double step_ms_p50, step_ms_p99, step_ms_p999;   /* device time of the launch carrying each step */
+    double request_ms_p50, request_ms_p99;           /* arrival -> last step observed complete */
+    double queue_ms_p50, queue_ms_p99;               /* arrival -> admission */
+    double mean_batch;                               /* requests per launch */
+    int64_t admission_waits;                         /* admissions deferred for lack of scratch memory */
+    uint64_t scratch_used_bytes;                     /* at the end of the run (0 when every request finished) */
+} rvh_server_stats;
+rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_server** out);
+rvh_status rvh_server_destroy(rvh_server* s);
+/* Registers a resident character; its grids become per-request scratch from
+ * the server's pool.  Frames: dt fixed, t = (steps+1)*dt, wind from `wind`
+ * (NULL = none) evaluated at the character's own step count. */
+rvh_status rvh_server_add_character(rvh_server* s, rvh_asset* a, const rvh_wind_desc* wind, float dt, int32_t* id);
+rvh_status rvh_server_character_steps(rvh_server* s, int32_t id, int64_t* steps);
+/* Runs a request trace to completion (requests arrive at their arrival_s on the wall clock). */
+rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh_request_result* results,
+                          rvh_server_stats* stats);
 
 /* ---- differentiation --------------------------------------------------------
  * Reverse-mode derivative of n_steps steps from the asset's current state,

@@ -128,6 +128,163 @@ rvh_status enqueue_launch(Batch* b, cudaStream_t s) {
 }
 
 }  // namespace
+
+// ---- dynamic batches (used by the request server) ---------------------------------
+// The asset set changes from launch to launch: the plan and the per-asset
+// tables are rebuilt and uploaded before each launch (no graph).
+struct DynBatch {
+    Batch b;
+    size_t cap_assets = 0, cap_items = 0;
+    WorkItem* h_items[2] = {nullptr, nullptr};
+    unsigned* h_need[2] = {nullptr, nullptr};
+};
+
+static rvh_status dyn_reserve(DynBatch* d, size_t na, size_t ni) {
+    Batch& b = d->b;
+    if (na <= d->cap_assets && ni <= d->cap_items) return RVH_OK;
+    RVH_CUDA(cudaStreamSynchronize(b.ctx->stream));
+    for (int i = 0; i < 2; ++i) {
+        if (b.staged[i]) RVH_CUDA(cudaEventSynchronize(b.staged[i]));
+    }
+    const size_t ca = std::max(na, d->cap_assets * 2 + 1), ci = std::max(ni, d->cap_items * 2 + 1);
+    b.ctx->free(b.d_assets);
+    b.ctx->free(b.d_items);
+    b.ctx->free(b.d_need);
+    b.ctx->free(b.d_done);
+    rvh_status s;
+    if ((s = b.ctx->alloc(b.d_assets, sizeof(DevAsset) * ca)) != RVH_OK) return s;
+    if ((s = b.ctx->alloc(b.d_items, sizeof(WorkItem) * ci)) != RVH_OK) return s;
+    if ((s = b.ctx->alloc(b.d_need, sizeof(unsigned) * ca)) != RVH_OK) return s;
+    if ((s = b.ctx->alloc(b.d_done, sizeof(unsigned) * ca)) != RVH_OK) return s;
+    for (int i = 0; i < 2; ++i) {
+        if (b.h_stage[i]) cudaFreeHost(b.h_stage[i]);
+        if (d->h_items[i]) cudaFreeHost(d->h_items[i]);
+        if (d->h_need[i]) cudaFreeHost(d->h_need[i]);
+        b.h_stage[i] = nullptr;
+        d->h_items[i] = nullptr;
+        d->h_need[i] = nullptr;
+        RVH_CUDA(cudaMallocHost(&b.h_stage[i], sizeof(DevAsset) * ca));
+        RVH_CUDA(cudaMallocHost(&d->h_items[i], sizeof(WorkItem) * ci));
+        RVH_CUDA(cudaMallocHost(&d->h_need[i], sizeof(unsigned) * ca));
+    }
+    d->cap_assets = ca;
+    d->cap_items = ci;
+    b.dev.assets = static_cast<const DevAsset*>(b.d_assets.ptr);
+    b.dev.items = static_cast<const WorkItem*>(b.d_items.ptr);
+    b.dev.done_a = static_cast<unsigned*>(b.d_done.ptr);
+    b.dev.need_a = static_cast<const unsigned*>(b.d_need.ptr);
+    return RVH_OK;
+}
+
+DynBatch* dyn_batch_new(Context* ctx, int lanes, rvh_status* st) {
+    *st = RVH_OK;
+    if (!batch_supported(lanes)) {
+        *st = fail(RVH_ERR_UNSUPPORTED, "lanes_per_strand must be 4, 8, 16 or 32");
+        return nullptr;
+    }
+    DynBatch* d = new (std::nothrow) DynBatch();
+    if (!d) {
+        *st = fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");
+        return nullptr;
+    }
+    Batch& b = d->b;
+    b.ctx = ctx;
+    b.lanes = lanes;
+    b.exact = ctx->math == RVH_MATH_EXACT;
+    b.use_graph = false;
+    b.kernel = batch_kernel(lanes, b.exact);
+    int per_sm = 0;
+    if (!prepare_kernel(b.kernel) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b.kernel, kThreads, kSmemBytes) != cudaSuccess) {
+        *st = fail(RVH_ERR_CUDA, "cannot prepare the batch kernel");
+        delete d;
+        return nullptr;
+    }
+    b.n_ctas = std::max(1, per_sm) * ctx->sm_count;
+    rvh_status s;
+    if ((s = ctx->alloc(b.d_head, sizeof(unsigned))) != RVH_OK || (s = ctx->alloc(b.d_error, sizeof(int))) != RVH_OK ||
+        (s = ctx->alloc(b.d_stats, 4 * sizeof(unsigned))) != RVH_OK) {
+        *st = s;
+        dyn_batch_free(d);
+        return nullptr;
+    }
+    cudaMemset(b.d_error.ptr, 0, sizeof(int));
+    cudaMemset(b.d_stats.ptr, 0, 4 * sizeof(unsigned));
+    for (int i = 0; i < 2; ++i) cudaEventCreateWithFlags(&b.staged[i], cudaEventDisableTiming);
+    b.dev.spin_limit = kSpinLimit;
+    b.dev.head = static_cast<unsigned*>(b.d_head.ptr);
+    b.dev.error = static_cast<int*>(b.d_error.ptr);
+    b.dev.stats = static_cast<unsigned*>(b.d_stats.ptr);
+    return d;
+}
+
+void dyn_batch_free(DynBatch* d) {
+    if (!d) return;
+    for (int i = 0; i < 2; ++i) {
+        if (d->h_items[i]) cudaFreeHost(d->h_items[i]);
+        if (d->h_need[i]) cudaFreeHost(d->h_need[i]);
+        d->h_items[i] = nullptr;
+        d->h_need[i] = nullptr;
+    }
+    Batch* b = new Batch();
+    *b = d->b;      // hand the buffers to the common destructor
+    d->b = Batch();
+    destroy(b);
+    delete d;
+}
+
+rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<rvh_frame>& frames,
+                            cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop, int64_t* points) {
+    Batch& b = d->b;
+    b.assets = assets;
+    plan(b, 0);
+    b.dev.n_items = int32_t(b.items.size());
+    int64_t pts = 0;
+    for (Asset* a : assets) pts += int64_t(a->n_strands) * a->n_points;
+    if (points) *points = pts;
+    if (b.items.empty()) return RVH_OK;
+    rvh_status st = dyn_reserve(d, assets.size(), b.items.size());
+    if (st != RVH_OK) return st;
+    const int slot = b.slot;
+    b.slot ^= 1;
+    RVH_CUDA(cudaEventSynchronize(b.staged[slot]));
+    for (size_t i = 0; i < assets.size(); ++i) {
+        Asset* a = assets[i];
+        if (a->params.grid_enabled && a->grid_dirty[a->parity])
+            RVH_CUDA(cudaMemsetAsync(a->grid[a->parity].ptr, 0, a->grid_bytes(), s));
+        b.h_stage[slot][i] = a->device_view(frames[i], a->parity);
+        d->h_need[slot][i] = b.need_a[i];
+    }
+    std::memcpy(d->h_items[slot], b.items.data(), sizeof(WorkItem) * b.items.size());
+    RVH_CUDA(cudaMemcpyAsync(b.d_assets.ptr, b.h_stage[slot], sizeof(DevAsset) * assets.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaMemcpyAsync(b.d_items.ptr, d->h_items[slot], sizeof(WorkItem) * b.items.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaMemcpyAsync(b.d_need.ptr, d->h_need[slot], sizeof(unsigned) * assets.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaEventRecord(b.staged[slot], s));
+    if (ev_start) RVH_CUDA(cudaEventRecord(ev_start, s));
+    rvh_status ls = enqueue_launch(&b, s);
+    if (ls != RVH_OK) return ls;
+    if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
+    for (Asset* a : assets) {
+        if (!a->params.grid_enabled) continue;
+        a->grid_dirty[a->parity] = true;
+        a->grid_dirty[a->parity ^ 1] = false;
+        a->parity ^= 1;
+    }
+    return RVH_OK;
+}
+
+rvh_status dyn_batch_check(DynBatch* d) {
+    int err = 0;
+    RVH_CUDA(cudaMemcpy(&err, d->b.d_error.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        cudaMemset(d->b.d_error.ptr, 0, sizeof(int));
+        return fail(err, "server batch: a phase-B tile gave up waiting for its asset's phase A");
+    }
+    return RVH_OK;
+}
+
+int dyn_batch_ctas(const DynBatch* d) { return d->b.n_ctas; }
+
 }  // namespace rvh
 
 struct rvh_batch : rvh::Batch {};

@@ -134,7 +134,7 @@ DevAsset Asset::device_view(const rvh_frame& f, int which) const {
 }
 
 rvh_status ensure_grid(Asset* a) {
-    if (!a->params.grid_enabled) return RVH_OK;
+    if (!a->params.grid_enabled || a->server_managed) return RVH_OK;
     const size_t cells = size_t(a->params.grid_dims[0]) * a->params.grid_dims[1] * a->params.grid_dims[2];
     if (cells == a->grid_cells && a->grid[0].ptr) return RVH_OK;
     a->ctx->free(a->grid[0]);
@@ -155,6 +155,8 @@ rvh_status ensure_grid(Asset* a) {
 }
 
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s) {
+    if (a->params.grid_enabled && !a->grid[a->parity].ptr)
+        return fail(RVH_ERR_STATE, "step: the asset's grid is held by a request server and no request is active");
     const bool exact = a->ctx->math == RVH_MATH_EXACT;
     const void* ka = plain_a_kernel(a->n_points, a->lanes, exact);
     if (!ka) return fail(RVH_ERR_UNSUPPORTED, "no phase-A kernel for this (n_points, lanes_per_strand)");

@@ -142,7 +142,10 @@ __device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
         const DevCollider& c = A.col[j];
         if (c.kind == RVH_COLLIDER_SPHERE) {
             const f3 e = v_sub<M>(x, f3{c.c[0], c.c[1], c.c[2]});
-            const float dist = v_len<M>(e);
+            const float d2 = v_dot<M>(e, e);
+            // clearly outside: sqrt(d2) >= r whenever d2 > r^2 (1 + 1e-5); skips the sqrt
+            if (d2 > c.radius * c.radius * 1.00001f) continue;
+            const float dist = M::sqrt(d2);
             if (dist < c.radius) {
                 const float d = M::sub(c.radius, dist);
                 const f3 nrm = v_normalize<M>(e);
@@ -151,7 +154,9 @@ __device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
             }
         } else {
             const f3 q = mat_p1<M>(c.inv, x);
-            const float lq = v_len<M>(q);
+            const float q2 = v_dot<M>(q, q);
+            if (q2 > 1.00001f) continue;   // clearly outside (sqrt(q2) > 1)
+            const float lq = M::sqrt(q2);
             if (lq <= 1.0f) {
                 const f3 surf = mat_p1<M>(c.xf, v_normalize<M>(q));
                 const float d = v_len<M>(v_sub<M>(surf, x));

@@ -86,6 +86,7 @@ struct Asset {
     rvh_sim_params params{};
     std::vector<rvh_collider> colliders;
     bool has_wind = false;
+    bool server_managed = false;  // grids are lent by a request server while a request is active
 
     size_t record_bytes() const { return size_t(n_strands) * 48u * size_t(n_points); }
     size_t grid_bytes() const { return grid_cells * 32u; }
@@ -99,6 +100,15 @@ DevCollider pack_collider(const rvh_collider& c);
 int default_lanes(int n_points);
 rvh_status ensure_grid(Asset* a);
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s);
+
+// Batches whose asset set changes per launch (rvh_batch_host.cpp).
+struct DynBatch;
+DynBatch* dyn_batch_new(Context* ctx, int lanes, rvh_status* st);
+void dyn_batch_free(DynBatch* d);
+rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<rvh_frame>& frames,
+                            cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop, int64_t* points);
+rvh_status dyn_batch_check(DynBatch* d);
+int dyn_batch_ctas(const DynBatch* d);
 
 }  // namespace rvh
 

@@ -243,24 +243,30 @@ __device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end
     }
 }
 
-// Phase B (loop 3) for points [pbeg, pend) of one asset, at most kTileB points.
+// Phase B (loop 3) for strands [s0, s1) of one asset, at most kTileB points.
+// Thread t takes tile-local points t, t + kThreads, ...; 32-bit index math.
 template <class M>
-__device__ __forceinline__ void tile_b(const DevAsset& A, long long pbeg, long long pend, unsigned char* smem,
-                                       BoxShared& S, unsigned* stats) {
+__device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsigned char* smem, BoxShared& S,
+                                       unsigned* stats) {
     const int n = A.n_points;
+    const int npt = (s1 - s0) * n;
+    float4* const base = A.strands + (size_t)s0 * (3 * n);
     f3 x[kPtsB];
+    int off[kPtsB];   // record offset (float4 units) of the point's curvePoints slot
     unsigned m = 0u;
     int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
     int np = 0;
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
-        const long long p = pbeg + threadIdx.x + (long long)j * kThreads;
+        const int q = threadIdx.x + j * kThreads;
         x[j] = f3{0.f, 0.f, 0.f};
-        if (p >= pend) continue;
-        const long long s = p / n;
-        const int i = (int)(p - s * n);
+        off[j] = 0;
+        if (q >= npt) continue;
+        const int ls = q / n;
+        const int i = q - ls * n;
         if (i == 0) continue;
-        x[j] = xyz(ld_cg(A.strands + (size_t)s * (3 * n) + i));
+        off[j] = ls * (3 * n) + i;
+        x[j] = xyz(ld_cg(base + off[j]));
         m |= 1u << j;
         const Corners C = corners_of<M>(A, x[j]);
         if (!has_corners(C)) continue;
@@ -292,11 +298,8 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, long long pbeg, long l
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
         if (!((m >> j) & 1u)) continue;
-        const long long p = pbeg + threadIdx.x + (long long)j * kThreads;
-        const long long s = p / n;
-        const int i = (int)(p - s * n);
-        float4* rec = A.strands + (size_t)s * (3 * n);
-        const f3 v = xyz(ld_cg(rec + n + i));
+        float4* vp = base + off[j] + n;
+        const f3 v = xyz(ld_cg(vp));
         const Corners C = corners_of<M>(A, x[j]);
         f3 out;
         if (use) {
@@ -311,7 +314,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, long long pbeg, long l
                 return cell_from_global<M>(A, (unsigned)(a + b * A.nx + c * nxny));
             });
         }
-        st_f4(rec + n + i, out, 0.0f);
+        st_f4(vp, out, 0.0f);
     }
     __syncthreads();  // every read of S and of the box is done before the next tile resets them
 }
@@ -342,9 +345,9 @@ template <class M>
 __global__ void __launch_bounds__(kThreads) k_plain_b(const __grid_constant__ DevAsset A) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
-    const long long total = (long long)A.n_strands * A.n_points;
-    for (long long t = (long long)blockIdx.x * kTileB; t < total; t += (long long)gridDim.x * kTileB)
-        tile_b<M>(A, t, min(total, t + kTileB), dsm, S, nullptr);
+    const int per_tile = max(1, kTileB / A.n_points);
+    for (int s0 = blockIdx.x * per_tile; s0 < A.n_strands; s0 += gridDim.x * per_tile)
+        tile_b<M>(A, s0, min(A.n_strands, s0 + per_tile), dsm, S, nullptr);
     if (blockIdx.x == 0 && threadIdx.x == 0) write_draw(A);
 }
 
@@ -355,13 +358,25 @@ __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ Batc
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
     __shared__ int s_item;
+    __shared__ int s_asset;
+    // The current item's asset, copied once into shared memory: reads of its
+    // fields then cannot alias the global stores of the step.
+    __shared__ __align__(16) DevAsset A;
+    if (threadIdx.x == 0) s_asset = -1;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int)atomicAdd(B.head, 1u);
         __syncthreads();
         const int it = s_item;
         if (it >= B.n_items) break;
         const WorkItem w = B.items[it];
-        const DevAsset& A = B.assets[w.asset];
+        if (w.asset != s_asset) {
+            constexpr int words = (int)(sizeof(DevAsset) / 4);
+            const int* src = reinterpret_cast<const int*>(B.assets + w.asset);
+            int* dst = reinterpret_cast<int*>(&A);
+            for (int q = threadIdx.x; q < words; q += kThreads) dst[q] = src[q];
+            __syncthreads();
+            if (threadIdx.x == 0) s_asset = w.asset;
+        }
         if (w.kind == ITEM_A) {
             tile_a_any<L, M>(A, w.begin, w.end, reinterpret_cast<int*>(dsm), S, B.stats);
             if (!A.grid_enabled && w.begin == 0 && threadIdx.x == 0) write_draw(A);
@@ -383,7 +398,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ Batc
                 }
             }
             __syncthreads();
-            tile_b<M>(A, (long long)w.begin * A.n_points, (long long)w.end * A.n_points, dsm, S, B.stats);
+            tile_b<M>(A, w.begin, w.end, dsm, S, B.stats);
             if (w.begin == 0 && threadIdx.x == 0) write_draw(A);
         } else {
             uint4* g = reinterpret_cast<uint4*>(A.grid_next);

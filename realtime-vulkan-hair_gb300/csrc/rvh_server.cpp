@@ -1,0 +1,414 @@
+// rvh_server.cpp — a request loop with continuous batching for resident
+// characters (the serving counterpart of the reference's per-frame
+// UpdateTime -> Frame -> translateSphere loop, src/main.cpp:257-285).
+//
+// Every character's Strand records stay in HBM.  A request asks for k steps of
+// one character.  Each launch advances every ADMITTED request by one step in
+// one persistent batch launch; a request holds its slot (and its grid scratch)
+// from admission until its last step completes.  Requests are admitted in
+// arrival order as soon as (a) a slot is free, (b) its character has no other
+// request in flight, and (c) the grid scratch fits the server's HBM budget.
+// Up to `pipeline_depth` launches are in flight, so new arrivals join the next
+// launch while earlier ones still run on the device.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <deque>
+#include <map>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "../../include/rvh_scene.h"
+#include "rvh_internal.hpp"
+
+namespace rvh {
+
+namespace {
+
+// First-fit allocator over one device slab (offsets in bytes, 256-B aligned).
+class SlabPool {
+public:
+    void init(size_t bytes) {
+        free_.clear();
+        if (bytes) free_[0] = bytes;
+        size_ = bytes;
+    }
+    bool take(size_t bytes, size_t* off) {
+        bytes = (bytes + 255) & ~size_t(255);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                *off = it->first;
+                const size_t rest = it->second - bytes;
+                const size_t noff = it->first + bytes;
+                free_.erase(it);
+                if (rest) free_[noff] = rest;
+                used_ += bytes;
+                return true;
+            }
+        }
+        return false;
+    }
+    void give(size_t off, size_t bytes) {
+        bytes = (bytes + 255) & ~size_t(255);
+        used_ -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t used() const { return used_; }
+
+private:
+    std::map<size_t, size_t> free_;
+    size_t size_ = 0, used_ = 0;
+};
+
+struct Character {
+    Asset* asset = nullptr;
+    rvh_wind_desc wind{};
+    bool has_wind = false;
+    float dt = 1.0f / 60.0f;
+    int64_t steps = 0;      // steps completed or enqueued so far
+    bool busy = false;
+};
+
+struct Active {
+    int req;
+    int remaining;          // steps still to enqueue
+    int in_flight = 0;      // launches containing this request not yet completed
+    size_t off = 0, bytes = 0;
+};
+
+struct Launch {
+    cudaEvent_t start, stop;
+    std::vector<int> reqs;  // requests with a step in this launch
+    std::vector<int> last;  // requests whose final step is in this launch
+    int64_t points = 0;
+};
+
+double pct(std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    const double idx = p * double(v.size() - 1);
+    const size_t lo = size_t(std::floor(idx)), hi = std::min(v.size() - 1, lo + 1);
+    return v[lo] + (v[hi] - v[lo]) * (idx - double(lo));
+}
+
+}  // namespace
+
+struct Server {
+    Context* ctx = nullptr;
+    rvh_server_desc desc{};
+    std::vector<Character> chars;
+    DynBatch* batch = nullptr;
+    DevBuf slab;
+    SlabPool pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> events;
+};
+
+}  // namespace rvh
+
+struct rvh_server : rvh::Server {};
+
+using namespace rvh;
+
+extern "C" {
+
+rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_server** out) {
+    if (!ctx || !out) return fail(RVH_ERR_INVALID_ARG, "server_create: NULL argument");
+    *out = nullptr;
+    rvh_server_desc d{};
+    d.max_active = 16;
+    d.lanes_per_strand = 4;
+    d.pipeline_depth = 2;
+    if (desc) d = *desc;
+    if (d.max_active < 1 || d.max_active > 4096) return fail(RVH_ERR_INVALID_ARG, "server: max_active in [1, 4096]");
+    if (d.pipeline_depth < 1 || d.pipeline_depth > 8) return fail(RVH_ERR_INVALID_ARG, "server: pipeline_depth in [1, 8]");
+    if (!d.lanes_per_strand) d.lanes_per_strand = 4;
+    cudaSetDevice(ctx->device);
+    rvh_server* s = new (std::nothrow) rvh_server();
+    if (!s) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");
+    s->ctx = ctx;
+    s->desc = d;
+    rvh_status st;
+    s->batch = dyn_batch_new(ctx, d.lanes_per_strand, &st);
+    if (!s->batch) {
+        delete s;
+        return st;
+    }
+    if (d.scratch_budget_bytes) {
+        if ((st = ctx->alloc(s->slab, d.scratch_budget_bytes)) != RVH_OK) {
+            dyn_batch_free(s->batch);
+            delete s;
+            return st;
+        }
+        s->pool.init(s->slab.bytes);
+    }
+    *out = s;
+    return RVH_OK;
+}
+
+rvh_status rvh_server_destroy(rvh_server* s) {
+    if (!s) return RVH_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    for (auto& e : s->events) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
+    for (Character& c : s->chars) {
+        Asset* a = c.asset;
+        a->grid[0] = a->grid[1] = DevBuf{};
+        a->server_managed = false;
+        ensure_grid(a);  // hand the asset back with grids of its own
+    }
+    dyn_batch_free(s->batch);
+    s->ctx->free(s->slab);
+    delete s;
+    return RVH_OK;
+}
+
+rvh_status rvh_server_add_character(rvh_server* s, rvh_asset* a, const rvh_wind_desc* wind, float dt, int32_t* id) {
+    if (!s || !a || !id) return fail(RVH_ERR_INVALID_ARG, "server_add_character: NULL argument");
+    if (a->ctx != s->ctx) return fail(RVH_ERR_INVALID_ARG, "server_add_character: asset of another context");
+    if (!std::isfinite(dt) || !(dt > 0.f)) return fail(RVH_ERR_INVALID_ARG, "server_add_character: dt must be > 0");
+    for (const Character& c : s->chars)
+        if (c.asset == a) return fail(RVH_ERR_INVALID_ARG, "server_add_character: asset already registered");
+    if (a->params.grid_enabled && !s->slab.ptr)
+        return fail(RVH_ERR_BUDGET, "server_add_character: the server has no scratch budget for grids");
+    cudaSetDevice(s->ctx->device);
+    RVH_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    // the grids become per-request scratch lent from the server's pool
+    s->ctx->free(a->grid[0]);
+    s->ctx->free(a->grid[1]);
+    a->server_managed = true;
+    Character c;
+    c.asset = a;
+    c.dt = dt;
+    if (wind) {
+        c.wind = *wind;
+        c.has_wind = true;
+    }
+    s->chars.push_back(c);
+    *id = int32_t(s->chars.size() - 1);
+    return RVH_OK;
+}
+
+rvh_status rvh_server_character_steps(rvh_server* s, int32_t id, int64_t* steps) {
+    if (!s || !steps || id < 0 || id >= int32_t(s->chars.size()))
+        return fail(RVH_ERR_INVALID_ARG, "server_character_steps: bad argument");
+    *steps = s->chars[id].steps;
+    return RVH_OK;
+}
+
+rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh_request_result* results,
+                          rvh_server_stats* stats) {
+    if (!s || (n > 0 && (!reqs || !results))) return fail(RVH_ERR_INVALID_ARG, "server_run: NULL argument");
+    cudaSetDevice(s->ctx->device);
+    using clk = std::chrono::steady_clock;
+    const cudaStream_t stream = s->ctx->stream;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return reqs[x].arrival_s < reqs[y].arrival_s; });
+    for (int i = 0; i < n; ++i) {
+        results[i] = rvh_request_result{};
+        results[i].status = RVH_OK;
+        if (reqs[i].character < 0 || reqs[i].character >= int32_t(s->chars.size()) || reqs[i].n_steps < 1) {
+            results[i].status = RVH_ERR_INVALID_ARG;
+        }
+    }
+    size_t next = 0;                      // next request (in arrival order) not yet queued
+    std::deque<int> waiting;              // arrived, not admitted
+    std::vector<Active> active;
+    std::deque<Launch> flight;
+    std::vector<cudaEvent_t> free_ev;
+    auto get_ev = [&]() {
+        if (!free_ev.empty()) {
+            cudaEvent_t e = free_ev.back();
+            free_ev.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    };
+    std::vector<double> step_ms, req_ms, queue_ms;
+    int64_t point_steps = 0, steps_total = 0, admission_waits = 0;
+    int launches = 0, max_active_seen = 0;
+    double active_sum = 0.0;
+    rvh_status err = RVH_OK;
+    const auto t0 = clk::now();
+    auto now_s = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
+    int done = 0;
+    for (int i = 0; i < n; ++i)
+        if (results[i].status != RVH_OK) ++done;
+    auto complete = [&](Launch& L) {
+        cudaEventSynchronize(L.stop);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, L.start, L.stop);
+        const double t = now_s();
+        for (int r : L.reqs) {
+            step_ms.push_back(ms);
+            results[r].steps_done++;
+            results[r].max_step_ms = std::max(results[r].max_step_ms, ms);
+        }
+        for (int r : L.last) {
+            results[r].done_s = t;
+            req_ms.push_back(1e3 * (t - reqs[r].arrival_s));
+            for (size_t k = 0; k < active.size(); ++k)
+                if (active[k].req == r) {
+                    if (active[k].bytes) s->pool.give(active[k].off, active[k].bytes);
+                    Asset* a = s->chars[reqs[r].character].asset;
+                    a->grid[0] = a->grid[1] = DevBuf{};
+                    s->chars[reqs[r].character].busy = false;
+                    active.erase(active.begin() + k);
+                    break;
+                }
+            ++done;
+        }
+        for (int r : L.reqs)
+            for (Active& ac : active)
+                if (ac.req == r) ac.in_flight--;
+        point_steps += L.points;
+        free_ev.push_back(L.start);
+        free_ev.push_back(L.stop);
+    };
+    while (done < n && err == RVH_OK) {
+        const double t = now_s();
+        while (next < size_t(n) && reqs[order[next]].arrival_s <= t) {
+            if (results[order[next]].status == RVH_OK) waiting.push_back(order[next]);
+            ++next;
+        }
+        // admission: arrival order, skipping requests whose character is busy
+        for (auto it = waiting.begin(); it != waiting.end() && int(active.size()) < s->desc.max_active;) {
+            const int r = *it;
+            Character& ch = s->chars[reqs[r].character];
+            if (ch.busy) {
+                ++it;
+                continue;
+            }
+            Active ac{r, reqs[r].n_steps};
+            Asset* a = ch.asset;
+            if (a->params.grid_enabled) {
+                const size_t gb = a->grid_bytes();
+                const size_t pair = 2 * ((gb + 255) & ~size_t(255));
+                size_t off = 0;
+                if (!s->pool.take(pair, &off)) {  // wait for memory; later requests may still fit
+                    ++admission_waits;
+                    ++it;
+                    continue;
+                }
+                ac.off = off;
+                ac.bytes = pair;
+                char* base = static_cast<char*>(s->slab.ptr) + off;
+                a->grid[0] = DevBuf{base, gb, s->ctx, false};
+                a->grid[1] = DevBuf{base + pair / 2, gb, s->ctx, false};
+                cudaMemsetAsync(base, 0, pair, stream);
+                a->parity = 0;
+                a->grid_dirty[0] = a->grid_dirty[1] = false;
+            }
+            ch.busy = true;
+            results[r].admit_s = t;
+            queue_ms.push_back(1e3 * (t - reqs[r].arrival_s));
+            active.push_back(ac);
+            it = waiting.erase(it);
+        }
+        max_active_seen = std::max(max_active_seen, int(active.size()));
+        // launch one step of every admitted request that still has steps to enqueue
+        std::vector<Asset*> la;
+        std::vector<rvh_frame> lf;
+        Launch L;
+        for (Active& ac : active) {
+            if (ac.remaining == 0) continue;
+            Character& ch = s->chars[reqs[ac.req].character];
+            rvh_frame f{};
+            f.dt = ch.dt;
+            f.t = float(double(ch.steps + 1) * double(ch.dt));
+            if (ch.has_wind) rvh_wind_at(&ch.wind, ch.steps, f.t, f.wind);
+            la.push_back(ch.asset);
+            lf.push_back(f);
+            L.reqs.push_back(ac.req);
+            if (ac.remaining == 1) L.last.push_back(ac.req);
+        }
+        if (!la.empty() && int(flight.size()) < s->desc.pipeline_depth) {
+            L.start = get_ev();
+            L.stop = get_ev();
+            err = dyn_batch_launch(s->batch, la, lf, stream, L.start, L.stop, &L.points);
+            if (err != RVH_OK) break;
+            for (Active& ac : active)
+                if (ac.remaining > 0) {
+                    ac.remaining--;
+                    ac.in_flight++;
+                    s->chars[reqs[ac.req].character].steps++;
+                }
+            steps_total += int64_t(la.size());
+            active_sum += double(la.size());
+            ++launches;
+            flight.push_back(L);
+            continue;
+        }
+        if (!flight.empty()) {
+            // a launch is in flight: retire it when it completes (or right away if the pipeline is full)
+            if (int(flight.size()) >= s->desc.pipeline_depth || la.empty() ||
+                cudaEventQuery(flight.front().stop) == cudaSuccess) {
+                complete(flight.front());
+                flight.pop_front();
+            }
+            continue;
+        }
+        if (next < size_t(n)) {  // idle until the next arrival
+            const double wait = reqs[order[next]].arrival_s - now_s();
+            if (wait > 2e-4) std::this_thread::sleep_for(std::chrono::duration<double>(wait * 0.5));
+            continue;
+        }
+        if (!waiting.empty() && active.empty()) {  // nothing can ever be admitted
+            err = fail(RVH_ERR_BUDGET, "server_run: a request's grid scratch exceeds the server budget");
+            for (int r : waiting) results[r].status = RVH_ERR_BUDGET;
+            break;
+        }
+    }
+    while (!flight.empty()) {
+        complete(flight.front());
+        flight.pop_front();
+    }
+    for (Active& ac : active) {   // only after an error
+        if (ac.bytes) s->pool.give(ac.off, ac.bytes);
+        Asset* a = s->chars[reqs[ac.req].character].asset;
+        a->grid[0] = a->grid[1] = DevBuf{};
+        s->chars[reqs[ac.req].character].busy = false;
+    }
+    for (cudaEvent_t e : free_ev) cudaEventDestroy(e);
+    const double wall = now_s();
+    rvh_status chk = dyn_batch_check(s->batch);
+    if (err == RVH_OK) err = chk;
+    if (stats) {
+        *stats = rvh_server_stats{};
+        stats->requests = n;
+        stats->steps = steps_total;
+        stats->point_steps = point_steps;
+        stats->launches = launches;
+        stats->wall_s = wall;
+        stats->point_steps_per_s = wall > 0 ? double(point_steps) / wall : 0.0;
+        stats->step_ms_p50 = pct(step_ms, 0.50);
+        stats->step_ms_p99 = pct(step_ms, 0.99);
+        stats->step_ms_p999 = pct(step_ms, 0.999);
+        stats->request_ms_p50 = pct(req_ms, 0.50);
+        stats->request_ms_p99 = pct(req_ms, 0.99);
+        stats->queue_ms_p50 = pct(queue_ms, 0.50);
+        stats->queue_ms_p99 = pct(queue_ms, 0.99);
+        stats->mean_batch = launches ? active_sum / launches : 0.0;
+        stats->max_active = max_active_seen;
+        stats->admission_waits = admission_waits;
+        stats->scratch_used_bytes = s->pool.used();
+    }
+    return err;
+}
+
+}  // extern "C"

@@ -55,6 +55,11 @@ PROTOTYPES = [
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_batch_timing_enable", _st, [_vp, C.c_int32]),
     ("rvh_batch_timing_read", _st, [_vp, _P(C.c_double), _P(C.c_int32)]),
+    ("rvh_server_create", _st, [_vp, _vp, _P(_vp)]),
+    ("rvh_server_destroy", _st, [_vp]),
+    ("rvh_server_add_character", _st, [_vp, _vp, _vp, C.c_float, _P(C.c_int32)]),
+    ("rvh_server_character_steps", _st, [_vp, C.c_int32, _P(C.c_int64)]),
+    ("rvh_server_run", _st, [_vp, _vp, C.c_int32, _vp, _vp]),
     ("rvh_adjoint", _st, [_vp, _P(T.Frame), C.c_int32, C.c_int32, _P(C.c_float), _P(C.c_double),
                           _P(C.c_float), _P(C.c_float), _P(C.c_float)]),
     ("rvh_generate_head", _st, [_vp, _vp, _P(C.c_float), _P(T.SimParams), _P(T.Collider), _P(C.c_int32)]),

@@ -45,6 +45,32 @@ class Orbit(C.Structure):
                 ("phase", C.c_float), ("sphere_radius", C.c_float)]
 
 
+class ServerDesc(C.Structure):
+    _fields_ = [("max_active", C.c_int32), ("lanes_per_strand", C.c_int32), ("pipeline_depth", C.c_int32),
+                ("reserved", C.c_int32), ("scratch_budget_bytes", C.c_uint64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("character", C.c_int32), ("n_steps", C.c_int32), ("arrival_s", C.c_double)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("admit_s", C.c_double), ("done_s", C.c_double), ("max_step_ms", C.c_float),
+                ("steps_done", C.c_int32), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_int64), ("steps", C.c_int64), ("point_steps", C.c_int64), ("launches", C.c_int32),
+                ("max_active", C.c_int32), ("wall_s", C.c_double), ("point_steps_per_s", C.c_double),
+                ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double), ("step_ms_p999", C.c_double),
+                ("request_ms_p50", C.c_double), ("request_ms_p99", C.c_double), ("queue_ms_p50", C.c_double),
+                ("queue_ms_p99", C.c_double), ("mean_batch", C.c_double), ("admission_waits", C.c_int64),
+                ("scratch_used_bytes", C.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 MATH_FAST = 0
 MATH_EXACT = 1
 
@@ -226,6 +252,43 @@ class Batch:
         l, it, ct, pts = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
         check(self.lib.rvh_batch_info(self.h, C.byref(l), C.byref(it), C.byref(ct), C.byref(pts)))
         return {"lanes": l.value, "items": it.value, "ctas": ct.value, "points": pts.value}
+
+
+class Server:
+    """Continuous-batching request loop over resident characters (C++)."""
+
+    def __init__(self, ctx, max_active=16, lanes=4, pipeline_depth=2, scratch_budget_bytes=1 << 30):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        d = ServerDesc(max_active, lanes, pipeline_depth, 0, scratch_budget_bytes)
+        h = C.c_void_p()
+        check(self.lib.rvh_server_create(ctx.h, C.byref(d), C.byref(h)))
+        self.h = h
+
+    def add_character(self, asset, wind=None, dt=1.0 / 60.0):
+        i = C.c_int32()
+        check(self.lib.rvh_server_add_character(self.h, asset.h, None if wind is None else C.byref(wind), dt,
+                                                C.byref(i)))
+        return i.value
+
+    def character_steps(self, cid):
+        v = C.c_int64()
+        check(self.lib.rvh_server_character_steps(self.h, cid, C.byref(v)))
+        return v.value
+
+    def run(self, requests):
+        """requests: list of (character, n_steps, arrival_s). Returns (results, stats)."""
+        n = len(requests)
+        arr = (Request * max(1, n))(*[Request(c, k, t) for c, k, t in requests])
+        res = (RequestResult * max(1, n))()
+        st = ServerStats()
+        status = self.lib.rvh_server_run(self.h, arr, n, res, C.byref(st))
+        return status, [res[i] for i in range(n)], st
+
+    def close(self):
+        if self.h:
+            self.lib.rvh_server_destroy(self.h)
+            self.h = None
 
 
 # ---- scene helpers -------------------------------------------------------------
