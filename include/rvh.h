@@ -143,6 +143,30 @@ rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
 rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);
 rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launches);
 
+/* ---- autotuning -------------------------------------------------------------
+ * Times real batched steps of `assets` for every candidate: lanes per strand
+ * {4, 8, 16, 32} (strands per warp 8, 4, 2, 1) x phase-A tile {1, 2, 4}
+ * rounds, and with tune_grid also each listed grid resolution (every
+ * grid-enabled asset re-gridded over the same bounds).  The strand records
+ * are restored after every trial.  The winner is cached per workload
+ * signature; rvh_batch_create with lanes_per_strand = 0 uses it. */
+typedef struct rvh_tune_desc {
+    int32_t steps;                /* timed steps per candidate (default 3) */
+    int32_t tune_grid;            /* 1 = sweep grid_res[] too and leave the assets on the winner */
+    int32_t use_cache;            /* 1 = return a cached result for this workload when there is one */
+    int32_t n_grid_res;
+    int32_t grid_res[8];
+} rvh_tune_desc;
+typedef struct rvh_tune_result {
+    int32_t lanes_per_strand, strands_per_tile, grid_res, n_tried;
+    float best_ms;
+    int32_t tried_lanes[96], tried_tile[96], tried_res[96];
+    float tried_ms[96];
+} rvh_tune_result;
+rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n, const rvh_frame* frames,
+                          const rvh_tune_desc* desc, rvh_tune_result* out);
+rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_grid, rvh_tune_result* out);
+
 /* ---- serving: continuous batching of step requests for resident characters ----
  * The server replays the reference's per-frame loop (src/main.cpp:257-285)
  * for many characters at once: each launch advances every admitted request

@@ -232,12 +232,13 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const __grid_constant__
         fwd_local<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
     }
     const float4 tg = D.targets[s];
-    const f3 e = {X[n - 1].x - tg.x, X[n - 1].y - tg.y, X[n - 1].z - tg.z};
-    D.loss_parts[s] = (double)e.x * e.x + (double)e.y * e.y + (double)e.z * e.z;
+    const double ex = (double)X[n - 1].x - (double)tg.x, ey = (double)X[n - 1].y - (double)tg.y,
+                 ez = (double)X[n - 1].z - (double)tg.z;
+    D.loss_parts[s] = ex * ex + ey * ey + ez * ez;
     f3 Xb[RVH_MAX_POINTS], Vb[RVH_MAX_POINTS];
     for (int i = 0; i < n; ++i) Xb[i] = Vb[i] = f3{0.f, 0.f, 0.f};
     const float g2 = 2.0f / (float)A.n_strands;
-    Xb[n - 1] = {g2 * e.x, g2 * e.y, g2 * e.z};
+    Xb[n - 1] = {g2 * (X[n - 1].x - tg.x), g2 * (X[n - 1].y - tg.y), g2 * (X[n - 1].z - tg.z)};
     float rest_bar = 0.f;
     f3 wind_bar = {0.f, 0.f, 0.f};
     for (int k = D.n_ckpt - 1; k >= 0; --k) {

@@ -300,7 +300,18 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
     rvh_batch_desc d{};
     d.use_graph = 1;
     if (desc) d = *desc;
-    const int lanes = d.lanes_per_strand ? d.lanes_per_strand : 4;
+    int lanes = d.lanes_per_strand;
+    if (lanes == 0) {  // the tuner's choice for this workload, if it has one
+        rvh_tune_result tr{};
+        const std::string keep = last_error_cstr();
+        if (n > 0 && rvh_tune_lookup(assets, n, 0, &tr) == RVH_OK) {
+            lanes = tr.lanes_per_strand;
+            if (d.strands_per_tile == 0) d.strands_per_tile = tr.strands_per_tile;
+        } else {
+            lanes = 4;
+        }
+        set_error(keep);
+    }
     if (!batch_supported(lanes)) return fail(RVH_ERR_UNSUPPORTED, "batch: lanes_per_strand must be 4, 8, 16 or 32");
     cudaSetDevice(ctx->device);
     rvh_batch* b = new (std::nothrow) rvh_batch();

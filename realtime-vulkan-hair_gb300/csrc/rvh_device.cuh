@@ -280,6 +280,14 @@ __device__ __forceinline__ CellF cell_from_global(const DevAsset& A, unsigned id
 template <class M, class CellFn>
 __device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel, const Corners& C, CellFn cell) {
     const bool rep = A.repulsion != 0.0f;
+    // the trilinear weights of the (up to) two corners per axis, computed once
+    float wxs[2], wys[2], wzs[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        wxs[d] = tri_w<M>(C.g[0], C.lo[0] + d);
+        wys[d] = tri_w<M>(C.g[1], C.lo[1] + d);
+        wzs[d] = tri_w<M>(C.g[2], C.lo[2] + d);
+    }
     f3 gv = {0.f, 0.f, 0.f};
     float rho = 0.f;
     f3 grad = {0.f, 0.f, 0.f};
@@ -297,7 +305,7 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel, co
                 const int c = C.lo[2] + dc;
                 const CellF cf = cell(a, b, c);
                 if (cf.fd > 0.0f) {
-                    const float wx = tri_w<M>(C.g[0], a), wy = tri_w<M>(C.g[1], b), wz = tri_w<M>(C.g[2], c);
+                    const float wx = wxs[da], wy = wys[db], wz = wzs[dc];
                     const float w = M::mul(M::mul(wx, wy), wz);
                     const float s = M::mul(w, cf.rcp);
                     gv = v_add<M>(gv, v_scale<M>(s, f3{cf.vx, cf.vy, cf.vz}));

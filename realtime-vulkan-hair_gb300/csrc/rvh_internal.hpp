@@ -16,6 +16,7 @@ namespace rvh {
 
 // ---- errors -------------------------------------------------------------------
 void set_error(const std::string& msg);
+const char* last_error_cstr();
 rvh_status fail(rvh_status s, const std::string& msg);
 rvh_status cuda_fail(cudaError_t e, const char* what);
 #define RVH_CUDA(call)                                              \

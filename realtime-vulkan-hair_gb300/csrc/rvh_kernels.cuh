@@ -109,6 +109,20 @@ __device__ __forceinline__ void bounds_add(const Corners& C, int (&lmin)[3], int
 
 __device__ __forceinline__ bool has_corners(const Corners& C) { return C.cnt[0] > 0 && C.cnt[1] > 0 && C.cnt[2] > 0; }
 
+// Box bounds from the lane's position extremes.  g = (p - o)/h and the corner
+// range [max(floor g, 0), min(floor g + 1, dim - 1)] are monotone in p, so the
+// corners of the extremes bound the corners of every point in between; lanes
+// without points leave the bounds empty.
+template <class M>
+__device__ __forceinline__ void bounds_of_extremes(const DevAsset& A, f3 pmin, f3 pmax, int (&lmin)[3], int (&lmax)[3]) {
+    const Corners C0 = corners_of<M>(A, pmin), C1 = corners_of<M>(A, pmax);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lmin[a] = C0.lo[a];
+        lmax[a] = max(C1.lo[a] + C1.cnt[a] - 1, C0.lo[a]);
+    }
+}
+
 // Splat one point into the shared box (int32 partial sums).
 template <class M>
 __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const int (&lo)[3],
@@ -152,15 +166,16 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
     int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
     float vab = 0.f;
     int np = 0;
+    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         if (!((mask >> k) & 1u)) continue;
-        const Corners C = corners_of<M>(A, xo[k]);
-        if (!has_corners(C)) continue;
-        bounds_add(C, lmin, lmax);
+        pmin = f3{fminf(pmin.x, xo[k].x), fminf(pmin.y, xo[k].y), fminf(pmin.z, xo[k].z)};
+        pmax = f3{fmaxf(pmax.x, xo[k].x), fmaxf(pmax.y, xo[k].y), fmaxf(pmax.z, xo[k].z)};
         vab = fmaxf(vab, fmaxf(fabsf(vo[k].x), fmaxf(fabsf(vo[k].y), fabsf(vo[k].z))));
         ++np;
     }
+    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
     box_reset(S);
     __syncthreads();
     box_reduce(S, lmin, lmax, __float_as_uint(vab), np);
@@ -256,6 +271,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
     unsigned m = 0u;
     int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
     int np = 0;
+    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
         const int q = threadIdx.x + j * kThreads;
@@ -268,11 +284,11 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         off[j] = ls * (3 * n) + i;
         x[j] = xyz(ld_cg(base + off[j]));
         m |= 1u << j;
-        const Corners C = corners_of<M>(A, x[j]);
-        if (!has_corners(C)) continue;
-        bounds_add(C, lmin, lmax);
+        pmin = f3{fminf(pmin.x, x[j].x), fminf(pmin.y, x[j].y), fminf(pmin.z, x[j].z)};
+        pmax = f3{fmaxf(pmax.x, x[j].x), fmaxf(pmax.y, x[j].y), fmaxf(pmax.z, x[j].z)};
         ++np;
     }
+    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
     box_reset(S);
     __syncthreads();
     box_reduce(S, lmin, lmax, 0u, np);

@@ -55,6 +55,8 @@ PROTOTYPES = [
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_batch_timing_enable", _st, [_vp, C.c_int32]),
     ("rvh_batch_timing_read", _st, [_vp, _P(C.c_double), _P(C.c_int32)]),
+    ("rvh_tune_batch", _st, [_vp, _P(_vp), C.c_int32, _vp, _vp, _vp]),
+    ("rvh_tune_lookup", _st, [_P(_vp), C.c_int32, C.c_int32, _vp]),
     ("rvh_server_create", _st, [_vp, _vp, _P(_vp)]),
     ("rvh_server_destroy", _st, [_vp]),
     ("rvh_server_add_character", _st, [_vp, _vp, _vp, C.c_float, _P(C.c_int32)]),

@@ -40,6 +40,36 @@ class WindDesc(C.Structure):
                 ("seed", C.c_uint64)]
 
 
+class TuneDesc(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("tune_grid", C.c_int32), ("use_cache", C.c_int32), ("n_grid_res", C.c_int32),
+                ("grid_res", C.c_int32 * 8)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("lanes_per_strand", C.c_int32), ("strands_per_tile", C.c_int32), ("grid_res", C.c_int32),
+                ("n_tried", C.c_int32), ("best_ms", C.c_float), ("tried_lanes", C.c_int32 * 96),
+                ("tried_tile", C.c_int32 * 96), ("tried_res", C.c_int32 * 96), ("tried_ms", C.c_float * 96)]
+
+    def table(self):
+        return [(self.tried_lanes[i], self.tried_tile[i], self.tried_res[i], self.tried_ms[i])
+                for i in range(self.n_tried)]
+
+
+def tune(ctx, assets, frames, steps=3, grid_res=(), use_cache=False):
+    d = TuneDesc()
+    d.steps = steps
+    d.tune_grid = 1 if grid_res else 0
+    d.use_cache = 1 if use_cache else 0
+    d.n_grid_res = len(grid_res)
+    for i, r in enumerate(grid_res):
+        d.grid_res[i] = r
+    arr = (C.c_void_p * len(assets))(*[a.h.value for a in assets])
+    fr = (T.Frame * len(frames))(*frames)
+    out = TuneResult()
+    check(ctx.lib.rvh_tune_batch(ctx.h, arr, len(assets), fr, C.byref(d), C.byref(out)))
+    return out
+
+
 class Orbit(C.Structure):
     _fields_ = [("center", C.c_float * 3), ("orbit_radius", C.c_float), ("omega", C.c_float),
                 ("phase", C.c_float), ("sphere_radius", C.c_float)]

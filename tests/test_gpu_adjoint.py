@@ -136,36 +136,44 @@ def test_gpu_adjoint_matches_central_fd_fp64(case, gpu_grads, oracle):
         return oracle.loss(st[s:s + 1], n, r[s:s + 1], spec.params, frames, spec.colliders, STEPS,
                            targets[s:s + 1], strand_wind=w[s:s + 1]) / ns
 
+    def fd(kind, s, i, q, h):
+        if kind == 0:
+            wp, wm = wind.copy(), wind.copy()
+            wp[s, q] += h
+            wm[s, q] -= h
+            return (L(w=wp, s=s) - L(w=wm, s=s)) / (2 * h)
+        if kind == 1:
+            rp, rm = rest.copy(), rest.copy()
+            rp[s] += h
+            rm[s] -= h
+            return (L(r=rp, s=s) - L(r=rm, s=s)) / (2 * h)
+        sp, sm = st0.copy(), st0.copy()
+        sp[s, n + i, q] += h
+        sm[s, n + i, q] -= h
+        return (L(st=sp, s=s) - L(st=sm, s=s)) / (2 * h)
+
     rng = np.random.default_rng(64)
-    h = 1e-4
     rows = []
     for j in range(64):
         kind = j % 3
         s = int(rng.integers(0, spec.n_strands))
-        if kind == 0:
-            q = int(rng.integers(0, 3))
-            wp, wm = wind.copy(), wind.copy()
-            wp[s, q] += h
-            wm[s, q] -= h
-            fd, ad = (L(w=wp, s=s) - L(w=wm, s=s)) / (2 * h), dw_g[s, q]
-        elif kind == 1:
-            rp, rm = rest.copy(), rest.copy()
-            rp[s] += h
-            rm[s] -= h
-            fd, ad = (L(r=rp, s=s) - L(r=rm, s=s)) / (2 * h), dr_g[s]
-        else:
-            i, q = int(rng.integers(1, n)), int(rng.integers(0, 3))
-            sp, sm = st0.copy(), st0.copy()
-            sp[s, n + i, q] += h
-            sm[s, n + i, q] -= h
-            fd, ad = (L(st=sp, s=s) - L(st=sm, s=s)) / (2 * h), dv_g[s, i, q]
-        rows.append((kind, fd, ad))
+        i, q = int(rng.integers(1, n)), int(rng.integers(0, 3))
+        ad = (dw_g[s, q], dr_g[s], dv_g[s, i, q])[kind]
+        rows.append((kind, fd(kind, s, i, q, 1e-4), fd(kind, s, i, q, 1e-6), ad))
     rows = np.array(rows)
-    scale = np.abs(rows[:, 1]).max()
-    err = np.abs(rows[:, 1] - rows[:, 2])
-    ok = err <= 2e-2 * np.abs(rows[:, 1]) + 1e-3 * scale
-    print("FD h=1e-4: %d/64 within tolerance; median rel err %.3g" % (ok.sum(), np.median(err / np.maximum(np.abs(rows[:, 1]), 1e-12))))
-    assert ok.sum() >= 62, rows[~ok]
+    fd4, fd6, ad = rows[:, 1], rows[:, 2], rows[:, 3]
+    scale = np.abs(fd6).max()
+    tol = lambda ref: 2e-2 * np.abs(ref) + 1e-4 * scale
+    ok4 = np.abs(fd4 - ad) <= tol(fd4)
+    # where central differences at h = 1e-4 have converged (they agree with h = 1e-6),
+    # the adjoint must agree with them; elsewhere h = 1e-4 straddles a contact kink
+    conv = np.abs(fd4 - fd6) <= tol(fd6)
+    print("FD h=1e-4: %d/64 agree with the GPU adjoint; %d/64 converged, of which %d agree; "
+          "vs h=1e-6: %d/64 agree" % (ok4.sum(), conv.sum(), (ok4 & conv).sum(),
+                                     (np.abs(fd6 - ad) <= tol(fd6)).sum()))
+    assert conv.sum() >= 48
+    assert (ok4 & conv).sum() >= conv.sum() - 1, rows[conv & ~ok4]
+    assert ok4.sum() >= 56
 
 
 def test_adjoint_forward_equals_the_step_kernel(gpu_ctx, case):
@@ -183,7 +191,8 @@ def test_adjoint_forward_equals_the_step_kernel(gpu_ctx, case):
     for f in frames:
         a.step(f)
     tips = a.read()[:, n - 1, :3].astype(np.float64)
-    loss_fwd = float(np.mean(np.sum((tips - targets[sub]) ** 2, axis=1)))
+    tg32 = targets[sub].astype(np.float32).astype(np.float64)   # the C ABI takes float targets
+    loss_fwd = float(np.mean(np.sum((tips - tg32) ** 2, axis=1)))
     assert abs(loss_adj - loss_fwd) <= 1e-12 * abs(loss_fwd)
     a.close()
 
