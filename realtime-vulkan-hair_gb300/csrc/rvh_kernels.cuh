@@ -53,6 +53,15 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     return v;
 }
 
+// Unsigned division by a runtime divisor d via a multiply-high: with
+// m = floor((2^32 - 1) / d) + 1, umulhi(c, m) = floor(c / d) whenever
+// c * d < 2^32 (box cells and tile points here stay below 2^16).
+struct FastDiv {
+    unsigned m, d;
+    __device__ __forceinline__ explicit FastDiv(unsigned dd) : m(dd > 1 ? 0xffffffffu / dd + 1u : 0u), d(dd) {}
+    __device__ __forceinline__ unsigned div(unsigned c) const { return d > 1 ? __umulhi(c, m) : c; }
+};
+
 // ---- shared-memory grid boxes ----------------------------------------------------
 // A CTA's points touch a compact block of grid cells.  Phase A accumulates its
 // splat in that box with shared-memory int32 atomics and flushes each touched
@@ -204,10 +213,13 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
             use = __syncthreads_and(ok);
             if (use) {
                 const int nxny = A.nx * A.ny;
+                const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
                 for (int c = threadIdx.x; c < (int)vol; c += kThreads) {
                     const int4 v = b4[c];
                     if (!(v.x | v.y | v.z | v.w)) continue;
-                    const int a = lo[0] + c % bw, b = lo[1] + (c / bw) % bh, cc = lo[2] + c / (bw * bh);
+                    const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
+                    const int qy = (int)dw.div((unsigned)rz);
+                    const int a = lo[0] + (rz - qy * bw), b = lo[1] + qy, cc = lo[2] + qz;
                     unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + cc * nxny);
                     red_add_s64(cell + 0, v.x);
                     red_add_s64(cell + 1, v.y);
@@ -266,6 +278,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
     const int n = A.n_points;
     const int npt = (s1 - s0) * n;
     float4* const base = A.strands + (size_t)s0 * (3 * n);
+    const FastDiv dn((unsigned)n);
     f3 x[kPtsB];
     int off[kPtsB];   // record offset (float4 units) of the point's curvePoints slot
     unsigned m = 0u;
@@ -278,7 +291,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         x[j] = f3{0.f, 0.f, 0.f};
         off[j] = 0;
         if (q >= npt) continue;
-        const int ls = q / n;
+        const int ls = (int)dn.div((unsigned)q);
         const int i = q - ls * n;
         if (i == 0) continue;
         off[j] = ls * (3 * n) + i;
@@ -302,8 +315,11 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
     if (use) {
         const int vol = bw * bh * bd;
         const int nxny = A.nx * A.ny;
+        const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
         for (int c = threadIdx.x; c < vol; c += kThreads) {
-            const int a = lo[0] + c % bw, b = lo[1] + (c / bw) % bh, cc = lo[2] + c / (bw * bh);
+            const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
+            const int qy = (int)dw.div((unsigned)rz);
+            const int a = lo[0] + (rz - qy * bw), b = lo[1] + qy, cc = lo[2] + qz;
             const CellF cf = cell_from_global<M>(A, (unsigned)(a + b * A.nx + cc * nxny));
             bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
             br[c] = cf.rcp;
