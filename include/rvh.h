@@ -59,6 +59,9 @@ rvh_status rvh_context_synchronize(rvh_context* ctx);
 /* bytes the context has admitted against its budget, and the budget */
 rvh_status rvh_context_memory(rvh_context* ctx, uint64_t* used, uint64_t* budget);
 const char* rvh_last_error(void);
+/* Page-locked host memory (for asynchronous copies). */
+rvh_status rvh_pinned_alloc(size_t bytes, void** out);
+rvh_status rvh_pinned_free(void* p);
 const char* rvh_status_string(rvh_status s);
 int32_t rvh_abi_version(void);
 
@@ -121,12 +124,23 @@ typedef struct rvh_batch_desc {
     int32_t strands_per_tile;     /* phase-A tile size; 0 = tuner's choice */
     int32_t ctas_per_sm;          /* 0 = occupancy limit */
     int32_t use_graph;            /* 1 = capture the launch in a CUDA graph (default) */
+    int32_t full_steps;           /* 0 (default): fused steps - each launch first applies the previous
+                                     step's gather + friction (loop 3), then runs loops 1-2, so a step is
+                                     one pass over the records with no wait inside the launch; positions
+                                     are final after every step, velocities after rvh_batch_finish (and
+                                     every read).  1: every launch completes its step (phase B waits on
+                                     its asset's phase A inside the launch). */
+    int32_t reserved;
 } rvh_batch_desc;
 rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t n, const rvh_batch_desc* desc,
                             rvh_batch** out);
 rvh_status rvh_batch_destroy(rvh_batch* b);
 /* One step of every asset; frames[i] belongs to assets[i]. */
 rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream);
+/* Applies the last step's pending gather + friction of every asset (fused
+ * steps only); afterwards the records hold the exact step result.  Reads,
+ * plain steps and parameter changes of an asset do this for it implicitly. */
+rvh_status rvh_batch_finish(rvh_batch* b, void* stream);
 /* Nonzero device-side status of the last finished batch launch (RVH_ERR_TIMEOUT if a bounded wait gave up). */
 rvh_status rvh_batch_check(rvh_batch* b);
 rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_t* n_ctas, int64_t* n_points);
@@ -138,6 +152,14 @@ rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_
  * the shared-memory box, rounds splatted with direct global atomics, phase-B
  * tiles gathered from the box, tiles gathered from the global grid. */
 rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]);
+/* Every asset's curvePoints (float4 per point, asset after asset in batch
+ * order) copied to host memory: a packing kernel on `stream` writes a device
+ * staging buffer, then a copy stream moves it while later steps run.  Two
+ * staging slots alternate; host_dst should be pinned (rvh_pinned_alloc) for
+ * the copy to overlap.  rvh_batch_positions_wait blocks until every copy is
+ * done. */
+rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream);
+rvh_status rvh_batch_positions_wait(rvh_batch* b);
 /* Bytes rvh_batch_step copies host->device per step (per-asset frame and collider tables). */
 rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);
 rvh_status rvh_batch_timing_enable(rvh_batch* b, int32_t on);

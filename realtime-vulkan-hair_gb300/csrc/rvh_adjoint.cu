@@ -307,7 +307,7 @@ rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, i
         return cuda_fail(e, "adjoint upload");
     }
     AdjDev D{};
-    D.A = a->device_view(frames[0], a->parity);
+    D.A = a->device_view(frames[0], -1);
     D.frames = static_cast<const rvh_frame*>(fr.ptr);
     D.n_steps = n_steps;
     D.ckpt = C;

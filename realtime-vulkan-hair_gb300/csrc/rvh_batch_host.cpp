@@ -16,9 +16,12 @@
 
 namespace rvh {
 
+enum { MODE_FUSED = 0, MODE_FULL = 1, MODE_FINISH = 2 };
+
 struct Batch {
     Context* ctx = nullptr;
     std::vector<Asset*> assets;
+    std::vector<int> modes;   // per asset: MODE_FUSED (loop 3 left pending), MODE_FULL, MODE_FINISH
     int lanes = 4;
     bool exact = false;
     bool use_graph = true;
@@ -35,9 +38,35 @@ struct Batch {
     BatchDev dev{};
     const void* kernel = nullptr;
     bool timing = false;
+    // positions read-back: packed device staging (two slots) and a copy stream
+    DevBuf pos_stage[2], d_first;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t packed[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    int pos_slot = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs;   // recorded, not yet read
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
 };
+
+// Packs the curvePoints of every asset of a batch into one contiguous float4
+// array (asset after asset): out[first[a] + s*n + i] = strands[s*3n + i].
+__global__ void __launch_bounds__(kThreads) k_pack_positions(const DevAsset* __restrict__ assets,
+                                                             const long long* __restrict__ first, int n_assets,
+                                                             long long total, float4* __restrict__ out) {
+    for (long long p = (long long)blockIdx.x * kThreads + threadIdx.x; p < total; p += (long long)gridDim.x * kThreads) {
+        int lo = 0, hi = n_assets - 1;  // last asset with first[a] <= p
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= p) lo = mid;
+            else hi = mid - 1;
+        }
+        const DevAsset& A = assets[lo];
+        const int n = A.n_points;
+        const long long q = p - first[lo];
+        const long long s = q / n;
+        const int i = (int)(q - s * n);
+        out[p] = __ldcs(A.strands + s * (3 * n) + i);
+    }
+}
 
 namespace {
 
@@ -78,6 +107,11 @@ void plan(Batch& b, int strands_per_tile) {
     for (int ai : order) {
         const Asset* a = b.assets[ai];
         if (a->n_strands == 0) continue;
+        const int mode = b.modes.empty() ? MODE_FUSED : b.modes[ai];
+        if (mode == MODE_FINISH) {  // gather-only items of an earlier step: nothing to wait for
+            emit_b(ai);
+            continue;
+        }
         int ta = strands_per_tile > 0 ? strands_per_tile : kTargetPointsA / a->n_points;
         ta = std::max(quantum, (ta + quantum - 1) / quantum * quantum);
         for (int s = 0; s < a->n_strands; s += ta) {
@@ -91,14 +125,66 @@ void plan(Batch& b, int strands_per_tile) {
             for (int c = 0; c < chunks; c += kClearChunk)
                 b.items.push_back({ITEM_CLEAR, ai, c, std::min(chunks, c + kClearChunk)});
         }
-        pending.push_back({ai, last});
+        if (mode == MODE_FULL) pending.push_back({ai, last});
     }
     flush(true);
+}
+
+// Grid choice of one asset for one batched step: gather the pending friction from
+// grid[prev], splat into grid[t] (cleared first if dirty), clear grid[u] in-kernel.
+struct GridUse {
+    int prev = -1, t = -1, u = -1;
+};
+
+rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s, DevAsset* view, GridUse* gu) {
+    *gu = GridUse{};
+    if (!a->params.grid_enabled) {
+        *view = a->device_view(f, -1);
+        return RVH_OK;
+    }
+    if (!a->grid[0].ptr || !a->grid[1].ptr || !a->grid[2].ptr)
+        return fail(RVH_ERR_STATE, "batch: an asset's grids are held by a request server");
+    if (mode == MODE_FINISH) {
+        rvh_frame fp = f;
+        fp.dt = a->dt_prev;
+        *view = a->device_view(fp, a->pend);
+        gu->prev = a->pend;
+        return RVH_OK;
+    }
+    gu->prev = a->pending ? a->pend : -1;
+    gu->t = a->pick_grid(gu->prev, -1);
+    if (a->grid_dirty[gu->t]) RVH_CUDA(cudaMemsetAsync(a->grid[gu->t].ptr, 0, a->grid_bytes(), s));
+    gu->u = a->pick_grid(gu->prev, gu->t);
+    *view = a->device_view(f, gu->t, gu->prev, gu->u);
+    return RVH_OK;
+}
+
+void commit_asset(Asset* a, int mode, const GridUse& gu, float dt) {
+    if (!a->params.grid_enabled) return;
+    if (mode == MODE_FINISH) {
+        a->pending = false;
+        a->grid_dirty[gu.prev] = true;
+        return;
+    }
+    if (gu.prev >= 0) a->grid_dirty[gu.prev] = true;
+    a->grid_dirty[gu.u] = false;  // the launch's clear items zero it
+    a->grid_dirty[gu.t] = true;
+    a->last_grid = gu.t;
+    a->pending = mode == MODE_FUSED;
+    a->pend = gu.t;
+    a->dt_prev = dt;
 }
 
 void destroy(Batch* b) {
     if (!b) return;
     if (b->ctx) cudaStreamSynchronize(b->ctx->stream);
+    if (b->copy_stream) cudaStreamSynchronize(b->copy_stream), cudaStreamDestroy(b->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        if (b->packed[i]) cudaEventDestroy(b->packed[i]);
+        if (b->copied[i]) cudaEventDestroy(b->copied[i]);
+        if (b->ctx) b->ctx->free(b->pos_stage[i]);
+    }
+    if (b->ctx) b->ctx->free(b->d_first);
     for (auto& e : b->ev_pairs) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     for (auto& e : b->ev_free) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -234,9 +320,11 @@ void dyn_batch_free(DynBatch* d) {
 }
 
 rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<rvh_frame>& frames,
-                            cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop, int64_t* points) {
+                            const std::vector<int>& modes, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop,
+                            int64_t* points) {
     Batch& b = d->b;
     b.assets = assets;
+    b.modes = modes;
     plan(b, 0);
     b.dev.n_items = int32_t(b.items.size());
     int64_t pts = 0;
@@ -248,11 +336,10 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     const int slot = b.slot;
     b.slot ^= 1;
     RVH_CUDA(cudaEventSynchronize(b.staged[slot]));
+    std::vector<GridUse> gus(assets.size());
     for (size_t i = 0; i < assets.size(); ++i) {
-        Asset* a = assets[i];
-        if (a->params.grid_enabled && a->grid_dirty[a->parity])
-            RVH_CUDA(cudaMemsetAsync(a->grid[a->parity].ptr, 0, a->grid_bytes(), s));
-        b.h_stage[slot][i] = a->device_view(frames[i], a->parity);
+        rvh_status ps = prepare_asset(assets[i], modes[i], frames[i], s, &b.h_stage[slot][i], &gus[i]);
+        if (ps != RVH_OK) return ps;
         d->h_need[slot][i] = b.need_a[i];
     }
     std::memcpy(d->h_items[slot], b.items.data(), sizeof(WorkItem) * b.items.size());
@@ -264,12 +351,7 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     rvh_status ls = enqueue_launch(&b, s);
     if (ls != RVH_OK) return ls;
     if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
-    for (Asset* a : assets) {
-        if (!a->params.grid_enabled) continue;
-        a->grid_dirty[a->parity] = true;
-        a->grid_dirty[a->parity ^ 1] = false;
-        a->parity ^= 1;
-    }
+    for (size_t i = 0; i < assets.size(); ++i) commit_asset(assets[i], modes[i], gus[i], frames[i].dt);
     return RVH_OK;
 }
 
@@ -331,6 +413,7 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
                 return fail(RVH_ERR_INVALID_ARG, "batch_create: an asset appears twice");
             }
         b->assets.push_back(assets[i]);
+        b->modes.push_back(d.full_steps ? MODE_FULL : MODE_FUSED);
         b->n_points += int64_t(assets[i]->n_strands) * assets[i]->n_points;
     }
     b->kernel = batch_kernel(lanes, b->exact);
@@ -425,11 +508,10 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
     b->slot ^= 1;
     RVH_CUDA(cudaEventSynchronize(b->staged[slot]));  // the copy that last read this staging buffer is done
     DevAsset* st = b->h_stage[slot];
+    std::vector<GridUse> gus(b->assets.size());
     for (size_t i = 0; i < b->assets.size(); ++i) {
-        Asset* a = b->assets[i];
-        if (a->params.grid_enabled && a->grid_dirty[a->parity])  // left dirty by a plain step
-            RVH_CUDA(cudaMemsetAsync(a->grid[a->parity].ptr, 0, a->grid_bytes(), s));
-        st[i] = a->device_view(frames[i], a->parity);
+        rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i]);
+        if (ps != RVH_OK) return ps;
     }
     RVH_CUDA(cudaMemcpyAsync(b->d_assets.ptr, st, sizeof(DevAsset) * b->assets.size(), cudaMemcpyHostToDevice, s));
     RVH_CUDA(cudaEventRecord(b->staged[slot], s));
@@ -454,11 +536,17 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
         RVH_CUDA(cudaEventRecord(ev.second, s));
         b->ev_pairs.push_back(ev);
     }
+    for (size_t i = 0; i < b->assets.size(); ++i) commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt);
+    return RVH_OK;
+}
+
+rvh_status rvh_batch_finish(rvh_batch* b, void* stream) {
+    if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_finish: NULL");
+    cudaSetDevice(b->ctx->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
     for (Asset* a : b->assets) {
-        if (!a->params.grid_enabled) continue;
-        a->grid_dirty[a->parity] = true;       // used by this step (read back by rvh_asset_read_grid)
-        a->grid_dirty[a->parity ^ 1] = false;  // cleared by this step
-        a->parity ^= 1;
+        rvh_status st = finish_pending(a, s);
+        if (st != RVH_OK) return st;
     }
     return RVH_OK;
 }
@@ -474,6 +562,59 @@ rvh_status rvh_batch_check(rvh_batch* b) {
         RVH_CUDA(cudaMemset(b->d_error.ptr, 0, sizeof(int)));
         return fail(err, "batch: a phase-B tile gave up waiting for its asset's phase A");
     }
+    return RVH_OK;
+}
+
+rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream) {
+    if (!b || (!host_dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: NULL argument");
+    const size_t need = size_t(b->n_points) * 16u;
+    if (bytes != need) return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: size must be 16 * total points");
+    if (!need) return RVH_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
+    if (!b->copy_stream) {  // first use: staging, offsets, copy stream
+        rvh_status st;
+        for (int i = 0; i < 2; ++i)
+            if ((st = b->ctx->alloc(b->pos_stage[i], need)) != RVH_OK) return st;
+        std::vector<long long> first(b->assets.size());
+        long long acc = 0;
+        for (size_t i = 0; i < b->assets.size(); ++i) {
+            first[i] = acc;
+            acc += (long long)b->assets[i]->n_strands * b->assets[i]->n_points;
+        }
+        if ((st = b->ctx->alloc(b->d_first, sizeof(long long) * std::max<size_t>(1, first.size()))) != RVH_OK) return st;
+        RVH_CUDA(cudaMemcpy(b->d_first.ptr, first.data(), sizeof(long long) * first.size(), cudaMemcpyHostToDevice));
+        RVH_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            RVH_CUDA(cudaEventCreateWithFlags(&b->packed[i], cudaEventDisableTiming));
+            RVH_CUDA(cudaEventCreateWithFlags(&b->copied[i], cudaEventDisableTiming));
+        }
+    }
+    const int slot = b->pos_slot;
+    b->pos_slot ^= 1;
+    RVH_CUDA(cudaStreamWaitEvent(s, b->copied[slot], 0));   // the copy that last read this slot is done
+    const long long total = b->n_points;
+    long long blocks = (total + kThreads - 1) / kThreads;
+    blocks = std::min<long long>(blocks, (long long)b->ctx->sm_count * 16);
+    const DevAsset* assets = static_cast<const DevAsset*>(b->d_assets.ptr);
+    const long long* first = static_cast<const long long*>(b->d_first.ptr);
+    int na = int(b->assets.size());
+    float4* out = static_cast<float4*>(b->pos_stage[slot].ptr);
+    void* args[] = {&assets, &first, &na, const_cast<long long*>(&total), &out};
+    RVH_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pack_positions), dim3(unsigned(blocks)), dim3(kThreads),
+                              args, 0, s));
+    RVH_CUDA(cudaEventRecord(b->packed[slot], s));
+    RVH_CUDA(cudaStreamWaitEvent(b->copy_stream, b->packed[slot], 0));
+    RVH_CUDA(cudaMemcpyAsync(host_dst, out, need, cudaMemcpyDeviceToHost, b->copy_stream));
+    RVH_CUDA(cudaEventRecord(b->copied[slot], b->copy_stream));
+    return RVH_OK;
+}
+
+rvh_status rvh_batch_positions_wait(rvh_batch* b) {
+    if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_positions_wait: NULL");
+    if (!b->copy_stream) return RVH_OK;
+    cudaSetDevice(b->ctx->device);
+    RVH_CUDA(cudaStreamSynchronize(b->copy_stream));
     return RVH_OK;
 }
 

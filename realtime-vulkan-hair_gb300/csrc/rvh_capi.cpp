@@ -100,13 +100,26 @@ int default_lanes(int n) {
     return 4;
 }
 
-DevAsset Asset::device_view(const rvh_frame& f, int which) const {
+int Asset::pick_grid(int avoid1, int avoid2) const {
+    int fallback = -1;
+    for (int i = 0; i < 3; ++i) {
+        if (i == avoid1 || i == avoid2) continue;
+        if (!grid_dirty[i]) return i;
+        if (fallback < 0) fallback = i;
+    }
+    return fallback;
+}
+
+DevAsset Asset::device_view(const rvh_frame& f, int g, int prev, int next) const {
     DevAsset A{};
     A.strands = static_cast<float4*>(strands.ptr);
     A.rest = static_cast<const float*>(rest.ptr);
     A.strand_wind = has_wind ? static_cast<const float4*>(wind.ptr) : nullptr;
-    A.grid = static_cast<unsigned long long*>(grid[which].ptr);
-    A.grid_next = static_cast<unsigned long long*>(grid[which ^ 1].ptr);
+    auto gp = [&](int i) { return i >= 0 ? static_cast<unsigned long long*>(grid[i].ptr) : nullptr; };
+    A.grid = gp(g);
+    A.grid_next = gp(next);
+    A.grid_prev = gp(prev);
+    A.dt_prev = dt_prev;
     A.draw = static_cast<rvh_draw_indirect*>(draw.ptr);
     A.n_strands = n_strands;
     A.n_points = n_points;
@@ -137,32 +150,59 @@ rvh_status ensure_grid(Asset* a) {
     if (!a->params.grid_enabled || a->server_managed) return RVH_OK;
     const size_t cells = size_t(a->params.grid_dims[0]) * a->params.grid_dims[1] * a->params.grid_dims[2];
     if (cells == a->grid_cells && a->grid[0].ptr) return RVH_OK;
-    a->ctx->free(a->grid[0]);
-    a->ctx->free(a->grid[1]);
+    for (int i = 0; i < 3; ++i) a->ctx->free(a->grid[i]);
     a->grid_cells = cells;
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
         rvh_status s = a->ctx->alloc(a->grid[i], a->grid_bytes());
         if (s != RVH_OK) {
-            a->ctx->free(a->grid[0]);
+            for (int j = 0; j < 3; ++j) a->ctx->free(a->grid[j]);
             a->grid_cells = 0;
             return s;
         }
         RVH_CUDA(cudaMemset(a->grid[i].ptr, 0, a->grid_bytes()));
+        a->grid_dirty[i] = false;
     }
-    a->grid_dirty[0] = a->grid_dirty[1] = false;
-    a->parity = 0;
+    a->pending = false;
+    a->last_grid = -1;
+    return RVH_OK;
+}
+
+static rvh_status launch_plain_b(Asset* a, const DevAsset& A, cudaStream_t s) {
+    const void* kb = plain_b_kernel(a->ctx->math == RVH_MATH_EXACT);
+    if (!prepare_kernel(kb)) return fail(RVH_ERR_CUDA, "cannot opt the step kernels into shared memory");
+    const long long pts = (long long)a->n_strands * a->n_points;
+    long long blocks = (pts + kTileB - 1) / kTileB;
+    const long long cap = (long long)a->ctx->sm_count * 2 * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    void* args[] = {const_cast<DevAsset*>(&A)};
+    RVH_CUDA(cudaLaunchKernel(kb, dim3(unsigned(blocks)), dim3(kThreads), args, kSmemBytes, s));
+    return RVH_OK;
+}
+
+rvh_status finish_pending(Asset* a, cudaStream_t s) {
+    if (!a->pending) return RVH_OK;
+    if (!a->grid[a->pend].ptr) return fail(RVH_ERR_STATE, "finish: the pending grid is gone");
+    rvh_frame f{};
+    f.dt = a->dt_prev;
+    const DevAsset A = a->device_view(f, a->pend);
+    rvh_status st = launch_plain_b(a, A, s);
+    if (st != RVH_OK) return st;
+    a->pending = false;
+    a->grid_dirty[a->pend] = true;
     return RVH_OK;
 }
 
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s) {
-    if (a->params.grid_enabled && !a->grid[a->parity].ptr)
+    if (a->params.grid_enabled && (!a->grid[0].ptr || !a->grid[1].ptr || !a->grid[2].ptr))
         return fail(RVH_ERR_STATE, "step: the asset's grid is held by a request server and no request is active");
     const bool exact = a->ctx->math == RVH_MATH_EXACT;
     const void* ka = plain_a_kernel(a->n_points, a->lanes, exact);
     if (!ka) return fail(RVH_ERR_UNSUPPORTED, "no phase-A kernel for this (n_points, lanes_per_strand)");
-    const void* kb = plain_b_kernel(exact);
-    if (!prepare_kernel(ka) || !prepare_kernel(kb)) return fail(RVH_ERR_CUDA, "cannot opt the step kernels into shared memory");
-    const int which = a->parity;
+    if (!prepare_kernel(ka)) return fail(RVH_ERR_CUDA, "cannot opt the step kernels into shared memory");
+    rvh_status fs = finish_pending(a, s);
+    if (fs != RVH_OK) return fs;
+    const int which = a->params.grid_enabled ? a->pick_grid(-1, -1) : -1;
     DevAsset A = a->device_view(f, which);
     if (a->params.grid_enabled) RVH_CUDA(cudaMemsetAsync(A.grid, 0, a->grid_bytes(), s));
     const int per_cta = kWarps * (32 / a->lanes);
@@ -170,13 +210,10 @@ rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s) {
     void* args[] = {&A};
     if (blocks_a > 0) RVH_CUDA(cudaLaunchKernel(ka, dim3(blocks_a), dim3(kThreads), args, kSmemBytes, s));
     if (a->params.grid_enabled) {
-        const long long pts = (long long)a->n_strands * a->n_points;
-        long long blocks = (pts + kTileB - 1) / kTileB;
-        const long long cap = (long long)a->ctx->sm_count * 2 * 8;
-        if (blocks > cap) blocks = cap;
-        if (blocks < 1) blocks = 1;
-        RVH_CUDA(cudaLaunchKernel(kb, dim3(unsigned(blocks)), dim3(kThreads), args, kSmemBytes, s));
+        rvh_status st = launch_plain_b(a, A, s);
+        if (st != RVH_OK) return st;
         a->grid_dirty[which] = true;
+        a->last_grid = which;
     }
     return RVH_OK;
 }
@@ -334,6 +371,19 @@ rvh_status rvh_context_synchronize(rvh_context* ctx) {
     if (!ctx) return fail(RVH_ERR_INVALID_ARG, "ctx is NULL");
     DeviceGuard g(ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
+    return RVH_OK;
+}
+
+rvh_status rvh_pinned_alloc(size_t bytes, void** out) {
+    if (!out) return fail(RVH_ERR_INVALID_ARG, "pinned_alloc: NULL");
+    *out = nullptr;
+    if (!bytes) return RVH_OK;
+    RVH_CUDA(cudaMallocHost(out, bytes));
+    return RVH_OK;
+}
+
+rvh_status rvh_pinned_free(void* p) {
+    if (p) RVH_CUDA(cudaFreeHost(p));
     return RVH_OK;
 }
 
@@ -498,10 +548,8 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     c->free(a->strands);
     c->free(a->rest);
     c->free(a->wind);
-    c->free(a->grid[0]);
-    c->free(a->grid[1]);
+    for (int i = 0; i < 3; ++i) c->free(a->grid[i]);
     c->free(a->draw);
-    c->free(a->positions);
     delete a;
     return RVH_OK;
 }
@@ -511,6 +559,8 @@ rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p) {
     rvh_status s = validate_params(*p);
     if (s != RVH_OK) return s;
     DeviceGuard g(a->ctx->device);
+    s = finish_pending(a, a->ctx->stream);  // the pending gather uses the old grid geometry
+    if (s != RVH_OK) return s;
     a->params = *p;
     return ensure_grid(a);
 }
@@ -588,6 +638,8 @@ rvh_status rvh_asset_read(rvh_asset* a, void* dst, size_t bytes) {
     if (!a || (!dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "asset_read: NULL argument");
     if (bytes != a->record_bytes()) return fail(RVH_ERR_INVALID_ARG, "asset_read: size must be 48*n_points*n_strands");
     DeviceGuard g(a->ctx->device);
+    rvh_status fs = finish_pending(a, a->ctx->stream);
+    if (fs != RVH_OK) return fs;
     RVH_CUDA(cudaDeviceSynchronize());
     if (bytes) RVH_CUDA(cudaMemcpy(dst, a->strands.ptr, bytes, cudaMemcpyDeviceToHost));
     return RVH_OK;
@@ -598,6 +650,7 @@ rvh_status rvh_asset_write(rvh_asset* a, const void* src, size_t bytes) {
     if (bytes != a->record_bytes()) return fail(RVH_ERR_INVALID_ARG, "asset_write: size must be 48*n_points*n_strands");
     DeviceGuard g(a->ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
+    a->pending = false;  // the new state carries no pending friction
     if (bytes) RVH_CUDA(cudaMemcpy(a->strands.ptr, src, bytes, cudaMemcpyHostToDevice));
     return RVH_OK;
 }
@@ -629,10 +682,8 @@ rvh_status rvh_asset_read_grid(rvh_asset* a, int64_t* dst, size_t bytes) {
     if (bytes != a->grid_bytes()) return fail(RVH_ERR_INVALID_ARG, "read_grid: size must be 32*cells");
     DeviceGuard g(a->ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
-    // the last step used the buffer marked dirty most recently; a plain step leaves `parity` dirty,
-    // a batched step flips parity after using it
-    const int which = a->grid_dirty[a->parity] ? a->parity : (a->parity ^ 1);
-    RVH_CUDA(cudaMemcpy(dst, a->grid[which].ptr, bytes, cudaMemcpyDeviceToHost));
+    if (a->last_grid < 0) return fail(RVH_ERR_STATE, "read_grid: no step has splatted yet");
+    RVH_CUDA(cudaMemcpy(dst, a->grid[a->last_grid].ptr, bytes, cudaMemcpyDeviceToHost));
     return RVH_OK;
 }
 

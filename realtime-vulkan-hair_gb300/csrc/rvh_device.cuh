@@ -70,8 +70,11 @@ struct DevAsset {
     float4* strands;             // n_strands records of 3*n float4 (Strand.h:11-15), updated in place
     const float* rest;           // per-strand rest segment length (compute.comp:139-140)
     const float4* strand_wind;   // optional per-strand wind (xyz), or null
-    unsigned long long* grid;    // 4 x int64 per cell {vx, vy, vz, density} for this step
-    unsigned long long* grid_next;  // the other grid buffer (cleared during a batched step)
+    unsigned long long* grid;    // 4 x int64 per cell {vx, vy, vz, density}: this step's splat target, or the
+                                 // grid a phase-B (gather-only) tile reads
+    unsigned long long* grid_next;  // the buffer a batched step clears for a later step
+    unsigned long long* grid_prev;  // fused batched step: the previous step's splat, whose gather + friction
+                                    // this pass applies before stepping (null: nothing pending)
     rvh_draw_indirect* draw;     // StrandDrawIndirect (Strand.h:53-58), or null
     int32_t n_strands;
     int32_t n_points;
@@ -83,6 +86,7 @@ struct DevAsset {
     float h;
     int32_t nx, ny, nz;
     // frame (rvh_frame)
+    float dt_prev;               // dt of the step whose friction is pending (with grid_prev)
     float dt;
     float t;
     float wind[3];
@@ -265,8 +269,8 @@ __device__ __forceinline__ CellF cell_from_sums(long long vx, long long vy, long
 }
 
 template <class M>
-__device__ __forceinline__ CellF cell_from_global(const DevAsset& A, unsigned idx) {
-    const ulonglong2* cell = reinterpret_cast<const ulonglong2*>(A.grid + 4ull * idx);
+__device__ __forceinline__ CellF cell_from_global(const DevAsset& A, const unsigned long long* grid, unsigned idx) {
+    const ulonglong2* cell = reinterpret_cast<const ulonglong2*>(grid + 4ull * idx);
     const bool wrap = A.wrap32 != 0;
     const ulonglong2 zw = __ldcg(cell + 1);
     const long long dens = grid_val(zw.y, wrap);
@@ -278,7 +282,7 @@ __device__ __forceinline__ CellF cell_from_global(const DevAsset& A, unsigned id
 // Gather + friction (+ repulsion) for one point (compute.comp:258-297);
 // cell(a, b, c) returns the CellF of corner (a, b, c).
 template <class M, class CellFn>
-__device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel, const Corners& C, CellFn cell) {
+__device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, f3 vel, const Corners& C, CellFn cell) {
     const bool rep = A.repulsion != 0.0f;
     // the trilinear weights of the (up to) two corners per axis, computed once
     float wxs[2], wys[2], wzs[2];
@@ -326,7 +330,7 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, f3 pos, f3 vel, co
     const float fr = A.friction;
     f3 out = v_add<M>(v_scale<M>(M::sub(1.0f, fr), vel), v_scale<M>(fr, gv));
     if (rep) {
-        const float coef = M::div(M::mul(A.repulsion, M::div(A.h, A.dt)), fmaxf(rho, 1.0f));
+        const float coef = M::div(M::mul(A.repulsion, M::div(A.h, dt)), fmaxf(rho, 1.0f));
         out = v_sub<M>(out, v_scale<M>(coef, grad));
     }
     return out;
@@ -350,11 +354,37 @@ struct PhaseA {
     static constexpr int K = (NMAX + L - 1) / L;
 };
 
-// Computes loops 1-2 for the lane's points, stores x', v, corr, and returns
-// the splat inputs: xo/vo for the lane's points, bit k of the result set
-// when point k is splatted (valid strand, 1 <= i < n).
+// Loads the lane's points (positions and velocities) of one strand; bit k of
+// the result is set when point k exists and is not the root.
+template <int NFIX, int L>
+__device__ __forceinline__ unsigned load_points(const DevAsset& A, int strand, bool valid,
+                                                f3 (&x)[PhaseA<NFIX, L>::K], f3 (&v)[PhaseA<NFIX, L>::K]) {
+    constexpr int K = PhaseA<NFIX, L>::K;
+    const int n = NFIX > 0 ? NFIX : A.n_points;
+    const int l = (threadIdx.x & 31) % L;
+    const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+    unsigned mask = 0u;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int i = k * L + l;
+        if (valid && i < n) {
+            x[k] = xyz(ld_cg(rec + i));
+            v[k] = xyz(ld_cg(rec + n + i));
+            if (i >= 1) mask |= 1u << k;
+        } else {
+            x[k] = f3{0.f, 0.f, 0.f};
+            v[k] = f3{0.f, 0.f, 0.f};
+        }
+    }
+    return mask;
+}
+
+// Computes loops 1-2 for the lane's points (x, v as loaded), stores x', v,
+// corr, and returns the splat inputs: xo/vo for the lane's points, bit k of
+// the result set when point k is splatted (valid strand, 1 <= i < n).
 template <int NFIX, int L, class M>
 __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand, bool valid,
+                                                   const f3 (&x)[PhaseA<NFIX, L>::K], const f3 (&vel_in)[PhaseA<NFIX, L>::K],
                                                    f3 (&xo)[PhaseA<NFIX, L>::K], f3 (&vo)[PhaseA<NFIX, L>::K]) {
     constexpr int NMAX = PhaseA<NFIX, L>::NMAX;
     constexpr int K = PhaseA<NFIX, L>::K;
@@ -365,21 +395,9 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
     const int base = lane - l;
     float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
 
-    f3 x[K], p[K], xn[K];
-    float4 vin[K];
+    f3 p[K], xn[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const int i = k * L + l;
-        if (valid && i < n) {
-            const float4 a = ld_cg(rec + i);
-            x[k] = xyz(a);
-            vin[k] = ld_cg(rec + n + i);
-        } else {
-            x[k] = f3{0.f, 0.f, 0.f};
-            vin[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        xn[k] = x[k];  // the root (i == 0) keeps its position
-    }
+    for (int k = 0; k < K; ++k) xn[k] = x[k];  // the root (i == 0) keeps its position
     const float dt = A.dt;
     const float r = valid ? A.rest[strand] : 0.f;
     f3 f0 = v_add<M>(f3{A.gravity[0], A.gravity[1], A.gravity[2]}, f3{A.wind[0], A.wind[1], A.wind[2]});
@@ -392,7 +410,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
         const int i = k * L + l;
         f3 force = f0;
         if (valid && i >= 1 && i < n) force = collide_force<M>(A, x[k], force);
-        const f3 v = xyz(vin[k]);
+        const f3 v = vel_in[k];
         // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
         p[k] = v_add<M>(v_add<M>(x[k], v_scale<M>(dt, v)), v_scale<M>(dt2, force));
     }

@@ -78,11 +78,17 @@ struct Asset {
     DevBuf strands;   // borrowed when created with RVH_MEM_DEVICE_BORROWED
     DevBuf rest;
     DevBuf wind;      // float4 per strand, or empty
-    DevBuf grid[2];   // 4 x int64 per cell, two buffers (a batched step clears the other one)
+    DevBuf grid[3];   // 4 x int64 per cell; a fused batched step gathers from one, splats into
+                      // another and clears the third
     DevBuf draw;
-    DevBuf positions; // scratch for rvh_asset_read_positions_async
-    int parity = 0;             // grid buffer the next step uses
-    bool grid_dirty[2] = {false, false};
+    bool grid_dirty[3] = {false, false, false};
+    // Fused batched steps leave the last step's gather + friction (loop 3) pending: positions
+    // are final, velocities still lack the friction blend, which the next fused step (or a
+    // finish) applies from grid[pend] with dt_prev.
+    bool pending = false;
+    int pend = 0;
+    float dt_prev = 0.f;
+    int last_grid = -1;         // grid of the most recent splat (rvh_asset_read_grid)
     size_t grid_cells = 0;
     rvh_sim_params params{};
     std::vector<rvh_collider> colliders;
@@ -91,8 +97,11 @@ struct Asset {
 
     size_t record_bytes() const { return size_t(n_strands) * 48u * size_t(n_points); }
     size_t grid_bytes() const { return grid_cells * 32u; }
-    // DevAsset for one step with frame f on grid buffer `which`.
-    DevAsset device_view(const rvh_frame& f, int which) const;
+    // DevAsset for one step with frame f: splat into / gather from grid[g], gather the pending
+    // friction from grid[prev] (or none: -1), clear grid[next] (or none: -1).
+    DevAsset device_view(const rvh_frame& f, int g, int prev = -1, int next = -1) const;
+    // A clean grid index other than the two given (-1 = none); dirty ones only if no clean one.
+    int pick_grid(int avoid1, int avoid2) const;
 };
 
 rvh_status validate_params(const rvh_sim_params& p);
@@ -101,13 +110,17 @@ DevCollider pack_collider(const rvh_collider& c);
 int default_lanes(int n_points);
 rvh_status ensure_grid(Asset* a);
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s);
+// Applies a pending friction (gather-only pass on grid[pend]); no-op when none is pending.
+rvh_status finish_pending(Asset* a, cudaStream_t s);
 
 // Batches whose asset set changes per launch (rvh_batch_host.cpp).
 struct DynBatch;
 DynBatch* dyn_batch_new(Context* ctx, int lanes, rvh_status* st);
 void dyn_batch_free(DynBatch* d);
+// modes: 0 = fused (the step's loop 3 stays pending), 1 = full step (loop 3 in the same launch)
 rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<rvh_frame>& frames,
-                            cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop, int64_t* points);
+                            const std::vector<int>& modes, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop,
+                            int64_t* points);
 rvh_status dyn_batch_check(DynBatch* d);
 int dyn_batch_ctas(const DynBatch* d);
 

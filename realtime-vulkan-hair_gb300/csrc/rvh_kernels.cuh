@@ -238,10 +238,72 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
     __syncthreads();  // every read of S and of the box is done before the next round resets them
 }
 
+// Loop 3 of the PREVIOUS step for the round's points (fused batched step):
+// gather from A.grid_prev at the positions the previous step produced and
+// blend the friction into v.  Same box scheme as phase B; every thread calls it.
+template <int K, class M>
+__device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K], f3 (&v)[K], unsigned mask,
+                                             unsigned char* smem, BoxShared& S, unsigned* stats) {
+    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+    int np = 0;
+    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        pmin = f3{fminf(pmin.x, x[k].x), fminf(pmin.y, x[k].y), fminf(pmin.z, x[k].z)};
+        pmax = f3{fmaxf(pmax.x, x[k].x), fmaxf(pmax.y, x[k].y), fmaxf(pmax.z, x[k].z)};
+        ++np;
+    }
+    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
+    box_reset(S);
+    __syncthreads();
+    box_reduce(S, lmin, lmax, 0u, np);
+    __syncthreads();
+    const int npts = S.npts;
+    const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
+    const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
+    const bool use = npts > 0 && (long long)bw * bh * bd <= kBoxCellsB;
+    float4* bf = reinterpret_cast<float4*>(smem);
+    float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
+    const unsigned long long* G = A.grid_prev;
+    const int nxny = A.nx * A.ny;
+    if (use) {
+        const int vol = bw * bh * bd;
+        const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
+        for (int c = threadIdx.x; c < vol; c += kThreads) {
+            const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
+            const int qy = (int)dw.div((unsigned)rz);
+            const CellF cf = cell_from_global<M>(A, G, (unsigned)(lo[0] + (rz - qy * bw) + (lo[1] + qy) * A.nx + (lo[2] + qz) * nxny));
+            bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
+            br[c] = cf.rcp;
+        }
+        __syncthreads();
+    }
+    if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        const Corners C = corners_of<M>(A, x[k]);
+        if (use) {
+            v[k] = gather_point<M>(A, A.dt_prev, x[k], v[k], C, [&](int a, int b, int c) {
+                const int li = (a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2]));
+                const float4 q = bf[li];
+                return CellF{q.x, q.y, q.z, q.w, br[li]};
+            });
+        } else {
+            v[k] = gather_point<M>(A, A.dt_prev, x[k], v[k], C, [&](int a, int b, int c) {
+                return cell_from_global<M>(A, G, (unsigned)(a + b * A.nx + c * nxny));
+            });
+        }
+    }
+    __syncthreads();  // the box memory is reused by the splat of this round
+}
+
 // Strands [begin, end) of one asset in rounds of kWarps * (32/L) strands; the
-// round count is the same for every warp (the box splat synchronises the CTA).
+// round count is the same for every warp (the boxes synchronise the CTA).
+// With A.grid_prev set, each round first finishes the previous step's loop 3.
 template <int NFIX, int L, class M>
-__device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, int* box, BoxShared& S,
+__device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
                                        unsigned* stats) {
     constexpr int SPW = 32 / L;
     constexpr int K = PhaseA<NFIX, L>::K;
@@ -252,21 +314,24 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, in
     for (int r = 0; r < rounds; ++r) {
         const int strand = begin + r * per_round + warp * SPW + g;
         const bool valid = g < SPW && strand < end;
+        f3 x[K], v[K];
+        const unsigned lmask = load_points<NFIX, L>(A, strand, valid, x, v);
+        if (A.grid_prev) gather_round<K, M>(A, x, v, lmask, smem, S, stats);
         f3 xo[K], vo[K];
-        const unsigned mask = strand_phase_a<NFIX, L, M>(A, strand, valid, xo, vo);
-        if (A.grid_enabled) splat_round<K, M>(A, xo, vo, mask, box, S, stats);
+        const unsigned mask = strand_phase_a<NFIX, L, M>(A, strand, valid, x, v, xo, vo);
+        if (A.grid_enabled) splat_round<K, M>(A, xo, vo, mask, reinterpret_cast<int*>(smem), S, stats);
     }
 }
 
 template <int L, class M>
-__device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end, int* box, BoxShared& S,
+__device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
                                            unsigned* stats) {
     switch (A.n_points) {
-        case 8: tile_a<8, L, M>(A, begin, end, box, S, stats); break;
-        case 16: tile_a<16, L, M>(A, begin, end, box, S, stats); break;
-        case 24: tile_a<24, L, M>(A, begin, end, box, S, stats); break;
-        case 32: tile_a<32, L, M>(A, begin, end, box, S, stats); break;
-        default: tile_a<0, L, M>(A, begin, end, box, S, stats); break;
+        case 8: tile_a<8, L, M>(A, begin, end, smem, S, stats); break;
+        case 16: tile_a<16, L, M>(A, begin, end, smem, S, stats); break;
+        case 24: tile_a<24, L, M>(A, begin, end, smem, S, stats); break;
+        case 32: tile_a<32, L, M>(A, begin, end, smem, S, stats); break;
+        default: tile_a<0, L, M>(A, begin, end, smem, S, stats); break;
     }
 }
 
@@ -320,7 +385,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
             const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
             const int qy = (int)dw.div((unsigned)rz);
             const int a = lo[0] + (rz - qy * bw), b = lo[1] + qy, cc = lo[2] + qz;
-            const CellF cf = cell_from_global<M>(A, (unsigned)(a + b * A.nx + cc * nxny));
+            const CellF cf = cell_from_global<M>(A, A.grid, (unsigned)(a + b * A.nx + cc * nxny));
             bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
             br[c] = cf.rcp;
         }
@@ -335,15 +400,15 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         const Corners C = corners_of<M>(A, x[j]);
         f3 out;
         if (use) {
-            out = gather_point<M>(A, x[j], v, C, [&](int a, int b, int c) {
+            out = gather_point<M>(A, A.dt, x[j], v, C, [&](int a, int b, int c) {
                 const int li = (a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2]));
                 const float4 q = bf[li];
                 return CellF{q.x, q.y, q.z, q.w, br[li]};
             });
         } else {
             const int nxny = A.nx * A.ny;
-            out = gather_point<M>(A, x[j], v, C, [&](int a, int b, int c) {
-                return cell_from_global<M>(A, (unsigned)(a + b * A.nx + c * nxny));
+            out = gather_point<M>(A, A.dt, x[j], v, C, [&](int a, int b, int c) {
+                return cell_from_global<M>(A, A.grid, (unsigned)(a + b * A.nx + c * nxny));
             });
         }
         st_f4(vp, out, 0.0f);
@@ -369,7 +434,7 @@ __global__ void __launch_bounds__(kThreads) k_plain_a(const __grid_constant__ De
     constexpr int SPW = 32 / L;
     const int begin = blockIdx.x * kWarps * SPW;
     const int end = min(begin + kWarps * SPW, A.n_strands);
-    tile_a<NFIX, L, M>(A, begin, end, reinterpret_cast<int*>(dsm), S, nullptr);
+    tile_a<NFIX, L, M>(A, begin, end, dsm, S, nullptr);
     if (!A.grid_enabled && blockIdx.x == 0 && threadIdx.x == 0) write_draw(A);
 }
 
@@ -410,7 +475,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ Batc
             if (threadIdx.x == 0) s_asset = w.asset;
         }
         if (w.kind == ITEM_A) {
-            tile_a_any<L, M>(A, w.begin, w.end, reinterpret_cast<int*>(dsm), S, B.stats);
+            tile_a_any<L, M>(A, w.begin, w.end, dsm, S, B.stats);
             if (!A.grid_enabled && w.begin == 0 && threadIdx.x == 0) write_draw(A);
             __syncthreads();
             if (threadIdx.x == 0) {

@@ -165,7 +165,8 @@ rvh_status rvh_server_destroy(rvh_server* s) {
     for (auto& e : s->events) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     for (Character& c : s->chars) {
         Asset* a = c.asset;
-        a->grid[0] = a->grid[1] = DevBuf{};
+        a->grid[0] = a->grid[1] = a->grid[2] = DevBuf{};
+        a->pending = false;
         a->server_managed = false;
         ensure_grid(a);  // hand the asset back with grids of its own
     }
@@ -186,8 +187,10 @@ rvh_status rvh_server_add_character(rvh_server* s, rvh_asset* a, const rvh_wind_
     cudaSetDevice(s->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(s->ctx->stream));
     // the grids become per-request scratch lent from the server's pool
-    s->ctx->free(a->grid[0]);
-    s->ctx->free(a->grid[1]);
+    rvh_status fs = finish_pending(a, s->ctx->stream);
+    if (fs != RVH_OK) return fs;
+    RVH_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    for (int g = 0; g < 3; ++g) s->ctx->free(a->grid[g]);
     a->server_managed = true;
     Character c;
     c.asset = a;
@@ -266,7 +269,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
                 if (active[k].req == r) {
                     if (active[k].bytes) s->pool.give(active[k].off, active[k].bytes);
                     Asset* a = s->chars[reqs[r].character].asset;
-                    a->grid[0] = a->grid[1] = DevBuf{};
+                    a->grid[0] = a->grid[1] = a->grid[2] = DevBuf{};
                     s->chars[reqs[r].character].busy = false;
                     active.erase(active.begin() + k);
                     break;
@@ -298,21 +301,23 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             Asset* a = ch.asset;
             if (a->params.grid_enabled) {
                 const size_t gb = a->grid_bytes();
-                const size_t pair = 2 * ((gb + 255) & ~size_t(255));
+                const size_t one = (gb + 255) & ~size_t(255);
                 size_t off = 0;
-                if (!s->pool.take(pair, &off)) {  // wait for memory; later requests may still fit
+                if (!s->pool.take(3 * one, &off)) {  // wait for memory; later requests may still fit
                     ++admission_waits;
                     ++it;
                     continue;
                 }
                 ac.off = off;
-                ac.bytes = pair;
+                ac.bytes = 3 * one;
                 char* base = static_cast<char*>(s->slab.ptr) + off;
-                a->grid[0] = DevBuf{base, gb, s->ctx, false};
-                a->grid[1] = DevBuf{base + pair / 2, gb, s->ctx, false};
-                cudaMemsetAsync(base, 0, pair, stream);
-                a->parity = 0;
-                a->grid_dirty[0] = a->grid_dirty[1] = false;
+                for (int g = 0; g < 3; ++g) {
+                    a->grid[g] = DevBuf{base + g * one, gb, s->ctx, false};
+                    a->grid_dirty[g] = false;
+                }
+                cudaMemsetAsync(base, 0, 3 * one, stream);
+                a->pending = false;
+                a->last_grid = -1;
             }
             ch.busy = true;
             results[r].admit_s = t;
@@ -324,6 +329,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         // launch one step of every admitted request that still has steps to enqueue
         std::vector<Asset*> la;
         std::vector<rvh_frame> lf;
+        std::vector<int> lm;   // fused steps, except each request's last step, which is run in full
         Launch L;
         for (Active& ac : active) {
             if (ac.remaining == 0) continue;
@@ -334,13 +340,14 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             if (ch.has_wind) rvh_wind_at(&ch.wind, ch.steps, f.t, f.wind);
             la.push_back(ch.asset);
             lf.push_back(f);
+            lm.push_back(ac.remaining == 1 ? 1 : 0);
             L.reqs.push_back(ac.req);
             if (ac.remaining == 1) L.last.push_back(ac.req);
         }
         if (!la.empty() && int(flight.size()) < s->desc.pipeline_depth) {
             L.start = get_ev();
             L.stop = get_ev();
-            err = dyn_batch_launch(s->batch, la, lf, stream, L.start, L.stop, &L.points);
+            err = dyn_batch_launch(s->batch, la, lf, lm, stream, L.start, L.stop, &L.points);
             if (err != RVH_OK) break;
             for (Active& ac : active)
                 if (ac.remaining > 0) {
@@ -381,7 +388,8 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
     for (Active& ac : active) {   // only after an error
         if (ac.bytes) s->pool.give(ac.off, ac.bytes);
         Asset* a = s->chars[reqs[ac.req].character].asset;
-        a->grid[0] = a->grid[1] = DevBuf{};
+        a->grid[0] = a->grid[1] = a->grid[2] = DevBuf{};
+        a->pending = false;
         s->chars[reqs[ac.req].character].busy = false;
     }
     for (cudaEvent_t e : free_ev) cudaEventDestroy(e);

@@ -116,7 +116,7 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
             for (int ti = 0; ti < 3 && st == RVH_OK; ++ti) {
                 const int lanes = lanes_c[li];
                 const int tile = tile_c[ti] * kWarps * (32 / lanes);
-                rvh_batch_desc bd{lanes, tile, 0, 1};
+                rvh_batch_desc bd{lanes, tile, 0, 1, 0, 0};
                 rvh_batch* b = nullptr;
                 st = rvh_batch_create(ctx, assets, n, &bd, &b);
                 if (st != RVH_OK) break;

@@ -24,6 +24,8 @@ PROTOTYPES = [
     ("rvh_context_create", _st, [_vp, _P(_vp)]),
     ("rvh_context_destroy", _st, [_vp]),
     ("rvh_context_synchronize", _st, [_vp]),
+    ("rvh_pinned_alloc", _st, [C.c_size_t, _P(_vp)]),
+    ("rvh_pinned_free", _st, [_vp]),
     ("rvh_context_memory", _st, [_vp, _P(C.c_uint64), _P(C.c_uint64)]),
     ("rvh_sim_params_reference", _st, [_P(T.SimParams)]),
     ("rvh_collider_from_trs", _st, [_P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32, C.c_float,
@@ -50,7 +52,10 @@ PROTOTYPES = [
     ("rvh_batch_destroy", _st, [_vp]),
     ("rvh_batch_step", _st, [_vp, _P(T.Frame), _vp]),
     ("rvh_batch_check", _st, [_vp]),
+    ("rvh_batch_finish", _st, [_vp, _vp]),
     ("rvh_batch_info", _st, [_vp, _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_int64)]),
+    ("rvh_batch_read_positions_async", _st, [_vp, _vp, C.c_size_t, _vp]),
+    ("rvh_batch_positions_wait", _st, [_vp]),
     ("rvh_batch_box_stats", _st, [_vp, _P(C.c_uint32)]),
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_batch_timing_enable", _st, [_vp, C.c_int32]),

@@ -23,7 +23,7 @@ class AssetDesc(C.Structure):
 
 class BatchDesc(C.Structure):
     _fields_ = [("lanes_per_strand", C.c_int32), ("strands_per_tile", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("use_graph", C.c_int32)]
+                ("use_graph", C.c_int32), ("full_steps", C.c_int32), ("reserved", C.c_int32)]
 
 
 class HeadDesc(C.Structure):
@@ -111,6 +111,25 @@ def _f32(a):
 
 def _fp(a):
     return None if a is None else a.ctypes.data_as(_P(C.c_float))
+
+
+class PinnedBuffer:
+    """Page-locked host memory from the library (for asynchronous copies)."""
+
+    def __init__(self, nbytes):
+        self.lib = load()
+        p = C.c_void_p()
+        check(self.lib.rvh_pinned_alloc(nbytes, C.byref(p)))
+        self.ptr, self.nbytes = p.value, nbytes
+
+    def array(self, shape, dtype=np.float32):
+        buf = (C.c_char * self.nbytes).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def close(self):
+        if self.ptr:
+            self.lib.rvh_pinned_free(C.c_void_p(self.ptr))
+            self.ptr = None
 
 
 class Context:
@@ -238,12 +257,12 @@ class Asset:
 
 
 class Batch:
-    def __init__(self, ctx, assets, lanes=0, strands_per_tile=0, ctas_per_sm=0, use_graph=True):
+    def __init__(self, ctx, assets, lanes=0, strands_per_tile=0, ctas_per_sm=0, use_graph=True, full_steps=False):
         self.ctx = ctx
         self.lib = ctx.lib
         self.assets = list(assets)
         arr = (C.c_void_p * max(1, len(self.assets)))(*[a.h.value for a in self.assets])
-        d = BatchDesc(lanes, strands_per_tile, ctas_per_sm, 1 if use_graph else 0)
+        d = BatchDesc(lanes, strands_per_tile, ctas_per_sm, 1 if use_graph else 0, 1 if full_steps else 0, 0)
         h = C.c_void_p()
         check(self.lib.rvh_batch_create(ctx.h, arr, len(self.assets), C.byref(d), C.byref(h)))
         self.h = h
@@ -259,6 +278,15 @@ class Batch:
 
     def check(self):
         check(self.lib.rvh_batch_check(self.h))
+
+    def finish(self, stream=None):
+        check(self.lib.rvh_batch_finish(self.h, stream))
+
+    def read_positions_async(self, host_ptr, nbytes, stream=None):
+        check(self.lib.rvh_batch_read_positions_async(self.h, C.c_void_p(host_ptr), nbytes, stream))
+
+    def positions_wait(self):
+        check(self.lib.rvh_batch_positions_wait(self.h))
 
     def box_stats(self):
         out = (C.c_uint32 * 4)()
