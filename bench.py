@@ -249,6 +249,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
@@ -267,10 +268,17 @@ def main():
     specs = shard(all_specs, rank, world)
     ctx = api.Context(device=dev, math=api.MATH_FAST)
     assets = make_assets(ctx, specs)
+    frames = [[s.frame(k) for s in specs] for k in range(args.warmup + args.steps)]
+    tuned = None
+    if args.lanes == 0 and not args.no_tune:
+        t0 = time.perf_counter()
+        tr = api.tune(ctx, assets, frames[0], steps=2)
+        tuned = {"lanes_per_strand": tr.lanes_per_strand, "strands_per_tile": tr.strands_per_tile,
+                 "best_ms": tr.best_ms, "seconds": time.perf_counter() - t0,
+                 "tried": [{"lanes": l, "tile": t, "ms": round(m, 3)} for l, t, _, m in tr.table()]}
     batch = api.Batch(ctx, assets, lanes=args.lanes)
     info = batch.info()
     alg_bytes, pts, cells = algorithmic_bytes(specs)
-    frames = [[s.frame(k) for s in specs] for k in range(args.warmup + args.steps)]
 
     # ---- batched step, device time ----
     for k in range(args.warmup):
@@ -304,6 +312,12 @@ def main():
         ms, _ = batch.read_timing()
         lat.append(ms)
     batch.timing(False)
+    # the last fused step's pending gather + friction, applied once at the end of a run
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    batch.finish()
+    ctx.synchronize()
+    finish_ms = (time.perf_counter() - t0) * 1e3
 
     # ---- plain step: one launch sequence per asset, no graph ----
     plain_value, plain_ms = None, None
@@ -322,29 +336,30 @@ def main():
         plain_value = total_pts / (plain_ms * 1e-3)
 
     # ---- e2e through the C ABI with host buffers ----
-    pos_bufs = [np.empty((s.n_strands, s.n_points, 4), np.float32) for s in specs]
-    import ctypes as C
-    from rvh._lib import check as _check
-    lib = ctx.lib
-    pin = []
-    try:
-        import torch
-        pin = [torch.empty(b.nbytes, dtype=torch.uint8).pin_memory() for b in pos_bufs]
-        ptrs = [p.data_ptr() for p in pin]
-    except Exception:
-        ptrs = [b.ctypes.data for b in pos_bufs]
-    d2h = sum(b.nbytes for b in pos_bufs)
+    # every step: frame tables host->device (inside rvh_batch_step) and every
+    # curve point's position device->host (packed on the device, copied on a
+    # second stream so the copy of step k overlaps step k+1)
+    pos_bytes = pts * 16
+    pinned = [api.PinnedBuffer(pos_bytes) for _ in range(2)]
     h2d = batch.h2d_bytes_per_step()
     ne2e = max(3, min(args.steps, 10))
+    for k in range(2):
+        batch.step(frames[k])
+        batch.read_positions_async(pinned[k % 2].ptr, pos_bytes)
+    batch.positions_wait()
+    ctx.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for k in range(ne2e):
         batch.step(frames[k])
-        for a, p, b in zip(assets, ptrs, pos_bufs):
-            _check(lib.rvh_asset_read_positions_async(a.h, C.c_void_p(p), b.nbytes, None))
+        batch.read_positions_async(pinned[k % 2].ptr, pos_bytes)
+    batch.positions_wait()
     ctx.synchronize()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / ne2e, world)
     e2e_value = total_pts / (e2e_ms * 1e-3)
+    d2h = pos_bytes
+    for p_ in pinned:
+        p_.close()
 
     # ---- CPU baseline on a bounded sample (rank 0, N=1 only) ----
     cpu = None
@@ -380,6 +395,7 @@ def main():
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (pts * 48 / 1e9),
                        "math": "fast"},
             "p50_step_ms": lat_sorted[len(lat_sorted) // 2], "p99_step_ms": lat_sorted[-1],
+            "finish_ms": finish_ms, "tuner": tuned,
             "plain": {"value": plain_value, "ms_per_step": plain_ms,
                       "speedup_batched_vs_plain": (value / plain_value) if plain_value else None},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

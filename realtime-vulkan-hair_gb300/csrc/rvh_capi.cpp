@@ -1,5 +1,6 @@
 // rvh_capi.cpp — context, assets, parameter helpers and the plain per-asset
 // step of the C ABI declared in include/rvh.h.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -85,6 +86,28 @@ DevCollider pack_collider(const rvh_collider& c) {
     d.kind = c.kind;
     d.radius = c.radius;
     for (int r = 0; r < 3; ++r) d.c[r] = c.transform[12 + r];
+    if (c.kind == RVH_COLLIDER_ELLIPSOID) {
+        // local = inv * (p, 1) with |local| <= 1 means p = T * (local, 1): |p - centre| <= |M local| <=
+        // max column norm of M times sqrt(3) in general; for T = translate * rotate * scale (Scene.h:35)
+        // the columns are orthogonal and the largest column norm bounds it.  The margin covers the
+        // FP32 inverse and a non-orthogonal M (Frobenius norm bound).
+        double fro = 0.0, colmax = 0.0;
+        for (int col = 0; col < 3; ++col) {
+            double n2 = 0.0;
+            for (int r = 0; r < 3; ++r) n2 += double(c.transform[col * 4 + r]) * double(c.transform[col * 4 + r]);
+            fro += n2;
+            colmax = std::max(colmax, std::sqrt(n2));
+        }
+        double dots = 0.0;  // orthogonality of the columns
+        for (int i = 0; i < 3; ++i)
+            for (int j = i + 1; j < 3; ++j) {
+                double dd = 0.0;
+                for (int r = 0; r < 3; ++r) dd += double(c.transform[i * 4 + r]) * double(c.transform[j * 4 + r]);
+                dots = std::max(dots, std::fabs(dd));
+            }
+        const double bound = (dots <= 1e-5 * fro) ? colmax : std::sqrt(fro);
+        d.radius = float(bound * 1.001 + 1e-6);
+    }
     for (int col = 0; col < 4; ++col)
         for (int r = 0; r < 3; ++r) {
             d.inv[col * 3 + r] = c.inv[col * 4 + r];

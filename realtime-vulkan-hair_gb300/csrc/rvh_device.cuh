@@ -58,8 +58,9 @@ struct FastMath {
 // src/Scene.h:23-27) into the 3x4 / 3x3 blocks the shader reads.
 struct DevCollider {
     int32_t kind;
-    float radius;
-    float c[3];      // sphere centre: transform[3].xyz (compute.comp:162)
+    float radius;    // sphere: its radius; ellipsoid: a bounding-sphere radius (largest column of
+                     // the transform's 3x3, enlarged by 1e-3) used only to skip far points
+    float c[3];      // centre: transform[3].xyz (compute.comp:162)
     float inv[12];   // inv, columns 0..3, rows xyz: local = inv * (p, 1) (compute.comp:65)
     float itr[9];    // invTrans, columns 0..2, rows xyz: n = invTrans * (q, 0) (compute.comp:72)
     float xf[12];    // transform, columns 0..3, rows xyz (compute.comp:78)
@@ -157,6 +158,9 @@ __device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
                 ++cnt;
             }
         } else {
+            // outside the bounding sphere: the exact test below would fail too
+            const f3 e = v_sub<M>(x, f3{c.c[0], c.c[1], c.c[2]});
+            if (v_dot<M>(e, e) > c.radius * c.radius) continue;
             const f3 q = mat_p1<M>(c.inv, x);
             const float q2 = v_dot<M>(q, q);
             if (q2 > 1.00001f) continue;   // clearly outside (sqrt(q2) > 1)

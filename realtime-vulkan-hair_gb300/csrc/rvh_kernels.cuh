@@ -133,33 +133,49 @@ __device__ __forceinline__ void bounds_of_extremes(const DevAsset& A, f3 pmin, f
 }
 
 // Splat one point into the shared box (int32 partial sums).
+// The box is laid out as four arrays (vx, vy, vz, density) of `vol` cells, so
+// one component's atomics from a warp spread over all 32 banks.  The six
+// trilinear weights of a point are computed once.  Exact math keeps the
+// oracle's int(scale * (w * v)); fast math shares scale * w.
 template <class M>
 __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const int (&lo)[3],
-                                                int bw, int bh) {
+                                                int bw, int bh, int vol) {
+    float wx[2], wy[2], wz[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        wx[d] = tri_w<M>(C.g[0], C.lo[0] + d);
+        wy[d] = tri_w<M>(C.g[1], C.lo[1] + d);
+        wz[d] = tri_w<M>(C.g[2], C.lo[2] + d);
+    }
+    int* const b0 = box + ((C.lo[0] - lo[0]) + bw * ((C.lo[1] - lo[1]) + bh * (C.lo[2] - lo[2])));
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
         if (da >= C.cnt[0]) continue;
-        const int a = C.lo[0] + da;
-        const float wx = tri_w<M>(C.g[0], a);
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
             if (db >= C.cnt[1]) continue;
-            const int b = C.lo[1] + db;
-            const float wxy = M::mul(wx, tri_w<M>(C.g[1], b));
+            const float wxy = M::mul(wx[da], wy[db]);
 #pragma unroll
             for (int dc = 0; dc < 2; ++dc) {
                 if (dc >= C.cnt[2]) continue;
-                const int c = C.lo[2] + dc;
-                const float w = M::mul(wxy, tri_w<M>(C.g[2], c));
-                int* cell = box + 4 * ((a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2])));
-                const int q0 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.x)));
-                const int q1 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.y)));
-                const int q2 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.z)));
+                const float w = M::mul(wxy, wz[dc]);
+                int* cell = b0 + (da + bw * (db + bh * dc));
+                int q0, q1, q2;
+                if (M::kExact) {
+                    q0 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.x)));
+                    q1 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.y)));
+                    q2 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.z)));
+                } else {
+                    const float sw = A.scale * w;
+                    q0 = __float2int_rz(sw * vel.x);
+                    q1 = __float2int_rz(sw * vel.y);
+                    q2 = __float2int_rz(sw * vel.z);
+                }
                 const int q3 = __float2int_rz(M::mul(A.scale, w));
-                if (q0) atomicAdd(cell + 0, q0);
-                if (q1) atomicAdd(cell + 1, q1);
-                if (q2) atomicAdd(cell + 2, q2);
-                if (q3) atomicAdd(cell + 3, q3);
+                if (q0) atomicAdd(cell, q0);
+                if (q1) atomicAdd(cell + vol, q1);
+                if (q2) atomicAdd(cell + 2 * vol, q2);
+                if (q3) atomicAdd(cell + 3 * vol, q3);
             }
         }
     }
@@ -196,26 +212,28 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
         bool use = vol <= kBoxCellsA && (float)npts * A.scale < 2.0e9f;
         if (use) {
             const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
+            const int nv = (int)vol;
             int4* b4 = reinterpret_cast<int4*>(box);
-            for (int c = threadIdx.x; c < (int)vol; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
+            const int n4 = (4 * nv + 3) / 4;
+            for (int c = threadIdx.x; c < n4; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 if (!((mask >> k) & 1u)) continue;
                 const Corners C = corners_of<M>(A, xo[k]);
-                splat_point_box<M>(A, C, vo[k], box, lo, bw, bh);
+                splat_point_box<M>(A, C, vo[k], box, lo, bw, bh, nv);
             }
             __syncthreads();
             const float vmax = __uint_as_float(S.vabs);
             bool ok = true;
-            for (int c = threadIdx.x; c < (int)vol; c += kThreads)
-                ok = ok && vmax * ((float)box[4 * c + 3] + (float)npts) < 2.0e9f;
+            for (int c = threadIdx.x; c < nv; c += kThreads)
+                ok = ok && vmax * ((float)box[3 * nv + c] + (float)npts) < 2.0e9f;
             use = __syncthreads_and(ok);
             if (use) {
                 const int nxny = A.nx * A.ny;
                 const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
-                for (int c = threadIdx.x; c < (int)vol; c += kThreads) {
-                    const int4 v = b4[c];
+                for (int c = threadIdx.x; c < nv; c += kThreads) {
+                    const int4 v = make_int4(box[c], box[nv + c], box[2 * nv + c], box[3 * nv + c]);
                     if (!(v.x | v.y | v.z | v.w)) continue;
                     const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
                     const int qy = (int)dw.div((unsigned)rz);
