@@ -80,9 +80,13 @@ void plan(Batch& b, int strands_per_tile) {
     const int quantum = kWarps * S;
     std::vector<int> order(b.assets.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
+    // grouped by points per strand (CTAs then mostly run one unrolled code path at a time),
+    // largest assets first inside a group
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return int64_t(b.assets[x]->n_strands) * b.assets[x]->n_points >
-               int64_t(b.assets[y]->n_strands) * b.assets[y]->n_points;
+        const Asset* ax = b.assets[x];
+        const Asset* ay = b.assets[y];
+        if (ax->n_points != ay->n_points) return ax->n_points > ay->n_points;
+        return int64_t(ax->n_strands) * ax->n_points > int64_t(ay->n_strands) * ay->n_points;
     });
     b.items.clear();
     b.need_a.assign(b.assets.size(), 0u);

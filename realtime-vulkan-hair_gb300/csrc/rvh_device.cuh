@@ -216,6 +216,25 @@ __device__ __forceinline__ long long fixed_of(float scale_times_x) {
     return (long long)__float2int_rz(scale_times_x);
 }
 
+// The four fixed-point contributions of one point to one corner, int(SCALE * w * v)
+// (compute.comp:245-248).  Exact math keeps the oracle's scale * (w * v); fast
+// math shares scale * w.  Every splat path calls this, so the box and the
+// direct-atomic paths add identical integers.
+template <class M>
+__device__ __forceinline__ void corner_contribs(float scale, float w, f3 vel, int& q0, int& q1, int& q2, int& q3) {
+    if (M::kExact) {
+        q0 = __float2int_rz(M::mul(scale, M::mul(w, vel.x)));
+        q1 = __float2int_rz(M::mul(scale, M::mul(w, vel.y)));
+        q2 = __float2int_rz(M::mul(scale, M::mul(w, vel.z)));
+    } else {
+        const float sw = scale * w;
+        q0 = __float2int_rz(sw * vel.x);
+        q1 = __float2int_rz(sw * vel.y);
+        q2 = __float2int_rz(sw * vel.z);
+    }
+    q3 = __float2int_rz(M::mul(scale, w));
+}
+
 __device__ __forceinline__ void red_add_s64(unsigned long long* p, long long v) {
     if (v != 0) atomicAdd(p, (unsigned long long)v);
 }
@@ -242,10 +261,12 @@ __device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel) {
                 const int c = C.lo[2] + dc;
                 const float w = M::mul(wxy, tri_w<M>(C.g[2], c));
                 unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + c * nxny);
-                red_add_s64(cell + 0, fixed_of(M::mul(A.scale, M::mul(w, vel.x))));
-                red_add_s64(cell + 1, fixed_of(M::mul(A.scale, M::mul(w, vel.y))));
-                red_add_s64(cell + 2, fixed_of(M::mul(A.scale, M::mul(w, vel.z))));
-                red_add_s64(cell + 3, fixed_of(M::mul(A.scale, w)));
+                int q0, q1, q2, q3;
+                corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
+                red_add_s64(cell + 0, q0);
+                red_add_s64(cell + 1, q1);
+                red_add_s64(cell + 2, q2);
+                red_add_s64(cell + 3, q3);
             }
         }
     }

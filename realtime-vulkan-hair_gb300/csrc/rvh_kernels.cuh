@@ -160,18 +160,8 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
                 if (dc >= C.cnt[2]) continue;
                 const float w = M::mul(wxy, wz[dc]);
                 int* cell = b0 + (da + bw * (db + bh * dc));
-                int q0, q1, q2;
-                if (M::kExact) {
-                    q0 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.x)));
-                    q1 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.y)));
-                    q2 = __float2int_rz(M::mul(A.scale, M::mul(w, vel.z)));
-                } else {
-                    const float sw = A.scale * w;
-                    q0 = __float2int_rz(sw * vel.x);
-                    q1 = __float2int_rz(sw * vel.y);
-                    q2 = __float2int_rz(sw * vel.z);
-                }
-                const int q3 = __float2int_rz(M::mul(A.scale, w));
+                int q0, q1, q2, q3;
+                corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
                 if (q0) atomicAdd(cell, q0);
                 if (q1) atomicAdd(cell + vol, q1);
                 if (q2) atomicAdd(cell + 2 * vol, q2);
