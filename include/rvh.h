@@ -118,6 +118,35 @@ rvh_status rvh_asset_read_grid(rvh_asset* a, int64_t* host_dst, size_t bytes);
  * Plain path: one launch sequence per call, no graph. */
 rvh_status rvh_step(rvh_asset* a, const rvh_frame* frame, void* stream);
 
+/* ---- the plain step without device allocations ------------------------------
+ * No counterpart in the reference.  For callers that cannot let the library
+ * allocate device memory (a frame loop where a cudaMalloc could stall the
+ * device, or a host application whose own allocator owns all GPU memory):
+ * the caller passes every buffer, and the step's only scratch, the hair-hair
+ * grid, lives in a static device array of RVH_NOALLOC_MAX_GRID_CELLS cells
+ * (8 MiB per GPU that loads the library, held until exit).  Larger grids are
+ * rejected with RVH_ERR_INVALID_ARG.  Each call clears the grid cells it
+ * uses; calls on one device whose work overlaps on the GPU race on the shared
+ * array.  The first call on a device looks up the array's address and should
+ * come before any stream capture.  Same results as rvh_step on an asset with
+ * the same state, params, colliders and math mode. */
+#define RVH_NOALLOC_MAX_GRID_CELLS (64 * 64 * 64)
+typedef struct rvh_noalloc_step_desc {
+    void* strands;                /* device: n_strands Strand records, updated in place */
+    const float* rest_lengths;    /* device: n_strands floats */
+    const float* strand_wind;     /* device: 4 floats per strand (xyz used), or NULL */
+    void* draw_indirect;          /* device: one rvh_draw_indirect to write, or NULL */
+    int32_t n_strands;
+    int32_t n_points;
+    int32_t lanes_per_strand;     /* 0 = default */
+    int32_t math;                 /* RVH_MATH_FAST or RVH_MATH_EXACT */
+    const rvh_sim_params* params; /* host */
+    const rvh_collider* colliders;/* host, n_colliders entries */
+    int32_t n_colliders;
+    int32_t reserved;
+} rvh_noalloc_step_desc;
+rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* desc, const rvh_frame* frame, void* stream);
+
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
     int32_t lanes_per_strand;     /* 0 = tuner's choice; else 4, 8, 16, 32 */

@@ -48,6 +48,7 @@ PROTOTYPES = [
     ("rvh_asset_read_draw", _st, [_vp, _P(T.DrawIndirect)]),
     ("rvh_asset_read_grid", _st, [_vp, _P(C.c_int64), C.c_size_t]),
     ("rvh_step", _st, [_vp, _P(T.Frame), _vp]),
+    ("rvh_step_noalloc", _st, [_vp, _P(T.Frame), _vp]),
     ("rvh_batch_create", _st, [_vp, _P(_vp), C.c_int32, _vp, _P(_vp)]),
     ("rvh_batch_destroy", _st, [_vp]),
     ("rvh_batch_step", _st, [_vp, _P(T.Frame), _vp]),
