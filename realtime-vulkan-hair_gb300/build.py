@@ -2,7 +2,9 @@
 
 Every source in csrc/ is compiled as CUDA (`-x cu`, one -gencode, -lineinfo)
 in parallel and linked into rvh/_build/librvh.so with the static CUDA
-runtime.  Rebuilds only when a source or header is newer than the library.
+runtime.  The two kernel-instantiation files are compiled once per kernel
+variant (PARTS), so no single translation unit holds every kernel.  Rebuilds
+only when a source or header is newer than the library.
 """
 import concurrent.futures as cf
 import glob
@@ -19,6 +21,15 @@ LIB = os.path.join(OUT_DIR, "librvh.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", INCLUDE]
+
+
+# source -> [(object suffix, defines)]: one translation unit per kernel variant
+PARTS = {
+    "rvh_batch.cu": [("_L%d_%s" % (lanes, "exact" if e else "fast"), ["-DRVH_LANES=%d" % lanes, "-DRVH_EXACT=%d" % e])
+                     for lanes in (4, 8, 16, 32) for e in (0, 1)],
+    "rvh_plain.cu": [("_N%d_%s" % (n, "exact" if e else "fast"), ["-DRVH_NFIX=%d" % n, "-DRVH_EXACT=%d" % e])
+                     for n in (0, 8, 10, 16, 24, 32) for e in (0, 1)],
+}
 
 
 def nvcc():
@@ -40,8 +51,18 @@ def headers():
             glob.glob(os.path.join(CSRC, "*.hpp")) + glob.glob(os.path.join(INCLUDE, "*.h")))
 
 
-def _compile(src, obj, verbose):
-    cmd = [nvcc(), "-x", "cu"] + ARCH + FLAGS + ["-c", src, "-o", obj]
+def units():
+    """(source, object basename, extra defines) of every translation unit."""
+    out = []
+    for s in sources():
+        b = os.path.basename(s)
+        for suffix, defs in PARTS.get(b, [("", [])]):
+            out.append((s, b + suffix + ".o", defs))
+    return out
+
+
+def _compile(src, obj, defs, verbose):
+    cmd = [nvcc(), "-x", "cu"] + ARCH + FLAGS + defs + ["-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,14 +82,14 @@ def build(force=False, verbose=False, jobs=None):
     hdr_t = max(os.path.getmtime(h) for h in headers() + [__file__])
     todo = []
     objs = []
-    for s in srcs:
-        o = os.path.join(obj_dir, os.path.basename(s) + ".o")
+    for s, ob, defs in units():
+        o = os.path.join(obj_dir, ob)
         objs.append(o)
         if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr_t):
-            todo.append((s, o))
+            todo.append((s, o, defs))
     jobs = jobs or min(len(todo) or 1, os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
-        for f in [ex.submit(_compile, s, o, verbose) for s, o in todo]:
+        for f in [ex.submit(_compile, s, o, d, verbose) for s, o, d in todo]:
             f.result()
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"]

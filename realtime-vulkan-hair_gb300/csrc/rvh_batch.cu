@@ -1,20 +1,29 @@
 // rvh_batch.cu — instantiations of the persistent batch kernel.
+//
+// The build compiles this file once per (lanes per strand, math mode) with
+// -DRVH_LANES=L -DRVH_EXACT=0|1, so the eight kernels compile in parallel;
+// compiled without them it instantiates all eight.
+#include <type_traits>
+
 #include "rvh_kernels.cuh"
 #include "rvh_registry.h"
 
 namespace rvh {
 
-const void* batch_kernel(int lanes, bool exact) {
-    switch (lanes) {
-#define RVH_CASE(LL)                                                                    \
-    case LL:                                                                            \
-        return exact ? reinterpret_cast<const void*>(&k_batch<LL, ExactMath>)           \
-                     : reinterpret_cast<const void*>(&k_batch<LL, FastMath>);
-        RVH_CASE(4) RVH_CASE(8) RVH_CASE(16) RVH_CASE(32)
-#undef RVH_CASE
-        default: return nullptr;
+#define RVH_BATCH_INST(LL, E)                                                                  \
+    template <>                                                                                \
+    const void* batch_kernel_inst<LL, E>() {                                                   \
+        using Math = std::conditional_t<E, ExactMath, FastMath>;                               \
+        return reinterpret_cast<const void*>(&k_batch<LL, Math>);                              \
     }
-}
-bool batch_supported(int lanes) { return batch_kernel(lanes, false) != nullptr; }
+
+#if defined(RVH_LANES)
+RVH_BATCH_INST(RVH_LANES, (RVH_EXACT != 0))
+#else
+RVH_BATCH_INST(4, false) RVH_BATCH_INST(4, true)
+RVH_BATCH_INST(8, false) RVH_BATCH_INST(8, true)
+RVH_BATCH_INST(16, false) RVH_BATCH_INST(16, true)
+RVH_BATCH_INST(32, false) RVH_BATCH_INST(32, true)
+#endif
 
 }  // namespace rvh

@@ -1,6 +1,9 @@
-// rvh_plain.cu — instantiations of the per-asset phase-A / phase-B kernels.
-#include <mutex>
-#include <set>
+// rvh_plain.cu — instantiations of the per-asset phase-A kernels.
+//
+// The build compiles this file once per (fixed point count, math mode) with
+// -DRVH_NFIX=N -DRVH_EXACT=0|1 (N = 0: any point count), so the kernels
+// compile in parallel; compiled without them it instantiates all of them.
+#include <type_traits>
 
 #include "rvh_kernels.cuh"
 #include "rvh_registry.h"
@@ -8,6 +11,8 @@
 namespace rvh {
 
 namespace {
+// Lanes per strand a phase-A kernel exists for: at most 10 points per lane and
+// at most two lanes per point.
 template <int NFIX, class M>
 const void* pick_a(int lanes) {
     constexpr int NMAX = NFIX > 0 ? NFIX : RVH_MAX_POINTS;
@@ -22,39 +27,23 @@ const void* pick_a(int lanes) {
         default: return nullptr;
     }
 }
-
-template <class M>
-const void* pick_n(int n, int lanes) {
-    switch (n) {
-        case 8: return pick_a<8, M>(lanes);
-        case 10: return pick_a<10, M>(lanes);
-        case 16: return pick_a<16, M>(lanes);
-        case 24: return pick_a<24, M>(lanes);
-        case 32: return pick_a<32, M>(lanes);
-        default: return (n >= RVH_MIN_POINTS && n <= RVH_MAX_POINTS) ? pick_a<0, M>(lanes) : nullptr;
-    }
-}
 }  // namespace
 
-bool prepare_kernel(const void* fn) {
-    static std::mutex mu;
-    static std::set<const void*> done;
-    std::lock_guard<std::mutex> g(mu);
-    if (!fn) return false;
-    if (done.count(fn)) return true;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) != cudaSuccess)
-        return false;
-    done.insert(fn);
-    return true;
-}
+#define RVH_PLAIN_INST(N, E)                                                                   \
+    template <>                                                                                \
+    const void* plain_a_inst<N, E>(int lanes) {                                                \
+        return pick_a<N, std::conditional_t<E, ExactMath, FastMath>>(lanes);                   \
+    }
 
-const void* plain_a_kernel(int n, int lanes, bool exact) {
-    return exact ? pick_n<ExactMath>(n, lanes) : pick_n<FastMath>(n, lanes);
-}
-bool plain_a_supported(int n, int lanes) { return plain_a_kernel(n, lanes, false) != nullptr; }
-const void* plain_b_kernel(bool exact) {
-    return exact ? reinterpret_cast<const void*>(&k_plain_b<ExactMath>)
-                 : reinterpret_cast<const void*>(&k_plain_b<FastMath>);
-}
+#if defined(RVH_NFIX)
+RVH_PLAIN_INST(RVH_NFIX, (RVH_EXACT != 0))
+#else
+RVH_PLAIN_INST(0, false) RVH_PLAIN_INST(0, true)
+RVH_PLAIN_INST(8, false) RVH_PLAIN_INST(8, true)
+RVH_PLAIN_INST(10, false) RVH_PLAIN_INST(10, true)
+RVH_PLAIN_INST(16, false) RVH_PLAIN_INST(16, true)
+RVH_PLAIN_INST(24, false) RVH_PLAIN_INST(24, true)
+RVH_PLAIN_INST(32, false) RVH_PLAIN_INST(32, true)
+#endif
 
 }  // namespace rvh

@@ -12,6 +12,13 @@ const void* plain_b_kernel(bool exact);
 // Persistent batch kernel; lanes in {4, 8, 16, 32}.
 const void* batch_kernel(int lanes, bool exact);
 bool batch_supported(int lanes);
+// One translation unit per instantiation (compiled in parallel): the
+// persistent batch kernel for (lanes, math) and the phase-A kernels for a
+// fixed point count (0: any count) and math, by lanes per strand.
+template <int L, bool EXACT>
+const void* batch_kernel_inst();
+template <int NFIX, bool EXACT>
+const void* plain_a_inst(int lanes);
 // Opts a kernel into kSmemBytes of dynamic shared memory (once per kernel).
 bool prepare_kernel(const void* fn);
 
