@@ -73,6 +73,13 @@ PROTOTYPES = [
     ("rvh_generate_head", _st, [_vp, _vp, _P(C.c_float), _P(T.SimParams), _P(T.Collider), _P(C.c_int32)]),
     ("rvh_wind_at", _st, [_vp, C.c_int64, C.c_float, _P(C.c_float)]),
     ("rvh_sphere_on_orbit", _st, [_vp, C.c_float, _P(T.Collider)]),
+    ("rvh_mesh_load_obj", _st, [C.c_char_p, _P(_vp)]),
+    ("rvh_mesh_from_triangles", _st, [_P(C.c_float), _P(C.c_float), C.c_int32, _P(_vp)]),
+    ("rvh_mesh_destroy", None, [_vp]),
+    ("rvh_mesh_info", _st, [_vp, _P(C.c_int32), _P(C.c_double)]),
+    ("rvh_mesh_triangles", _st, [_vp, _P(C.c_float), _P(C.c_float)]),
+    ("rvh_mesh_sample_roots", _st, [_vp, _vp, _P(C.c_float), _P(C.c_float)]),
+    ("rvh_libc_rand_sequence", _st, [C.c_uint32, C.c_int32, _P(C.c_int32)]),
     ("rvh_rng_u64", C.c_uint64, [C.c_uint64, C.c_uint64]),
     ("rvh_rng_uniform", C.c_double, [C.c_uint64, C.c_uint64]),
     ("rvh_rng_normal", C.c_double, [C.c_uint64, C.c_uint64]),

@@ -1,6 +1,7 @@
 """Python host-side mirror of the C ABI: Context, Asset (the reference's Hair),
 Batch, and the scene helpers.  Every call goes through librvh.so."""
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -412,3 +413,71 @@ def sphere_on_orbit(orbit, t):
     c = T.Collider()
     check(load().rvh_sphere_on_orbit(C.byref(orbit), t, C.byref(c)))
     return c
+
+
+# ---- scalp meshes and root sampling ----------------------------------------------
+MESH_ROOTS_REFERENCE = 0
+MESH_ROOTS_AREA = 1
+ROOT_NORMAL_FIRST_CORNER = 0
+ROOT_NORMAL_INTERPOLATED = 1
+
+
+class MeshRootsDesc(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("n_roots", C.c_int32), ("seed", C.c_uint64), ("normal_mode", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class Mesh:
+    """A triangle mesh in the reference's face-vertex form (rvh_mesh)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    @classmethod
+    def load_obj(cls, path):
+        h = C.c_void_p()
+        check(load().rvh_mesh_load_obj(os.fsencode(path), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_triangles(cls, positions, normals):
+        p, n = _f32(positions).reshape(-1, 9), _f32(normals).reshape(-1, 9)
+        h = C.c_void_p()
+        check(load().rvh_mesh_from_triangles(_fp(p), _fp(n), p.shape[0], C.byref(h)))
+        return cls(h.value)
+
+    def close(self):
+        if self._h and self._h.value:
+            load().rvh_mesh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        nt, area = C.c_int32(), C.c_double()
+        check(load().rvh_mesh_info(self._h, C.byref(nt), C.byref(area)))
+        return nt.value, area.value
+
+    def triangles(self):
+        nt = self.info()[0]
+        p = np.empty((nt, 3, 3), np.float32)
+        n = np.empty((nt, 3, 3), np.float32)
+        check(load().rvh_mesh_triangles(self._h, _fp(p), _fp(n)))
+        return p, n
+
+    def sample_roots(self, n_roots, mode=MESH_ROOTS_REFERENCE, seed=8, normal_mode=ROOT_NORMAL_FIRST_CORNER):
+        d = MeshRootsDesc(mode, n_roots, seed, normal_mode, 0)
+        roots = np.empty((n_roots, 3), np.float32)
+        normals = np.empty((n_roots, 3), np.float32)
+        check(load().rvh_mesh_sample_roots(self._h, C.byref(d), _fp(roots), _fp(normals)))
+        return roots, normals
+
+
+def libc_rand_sequence(seed, n):
+    out = np.empty(n, np.int32)
+    check(load().rvh_libc_rand_sequence(seed, n, out.ctypes.data_as(C.POINTER(C.c_int32))))
+    return out
