@@ -75,6 +75,13 @@ rvh_status rvh_collider_from_trs(const float trans[3], const float rot_deg[3], c
 /* Scene::translateSphere (src/Scene.cpp:110-120): transform = transform *
  * translate(delta); inv and invTrans recomputed. */
 rvh_status rvh_collider_translate(rvh_collider* c, const float delta[3]);
+/* A collider carried by a rigid head motion m (column-major 4x4 affine, glm
+ * layout): transform = m * rest.transform, inv = inverse(transform), inv_trans =
+ * transpose(inv), computed in double and rounded once.  Scene::translateSphere
+ * (src/Scene.cpp:110-120) is the special case m = translate(delta) applied on
+ * the right; this is the head-follows-motion form the asset uses for colliders
+ * with attach_to_head set. */
+rvh_status rvh_collider_follow(const rvh_collider* rest, const float m[16], rvh_collider* out);
 /* Initial straight strands as Hair::Hair builds them (src/Strand.cpp:157-175):
  * point j = root + j*seg*(normal + dir_offset), velocity (0,0,-1), correction 0.
  * The reference uses seg = 2.5/9 and dir_offset = (0.05, 5, -2). */
@@ -90,6 +97,17 @@ rvh_status rvh_asset_destroy(rvh_asset* a);
 /* Time/Collider/Grid uniforms of sets 1-3 (compute.comp:20-42, Scene.cpp:4-20). */
 rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p);
 rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t n);
+/* Kinematic head: the pose m (column-major 4x4 affine) of the asset's head for
+ * the following steps, relative to its pose when head motion was first set.
+ * Each step then places every strand's root at m * root_rest (root_rest = the
+ * roots at that first call; the reference pins them where Hair::Hair put them,
+ * compute.comp:144 starts at point 1) before the FTL chain, and uses
+ * rvh_collider_follow(c, m) for each collider with attach_to_head set.  In the
+ * reference only collider 0 and the head model move, by keyboard translations
+ * (Scene::translateSphere, src/Scene.cpp:110-135; src/main.cpp:133-157); here
+ * the roots and the attached colliders move together, so hair follows its
+ * head.  m = NULL stops the motion (roots stay where the last step put them). */
+rvh_status rvh_asset_set_head_transform(rvh_asset* a, const float m[16]);
 /* Per-strand rest segment lengths (host array, n_strands floats; the
  * reference's strandLength/(n-1), compute.comp:139-140) and per-strand wind
  * (host array, 3 floats per strand, or NULL to remove it). */

@@ -54,7 +54,8 @@ typedef struct rvh_collider {
     float inv_trans[16];
     int32_t kind;
     float radius;
-    int32_t reserved[2];
+    int32_t attach_to_head;   /* 1: moves with the asset's head (rvh_asset_set_head_transform) */
+    int32_t reserved;
 } rvh_collider;
 
 /*

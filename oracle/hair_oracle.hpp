@@ -260,10 +260,23 @@ inline v3<T> base_force(const rvh_sim_params& P, const rvh_frame& F, const float
  * state: n_strands * 12 * n scalars.  threads > 1 runs strands in parallel with
  * OpenMP; int64 sums make the result independent of the thread count.
  */
+/* Kinematic head (no counterpart in the reference, whose roots stay where
+ * Hair::Hair put them): root = head * (root_rest, 1) for a column-major 4x4
+ * affine head, each row summed as ((m0 x + m1 y) + m2 z) + m3. */
+template <class T>
+inline v3<T> head_point(const float* m, const float* r) {
+    const T x = T(r[0]), y = T(r[1]), z = T(r[2]);
+    v3<T> o;
+    o.x = ((T(m[0]) * x + T(m[4]) * y) + T(m[8]) * z) + T(m[12]);
+    o.y = ((T(m[1]) * x + T(m[5]) * y) + T(m[9]) * z) + T(m[13]);
+    o.z = ((T(m[2]) * x + T(m[6]) * y) + T(m[10]) * z) + T(m[14]);
+    return o;
+}
+
 template <class T>
 void step_asset(T* state, int ns, int n, const float* rest, const float* strand_wind,
                 const rvh_sim_params& P, const rvh_frame& F, const rvh_collider* cols, int ncol,
-                Grid& G, int threads) {
+                Grid& G, int threads, const float* head = nullptr, const float* root_rest = nullptr) {
     const T dt = T(F.dt);
     const bool grid = P.grid_enabled != 0;
     if (grid) G.reset(P);
@@ -272,6 +285,7 @@ void step_asset(T* state, int ns, int n, const float* rest, const float* strand_
 #pragma omp parallel for schedule(static) num_threads(threads) if (threads > 1)
     for (int s = 0; s < ns; ++s) {
         T* rec = state + stride * s;
+        if (head) st(rec, head_point<T>(head, root_rest + 3 * size_t(s)), T(1));
         strand_predict<T>(rec, n, T(rest[s]), base_force<T>(P, F, strand_wind, s), cols, ncol, P, dt);
         if (grid) {
             for (int i = 1; i < n; ++i) {

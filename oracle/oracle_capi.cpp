@@ -18,7 +18,7 @@ namespace {
 template <class T>
 int run(T* state, int ns, int n, const float* rest, const float* strand_wind, const rvh_sim_params* P,
         const rvh_frame* frames, const rvh_collider* cols, int ncol, int n_steps, int threads,
-        int64_t* grid_out) {
+        int64_t* grid_out, const float* heads = nullptr, const float* root_rest = nullptr) {
     if (!state || !rest || !P || !frames || ns < 0 || n < RVH_MIN_POINTS || n > RVH_MAX_POINTS ||
         ncol < 0 || ncol > RVH_MAX_COLLIDERS || n_steps < 0 || (ncol > 0 && !cols))
         return 1;
@@ -26,7 +26,7 @@ int run(T* state, int ns, int n, const float* rest, const float* strand_wind, co
     oracle::Grid G;
     for (int s = 0; s < n_steps; ++s)
         oracle::step_asset<T>(state, ns, n, rest, strand_wind, *P, frames[s], cols + size_t(s) * ncol, ncol,
-                              G, threads);
+                              G, threads, heads ? heads + 16 * size_t(s) : nullptr, root_rest);
     if (grid_out && P->grid_enabled && !G.cells.empty())
         std::copy(G.cells.begin(), G.cells.end(), grid_out);
     return 0;
@@ -52,6 +52,23 @@ int oracle_run_f32(float* state, int ns, int n, const float* rest, const float* 
     return run<float>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out);
 }
 
+/* As oracle_run_f64/f32 with a kinematic head: heads = n_steps column-major
+ * 4x4 affine poses, root_rest = ns*3 rest roots; each step first places the
+ * roots at heads[s] * root_rest. */
+int oracle_run_head_f64(double* state, int ns, int n, const float* rest, const float* strand_wind,
+                        const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                        int n_steps, int threads, int64_t* grid_out, const float* heads, const float* root_rest) {
+    if (!heads || !root_rest) return 1;
+    return run<double>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out, heads,
+                       root_rest);
+}
+int oracle_run_head_f32(float* state, int ns, int n, const float* rest, const float* strand_wind,
+                        const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                        int n_steps, int threads, int64_t* grid_out, const float* heads, const float* root_rest) {
+    if (!heads || !root_rest) return 1;
+    return run<float>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out, heads,
+                      root_rest);
+}
 /* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */
 int oracle_adjoint_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,
                        const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,

@@ -35,11 +35,14 @@ def lib():
                   C.c_int, C.c_int, C.c_int, _P(C.c_int64)]
         l.oracle_run_f64.argtypes = [_P(C.c_double)] + common
         l.oracle_run_f32.argtypes = [_P(C.c_float)] + common
+        l.oracle_run_head_f64.argtypes = [_P(C.c_double)] + common + [_P(C.c_float), _P(C.c_float)]
+        l.oracle_run_head_f32.argtypes = [_P(C.c_float)] + common + [_P(C.c_float), _P(C.c_float)]
         adj = [_P(C.c_double), C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(T.SimParams), _P(T.Frame),
                _P(T.Collider), C.c_int, C.c_int, _P(C.c_double), C.c_int, _P(C.c_double)]
         l.oracle_adjoint_f64.argtypes = adj + [_P(C.c_double), _P(C.c_double), _P(C.c_double)]
         l.oracle_loss_f64.argtypes = adj
-        for f in (l.oracle_run_f64, l.oracle_run_f32, l.oracle_adjoint_f64, l.oracle_loss_f64):
+        for f in (l.oracle_run_f64, l.oracle_run_f32, l.oracle_run_head_f64, l.oracle_run_head_f32,
+                  l.oracle_adjoint_f64, l.oracle_loss_f64):
             f.restype = C.c_int
         l.oracle_max_threads.restype = C.c_int
         _lib = l
@@ -69,10 +72,12 @@ def _frames(frames, n_steps):
 
 
 def run(state, n_points, rest, params, frames, colliders, n_steps, strand_wind=None, threads=1,
-        want_grid=False):
+        want_grid=False, heads=None, root_rest=None):
     """Advance `state` (float64 -> FP64 oracle, float32 -> FP32 twin) in place.
 
     state: (ns, 3*n_points, 4) array in the Strand record layout.
+    heads (n_steps, 16) column-major head poses and root_rest (ns, 3): each step
+    first places the roots at heads[s] * root_rest (kinematic head).
     Returns the last step's grid (nx*ny*nz, 4) int64 when want_grid."""
     assert state.flags.c_contiguous
     ns = state.shape[0]
@@ -84,14 +89,21 @@ def run(state, n_points, rest, params, frames, colliders, n_steps, strand_wind=N
     if want_grid and params.grid_enabled:
         d = params.grid_dims
         grid = np.zeros((d[0] * d[1] * d[2], 4), np.int64)
+    head_args = ()
+    suffix = ""
+    if heads is not None:
+        hd = np.ascontiguousarray(heads, np.float32).reshape(n_steps, 16)
+        rr = np.ascontiguousarray(root_rest, np.float32).reshape(ns, 3)
+        head_args = (_fptr(hd, C.c_float), _fptr(rr, C.c_float))
+        suffix = "head_"
     if state.dtype == np.float64:
-        fn, ptr = lib().oracle_run_f64, _fptr(state, C.c_double)
+        fn, ptr = getattr(lib(), "oracle_run_%sf64" % suffix), _fptr(state, C.c_double)
     elif state.dtype == np.float32:
-        fn, ptr = lib().oracle_run_f32, _fptr(state, C.c_float)
+        fn, ptr = getattr(lib(), "oracle_run_%sf32" % suffix), _fptr(state, C.c_float)
     else:
         raise TypeError(state.dtype)
     rc = fn(ptr, ns, n_points, _fptr(rest, C.c_float), _fptr(wind, C.c_float), C.byref(params), fr, cols, ncol,
-            n_steps, threads, _fptr(grid, C.c_int64))
+            n_steps, threads, _fptr(grid, C.c_int64), *head_args)
     if rc != 0:
         raise RuntimeError("oracle_run failed: %d" % rc)
     return grid

@@ -272,6 +272,7 @@ rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, i
     if (checkpoint_every < 1) checkpoint_every = 10;
     if (a->params.grid_enabled)
         return fail(RVH_ERR_UNSUPPORTED, "adjoint: the hair-hair grid must be disabled (FTL+DFTL+collisions only)");
+    if (a->head_active) return fail(RVH_ERR_UNSUPPORTED, "adjoint: a kinematic head motion is set");
     for (int t = 0; t < n_steps; ++t) {
         rvh_status st = validate_frame(frames[t]);
         if (st != RVH_OK) return st;

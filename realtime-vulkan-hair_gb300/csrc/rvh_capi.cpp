@@ -165,7 +165,16 @@ DevAsset Asset::device_view(const rvh_frame& f, int g, int prev, int next) const
     A.t = f.t;
     for (int i = 0; i < 3; ++i) A.wind[i] = f.wind[i];
     A.n_colliders = int32_t(colliders.size());
-    for (size_t j = 0; j < colliders.size(); ++j) A.col[j] = pack_collider(colliders[j]);
+    for (size_t j = 0; j < colliders.size(); ++j) {
+        rvh_collider moved;
+        if (head_active && colliders[j].attach_to_head && follow_collider(colliders[j], head, &moved))
+            A.col[j] = pack_collider(moved);
+        else
+            A.col[j] = pack_collider(colliders[j]);
+    }
+    A.root_rest = head_active ? static_cast<const float4*>(root_rest.ptr) : nullptr;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) A.head[r * 4 + c] = head[c * 4 + r];   // row-major 3 x 4 of m
     return A;
 }
 
@@ -324,7 +333,25 @@ bool fill_collider(const M4& T, int32_t kind, float radius, rvh_collider* out) {
     out->radius = radius;
     return true;
 }
+// m: finite, column-major, last row (0, 0, 0, 1)
+bool affine_finite(const float* m) {
+    for (int k = 0; k < 16; ++k)
+        if (!std::isfinite(m[k])) return false;
+    return m[3] == 0.f && m[7] == 0.f && m[11] == 0.f && m[15] == 1.f;
+}
 }  // namespace
+
+// transform = m * rest.transform in double, inverse and inverse-transpose from it
+bool rvh::follow_collider(const rvh_collider& rest, const float* m, rvh_collider* out) {
+    M4 H{}, T{};
+    for (int i = 0; i < 16; ++i) {
+        H.m[i] = m[i];
+        T.m[i] = rest.transform[i];
+    }
+    if (!fill_collider(mat_mul(H, T), rest.kind, rest.radius, out)) return false;
+    out->attach_to_head = rest.attach_to_head;
+    return true;
+}
 
 extern "C" {
 
@@ -465,7 +492,18 @@ rvh_status rvh_collider_translate(rvh_collider* c, const float delta[3]) {
     M4 D = mat_identity();
     for (int i = 0; i < 3; ++i) D.m[12 + i] = delta[i];
     const M4 N = mat_mul(M, D);
+    const int32_t attach = c->attach_to_head;
     if (!fill_collider(N, c->kind, c->radius, c)) return fail(RVH_ERR_INVALID_ARG, "collider_translate: singular");
+    c->attach_to_head = attach;
+    return RVH_OK;
+}
+
+rvh_status rvh_collider_follow(const rvh_collider* rest, const float m[16], rvh_collider* out) {
+    if (!rest || !m || !out) return fail(RVH_ERR_INVALID_ARG, "collider_follow: NULL argument");
+    if (!affine_finite(m)) return fail(RVH_ERR_INVALID_ARG, "collider_follow: m must be a finite affine matrix");
+    rvh_collider c;
+    if (!follow_collider(*rest, m, &c)) return fail(RVH_ERR_INVALID_ARG, "collider_follow: singular transform");
+    *out = c;
     return RVH_OK;
 }
 
@@ -573,6 +611,7 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     c->free(a->wind);
     for (int i = 0; i < 3; ++i) c->free(a->grid[i]);
     c->free(a->draw);
+    c->free(a->root_rest);
     delete a;
     return RVH_OK;
 }
@@ -601,6 +640,27 @@ rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t 
                 return fail(RVH_ERR_INVALID_ARG, "set_colliders: non-finite matrix");
     }
     a->colliders.assign(c, c + n);
+    return RVH_OK;
+}
+
+rvh_status rvh_asset_set_head_transform(rvh_asset* a, const float m[16]) {
+    if (!a) return fail(RVH_ERR_INVALID_ARG, "set_head_transform: NULL asset");
+    if (!m) {
+        a->head_active = false;
+        return RVH_OK;
+    }
+    if (!affine_finite(m)) return fail(RVH_ERR_INVALID_ARG, "set_head_transform: m must be a finite affine matrix");
+    if (!a->root_rest.ptr && a->n_strands > 0) {
+        // the roots now are the rest pose of m = identity (roots never move without a head motion)
+        DeviceGuard g(a->ctx->device);
+        rvh_status s = a->ctx->alloc(a->root_rest, size_t(a->n_strands) * 16u);
+        if (s != RVH_OK) return s;
+        RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
+        RVH_CUDA(cudaMemcpy2D(a->root_rest.ptr, 16, a->strands.ptr, size_t(48) * a->n_points, 16, size_t(a->n_strands),
+                              cudaMemcpyDeviceToDevice));
+    }
+    std::memcpy(a->head, m, sizeof(a->head));
+    a->head_active = true;
     return RVH_OK;
 }
 

@@ -93,6 +93,10 @@ struct DevAsset {
     float wind[3];
     int32_t n_colliders;
     DevCollider col[RVH_MAX_COLLIDERS];
+    // kinematic head: with root_rest set, each strand's root is placed at head * root_rest
+    // (head: row-major 3 x 4 affine) before the FTL chain
+    const float4* root_rest;
+    float head[12];
 };
 
 struct f3 {
@@ -240,14 +244,16 @@ __device__ __forceinline__ void red_add_s64(unsigned long long* p, long long v) 
 }
 
 // Splat one point: 4 x int64 atomics per touched corner, sums wrap-free.
+// Only corners with x index in [xlo, xhi) are added.
 template <class M>
-__device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel) {
+__device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel, int xlo = 0, int xhi = 0x7fffffff) {
     const Corners C = corners_of<M>(A, pos);
     const int nxny = A.nx * A.ny;
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
         if (da >= C.cnt[0]) continue;
         const int a = C.lo[0] + da;
+        if (a < xlo || a >= xhi) continue;
         const float wx = tri_w<M>(C.g[0], a);
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
@@ -276,20 +282,22 @@ __device__ __forceinline__ long long grid_val(unsigned long long raw, bool wrap3
     return wrap32 ? (long long)(int)(unsigned)(raw & 0xffffffffull) : (long long)raw;
 }
 
-// One grid cell as the gather reads it: velocity sums as floats, the density
-// as a float (fd > 0 exactly when the integer density is > 0) and 1/fd.
+// One grid cell as the gather reads it: velocity sums as floats, the
+// repulsion density rc = density / scale and rcp = 1 / density (rcp > 0
+// exactly when the integer density is > 0).
 struct CellF {
-    float vx, vy, vz, fd, rcp;
+    float vx, vy, vz, rc, rcp;
 };
 
 template <class M>
-__device__ __forceinline__ CellF cell_from_sums(long long vx, long long vy, long long vz, long long dens) {
+__device__ __forceinline__ CellF cell_from_sums(long long vx, long long vy, long long vz, long long dens, float scale) {
     CellF c;
     c.vx = (float)vx;
     c.vy = (float)vy;
     c.vz = (float)vz;
-    c.fd = (float)dens;
-    c.rcp = dens > 0 ? M::rcp(c.fd) : 0.0f;
+    const float fd = (float)dens;
+    c.rc = M::div(fd, scale);
+    c.rcp = M::rcp(fd);
     return c;
 }
 
@@ -301,21 +309,34 @@ __device__ __forceinline__ CellF cell_from_global(const DevAsset& A, const unsig
     const long long dens = grid_val(zw.y, wrap);
     if (dens <= 0) return CellF{0.f, 0.f, 0.f, 0.f, 0.f};
     const ulonglong2 xy = __ldcg(cell);
-    return cell_from_sums<M>(grid_val(xy.x, wrap), grid_val(xy.y, wrap), grid_val(zw.x, wrap), dens);
+    return cell_from_sums<M>(grid_val(xy.x, wrap), grid_val(xy.y, wrap), grid_val(zw.x, wrap), dens, A.scale);
+}
+
+// d(weight)/d(g) sign of corner a on one axis: -1 left of the point, +1 right
+// of it, 0 outside the unit support (compute.comp repulsion extension).
+template <class M>
+__device__ __forceinline__ float grad_sign(float g, int a) {
+    const float ga = M::sub(g, (float)a);
+    return fabsf(ga) < 1.0f ? (ga >= 0.0f ? -1.0f : 1.0f) : 0.0f;
 }
 
 // Gather + friction (+ repulsion) for one point (compute.comp:258-297);
-// cell(a, b, c) returns the CellF of corner (a, b, c).
+// cell(a, b, c) returns the CellF of corner (a, b, c).  The per-axis weights,
+// their pairwise products and the gradient signs are computed once per point;
+// with signs in {-1, 0, 1} and weights >= 0, d * (w1 * w2) has the bits of
+// (d * w1) * w2, so every corner term equals the oracle's.
 template <class M, class CellFn>
 __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, f3 vel, const Corners& C, CellFn cell) {
     const bool rep = A.repulsion != 0.0f;
-    // the trilinear weights of the (up to) two corners per axis, computed once
-    float wxs[2], wys[2], wzs[2];
+    float wxs[2], wys[2], wzs[2], sx[2], sy[2], sz[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         wxs[d] = tri_w<M>(C.g[0], C.lo[0] + d);
         wys[d] = tri_w<M>(C.g[1], C.lo[1] + d);
         wzs[d] = tri_w<M>(C.g[2], C.lo[2] + d);
+        sx[d] = grad_sign<M>(C.g[0], C.lo[0] + d);
+        sy[d] = grad_sign<M>(C.g[1], C.lo[1] + d);
+        sz[d] = grad_sign<M>(C.g[2], C.lo[2] + d);
     }
     f3 gv = {0.f, 0.f, 0.f};
     float rho = 0.f;
@@ -328,25 +349,21 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
         for (int db = 0; db < 2; ++db) {
             if (db >= C.cnt[1]) continue;
             const int b = C.lo[1] + db;
+            const float wxy = M::mul(wxs[da], wys[db]);
 #pragma unroll
             for (int dc = 0; dc < 2; ++dc) {
                 if (dc >= C.cnt[2]) continue;
                 const int c = C.lo[2] + dc;
                 const CellF cf = cell(a, b, c);
-                if (cf.fd > 0.0f) {
-                    const float wx = wxs[da], wy = wys[db], wz = wzs[dc];
-                    const float w = M::mul(M::mul(wx, wy), wz);
+                if (cf.rcp > 0.0f) {
+                    const float w = M::mul(wxy, wzs[dc]);
                     const float s = M::mul(w, cf.rcp);
                     gv = v_add<M>(gv, v_scale<M>(s, f3{cf.vx, cf.vy, cf.vz}));
                     if (rep) {
-                        const float rc = M::div(cf.fd, A.scale);
-                        const float ga = M::sub(C.g[0], (float)a), gb = M::sub(C.g[1], (float)b), gc = M::sub(C.g[2], (float)c);
-                        const float dx = fabsf(ga) < 1.0f ? (ga >= 0.0f ? -1.0f : 1.0f) : 0.0f;
-                        const float dy = fabsf(gb) < 1.0f ? (gb >= 0.0f ? -1.0f : 1.0f) : 0.0f;
-                        const float dz = fabsf(gc) < 1.0f ? (gc >= 0.0f ? -1.0f : 1.0f) : 0.0f;
-                        rho = M::add(rho, M::mul(w, rc));
-                        const f3 dw = {M::mul(M::mul(dx, wy), wz), M::mul(M::mul(wx, dy), wz), M::mul(M::mul(wx, wy), dz)};
-                        grad = v_add<M>(grad, v_scale<M>(rc, dw));
+                        rho = M::add(rho, M::mul(w, cf.rc));
+                        const f3 dw = {M::mul(sx[da], M::mul(wys[db], wzs[dc])),
+                                       M::mul(sy[db], M::mul(wxs[da], wzs[dc])), M::mul(sz[dc], wxy)};
+                        grad = v_add<M>(grad, v_scale<M>(cf.rc, dw));
                     }
                 }
             }
@@ -359,6 +376,16 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
         out = v_sub<M>(out, v_scale<M>(coef, grad));
     }
     return out;
+}
+
+// head * (p, 1) for a row-major 3 x 4 affine head: ((h0 x + h1 y) + h2 z) + h3 per row.
+template <class M>
+__device__ __forceinline__ f3 head_point(const float (&h)[12], f3 p) {
+    f3 o;
+    o.x = M::add(M::add(M::add(M::mul(h[0], p.x), M::mul(h[1], p.y)), M::mul(h[2], p.z)), h[3]);
+    o.y = M::add(M::add(M::add(M::mul(h[4], p.x), M::mul(h[5], p.y)), M::mul(h[6], p.z)), h[7]);
+    o.z = M::add(M::add(M::add(M::mul(h[8], p.x), M::mul(h[9], p.y)), M::mul(h[10], p.z)), h[11]);
+    return o;
 }
 
 // ---------------------------------------------------------------------------
@@ -377,6 +404,10 @@ template <int NFIX, int L>
 struct PhaseA {
     static constexpr int NMAX = NFIX > 0 ? NFIX : RVH_MAX_POINTS;
     static constexpr int K = (NMAX + L - 1) / L;
+    // point held in slot k of lane l, and the (lane, slot) holding point i
+    static __device__ __forceinline__ int point(int l, int k) { return k * L + l; }
+    static __device__ __forceinline__ int owner(int i) { return i % L; }
+    static __device__ __forceinline__ int slot(int i) { return i / L; }
 };
 
 // Loads the lane's points (positions and velocities) of one strand; bit k of
@@ -391,7 +422,7 @@ __device__ __forceinline__ unsigned load_points(const DevAsset& A, int strand, b
     unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        const int i = k * L + l;
+        const int i = PhaseA<NFIX, L>::point(l, k);
         if (valid && i < n) {
             x[k] = xyz(ld_cg(rec + i));
             v[k] = xyz(ld_cg(rec + n + i));
@@ -432,7 +463,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
     // loop 1, independent part: force and predicted position of each point
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        const int i = k * L + l;
+        const int i = PhaseA<NFIX, L>::point(l, k);
         f3 force = f0;
         if (valid && i >= 1 && i < n) force = collide_force<M>(A, x[k], force);
         const f3 v = vel_in[k];
@@ -449,10 +480,17 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
         par.y = __shfl_sync(FULL, x[0].y, base);
         par.z = __shfl_sync(FULL, x[0].z, base);
     }
+    const bool moving = A.root_rest != nullptr;
+    if (moving) {
+        // kinematic head: the root follows it (every lane of the strand computes the same root)
+        const f3 r0 = valid ? xyz(A.root_rest[strand]) : f3{0.f, 0.f, 0.f};
+        par = head_point<M>(A.head, r0);
+        if (l == 0) xn[0] = par;
+    }
 #pragma unroll
     for (int i = 1; i < NMAX; ++i) {
         if (NFIX == 0 && i >= n) break;  // n is uniform across the warp
-        const int k = i / L, own = i % L;
+        const int k = PhaseA<NFIX, L>::slot(i), own = PhaseA<NFIX, L>::owner(i);
         f3 pi;
         if (L == 1) {
             pi = p[k];
@@ -478,6 +516,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
     }
 
     // loop 2: v_i -= corr_{i+1} / dt for i < n-1 (compute.comp:213-215)
+    // point i+1 is the same slot of the next lane, or the next slot of lane 0
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         f3 cn;
@@ -494,15 +533,16 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
             wrap.z = __shfl_sync(FULL, nxt.z, base);
             cn = (l + 1 < L) ? same : wrap;
         }
-        const int i = k * L + l;
+        const int i = PhaseA<NFIX, L>::point(l, k);
         if (i >= 1 && i < n - 1) vel[k] = v_sub<M>(vel[k], v_div<M>(cn, dt));
     }
 
-    // store x', v, corr for points 1..n-1 (the root is never written)
+    // store x', v, corr for points 1..n-1 (the root is written only when a head moves it)
+    if (moving && valid && l == 0) st_f4(rec, xn[0], 1.0f);
     unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        const int i = k * L + l;
+        const int i = PhaseA<NFIX, L>::point(l, k);
         if (valid && i >= 1 && i < n) {
             st_f4(rec + i, xn[k], 1.0f);
             st_f4(rec + n + i, vel[k], 0.0f);

@@ -94,6 +94,10 @@ struct Asset {
     std::vector<rvh_collider> colliders;
     bool has_wind = false;
     bool server_managed = false;  // grids are lent by a request server while a request is active
+    // kinematic head (rvh_asset_set_head_transform): roots = head * root_rest each step
+    bool head_active = false;
+    float head[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};   // column-major
+    DevBuf root_rest;   // float4 per strand, captured at the first head transform
 
     size_t record_bytes() const { return size_t(n_strands) * 48u * size_t(n_points); }
     size_t grid_bytes() const { return grid_cells * 32u; }
@@ -107,6 +111,8 @@ struct Asset {
 rvh_status validate_params(const rvh_sim_params& p);
 rvh_status validate_frame(const rvh_frame& f);
 DevCollider pack_collider(const rvh_collider& c);
+// rest carried by the head motion m (column-major affine): transform = m * rest.transform
+bool follow_collider(const rvh_collider& rest, const float* m, rvh_collider* out);
 int default_lanes(int n_points);
 rvh_status ensure_grid(Asset* a);
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s);

@@ -19,7 +19,8 @@ namespace rvh {
 
 constexpr int kThreads = 256;          // CTA size of every step kernel
 constexpr int kWarps = kThreads / 32;
-constexpr int kSmemBytes = 96 * 1024;  // dynamic shared memory per CTA (grid boxes)
+constexpr int kSmemBytes = 72 * 1024;  // dynamic shared memory per CTA (grid boxes)
+constexpr int kMinCtasPerSm = 3;       // 3 x 72 KB of boxes and <= 80 registers per thread per SM
 constexpr int kBoxCellsA = kSmemBytes / 16;   // phase A: 4 x int32 partial sums per cell
 constexpr int kBoxCellsB = kSmemBytes / 20;   // phase B: CellF without padding (float4 + rcp)
 constexpr int kTileB = 2048;           // points per phase-B tile
@@ -132,14 +133,60 @@ __device__ __forceinline__ void bounds_of_extremes(const DevAsset& A, f3 pmin, f
     }
 }
 
-// Splat one point into the shared box (int32 partial sums).
+// Shape of a box in shared memory: cells [lo, lo + ext) of the grid, x
+// fastest, with odd row and slab pitches (py = ext_x | 1, pz = (py * ext_y) | 1)
+// so that cells one row or one slab apart fall in different banks; the padding
+// cells are never touched by a point.  vol counts the padded cells.
+struct BoxGeom {
+    int lo[3];
+    int ext[3];
+    int py, pz;
+    long long vol;
+    __device__ __forceinline__ int offset(int a, int b, int c) const {
+        return (a - lo[0]) + py * (b - lo[1]) + pz * (c - lo[2]);
+    }
+};
+
+__device__ __forceinline__ BoxGeom box_geom(const BoxShared& S) {
+    BoxGeom G;
+    long long e[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        G.lo[a] = S.lo[a];
+        e[a] = (long long)S.hi[a] - S.lo[a] + 1;   // <= 0 for an empty box
+        G.ext[a] = (int)(e[a] > 0 ? (e[a] < 0x40000000LL ? e[a] : 0x40000000LL) : 0);
+    }
+    const long long py = e[0] > 0 ? (e[0] | 1) : 1;
+    const long long pz = (py * (e[1] > 0 ? e[1] : 0)) | 1;
+    G.vol = (e[0] > 0 && e[1] > 0 && e[2] > 0) ? pz * e[2] : (1LL << 62);   // an empty box is never used
+    G.py = (int)(py < 0x40000000LL ? py : 0x40000000LL);
+    G.pz = (int)(pz < 0x40000000LL ? pz : 0x40000000LL);
+    return G;
+}
+
+// Grid coordinates of padded box cell c, false for a padding cell.
+struct BoxWalk {
+    FastDiv dy, dz;
+    __device__ __forceinline__ explicit BoxWalk(const BoxGeom& G) : dy((unsigned)G.py), dz((unsigned)G.pz) {}
+    __device__ __forceinline__ bool cell(const BoxGeom& G, int c, int& a, int& b, int& cc) const {
+        const int qz = (int)dz.div((unsigned)c), rz = c - qz * G.pz;
+        const int qy = (int)dy.div((unsigned)rz), rx = rz - qy * G.py;
+        a = G.lo[0] + rx;
+        b = G.lo[1] + qy;
+        cc = G.lo[2] + qz;
+        return rx < G.ext[0] && qy < G.ext[1];
+    }
+};
+
+// Splat one point into the shared box (int32 partial sums): its corners with
+// x index in [G.lo[0], G.lo[0] + G.ext[0]).
 // The box is laid out as four arrays (vx, vy, vz, density) of `vol` cells, so
-// one component's atomics from a warp spread over all 32 banks.  The six
+// one component's atomics from a warp spread over the banks.  The six
 // trilinear weights of a point are computed once.  Exact math keeps the
 // oracle's int(scale * (w * v)); fast math shares scale * w.
 template <class M>
-__device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const int (&lo)[3],
-                                                int bw, int bh, int vol) {
+__device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const BoxGeom& G,
+                                                int vol) {
     float wx[2], wy[2], wz[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
@@ -147,10 +194,11 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
         wy[d] = tri_w<M>(C.g[1], C.lo[1] + d);
         wz[d] = tri_w<M>(C.g[2], C.lo[2] + d);
     }
-    int* const b0 = box + ((C.lo[0] - lo[0]) + bw * ((C.lo[1] - lo[1]) + bh * (C.lo[2] - lo[2])));
+    const int o0 = G.offset(C.lo[0], C.lo[1], C.lo[2]);      // -1 when the first corner is left of the slab
+    const int x0 = G.lo[0] - C.lo[0], x1 = x0 + G.ext[0];   // da range of the slab
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
-        if (da >= C.cnt[0]) continue;
+        if (da >= C.cnt[0] || da < x0 || da >= x1) continue;
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
             if (db >= C.cnt[1]) continue;
@@ -159,7 +207,7 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
             for (int dc = 0; dc < 2; ++dc) {
                 if (dc >= C.cnt[2]) continue;
                 const float w = M::mul(wxy, wz[dc]);
-                int* cell = b0 + (da + bw * (db + bh * dc));
+                int* cell = box + (o0 + da + G.py * db + G.pz * dc);
                 int q0, q1, q2, q3;
                 corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
                 if (q0) atomicAdd(cell, q0);
@@ -171,10 +219,22 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
     }
 }
 
+// Widest x slab of box G whose padded cells fit `cap` cells (0: none fits).
+__device__ __forceinline__ int slab_width(const BoxGeom& G, int cap) {
+    if (G.vol <= cap) return G.ext[0];
+    // vol(w) = (((w | 1) * e1) | 1) * e2 <= ((w + 1) * e1 + 1) * e2
+    const long long per = cap / G.ext[2] - 1;
+    const long long w = per / G.ext[1] - 1;
+    return (int)(w > 0 ? (w < G.ext[0] ? w : G.ext[0]) : 0);
+}
+
 // Splat the round's points: one call per CTA round, every thread calls it.
-// Falls back to direct global atomics when the box does not fit, or when the
-// int32 partial sums cannot be proven free of overflow (|partial| <=
-// vmax * (density + npts) since |int(s w v)| <= vmax * (int(s w) + 1)).
+// The round's cell box is accumulated in shared memory in x slabs that fit
+// (one slab in almost every round), each flushed once with int64 global
+// atomics.  A slab falls back to direct global atomics when its int32 partial
+// sums cannot be proven free of overflow (|partial| <= vmax * (density + npts)
+// since |int(s w v)| <= vmax * (int(s w) + 1)); the whole round does when not
+// even a one-cell-wide slab fits.
 template <int K, class M>
 __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K], const f3 (&vo)[K], unsigned mask,
                                             int* box, BoxShared& S, unsigned* stats) {
@@ -197,53 +257,79 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
     __syncthreads();
     const int npts = S.npts;
     if (npts > 0) {
-        const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
-        const long long vol = (long long)bw * bh * bd;
-        bool use = vol <= kBoxCellsA && (float)npts * A.scale < 2.0e9f;
-        if (use) {
-            const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
-            const int nv = (int)vol;
+        const BoxGeom G = box_geom(S);
+        const int w = (float)npts * A.scale < 2.0e9f ? slab_width(G, kBoxCellsA) : 0;
+        const float vmax = __uint_as_float(S.vabs);
+        const int nxny = A.nx * A.ny;
+        bool all_box = w > 0;
+        for (int x0 = G.lo[0]; w > 0 && x0 < G.lo[0] + G.ext[0]; x0 += w) {
+            BoxGeom P = G;   // the slab [x0, x0 + w) of G
+            P.lo[0] = x0;
+            P.ext[0] = min(w, G.lo[0] + G.ext[0] - x0);
+            P.py = P.ext[0] | 1;
+            P.pz = (P.py * P.ext[1]) | 1;
+            const int nv = P.pz * P.ext[2];
             int4* b4 = reinterpret_cast<int4*>(box);
-            const int n4 = (4 * nv + 3) / 4;
-            for (int c = threadIdx.x; c < n4; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
+            for (int c = threadIdx.x; c < nv; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 if (!((mask >> k) & 1u)) continue;
                 const Corners C = corners_of<M>(A, xo[k]);
-                splat_point_box<M>(A, C, vo[k], box, lo, bw, bh, nv);
+                splat_point_box<M>(A, C, vo[k], box, P, nv);
             }
             __syncthreads();
-            const float vmax = __uint_as_float(S.vabs);
             bool ok = true;
             for (int c = threadIdx.x; c < nv; c += kThreads)
                 ok = ok && vmax * ((float)box[3 * nv + c] + (float)npts) < 2.0e9f;
-            use = __syncthreads_and(ok);
-            if (use) {
-                const int nxny = A.nx * A.ny;
-                const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
+            if (__syncthreads_and(ok)) {
+                const BoxWalk W(P);
                 for (int c = threadIdx.x; c < nv; c += kThreads) {
                     const int4 v = make_int4(box[c], box[nv + c], box[2 * nv + c], box[3 * nv + c]);
-                    if (!(v.x | v.y | v.z | v.w)) continue;
-                    const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
-                    const int qy = (int)dw.div((unsigned)rz);
-                    const int a = lo[0] + (rz - qy * bw), b = lo[1] + qy, cc = lo[2] + qz;
+                    if (!(v.x | v.y | v.z | v.w)) continue;   // untouched (padding cells always are)
+                    int a, b, cc;
+                    W.cell(P, c, a, b, cc);
                     unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + cc * nxny);
                     red_add_s64(cell + 0, v.x);
                     red_add_s64(cell + 1, v.y);
                     red_add_s64(cell + 2, v.z);
                     red_add_s64(cell + 3, v.w);
                 }
+            } else {
+                all_box = false;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if ((mask >> k) & 1u) splat_point<M>(A, xo[k], vo[k], x0, x0 + P.ext[0]);
             }
+            __syncthreads();   // the box is cleared again by the next slab
         }
-        if (!use) {
+        if (w == 0) {
 #pragma unroll
             for (int k = 0; k < K; ++k)
                 if ((mask >> k) & 1u) splat_point<M>(A, xo[k], vo[k]);
         }
-        if (stats && threadIdx.x == 0) atomicAdd(stats + (use ? 0 : 1), 1u);
+        if (stats && threadIdx.x == 0) atomicAdd(stats + (all_box ? 0 : 1), 1u);
     }
     __syncthreads();  // every read of S and of the box is done before the next round resets them
+}
+
+// Copies the box's cells of grid G into shared memory as CellF (float4
+// {vx, vy, vz, rc} at bf[c], rcp at br[c]).  Padding cells are skipped, and so
+// are cells past the grid's last layer: a point beyond the grid has no corner
+// on that axis but still widens the box there.
+template <class M>
+__device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigned long long* grid, const BoxGeom& G,
+                                                float4* bf, float* br) {
+    const int nxny = A.nx * A.ny;
+    const int vol = (int)G.vol;
+    const BoxWalk W(G);
+    for (int c = threadIdx.x; c < vol; c += kThreads) {
+        int a, b, cc;
+        if (!W.cell(G, c, a, b, cc) || a >= A.nx || b >= A.ny || cc >= A.nz) continue;
+        const CellF cf = cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + cc * nxny));
+        bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.rc);
+        br[c] = cf.rcp;
+    }
 }
 
 // Loop 3 of the PREVIOUS step for the round's points (fused batched step):
@@ -268,23 +354,14 @@ __device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K]
     box_reduce(S, lmin, lmax, 0u, np);
     __syncthreads();
     const int npts = S.npts;
-    const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
-    const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
-    const bool use = npts > 0 && (long long)bw * bh * bd <= kBoxCellsB;
+    const BoxGeom BG = box_geom(S);
+    const bool use = npts > 0 && BG.vol <= kBoxCellsB;
     float4* bf = reinterpret_cast<float4*>(smem);
     float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
     const unsigned long long* G = A.grid_prev;
     const int nxny = A.nx * A.ny;
     if (use) {
-        const int vol = bw * bh * bd;
-        const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
-        for (int c = threadIdx.x; c < vol; c += kThreads) {
-            const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
-            const int qy = (int)dw.div((unsigned)rz);
-            const CellF cf = cell_from_global<M>(A, G, (unsigned)(lo[0] + (rz - qy * bw) + (lo[1] + qy) * A.nx + (lo[2] + qz) * nxny));
-            bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
-            br[c] = cf.rcp;
-        }
+        load_gather_box<M>(A, G, BG, bf, br);
         __syncthreads();
     }
     if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
@@ -294,7 +371,7 @@ __device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K]
         const Corners C = corners_of<M>(A, x[k]);
         if (use) {
             v[k] = gather_point<M>(A, A.dt_prev, x[k], v[k], C, [&](int a, int b, int c) {
-                const int li = (a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2]));
+                const int li = BG.offset(a, b, c);
                 const float4 q = bf[li];
                 return CellF{q.x, q.y, q.z, q.w, br[li]};
             });
@@ -320,7 +397,8 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
     const int per_round = kWarps * SPW;
     const int rounds = (end - begin + per_round - 1) / per_round;
     for (int r = 0; r < rounds; ++r) {
-        const int strand = begin + r * per_round + warp * SPW + g;
+        // a warp's strands are spread over the round (neighbouring strands share cells)
+        const int strand = begin + r * per_round + g * kWarps + warp;
         const bool valid = g < SPW && strand < end;
         f3 x[K], v[K];
         const unsigned lmask = load_points<NFIX, L>(A, strand, valid, x, v);
@@ -380,23 +458,12 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
     box_reduce(S, lmin, lmax, 0u, np);
     __syncthreads();
     const int npts = S.npts;
-    const int lo[3] = {S.lo[0], S.lo[1], S.lo[2]};
-    const int bw = S.hi[0] - S.lo[0] + 1, bh = S.hi[1] - S.lo[1] + 1, bd = S.hi[2] - S.lo[2] + 1;
-    const bool use = npts > 0 && (long long)bw * bh * bd <= kBoxCellsB;
+    const BoxGeom BG = box_geom(S);
+    const bool use = npts > 0 && BG.vol <= kBoxCellsB;
     float4* bf = reinterpret_cast<float4*>(smem);
     float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
     if (use) {
-        const int vol = bw * bh * bd;
-        const int nxny = A.nx * A.ny;
-        const FastDiv dw((unsigned)bw), dwh((unsigned)(bw * bh));
-        for (int c = threadIdx.x; c < vol; c += kThreads) {
-            const int qz = (int)dwh.div((unsigned)c), rz = c - qz * bw * bh;
-            const int qy = (int)dw.div((unsigned)rz);
-            const int a = lo[0] + (rz - qy * bw), b = lo[1] + qy, cc = lo[2] + qz;
-            const CellF cf = cell_from_global<M>(A, A.grid, (unsigned)(a + b * A.nx + cc * nxny));
-            bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.fd);
-            br[c] = cf.rcp;
-        }
+        load_gather_box<M>(A, A.grid, BG, bf, br);
         __syncthreads();
     }
     if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
@@ -409,7 +476,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         f3 out;
         if (use) {
             out = gather_point<M>(A, A.dt, x[j], v, C, [&](int a, int b, int c) {
-                const int li = (a - lo[0]) + bw * ((b - lo[1]) + bh * (c - lo[2]));
+                const int li = BG.offset(a, b, c);
                 const float4 q = bf[li];
                 return CellF{q.x, q.y, q.z, q.w, br[li]};
             });
@@ -436,7 +503,7 @@ __device__ __forceinline__ void write_draw(const DevAsset& A) {
 // ---- plain path -------------------------------------------------------------
 
 template <int NFIX, int L, class M>
-__global__ void __launch_bounds__(kThreads) k_plain_a(const __grid_constant__ DevAsset A) {
+__global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_plain_a(const __grid_constant__ DevAsset A) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
     constexpr int SPW = 32 / L;
@@ -447,7 +514,7 @@ __global__ void __launch_bounds__(kThreads) k_plain_a(const __grid_constant__ De
 }
 
 template <class M>
-__global__ void __launch_bounds__(kThreads) k_plain_b(const __grid_constant__ DevAsset A) {
+__global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_plain_b(const __grid_constant__ DevAsset A) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
     const int per_tile = max(1, kTileB / A.n_points);
@@ -459,7 +526,7 @@ __global__ void __launch_bounds__(kThreads) k_plain_b(const __grid_constant__ De
 // ---- batched persistent path -----------------------------------------------
 
 template <int L, class M>
-__global__ void __launch_bounds__(kThreads) k_batch(const __grid_constant__ BatchDev B) {
+__global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_constant__ BatchDev B) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
     __shared__ int s_item;

@@ -31,12 +31,14 @@ PROTOTYPES = [
     ("rvh_collider_from_trs", _st, [_P(C.c_float), _P(C.c_float), _P(C.c_float), C.c_int32, C.c_float,
                                     _P(T.Collider)]),
     ("rvh_collider_translate", _st, [_P(T.Collider), _P(C.c_float)]),
+    ("rvh_collider_follow", _st, [_P(T.Collider), _P(C.c_float), _P(T.Collider)]),
     ("rvh_init_strands_reference", _st, [_P(C.c_float), _P(C.c_float), C.c_int32, C.c_int32, C.c_float,
                                          _P(C.c_float), _vp]),
     ("rvh_asset_create", _st, [_vp, _vp, _P(_vp)]),
     ("rvh_asset_destroy", _st, [_vp]),
     ("rvh_asset_set_params", _st, [_vp, _P(T.SimParams)]),
     ("rvh_asset_set_colliders", _st, [_vp, _P(T.Collider), C.c_int32]),
+    ("rvh_asset_set_head_transform", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_set_rest_lengths", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_set_strand_wind", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_device_ptr", _st, [_vp, _P(_vp)]),

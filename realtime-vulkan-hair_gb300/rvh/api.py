@@ -198,6 +198,14 @@ class Asset:
         arr = (T.Collider * max(1, len(cols)))(*cols)
         check(self.lib.rvh_asset_set_colliders(self.h, arr, len(cols)))
 
+    def set_head_transform(self, m):
+        """m: 4x4 head pose (numpy, row-major as written; passed column-major), or None to stop."""
+        if m is None:
+            check(self.lib.rvh_asset_set_head_transform(self.h, None))
+            return
+        cm = np.ascontiguousarray(np.asarray(m, np.float32).T)
+        check(self.lib.rvh_asset_set_head_transform(self.h, _fp(cm)))
+
     def step(self, frame, stream=None):
         check(self.lib.rvh_step(self.h, C.byref(frame), stream))
 
@@ -370,6 +378,14 @@ def collider_translate(c, delta):
     C.memmove(C.byref(out), C.byref(c), C.sizeof(T.Collider))
     d = _f32(delta)
     check(load().rvh_collider_translate(C.byref(out), _fp(d)))
+    return out
+
+
+def collider_follow(c, m):
+    """The collider carried by head pose m (4x4, row-major as written)."""
+    out = T.Collider()
+    cm = np.ascontiguousarray(np.asarray(m, np.float32).T)
+    check(load().rvh_collider_follow(C.byref(c), _fp(cm), C.byref(out)))
     return out
 
 

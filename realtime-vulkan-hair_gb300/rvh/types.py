@@ -28,7 +28,8 @@ MEM_DEVICE_BORROWED = 2
 class Collider(C.Structure):
     """struct Collider (src/Scene.h:23-27): transform, inv, invTrans (column-major) + kind."""
     _fields_ = [("transform", C.c_float * 16), ("inv", C.c_float * 16), ("inv_trans", C.c_float * 16),
-                ("kind", C.c_int32), ("radius", C.c_float), ("reserved", C.c_int32 * 2)]
+                ("kind", C.c_int32), ("radius", C.c_float), ("attach_to_head", C.c_int32),
+                ("reserved", C.c_int32)]
 
     def matrices(self):
         return (np.array(self.transform, np.float32).reshape(4, 4).T,
