@@ -167,7 +167,7 @@ rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* desc, const rvh_frame* 
 
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
-    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 4, 8, 16, 32 */
+    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1 (one thread walks each strand), 4, 8, 16, 32 */
     int32_t strands_per_tile;     /* phase-A tile size; 0 = tuner's choice */
     int32_t ctas_per_sm;          /* 0 = occupancy limit */
     int32_t use_graph;            /* 1 = capture the launch in a CUDA graph (default) */
@@ -214,7 +214,7 @@ rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launch
 
 /* ---- autotuning -------------------------------------------------------------
  * Times real batched steps of `assets` for every candidate: lanes per strand
- * {4, 8, 16, 32} (strands per warp 8, 4, 2, 1) x phase-A tile {1, 2, 4}
+ * {1, 4, 8, 16, 32} (strands per warp 32, 8, 4, 2, 1) x phase-A tile {1, 2, 4}
  * rounds, and with tune_grid also each listed grid resolution (every
  * grid-enabled asset re-gridded over the same bounds).  The strand records
  * are restored after every trial.  The winner is cached per workload
@@ -244,7 +244,7 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
  * on the device. */
 typedef struct rvh_server_desc {
     int32_t max_active;           /* requests co-scheduled per launch (default 16) */
-    int32_t lanes_per_strand;     /* batch kernel shape: 4, 8, 16, 32 (default 4) */
+    int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (default 4) */
     int32_t pipeline_depth;       /* launches in flight (default 2) */
     int32_t reserved;
     uint64_t scratch_budget_bytes;/* HBM for the grids of admitted requests; charged to the context */

@@ -26,7 +26,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
 # source -> [(object suffix, defines)]: one translation unit per kernel variant
 PARTS = {
     "rvh_batch.cu": [("_L%d_%s" % (lanes, "exact" if e else "fast"), ["-DRVH_LANES=%d" % lanes, "-DRVH_EXACT=%d" % e])
-                     for lanes in (4, 8, 16, 32) for e in (0, 1)],
+                     for lanes in (1, 4, 8, 16, 32) for e in (0, 1)],
     "rvh_plain.cu": [("_N%d_%s" % (n, "exact" if e else "fast"), ["-DRVH_NFIX=%d" % n, "-DRVH_EXACT=%d" % e])
                      for n in (0, 8, 10, 16, 24, 32) for e in (0, 1)],
 }

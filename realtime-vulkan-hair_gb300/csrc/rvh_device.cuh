@@ -289,13 +289,20 @@ struct CellF {
     float vx, vy, vz, rc, rcp;
 };
 
+// (float)x, rounded to nearest: the int32 conversion when x fits (the usual
+// case; the same value), the int64 one otherwise.
+__device__ __forceinline__ float i64_to_f32(long long x) {
+    const int lo = (int)x;
+    return (long long)lo == x ? __int2float_rn(lo) : __ll2float_rn(x);
+}
+
 template <class M>
 __device__ __forceinline__ CellF cell_from_sums(long long vx, long long vy, long long vz, long long dens, float scale) {
     CellF c;
-    c.vx = (float)vx;
-    c.vy = (float)vy;
-    c.vz = (float)vz;
-    const float fd = (float)dens;
+    c.vx = i64_to_f32(vx);
+    c.vy = i64_to_f32(vy);
+    c.vz = i64_to_f32(vz);
+    const float fd = i64_to_f32(dens);
     c.rc = M::div(fd, scale);
     c.rcp = M::rcp(fd);
     return c;

@@ -228,33 +228,39 @@ __device__ __forceinline__ int slab_width(const BoxGeom& G, int cap) {
     return (int)(w > 0 ? (w < G.ext[0] ? w : G.ext[0]) : 0);
 }
 
-// Splat the round's points: one call per CTA round, every thread calls it.
-// The round's cell box is accumulated in shared memory in x slabs that fit
-// (one slab in almost every round), each flushed once with int64 global
+// Bounds, |v| and count of a lane's points, accumulated one point at a time.
+struct LaneBounds {
+    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
+    float vab = 0.f;
+    int np = 0;
+    __device__ __forceinline__ void add(f3 p) {
+        pmin = f3{fminf(pmin.x, p.x), fminf(pmin.y, p.y), fminf(pmin.z, p.z)};
+        pmax = f3{fmaxf(pmax.x, p.x), fmaxf(pmax.y, p.y), fmaxf(pmax.z, p.z)};
+        ++np;
+    }
+    __device__ __forceinline__ void add_v(f3 v) { vab = fmaxf(vab, fmaxf(fabsf(v.x), fmaxf(fabsf(v.y), fabsf(v.z)))); }
+    // the CTA's cell box of every lane's points into S (all threads call it)
+    template <class M>
+    __device__ __forceinline__ void reduce(const DevAsset& A, BoxShared& S) const {
+        int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
+        if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
+        box_reset(S);
+        __syncthreads();
+        box_reduce(S, lmin, lmax, __float_as_uint(vab), np);
+        __syncthreads();
+    }
+};
+
+// Splats the CTA's points into A.grid; every thread calls it after
+// LaneBounds::reduce.  visit(f) calls f(position, velocity) for each of the
+// lane's points.  The cell box is accumulated in shared memory in x slabs that
+// fit (one slab in almost every round), each flushed once with int64 global
 // atomics.  A slab falls back to direct global atomics when its int32 partial
 // sums cannot be proven free of overflow (|partial| <= vmax * (density + npts)
 // since |int(s w v)| <= vmax * (int(s w) + 1)); the whole round does when not
 // even a one-cell-wide slab fits.
-template <int K, class M>
-__device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K], const f3 (&vo)[K], unsigned mask,
-                                            int* box, BoxShared& S, unsigned* stats) {
-    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
-    float vab = 0.f;
-    int np = 0;
-    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        pmin = f3{fminf(pmin.x, xo[k].x), fminf(pmin.y, xo[k].y), fminf(pmin.z, xo[k].z)};
-        pmax = f3{fmaxf(pmax.x, xo[k].x), fmaxf(pmax.y, xo[k].y), fmaxf(pmax.z, xo[k].z)};
-        vab = fmaxf(vab, fmaxf(fabsf(vo[k].x), fmaxf(fabsf(vo[k].y), fabsf(vo[k].z))));
-        ++np;
-    }
-    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
-    box_reset(S);
-    __syncthreads();
-    box_reduce(S, lmin, lmax, __float_as_uint(vab), np);
-    __syncthreads();
+template <class M, class Visit>
+__device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxShared& S, unsigned* stats, Visit visit) {
     const int npts = S.npts;
     if (npts > 0) {
         const BoxGeom G = box_geom(S);
@@ -272,12 +278,7 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
             int4* b4 = reinterpret_cast<int4*>(box);
             for (int c = threadIdx.x; c < nv; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
             __syncthreads();
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                if (!((mask >> k) & 1u)) continue;
-                const Corners C = corners_of<M>(A, xo[k]);
-                splat_point_box<M>(A, C, vo[k], box, P, nv);
-            }
+            visit([&](f3 p, f3 v) { splat_point_box<M>(A, corners_of<M>(A, p), v, box, P, nv); });
             __syncthreads();
             bool ok = true;
             for (int c = threadIdx.x; c < nv; c += kThreads)
@@ -297,20 +298,34 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
                 }
             } else {
                 all_box = false;
-#pragma unroll
-                for (int k = 0; k < K; ++k)
-                    if ((mask >> k) & 1u) splat_point<M>(A, xo[k], vo[k], x0, x0 + P.ext[0]);
+                const int x1 = x0 + P.ext[0];
+                visit([&](f3 p, f3 v) { splat_point<M>(A, p, v, x0, x1); });
             }
             __syncthreads();   // the box is cleared again by the next slab
         }
-        if (w == 0) {
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                if ((mask >> k) & 1u) splat_point<M>(A, xo[k], vo[k]);
-        }
+        if (w == 0) visit([&](f3 p, f3 v) { splat_point<M>(A, p, v); });
         if (stats && threadIdx.x == 0) atomicAdd(stats + (all_box ? 0 : 1), 1u);
     }
     __syncthreads();  // every read of S and of the box is done before the next round resets them
+}
+
+// Splat the round's points held in registers (bit k of mask: xo[k], vo[k]).
+template <int K, class M>
+__device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K], const f3 (&vo)[K], unsigned mask,
+                                            int* box, BoxShared& S, unsigned* stats) {
+    LaneBounds lb;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        if (!((mask >> k) & 1u)) continue;
+        lb.add(xo[k]);
+        lb.add_v(vo[k]);
+    }
+    lb.reduce<M>(A, S);
+    splat_points<M>(A, box, S, stats, [&](auto&& f) {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if ((mask >> k) & 1u) f(xo[k], vo[k]);
+    });
 }
 
 // Copies the box's cells of grid G into shared memory as CellF (float4
@@ -332,55 +347,61 @@ __device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigne
     }
 }
 
+// The CTA's gather box over grid `grid` (after LaneBounds::reduce of the
+// points to gather): loaded into shared memory when it fits, else the gather
+// reads the grid directly.  gather(x, v, dt) then returns loop 3's velocity.
+// A null grid builds an unused object (no synchronisation, no loads).
+template <class M>
+struct GatherBox {
+    const DevAsset& A;
+    const unsigned long long* grid;
+    BoxGeom G;
+    bool use;
+    const float4* bf;
+    const float* br;
+    __device__ __forceinline__ GatherBox(const DevAsset& a, const unsigned long long* g, unsigned char* smem,
+                                         const BoxShared& S, unsigned* stats)
+        : A(a), grid(g), G(box_geom(S)), bf(reinterpret_cast<const float4*>(smem)),
+          br(reinterpret_cast<const float*>(smem + 16 * kBoxCellsB)) {
+        use = false;
+        if (!grid) return;   // nothing to gather (uniform across the CTA)
+        const int npts = S.npts;
+        use = npts > 0 && G.vol <= kBoxCellsB;
+        if (use) load_gather_box<M>(A, grid, G, reinterpret_cast<float4*>(smem), reinterpret_cast<float*>(smem + 16 * kBoxCellsB));
+        __syncthreads();
+        if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+    }
+    __device__ __forceinline__ f3 gather(f3 x, f3 v, float dt) const {
+        const Corners C = corners_of<M>(A, x);
+        if (use) {
+            return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
+                const int li = G.offset(a, b, c);
+                const float4 q = bf[li];
+                return CellF{q.x, q.y, q.z, q.w, br[li]};
+            });
+        }
+        const int nxny = A.nx * A.ny;
+        return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
+            return cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + c * nxny));
+        });
+    }
+};
+
 // Loop 3 of the PREVIOUS step for the round's points (fused batched step):
 // gather from A.grid_prev at the positions the previous step produced and
 // blend the friction into v.  Same box scheme as phase B; every thread calls it.
 template <int K, class M>
 __device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K], f3 (&v)[K], unsigned mask,
                                              unsigned char* smem, BoxShared& S, unsigned* stats) {
-    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
-    int np = 0;
-    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
+    LaneBounds lb;
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        pmin = f3{fminf(pmin.x, x[k].x), fminf(pmin.y, x[k].y), fminf(pmin.z, x[k].z)};
-        pmax = f3{fmaxf(pmax.x, x[k].x), fmaxf(pmax.y, x[k].y), fmaxf(pmax.z, x[k].z)};
-        ++np;
-    }
-    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
-    box_reset(S);
-    __syncthreads();
-    box_reduce(S, lmin, lmax, 0u, np);
-    __syncthreads();
-    const int npts = S.npts;
-    const BoxGeom BG = box_geom(S);
-    const bool use = npts > 0 && BG.vol <= kBoxCellsB;
-    float4* bf = reinterpret_cast<float4*>(smem);
-    float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
-    const unsigned long long* G = A.grid_prev;
-    const int nxny = A.nx * A.ny;
-    if (use) {
-        load_gather_box<M>(A, G, BG, bf, br);
-        __syncthreads();
-    }
-    if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+    for (int k = 0; k < K; ++k)
+        if ((mask >> k) & 1u) lb.add(x[k]);
+    lb.reduce<M>(A, S);
+    const GatherBox<M> gb(A, A.grid_prev, smem, S, stats);
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        const Corners C = corners_of<M>(A, x[k]);
-        if (use) {
-            v[k] = gather_point<M>(A, A.dt_prev, x[k], v[k], C, [&](int a, int b, int c) {
-                const int li = BG.offset(a, b, c);
-                const float4 q = bf[li];
-                return CellF{q.x, q.y, q.z, q.w, br[li]};
-            });
-        } else {
-            v[k] = gather_point<M>(A, A.dt_prev, x[k], v[k], C, [&](int a, int b, int c) {
-                return cell_from_global<M>(A, G, (unsigned)(a + b * A.nx + c * nxny));
-            });
-        }
-    }
+    for (int k = 0; k < K; ++k)
+        if ((mask >> k) & 1u) v[k] = gb.gather(x[k], v[k], A.dt_prev);
     __syncthreads();  // the box memory is reused by the splat of this round
 }
 
@@ -409,6 +430,93 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
     }
 }
 
+// One thread per strand (lanes_per_strand = 1): strands [begin, end) of one
+// asset in rounds of kThreads strands.  Each thread walks its strand from the
+// root to the tip with a few registers of state, so any point count uses the
+// same code and no lane repeats another's FTL chain:
+//   1. (fused step) the cell box of the strand points' current positions is
+//      loaded from A.grid_prev for the pending loop 3;
+//   2. per point i = 1..n-1: pending gather + friction, collision force,
+//      prediction, FTL from the moved parent, velocity, clamp, correction;
+//      point i-1's DFTL term needs corr_i, so its velocity is stored one
+//      point later (the last point gets none, compute.comp:213);
+//   3. the round's new positions and velocities are read back (this thread's
+//      own stores) and splatted through the shared box.
+// Operation order per point is that of strand_phase_a, so exact math gives
+// the same bits as every other path.
+template <class M>
+__device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
+                                              unsigned* stats) {
+    const int n = A.n_points;
+    const float dt = A.dt;
+    const float dt2 = M::mul(dt, dt);
+    const bool moving = A.root_rest != nullptr;
+    for (int r0 = begin; r0 < end; r0 += kThreads) {
+        const int strand = r0 + (int)threadIdx.x;
+        const bool valid = strand < end;
+        const int np = valid ? n : 1;    // points this thread walks (none past the tile)
+        float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+
+        // 1. the pending gather's box
+        const bool pend_gather = A.grid_prev != nullptr;
+        if (pend_gather) {
+            LaneBounds lb;
+            for (int i = 1; i < np; ++i) lb.add(xyz(rec[i]));
+            lb.reduce<M>(A, S);
+        }
+        const GatherBox<M> gb(A, A.grid_prev, smem, S, stats);
+
+        // 2. loops 1-2 along the strand
+        f3 f0 = v_add<M>(f3{A.gravity[0], A.gravity[1], A.gravity[2]}, f3{A.wind[0], A.wind[1], A.wind[2]});
+        if (A.strand_wind != nullptr && valid) f0 = v_add<M>(f0, xyz(A.strand_wind[strand]));
+        const float r = valid ? A.rest[strand] : 0.f;
+        f3 par = valid ? xyz(rec[0]) : f3{0.f, 0.f, 0.f};
+        if (moving && valid) {
+            par = head_point<M>(A.head, xyz(A.root_rest[strand]));
+            st_f4(rec, par, 1.0f);
+        }
+        LaneBounds sb;
+        f3 vprev = {0.f, 0.f, 0.f};
+        for (int i = 1; i < np; ++i) {
+            const f3 x = xyz(rec[i]);
+            f3 v = xyz(rec[n + i]);
+            if (pend_gather) v = gb.gather(x, v, A.dt_prev);
+            const f3 force = collide_force<M>(A, x, f0);
+            // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
+            const f3 p = v_add<M>(v_add<M>(x, v_scale<M>(dt, v)), v_scale<M>(dt2, force));
+            const f3 dir = v_normalize<M>(v_sub<M>(p, par));
+            const f3 xn = v_add<M>(par, v_scale<M>(r, dir));
+            const f3 newVel = v_div<M>(v_sub<M>(xn, x), dt);
+            f3 vel = v_scale<M>(A.damping, newVel);
+            if (v_len<M>(vel) > A.vmax) vel = v_scale<M>(A.vmax, v_normalize<M>(vel));
+            const f3 cor = v_scale<M>(A.dftl, v_sub<M>(xn, p));
+            st_f4(rec + i, xn, 1.0f);
+            st_f4(rec + 2 * n + i, cor, 0.0f);
+            if (i >= 2) {   // point i-1: v -= corr_i / dt (compute.comp:213-215)
+                vprev = v_sub<M>(vprev, v_div<M>(cor, dt));
+                st_f4(rec + n + i - 1, vprev, 0.0f);
+                sb.add_v(vprev);
+            }
+            vprev = vel;
+            par = xn;
+            sb.add(xn);
+        }
+        if (np >= 2) {
+            st_f4(rec + n + np - 1, vprev, 0.0f);
+            sb.add_v(vprev);
+        }
+        if (pend_gather) __syncthreads();   // the gather box memory is reused by the splat
+
+        // 3. splat the round
+        if (A.grid_enabled) {
+            sb.reduce<M>(A, S);
+            splat_points<M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
+                for (int i = 1; i < np; ++i) f(xyz(rec[i]), xyz(rec[n + i]));
+            });
+        }
+    }
+}
+
 template <int L, class M>
 __device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
                                            unsigned* stats) {
@@ -433,9 +541,7 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
     f3 x[kPtsB];
     int off[kPtsB];   // record offset (float4 units) of the point's curvePoints slot
     unsigned m = 0u;
-    int lmin[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, lmax[3] = {-0x7fffffff - 1, -0x7fffffff - 1, -0x7fffffff - 1};
-    int np = 0;
-    f3 pmin = {3.0e38f, 3.0e38f, 3.0e38f}, pmax = {-3.0e38f, -3.0e38f, -3.0e38f};
+    LaneBounds lb;
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
         const int q = threadIdx.x + j * kThreads;
@@ -448,45 +554,15 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         off[j] = ls * (3 * n) + i;
         x[j] = xyz(ld_cg(base + off[j]));
         m |= 1u << j;
-        pmin = f3{fminf(pmin.x, x[j].x), fminf(pmin.y, x[j].y), fminf(pmin.z, x[j].z)};
-        pmax = f3{fmaxf(pmax.x, x[j].x), fmaxf(pmax.y, x[j].y), fmaxf(pmax.z, x[j].z)};
-        ++np;
+        lb.add(x[j]);
     }
-    if (np > 0) bounds_of_extremes<M>(A, pmin, pmax, lmin, lmax);
-    box_reset(S);
-    __syncthreads();
-    box_reduce(S, lmin, lmax, 0u, np);
-    __syncthreads();
-    const int npts = S.npts;
-    const BoxGeom BG = box_geom(S);
-    const bool use = npts > 0 && BG.vol <= kBoxCellsB;
-    float4* bf = reinterpret_cast<float4*>(smem);
-    float* br = reinterpret_cast<float*>(smem + 16 * kBoxCellsB);
-    if (use) {
-        load_gather_box<M>(A, A.grid, BG, bf, br);
-        __syncthreads();
-    }
-    if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+    lb.reduce<M>(A, S);
+    const GatherBox<M> gb(A, A.grid, smem, S, stats);
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
         if (!((m >> j) & 1u)) continue;
         float4* vp = base + off[j] + n;
-        const f3 v = xyz(ld_cg(vp));
-        const Corners C = corners_of<M>(A, x[j]);
-        f3 out;
-        if (use) {
-            out = gather_point<M>(A, A.dt, x[j], v, C, [&](int a, int b, int c) {
-                const int li = BG.offset(a, b, c);
-                const float4 q = bf[li];
-                return CellF{q.x, q.y, q.z, q.w, br[li]};
-            });
-        } else {
-            const int nxny = A.nx * A.ny;
-            out = gather_point<M>(A, A.dt, x[j], v, C, [&](int a, int b, int c) {
-                return cell_from_global<M>(A, A.grid, (unsigned)(a + b * A.nx + c * nxny));
-            });
-        }
-        st_f4(vp, out, 0.0f);
+        st_f4(vp, gb.gather(x[j], xyz(ld_cg(vp)), A.dt), 0.0f);
     }
     __syncthreads();  // every read of S and of the box is done before the next tile resets them
 }
@@ -550,7 +626,8 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_
             if (threadIdx.x == 0) s_asset = w.asset;
         }
         if (w.kind == ITEM_A) {
-            tile_a_any<L, M>(A, w.begin, w.end, dsm, S, B.stats);
+            if constexpr (L == 1) tile_a_stream<M>(A, w.begin, w.end, dsm, S, B.stats);
+            else tile_a_any<L, M>(A, w.begin, w.end, dsm, S, B.stats);
             if (!A.grid_enabled && w.begin == 0 && threadIdx.x == 0) write_draw(A);
             __syncthreads();
             if (threadIdx.x == 0) {

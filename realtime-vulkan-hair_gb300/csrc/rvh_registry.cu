@@ -45,6 +45,7 @@ const void* plain_b_kernel(bool exact) {
 
 const void* batch_kernel(int lanes, bool exact) {
     switch (lanes) {
+        case 1: return exact ? batch_kernel_inst<1, true>() : batch_kernel_inst<1, false>();
         case 4: return exact ? batch_kernel_inst<4, true>() : batch_kernel_inst<4, false>();
         case 8: return exact ? batch_kernel_inst<8, true>() : batch_kernel_inst<8, false>();
         case 16: return exact ? batch_kernel_inst<16, true>() : batch_kernel_inst<16, false>();

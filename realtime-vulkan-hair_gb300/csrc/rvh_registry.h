@@ -9,7 +9,7 @@ namespace rvh {
 bool plain_a_supported(int n, int lanes);
 const void* plain_a_kernel(int n, int lanes, bool exact);
 const void* plain_b_kernel(bool exact);
-// Persistent batch kernel; lanes in {4, 8, 16, 32}.
+// Persistent batch kernel; lanes in {1, 4, 8, 16, 32} (1: one thread per strand).
 const void* batch_kernel(int lanes, bool exact);
 bool batch_supported(int lanes);
 // One translation unit per instantiation (compiled in parallel): the

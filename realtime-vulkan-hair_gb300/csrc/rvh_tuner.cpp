@@ -1,6 +1,6 @@
 // rvh_tuner.cpp — autotuner for the batched step.
 //
-// Candidates: lanes per strand {4, 8, 16, 32} (strands per warp 8, 4, 2, 1),
+// Candidates: lanes per strand {1, 4, 8, 16, 32} (strands per warp 32, 8, 4, 2, 1),
 // phase-A tile size {1, 2, 4} rounds of kWarps * strands-per-warp strands,
 // and optionally the grid resolution of every grid-enabled asset (same
 // bounds, finer or coarser cells).  Each candidate times real batched steps
@@ -107,12 +107,12 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
     if (d.tune_grid && d.n_grid_res > 0) res_list.assign(d.grid_res, d.grid_res + d.n_grid_res);
     rvh_tune_result r{};
     r.best_ms = 1e30f;
-    const int lanes_c[4] = {4, 8, 16, 32};
+    const int lanes_c[5] = {1, 4, 8, 16, 32};
     const int tile_c[3] = {1, 2, 4};
     rvh_status st = RVH_OK;
     for (int res : res_list) {
         for (int i = 0; i < n && st == RVH_OK; ++i) st = set_grid_res(assets[i], res, orig[i]);
-        for (int li = 0; li < 4 && st == RVH_OK; ++li)
+        for (int li = 0; li < 5 && st == RVH_OK; ++li)
             for (int ti = 0; ti < 3 && st == RVH_OK; ++ti) {
                 const int lanes = lanes_c[li];
                 const int tile = tile_c[ti] * kWarps * (32 / lanes);

@@ -22,6 +22,9 @@ def make_assets(ctx, specs):
 @pytest.mark.parametrize("lanes", [4, 8, 16, 32])
 @pytest.mark.parametrize("use_graph", [True, False])
 def test_batch_equals_plain(gpu_ctx_fast, lanes, use_graph):
+    """Fast math: the register kernels share every device function with the
+    plain step, so the bits agree (the one-thread-per-strand kernel contracts
+    differently in fast math and is checked in exact math below)."""
     specs = configs.batched(n_assets=10, scale=0.03)
     plain = make_assets(gpu_ctx_fast, specs)
     batched = make_assets(gpu_ctx_fast, specs)
@@ -42,10 +45,11 @@ def test_batch_equals_plain(gpu_ctx_fast, lanes, use_graph):
         a.close()
 
 
-def test_batch_exact_equals_fp32_twin(gpu_ctx, oracle):
+@pytest.mark.parametrize("lanes", [0, 1])
+def test_batch_exact_equals_fp32_twin(gpu_ctx, oracle, lanes):
     specs = configs.batched(n_assets=6, scale=0.02, seed=9)
     assets = make_assets(gpu_ctx, specs)
-    b = api.Batch(gpu_ctx, assets)
+    b = api.Batch(gpu_ctx, assets, lanes=lanes)
     steps = 3
     for k in range(steps):
         b.step([s.frame(k) for s in specs])
@@ -87,3 +91,36 @@ def test_batch_then_plain_then_batch(gpu_ctx_fast):
     b.close()
     for a in x + y:
         a.close()
+
+
+@pytest.mark.parametrize("steps", [1, 5])
+def test_streaming_kernel_exact_equals_plain(gpu_ctx, steps):
+    """lanes_per_strand = 1 (one thread walks each strand) in exact math: the
+    same bits as the plain step, over fused steps and with a pending finish."""
+    specs = configs.batched(n_assets=8, scale=0.03, seed=5)
+    plain = make_assets(gpu_ctx, specs)
+    batched = make_assets(gpu_ctx, specs)
+    b = api.Batch(gpu_ctx, batched, lanes=1)
+    for k in range(steps):
+        for a, s in zip(plain, specs):
+            a.step(s.frame(k))
+        b.step([s.frame(k) for s in specs])
+    b.check()
+    for a, c in zip(plain, batched):
+        x, y = a.read(), c.read()
+        assert np.array_equal(x, y), "max diff %g" % np.abs(x - y).max()
+    b.close()
+
+
+def test_streaming_kernel_fast_close_to_fp64(gpu_ctx_fast, oracle):
+    specs = configs.batched(n_assets=4, scale=0.02, seed=6)
+    assets = make_assets(gpu_ctx_fast, specs)
+    b = api.Batch(gpu_ctx_fast, assets, lanes=1)
+    b.step([s.frame(0) for s in specs])
+    for a, s in zip(assets, specs):
+        ref64 = s.records.astype(np.float64)
+        oracle.run(ref64, s.n_points, s.rest, s.params, [s.frame(0)], s.colliders, 1, threads=8)
+        L = s.rest.astype(np.float64) * (s.n_points - 1)
+        mx, p99, mean = rel_pos_err(a.read(), ref64, s.n_points, L)
+        assert mx <= 1e-5, (mx, p99, mean)
+    b.close()
