@@ -244,7 +244,8 @@ __device__ __forceinline__ void red_add_s64(unsigned long long* p, long long v) 
 }
 
 // Splat one point: 4 x int64 atomics per touched corner, sums wrap-free.
-// Only corners with x index in [xlo, xhi) are added.
+// Only corners with x index in [xlo, xhi) are added.  (Inlined even where it
+// is a rare fallback: a call costs spills around it at the call sites.)
 template <class M>
 __device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel, int xlo = 0, int xhi = 0x7fffffff) {
     const Corners C = corners_of<M>(A, pos);

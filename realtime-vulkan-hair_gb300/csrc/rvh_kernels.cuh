@@ -309,10 +309,43 @@ __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxSha
     __syncthreads();  // every read of S and of the box is done before the next round resets them
 }
 
+// Rolled loops over a lane's K register-held points: the body is emitted once
+// and the point arrays rotate one slot per iteration (back in order after K),
+// so the large splat and gather bodies are not unrolled K times (instruction
+// cache).  kRolledPoints = false unrolls them instead.
+constexpr bool kRolledPoints = true;
+
+template <int K>
+__device__ __forceinline__ void rotate_points(f3 (&a)[K]) {
+    const f3 t = a[0];
+#pragma unroll
+    for (int k = 0; k + 1 < K; ++k) a[k] = a[k + 1];
+    a[K - 1] = t;
+}
+
+// f(x[k], v[k]) for every k with mask bit k set; v may be updated by f.
+template <int K, class F>
+__device__ __forceinline__ void for_lane_points(f3 (&x)[K], f3 (&v)[K], unsigned mask, F&& f) {
+    if (kRolledPoints && K > 1) {
+        unsigned m = mask;
+#pragma unroll 1
+        for (int k = 0; k < K; ++k) {
+            if (m & 1u) f(x[0], v[0]);
+            rotate_points(x);
+            rotate_points(v);
+            m = (m >> 1) | ((m & 1u) << (K - 1));
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if ((mask >> k) & 1u) f(x[k], v[k]);
+    }
+}
+
 // Splat the round's points held in registers (bit k of mask: xo[k], vo[k]).
 template <int K, class M>
-__device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K], const f3 (&vo)[K], unsigned mask,
-                                            int* box, BoxShared& S, unsigned* stats) {
+__device__ __forceinline__ void splat_round(const DevAsset& A, f3 (&xo)[K], f3 (&vo)[K], unsigned mask, int* box,
+                                            BoxShared& S, unsigned* stats) {
     LaneBounds lb;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -322,9 +355,7 @@ __device__ __forceinline__ void splat_round(const DevAsset& A, const f3 (&xo)[K]
     }
     lb.reduce<M>(A, S);
     splat_points<M>(A, box, S, stats, [&](auto&& f) {
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if ((mask >> k) & 1u) f(xo[k], vo[k]);
+        for_lane_points(xo, vo, mask, [&](f3& p, f3& v) { f(p, v); });
     });
 }
 
@@ -345,6 +376,16 @@ __device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigne
         bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.rc);
         br[c] = cf.rcp;
     }
+}
+
+// Loop 3 for one point read straight from the grid (the rare fallback of the
+// gather boxes).
+template <class M>
+__device__ __forceinline__ f3 gather_point_direct(const DevAsset& A, const unsigned long long* grid, float dt, f3 x, f3 v) {
+    const int nxny = A.nx * A.ny;
+    return gather_point<M>(A, dt, x, v, corners_of<M>(A, x), [&](int a, int b, int c) {
+        return cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + c * nxny));
+    });
 }
 
 // The CTA's gather box over grid `grid` (after LaneBounds::reduce of the
@@ -380,10 +421,7 @@ struct GatherBox {
                 return CellF{q.x, q.y, q.z, q.w, br[li]};
             });
         }
-        const int nxny = A.nx * A.ny;
-        return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
-            return cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + c * nxny));
-        });
+        return gather_point_direct<M>(A, grid, dt, x, v);
     }
 };
 
@@ -391,7 +429,7 @@ struct GatherBox {
 // gather from A.grid_prev at the positions the previous step produced and
 // blend the friction into v.  Same box scheme as phase B; every thread calls it.
 template <int K, class M>
-__device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K], f3 (&v)[K], unsigned mask,
+__device__ __forceinline__ void gather_round(const DevAsset& A, f3 (&x)[K], f3 (&v)[K], unsigned mask,
                                              unsigned char* smem, BoxShared& S, unsigned* stats) {
     LaneBounds lb;
 #pragma unroll
@@ -399,9 +437,7 @@ __device__ __forceinline__ void gather_round(const DevAsset& A, const f3 (&x)[K]
         if ((mask >> k) & 1u) lb.add(x[k]);
     lb.reduce<M>(A, S);
     const GatherBox<M> gb(A, A.grid_prev, smem, S, stats);
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if ((mask >> k) & 1u) v[k] = gb.gather(x[k], v[k], A.dt_prev);
+    for_lane_points(x, v, mask, [&](f3& p, f3& vel) { vel = gb.gather(p, vel, A.dt_prev); });
     __syncthreads();  // the box memory is reused by the splat of this round
 }
 
