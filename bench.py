@@ -208,6 +208,43 @@ def run_served(ctx, args, rank):
     return out, pts
 
 
+def run_tess(ctx, api, configs, warmup=3, reps=10):
+    """Strand tessellation of the 100k-strand head (32 points) after a few
+    steps, with the reference's levels (12 isolines x 42 segments): device
+    time by CUDA events on the launching stream."""
+    import torch
+    spec = configs.full_head()
+    a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest)
+    a.set_params(spec.params)
+    a.set_colliders(spec.colliders)
+    for k in range(3):
+        a.step(spec.frame(k))
+    ctx.synchronize()
+    d = api.tess_desc_reference()
+    ns, per = spec.n_strands, d.n_lines * (d.n_segments + 1)
+    out = torch.empty((ns * per * 4,), dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    for _ in range(warmup):
+        a.tessellate(out.data_ptr(), None, desc=d, stream=st.cuda_stream)
+    st.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        a.tessellate(out.data_ptr(), None, desc=d, stream=st.cuda_stream)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    a.close()
+    vertices = ns * per
+    alg = vertices * 16 + ns * spec.n_points * 16      # vertex writes + position reads
+    peak, _ = load_peaks()
+    gbs = alg / (ms * 1e-3) / 1e9
+    return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments per strand",
+            "vertices": vertices, "ms": ms, "vertices_per_s": vertices / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "bytes_per_launch": alg}}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle's OpenMP restatement on the host cores."""
     if rank != 0:
@@ -250,6 +287,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-tess", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
@@ -372,6 +410,10 @@ def main():
                "sample": "first %d assets (%d points) of the workload, 3 steps, FP32 OpenMP restatement "
                          "of the reference shader" % (len(sample), spts)}
 
+    tess = None
+    if world == 1 and not args.no_tess:
+        tess = run_tess(ctx, api, configs)
+
     served, served_pts = None, None
     if not args.no_served and world == 1:
         batch.close()
@@ -404,7 +446,7 @@ def main():
                          "fallback 6.8 TB/s"},
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches),
+            "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
             "served": None if served is None else {
                 "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
                             "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (

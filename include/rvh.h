@@ -165,6 +165,32 @@ typedef struct rvh_noalloc_step_desc {
 } rvh_noalloc_step_desc;
 rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* desc, const rvh_frame* frame, void* stream);
 
+/* ---- strand tessellation (src/shaders/hair.tesc:19-20, src/shaders/hair.tese) ----
+ * The reference's tessellation stages turn each guide strand into isolines of
+ * a Bezier curve offset by a clump width (single-strand clumping,
+ * hair.tese:153-330).  Without a graphics pipeline the same vertices are
+ * written to a device buffer: per strand n_lines isolines of n_segments + 1
+ * vertices, each a float4 {position xyz, strand width}, strand-major then
+ * isoline-major.  The per-strand hash uses a correctly rounded sin (the
+ * shader uses the platform's).  At v = 1 the curve ends at the tip (the shader
+ * reads past the strand there). */
+typedef struct rvh_tess_desc {
+    int32_t n_lines;        /* isolines per strand, 1..64 (gl_TessLevelOuter[0] = 12, hair.tesc:19) */
+    int32_t n_segments;     /* segments per isoline, 1..256 (gl_TessLevelOuter[1] = 42, hair.tesc:20) */
+    float clump_radius;     /* hair.tese:239: 0.5 */
+    float root_width;       /* hair.tese:324: 0.02 */
+    float tip_width;        /* hair.tese:325: 0.01 */
+    int32_t reserved;
+} rvh_tess_desc;
+/* The reference's constants. */
+rvh_status rvh_tess_desc_reference(rvh_tess_desc* d);
+/* Tessellates the asset's current positions on `stream` (NULL: the context's).
+ * vertices: device, n_strands * n_lines * (n_segments + 1) float4.
+ * frames: device or NULL, n_strands * (n_points - 1) * 3 float4 {tangent, b1,
+ * b2} per segment (hair.tese:289-297: normalized segment direction and its
+ * Frisvad orthonormal basis).  Both 16-byte aligned. */
+rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vertices, void* frames, void* stream);
+
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
     int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1 (one thread walks each strand), 4, 8, 16, 32 */

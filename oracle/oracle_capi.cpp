@@ -12,6 +12,7 @@
 
 #include "hair_adjoint.hpp"
 #include "hair_oracle.hpp"
+#include "tess_oracle.hpp"
 
 namespace {
 
@@ -68,6 +69,24 @@ int oracle_run_head_f32(float* state, int ns, int n, const float* rest, const fl
     if (!heads || !root_rest) return 1;
     return run<float>(state, ns, n, rest, strand_wind, P, frames, cols, ncol, n_steps, threads, grid_out, heads,
                       root_rest);
+}
+/* Strand tessellation (tess_oracle.hpp): out = ns * n_lines * (n_segments+1)
+ * float4; frames (nullable) = ns * (n-1) * 3 float4.  sin_mode 0: the C
+ * library's float sin in the hash (as the reference compiled here), 1: the
+ * double sin rounded once (the library's definition). */
+int oracle_tess(const float* records, int ns, int n, int n_lines, int n_segments, float clump_radius,
+                float root_width, float tip_width, int sin_mode, float* out, float* frames) {
+    if (!records || !out || ns < 0 || n < 2 || n > RVH_MAX_POINTS || n_lines < 1 || n_segments < 1) return 1;
+    oracle::tess::TessParams P;
+    P.n_lines = n_lines;
+    P.n_segments = n_segments;
+    P.clump_radius = clump_radius;
+    P.root_width = root_width;
+    P.tip_width = tip_width;
+    oracle::tess::tessellate(records, ns, n, P,
+                             sin_mode == 0 ? oracle::tess::RefSin::kFloat : oracle::tess::RefSin::kDouble, out,
+                       frames);
+    return 0;
 }
 /* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */
 int oracle_adjoint_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,

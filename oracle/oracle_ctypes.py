@@ -35,6 +35,9 @@ def lib():
                   C.c_int, C.c_int, C.c_int, _P(C.c_int64)]
         l.oracle_run_f64.argtypes = [_P(C.c_double)] + common
         l.oracle_run_f32.argtypes = [_P(C.c_float)] + common
+        l.oracle_tess.argtypes = [_P(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                  C.c_float, C.c_int, _P(C.c_float), _P(C.c_float)]
+        l.oracle_tess.restype = C.c_int
         l.oracle_run_head_f64.argtypes = [_P(C.c_double)] + common + [_P(C.c_float), _P(C.c_float)]
         l.oracle_run_head_f32.argtypes = [_P(C.c_float)] + common + [_P(C.c_float), _P(C.c_float)]
         adj = [_P(C.c_double), C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(T.SimParams), _P(T.Frame),
@@ -202,3 +205,18 @@ def ref_run(strands, colliders_steps, times, want_grid=False):
     if rc != 0:
         raise RuntimeError("ref_run failed")
     return grid, draw
+
+
+def tessellate(records, n_points, n_lines=12, n_segments=42, clump_radius=0.5, root_width=0.02, tip_width=0.01,
+               sin_mode=1, frames=False):
+    """Oracle tessellation: (ns, n_lines, n_segments+1, 4) float32 and, with
+    frames, (ns, n_points-1, 3, 4)."""
+    rec = np.ascontiguousarray(records, np.float32)
+    ns = rec.shape[0]
+    out = np.zeros((ns, n_lines, n_segments + 1, 4), np.float32)
+    fr = np.zeros((ns, n_points - 1, 3, 4), np.float32) if frames else None
+    rc = lib().oracle_tess(_fptr(rec, C.c_float), ns, n_points, n_lines, n_segments, clump_radius, root_width,
+                           tip_width, sin_mode, _fptr(out, C.c_float), _fptr(fr, C.c_float))
+    if rc != 0:
+        raise RuntimeError("oracle_tess failed: %d" % rc)
+    return (out, fr) if frames else out

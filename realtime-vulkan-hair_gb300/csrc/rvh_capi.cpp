@@ -117,10 +117,14 @@ DevCollider pack_collider(const rvh_collider& c) {
     return d;
 }
 
+// Fewest lanes per strand with a compiled phase-A kernel, starting from the
+// preferred count for n (point counts without a fixed-size kernel use the
+// generic one, which needs >= 4 lanes).
 int default_lanes(int n) {
-    if (n <= 10) return 1;
-    if (n <= 16) return 2;
-    return 4;
+    const int pref = n <= 10 ? 1 : n <= 16 ? 2 : 4;
+    for (int l = pref; l <= 32; l *= 2)
+        if (plain_a_supported(n, l)) return l;
+    return pref;
 }
 
 int Asset::pick_grid(int avoid1, int avoid2) const {
@@ -612,6 +616,7 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     for (int i = 0; i < 3; ++i) c->free(a->grid[i]);
     c->free(a->draw);
     c->free(a->root_rest);
+    c->free(a->tess_tables);
     delete a;
     return RVH_OK;
 }

@@ -98,6 +98,10 @@ struct Asset {
     bool head_active = false;
     float head[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};   // column-major
     DevBuf root_rest;   // float4 per strand, captured at the first head transform
+    // tessellation tables of the last descriptor (rvh_asset_tessellate)
+    DevBuf tess_tables;
+    rvh_tess_desc tess_desc{};
+    size_t tess_off[6] = {0, 0, 0, 0, 0, 0};
 
     size_t record_bytes() const { return size_t(n_strands) * 48u * size_t(n_points); }
     size_t grid_bytes() const { return grid_cells * 32u; }

@@ -209,6 +209,13 @@ class Asset:
     def step(self, frame, stream=None):
         check(self.lib.rvh_step(self.h, C.byref(frame), stream))
 
+    def tessellate(self, vertices_ptr, frames_ptr=None, desc=None, stream=None):
+        """Writes n_strands * n_lines * (n_segments+1) float4 vertices (and, with
+        frames_ptr, (n_points-1) * 3 float4 frames per strand) to device memory."""
+        d = desc if desc is not None else tess_desc_reference()
+        check(self.lib.rvh_asset_tessellate(self.h, C.byref(d), C.c_void_p(vertices_ptr),
+                                            C.c_void_p(frames_ptr) if frames_ptr else None, stream))
+
     def read(self):
         out = np.empty((self.n_strands, 3 * self.n_points, 4), np.float32)
         check(self.lib.rvh_asset_read(self.h, out.ctypes.data_as(C.c_void_p), out.nbytes))
@@ -429,6 +436,20 @@ def sphere_on_orbit(orbit, t):
     c = T.Collider()
     check(load().rvh_sphere_on_orbit(C.byref(orbit), t, C.byref(c)))
     return c
+
+
+# ---- strand tessellation ------------------------------------------------------------
+class TessDesc(C.Structure):
+    _fields_ = [("n_lines", C.c_int32), ("n_segments", C.c_int32), ("clump_radius", C.c_float),
+                ("root_width", C.c_float), ("tip_width", C.c_float), ("reserved", C.c_int32)]
+
+
+def tess_desc_reference(**kw):
+    d = TessDesc()
+    check(load().rvh_tess_desc_reference(C.byref(d)))
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
 
 
 # ---- scalp meshes and root sampling ----------------------------------------------

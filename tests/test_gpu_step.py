@@ -235,3 +235,14 @@ def test_borrowed_device_buffer_zero_copy(gpu_ctx_fast, oracle):
     assert np.array_equal(buf.cpu().numpy(), b.read())
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 7, 9, 11, 13, 31])
+def test_default_lanes_cover_every_point_count(gpu_ctx, oracle, n):
+    """An asset created without lanes_per_strand steps for any n in [2, 32]
+    (point counts without a fixed-size kernel take the generic one)."""
+    spec = small_head(n, seed=n, n_strands=64, grid_res=12)
+    a = asset_from_spec(gpu_ctx, spec)
+    got = gpu_run(a, spec, 2)
+    twin, _ = oracle_run(oracle, spec, 2, np.float32)
+    assert np.array_equal(got, twin)
