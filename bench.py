@@ -41,6 +41,11 @@ for _p in (ROOT, PKG):
 METRIC = "point-steps/s batched+served vs plain on 1 GB300 @1e-3 err; p50/p99 step ms"
 BYTES_PER_POINT = 80        # read x,v (32 B) + write x,v,corr (48 B) per point-step
 BYTES_PER_CELL = 16         # one clear/flush pass per grid cell-step
+# DRAM bytes per algorithmic byte of k_batch, from one ncu capture of the fused
+# step on the first 32 heads of the workload (dram__bytes_read.sum +
+# dram__bytes_write.sum over 80 B/point + 16 B/cell); traffic grows with points
+# and cells, so the full launch's traffic is this ratio times its bytes
+TRAFFIC_PER_ALG_BYTE = 972.5 / 833.0
 
 
 def load_peaks():
@@ -441,7 +446,9 @@ def main():
             "plain": {"value": plain_value, "ms_per_step": plain_ms,
                       "speedup_batched_vs_plain": (value / plain_value) if plain_value else None},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": alg_bytes * TRAFFIC_PER_ALG_BYTE,
+                         "traffic_source": "ncu DRAM bytes of k_batch on the first 32 heads, scaled by "
+                                           "algorithmic bytes",
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                          "fallback 6.8 TB/s"},
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,

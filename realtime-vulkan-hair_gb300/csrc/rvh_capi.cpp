@@ -64,7 +64,8 @@ rvh_status validate_params(const rvh_sim_params& p) {
     if (!(p.vmax > 0.f)) return fail(RVH_ERR_INVALID_ARG, "sim params: vmax must be > 0");
     if (p.grid_enabled) {
         if (!(p.grid_h > 0.f)) return fail(RVH_ERR_INVALID_ARG, "sim params: grid_h must be > 0");
-        if (!(p.grid_scale > 0.f)) return fail(RVH_ERR_INVALID_ARG, "sim params: grid_scale must be > 0");
+        if (!(p.grid_scale > 0.f && p.grid_scale <= 1e30f))
+            return fail(RVH_ERR_INVALID_ARG, "sim params: grid_scale must be in (0, 1e30]");
         for (int i = 0; i < 3; ++i)
             if (p.grid_dims[i] < 1 || p.grid_dims[i] > 512)
                 return fail(RVH_ERR_INVALID_ARG, "sim params: grid_dims must be in [1, 512]");

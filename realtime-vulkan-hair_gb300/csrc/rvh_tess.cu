@@ -18,6 +18,10 @@
 //   width = mix(rootWidth, tipWidth, v)                              (:324-326)
 //   optional per-segment frames {tangent, Frisvad b1, b2}            (:289-297)
 //
+// A CTA of 256 threads takes 8 strands at a time: their points and Bezier
+// control points in shared memory, their (strand, isoline) sd profiles, then
+// one thread per output vertex with coalesced float4 stores.
+//
 // Everything that depends only on (isoline, vertex) — the clump width, the
 // direction, the five sd profiles of v, the strand width — is a table the
 // host computes once per descriptor with the C library's float functions.
@@ -39,7 +43,8 @@
 namespace rvh {
 namespace {
 
-constexpr int kTessThreads = 128;
+constexpr int kTessThreads = 256;
+constexpr int kTessGroup = kTessThreads / RVH_MAX_POINTS;   // strands per CTA iteration (8)
 constexpr int kMaxLines = 64;
 constexpr int kMaxSegments = 256;
 
@@ -86,60 +91,69 @@ struct TessArgs {
 };
 
 __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_constant__ TessArgs A) {
-    __shared__ f3 pts[RVH_MAX_POINTS];
-    __shared__ f3 cb1[RVH_MAX_POINTS], cb2[RVH_MAX_POINTS];
-    __shared__ int prof[kMaxLines];
+    __shared__ f3 pts[kTessGroup][RVH_MAX_POINTS];
+    __shared__ f3 cb1[kTessGroup][RVH_MAX_POINTS], cb2[kTessGroup][RVH_MAX_POINTS];
+    __shared__ int prof[kTessGroup][kMaxLines];
     const int n = A.n_points, L = A.n_lines, S1 = A.n_segments + 1;
     const int per_strand = L * S1;
-    const FastDiv dS1((unsigned)S1);
-    for (int s = blockIdx.x; s < A.n_strands; s += gridDim.x) {
-        const float4* rec = A.strands + (size_t)s * (3 * n);
-        if (threadIdx.x < n) pts[threadIdx.x] = xyz(rec[threadIdx.x]);
+    const FastDiv dS1((unsigned)S1), dPer((unsigned)per_strand), dL((unsigned)L);
+    for (int s0 = blockIdx.x * kTessGroup; s0 < A.n_strands; s0 += gridDim.x * kTessGroup) {
+        const int ng = min(kTessGroup, A.n_strands - s0);   // strands of this group
+        // the group's points: thread t loads point t % 32 of strand t / 32
+        {
+            const int g = threadIdx.x / RVH_MAX_POINTS, i = threadIdx.x % RVH_MAX_POINTS;
+            if (g < ng && i < n) pts[g][i] = xyz(A.strands[(size_t)(s0 + g) * (3 * n) + i]);
+        }
         __syncthreads();
-        if (threadIdx.x + 1 < n) {   // control points and frame of segment sf (hair.tese:45-66)
-            const int sf = threadIdx.x;
-            const f3 p1 = pts[sf], p2 = pts[sf + 1];
-            const f3 p0 = sf == 0 ? v_add<EM>(p1, v_sub<EM>(p1, p2)) : pts[sf - 1];
-            const f3 p3 = sf + 1 == n - 1 ? v_add<EM>(p2, v_sub<EM>(p2, p1)) : pts[sf + 2];
-            const float third = 1.0f / 3.0f;
-            cb1[sf] = v_add<EM>(p1, v_scale<EM>(third, v_div<EM>(v_sub<EM>(p2, p0), 2.0f)));
-            cb2[sf] = v_sub<EM>(p2, v_scale<EM>(third, v_div<EM>(v_sub<EM>(p3, p1), 2.0f)));
-            if (A.frames) {
-                const f3 tg = v_normalize<EM>(v_sub<EM>(p2, p1));
-                f3 b1, b2;
-                frisvad_dev(tg, b1, b2);
-                float4* fr = A.frames + ((size_t)s * (n - 1) + sf) * 3;
-                fr[0] = make_float4(tg.x, tg.y, tg.z, 0.f);
-                fr[1] = make_float4(b1.x, b1.y, b1.z, 0.f);
-                fr[2] = make_float4(b2.x, b2.y, b2.z, 0.f);
+        {   // control points and frame of segment sf (hair.tese:45-66)
+            const int g = threadIdx.x / RVH_MAX_POINTS, sf = threadIdx.x % RVH_MAX_POINTS;
+            if (g < ng && sf + 1 < n) {
+                const f3 p1 = pts[g][sf], p2 = pts[g][sf + 1];
+                const f3 p0 = sf == 0 ? v_add<EM>(p1, v_sub<EM>(p1, p2)) : pts[g][sf - 1];
+                const f3 p3 = sf + 1 == n - 1 ? v_add<EM>(p2, v_sub<EM>(p2, p1)) : pts[g][sf + 2];
+                const float third = 1.0f / 3.0f;
+                cb1[g][sf] = v_add<EM>(p1, v_scale<EM>(third, v_div<EM>(v_sub<EM>(p2, p0), 2.0f)));
+                cb2[g][sf] = v_sub<EM>(p2, v_scale<EM>(third, v_div<EM>(v_sub<EM>(p3, p1), 2.0f)));
+                if (A.frames) {
+                    const f3 tg = v_normalize<EM>(v_sub<EM>(p2, p1));
+                    f3 b1, b2;
+                    frisvad_dev(tg, b1, b2);
+                    float4* fr = A.frames + ((size_t)(s0 + g) * (n - 1) + sf) * 3;
+                    fr[0] = make_float4(tg.x, tg.y, tg.z, 0.f);
+                    fr[1] = make_float4(b1.x, b1.y, b1.z, 0.f);
+                    fr[2] = make_float4(b2.x, b2.y, b2.z, 0.f);
+                }
             }
         }
-        if (threadIdx.x < L) {   // sd profile of isoline j: randomChoice (hair.tese:253-283)
-            const f3 root = pts[0];
-            const float choice = EM::mul(tess_random_dev(A.T.u[threadIdx.x], root.x), tess_random_dev(root.y, root.z));
+        // sd profile of (strand, isoline): randomChoice (hair.tese:253-283)
+        for (int q = threadIdx.x; q < ng * L; q += kTessThreads) {
+            const int g = (int)dL.div((unsigned)q), j = q - g * L;
+            const f3 root = pts[g][0];
+            const float choice = EM::mul(tess_random_dev(A.T.u[j], root.x), tess_random_dev(root.y, root.z));
             int p = 0;
             if (choice > 0.5f) p = choice > 0.9f ? 1 : choice > 0.8f ? 2 : choice > 0.7f ? 3 : choice > 0.6f ? 4 : 5;
-            prof[threadIdx.x] = p;
+            prof[g][j] = p;
         }
         __syncthreads();
-        float4* out = A.out + (size_t)s * per_strand;
-        for (int q = threadIdx.x; q < per_strand; q += kTessThreads) {
-            const int j = (int)dS1.div((unsigned)q), k = q - j * S1;
+        float4* out = A.out + (size_t)s0 * per_strand;
+        for (int q = threadIdx.x; q < ng * per_strand; q += kTessThreads) {
+            const int g = (int)dPer.div((unsigned)q), r = q - g * per_strand;
+            const int j = (int)dS1.div((unsigned)r), k = r - j * S1;
             const float v = __ldg(A.T.v + k);
             const float x = EM::mul(v, (float)(n - 1));
             int sf = (int)floorf(x);
             sf = min(sf, n - 2);
             const float t = EM::sub(x, (float)sf);
-            const f3 b0 = pts[sf], b1 = cb1[sf], b2 = cb2[sf], b3 = pts[sf + 1];
+            const f3 b0 = pts[g][sf], b1 = cb1[g][sf], b2 = cb2[g][sf], b3 = pts[g][sf + 1];
             const f3 b01 = e_mix(b0, b1, t), b11 = e_mix(b1, b2, t), b21 = e_mix(b2, b3, t);
             const f3 b02 = e_mix(b01, b11, t), b12 = e_mix(b11, b21, t);
             const f3 c = e_mix(b02, b12, t);
-            const float sd = __ldg(A.T.sd + prof[j] * S1 + k);
+            const float sd = __ldg(A.T.sd + prof[g][j] * S1 + k);
             const f3 dir = v_scale<EM>(sd, f3{__ldg(A.T.dir + 3 * j), __ldg(A.T.dir + 3 * j + 1), __ldg(A.T.dir + 3 * j + 2)});
             const f3 pos = v_add<EM>(c, v_scale<EM>(__ldg(A.T.width + j * S1 + k), dir));
             out[q] = make_float4(pos.x, pos.y, pos.z, __ldg(A.T.sw + k));
         }
-        __syncthreads();   // pts, cb1/cb2 and prof are rewritten for the next strand
+        __syncthreads();   // pts, cb1/cb2 and prof are rewritten for the next group
     }
 }
 
@@ -252,7 +266,8 @@ rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vert
                         base + a->tess_off[3], base + a->tess_off[4], base + a->tess_off[5]};
     A.out = static_cast<float4*>(vertices);
     A.frames = static_cast<float4*>(frames);
-    const int blocks = (int)std::min<long long>(a->n_strands, (long long)a->ctx->sm_count * 16);
+    const long long groups = (a->n_strands + kTessGroup - 1) / kTessGroup;
+    const int blocks = (int)std::min<long long>(groups, (long long)a->ctx->sm_count * 8);
     void* args[] = {&A};
     RVH_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(&k_tessellate), dim3(blocks), dim3(kTessThreads), args, 0, s));
     return RVH_OK;
