@@ -21,6 +21,7 @@ constexpr int kThreads = 256;          // CTA size of every step kernel
 constexpr int kWarps = kThreads / 32;
 constexpr int kSmemBytes = 72 * 1024;  // dynamic shared memory per CTA (grid boxes)
 constexpr int kMinCtasPerSm = 3;       // 3 x 72 KB of boxes and <= 80 registers per thread per SM
+constexpr int kUnionRounds = 4;        // rounds sharing one gather box and one splat box
 constexpr int kBoxCellsA = kSmemBytes / 16;   // phase A: 4 x int32 partial sums per cell
 constexpr int kBoxCellsB = kSmemBytes / 20;   // phase B: CellF without padding (float4 + rcp)
 constexpr int kTileB = 2048;           // points per phase-B tile
@@ -213,7 +214,7 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
                 if (q0) atomicAdd(cell, q0);
                 if (q1) atomicAdd(cell + vol, q1);
                 if (q2) atomicAdd(cell + 2 * vol, q2);
-                if (q3) atomicAdd(cell + 3 * vol, q3);
+                if (q3) atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
             }
         }
     }
@@ -255,16 +256,18 @@ struct LaneBounds {
 // LaneBounds::reduce.  visit(f) calls f(position, velocity) for each of the
 // lane's points.  The cell box is accumulated in shared memory in x slabs that
 // fit (one slab in almost every round), each flushed once with int64 global
-// atomics.  A slab falls back to direct global atomics when its int32 partial
-// sums cannot be proven free of overflow (|partial| <= vmax * (density + npts)
-// since |int(s w v)| <= vmax * (int(s w) + 1)); the whole round does when not
-// even a one-cell-wide slab fits.
+// atomics.  Velocity partials are int32, densities uint32 (npts * scale < 4e9
+// keeps them exact).  A slab falls back to direct global atomics when its
+// velocity partials cannot be proven free of overflow (|partial| <= vmax *
+// (density + npts) since |int(s w v)| <= vmax * (int(s w) + 1)); the whole
+// round does when not even a one-cell-wide slab fits or npts * scale >= 4e9.
 template <class M, class Visit>
 __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxShared& S, unsigned* stats, Visit visit) {
     const int npts = S.npts;
     if (npts > 0) {
         const BoxGeom G = box_geom(S);
-        const int w = (float)npts * A.scale < 2.0e9f ? slab_width(G, kBoxCellsA) : 0;
+        // density partials are unsigned (every int(s w) >= 0): exact below 2^32
+        const int w = (float)npts * A.scale < 4.0e9f ? slab_width(G, kBoxCellsA) : 0;
         const float vmax = __uint_as_float(S.vabs);
         const int nxny = A.nx * A.ny;
         bool all_box = w > 0;
@@ -282,7 +285,7 @@ __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxSha
             __syncthreads();
             bool ok = true;
             for (int c = threadIdx.x; c < nv; c += kThreads)
-                ok = ok && vmax * ((float)box[3 * nv + c] + (float)npts) < 2.0e9f;
+                ok = ok && vmax * ((float)(unsigned)box[3 * nv + c] + (float)npts) < 2.0e9f;
             if (__syncthreads_and(ok)) {
                 const BoxWalk W(P);
                 for (int c = threadIdx.x; c < nv; c += kThreads) {
@@ -294,7 +297,7 @@ __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxSha
                     red_add_s64(cell + 0, v.x);
                     red_add_s64(cell + 1, v.y);
                     red_add_s64(cell + 2, v.z);
-                    red_add_s64(cell + 3, v.w);
+                    red_add_s64(cell + 3, (long long)(unsigned)v.w);
                 }
             } else {
                 all_box = false;
@@ -342,23 +345,6 @@ __device__ __forceinline__ void for_lane_points(f3 (&x)[K], f3 (&v)[K], unsigned
     }
 }
 
-// Splat the round's points held in registers (bit k of mask: xo[k], vo[k]).
-template <int K, class M>
-__device__ __forceinline__ void splat_round(const DevAsset& A, f3 (&xo)[K], f3 (&vo)[K], unsigned mask, int* box,
-                                            BoxShared& S, unsigned* stats) {
-    LaneBounds lb;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        if (!((mask >> k) & 1u)) continue;
-        lb.add(xo[k]);
-        lb.add_v(vo[k]);
-    }
-    lb.reduce<M>(A, S);
-    splat_points<M>(A, box, S, stats, [&](auto&& f) {
-        for_lane_points(xo, vo, mask, [&](f3& p, f3& v) { f(p, v); });
-    });
-}
-
 // Copies the box's cells of grid G into shared memory as CellF (float4
 // {vx, vy, vz, rc} at bf[c], rcp at br[c]).  Padding cells are skipped, and so
 // are cells past the grid's last layer: a point beyond the grid has no corner
@@ -391,30 +377,41 @@ __device__ __forceinline__ f3 gather_point_direct(const DevAsset& A, const unsig
 // The CTA's gather box over grid `grid` (after LaneBounds::reduce of the
 // points to gather): loaded into shared memory when it fits, else the gather
 // reads the grid directly.  gather(x, v, dt) then returns loop 3's velocity.
-// A null grid builds an unused object (no synchronisation, no loads).
+// The box geometry lives in shared memory (G), so holding the object across a
+// group of rounds costs no registers.  A null grid builds an unused object (no
+// synchronisation, no loads).
+struct GatherShared {
+    BoxGeom G;
+    int use;
+};
+
 template <class M>
 struct GatherBox {
     const DevAsset& A;
     const unsigned long long* grid;
-    BoxGeom G;
-    bool use;
-    const float4* bf;
-    const float* br;
-    __device__ __forceinline__ GatherBox(const DevAsset& a, const unsigned long long* g, unsigned char* smem,
-                                         const BoxShared& S, unsigned* stats)
-        : A(a), grid(g), G(box_geom(S)), bf(reinterpret_cast<const float4*>(smem)),
-          br(reinterpret_cast<const float*>(smem + 16 * kBoxCellsB)) {
-        use = false;
+    const GatherShared& GS;
+    unsigned char* smem;
+    __device__ __forceinline__ GatherBox(const DevAsset& a, const unsigned long long* g, unsigned char* sm,
+                                         const BoxShared& S, GatherShared& gs, unsigned* stats)
+        : A(a), grid(g), GS(gs), smem(sm) {
         if (!grid) return;   // nothing to gather (uniform across the CTA)
         const int npts = S.npts;
-        use = npts > 0 && G.vol <= kBoxCellsB;
+        const BoxGeom G = box_geom(S);
+        const bool use = npts > 0 && G.vol <= kBoxCellsB;
         if (use) load_gather_box<M>(A, grid, G, reinterpret_cast<float4*>(smem), reinterpret_cast<float*>(smem + 16 * kBoxCellsB));
+        if (threadIdx.x == 0) {
+            gs.G = G;
+            gs.use = use ? 1 : 0;
+            if (stats && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
+        }
         __syncthreads();
-        if (stats && threadIdx.x == 0 && npts > 0) atomicAdd(stats + (use ? 2 : 3), 1u);
     }
     __device__ __forceinline__ f3 gather(f3 x, f3 v, float dt) const {
         const Corners C = corners_of<M>(A, x);
-        if (use) {
+        if (GS.use) {
+            const float4* bf = reinterpret_cast<const float4*>(smem);
+            const float* br = reinterpret_cast<const float*>(smem + 16 * kBoxCellsB);
+            const BoxGeom& G = GS.G;
             return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
                 const int li = G.offset(a, b, c);
                 const float4 q = bf[li];
@@ -425,44 +422,84 @@ struct GatherBox {
     }
 };
 
-// Loop 3 of the PREVIOUS step for the round's points (fused batched step):
-// gather from A.grid_prev at the positions the previous step produced and
-// blend the friction into v.  Same box scheme as phase B; every thread calls it.
-template <int K, class M>
-__device__ __forceinline__ void gather_round(const DevAsset& A, f3 (&x)[K], f3 (&v)[K], unsigned mask,
-                                             unsigned char* smem, BoxShared& S, unsigned* stats) {
-    LaneBounds lb;
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if ((mask >> k) & 1u) lb.add(x[k]);
-    lb.reduce<M>(A, S);
-    const GatherBox<M> gb(A, A.grid_prev, smem, S, stats);
-    for_lane_points(x, v, mask, [&](f3& p, f3& vel) { vel = gb.gather(p, vel, A.dt_prev); });
-    __syncthreads();  // the box memory is reused by the splat of this round
-}
-
-// Strands [begin, end) of one asset in rounds of kWarps * (32/L) strands; the
-// round count is the same for every warp (the boxes synchronise the CTA).
-// With A.grid_prev set, each round first finishes the previous step's loop 3.
+// Strands [begin, end) of one asset in rounds of kWarps * (32/L) strands,
+// handled in groups of U consecutive rounds that share one gather box and one
+// splat box (fewer box loads, flushes and barriers than a box per round; a
+// group's points stay below 4e9 / scale so its density partials stay exact):
+//   1. (fused step) the group's current positions bound the box of
+//      A.grid_prev, loaded once; each round then gathers the previous step's
+//      loop 3 into its velocities;
+//   2. each round runs loops 1-2 (strand_phase_a stores x', v, corr);
+//   3. the group's new points, read back from this thread's own stores, are
+//      splatted through one box.
+// The round count is the same for every warp (the boxes synchronise the CTA).
 template <int NFIX, int L, class M>
 __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
                                        unsigned* stats) {
     constexpr int SPW = 32 / L;
     constexpr int K = PhaseA<NFIX, L>::K;
+    const int n = NFIX > 0 ? NFIX : A.n_points;
     const int warp = threadIdx.x >> 5;
     const int g = (threadIdx.x & 31) / L;
+    const int l = (threadIdx.x & 31) % L;
     const int per_round = kWarps * SPW;
     const int rounds = (end - begin + per_round - 1) / per_round;
-    for (int r = 0; r < rounds; ++r) {
-        // a warp's strands are spread over the round (neighbouring strands share cells)
-        const int strand = begin + r * per_round + g * kWarps + warp;
-        const bool valid = g < SPW && strand < end;
-        f3 x[K], v[K];
-        const unsigned lmask = load_points<NFIX, L>(A, strand, valid, x, v);
-        if (A.grid_prev) gather_round<K, M>(A, x, v, lmask, smem, S, stats);
-        f3 xo[K], vo[K];
-        const unsigned mask = strand_phase_a<NFIX, L, M>(A, strand, valid, x, v, xo, vo);
-        if (A.grid_enabled) splat_round<K, M>(A, xo, vo, mask, reinterpret_cast<int*>(smem), S, stats);
+    const float cap = 4.0e9f / (A.scale * (float)(per_round * n));   // rounds per group, density-exact
+    const int U = max(1, min(kUnionRounds, (int)cap));
+    // a warp's strands are spread over the round (neighbouring strands share cells)
+    auto strand_of = [&](int r) { return begin + r * per_round + g * kWarps + warp; };
+    for (int r0 = 0; r0 < rounds; r0 += U) {
+        const int r1 = min(rounds, r0 + U);
+        if (A.grid_prev) {   // 1. the group's gather box
+            LaneBounds lb;
+            for (int r = r0; r < r1; ++r) {
+                const int strand = strand_of(r);
+                const bool valid = g < SPW && strand < end;
+                const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const int i = PhaseA<NFIX, L>::point(l, k);
+                    if (valid && i >= 1 && i < n) lb.add(xyz(ld_cg(rec + i)));
+                }
+            }
+            lb.reduce<M>(A, S);
+        }
+        __shared__ GatherShared gs;
+        const GatherBox<M> gb(A, A.grid_prev, smem, S, gs, stats);
+        LaneBounds sb;
+        for (int r = r0; r < r1; ++r) {   // 2. loops 1-2 per round
+            const int strand = strand_of(r);
+            const bool valid = g < SPW && strand < end;
+            f3 x[K], v[K];
+            const unsigned lmask = load_points<NFIX, L>(A, strand, valid, x, v);
+            if (A.grid_prev)
+                for_lane_points(x, v, lmask, [&](f3& p, f3& vel) { vel = gb.gather(p, vel, A.dt_prev); });
+            f3 xo[K], vo[K];
+            const unsigned mask = strand_phase_a<NFIX, L, M>(A, strand, valid, x, v, xo, vo);
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (!((mask >> k) & 1u)) continue;
+                sb.add(xo[k]);
+                sb.add_v(vo[k]);
+            }
+        }
+        if (A.grid_prev) __syncthreads();   // the gather box memory becomes the splat box
+        if (A.grid_enabled) {   // 3. splat the group
+            sb.reduce<M>(A, S);
+            splat_points<M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
+#pragma unroll 1
+                for (int r = r0; r < r1; ++r) {
+                    const int strand = strand_of(r);
+                    const bool valid = g < SPW && strand < end;
+                    const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+#pragma unroll 1
+                    for (int k = 0; k < K; ++k) {
+                        const int i = PhaseA<NFIX, L>::point(l, k);
+                        if (valid && i >= 1 && i < n) f(xyz(rec[i]), xyz(rec[n + i]));
+                    }
+                }
+            });
+        }
     }
 }
 
@@ -500,7 +537,8 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
             for (int i = 1; i < np; ++i) lb.add(xyz(rec[i]));
             lb.reduce<M>(A, S);
         }
-        const GatherBox<M> gb(A, A.grid_prev, smem, S, stats);
+        __shared__ GatherShared gs;
+        const GatherBox<M> gb(A, A.grid_prev, smem, S, gs, stats);
 
         // 2. loops 1-2 along the strand
         f3 f0 = v_add<M>(f3{A.gravity[0], A.gravity[1], A.gravity[2]}, f3{A.wind[0], A.wind[1], A.wind[2]});
@@ -593,7 +631,8 @@ __device__ __forceinline__ void tile_b(const DevAsset& A, int s0, int s1, unsign
         lb.add(x[j]);
     }
     lb.reduce<M>(A, S);
-    const GatherBox<M> gb(A, A.grid, smem, S, stats);
+    __shared__ GatherShared gs;
+    const GatherBox<M> gb(A, A.grid, smem, S, gs, stats);
 #pragma unroll
     for (int j = 0; j < kPtsB; ++j) {
         if (!((m >> j) & 1u)) continue;
