@@ -45,7 +45,7 @@ BYTES_PER_CELL = 16         # one clear/flush pass per grid cell-step
 # step on the first 32 heads of the workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over 80 B/point + 16 B/cell); traffic grows with points
 # and cells, so the full launch's traffic is this ratio times its bytes
-TRAFFIC_PER_ALG_BYTE = 972.5 / 833.0
+TRAFFIC_PER_ALG_BYTE = 994.9 / 833.0
 
 
 def load_peaks():
@@ -182,7 +182,7 @@ def time_cpu(specs, steps, threads):
     return pts * steps / dt, dt
 
 
-def run_served(ctx, args, rank):
+def run_served(ctx, args, rank, lanes):
     """1,000 resident characters sized as the batched workload; Poisson arrivals
     at 20k req/s, 1-8 steps each; continuous batching at 1, 4 and 16 requests
     per launch.  Returns {concurrency: stats}."""
@@ -198,7 +198,7 @@ def run_served(ctx, args, rank):
     pts = sum(s.n_total_points for s in specs)
     rng = np.random.default_rng(77)
     for conc in (1, 4, 16):
-        srv = api.Server(ctx, max_active=conc, pipeline_depth=2, scratch_budget_bytes=24 << 30)
+        srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=2, scratch_budget_bytes=24 << 30)
         ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
         t = np.cumsum(rng.exponential(1.0 / 20000.0, size=args.requests))
         reqs = [(ids[int(rng.integers(0, n_chars))], int(rng.integers(1, 9)), float(ti)) for ti in t]
@@ -425,7 +425,7 @@ def main():
         for a in assets:
             a.close()
         assets, batch = [], None
-        served, served_pts = run_served(ctx, args, rank)
+        served, served_pts = run_served(ctx, args, rank, info["lanes"])
 
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (step_ms * 1e-3) / 1e9

@@ -270,7 +270,7 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
  * on the device. */
 typedef struct rvh_server_desc {
     int32_t max_active;           /* requests co-scheduled per launch (default 16) */
-    int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (default 4) */
+    int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (0: 8) */
     int32_t pipeline_depth;       /* launches in flight (default 2) */
     int32_t reserved;
     uint64_t scratch_budget_bytes;/* HBM for the grids of admitted requests; charged to the context */

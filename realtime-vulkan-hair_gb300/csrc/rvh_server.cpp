@@ -129,12 +129,12 @@ rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_
     *out = nullptr;
     rvh_server_desc d{};
     d.max_active = 16;
-    d.lanes_per_strand = 4;
+    d.lanes_per_strand = 8;
     d.pipeline_depth = 2;
     if (desc) d = *desc;
     if (d.max_active < 1 || d.max_active > 4096) return fail(RVH_ERR_INVALID_ARG, "server: max_active in [1, 4096]");
     if (d.pipeline_depth < 1 || d.pipeline_depth > 8) return fail(RVH_ERR_INVALID_ARG, "server: pipeline_depth in [1, 8]");
-    if (!d.lanes_per_strand) d.lanes_per_strand = 4;
+    if (!d.lanes_per_strand) d.lanes_per_strand = 8;
     cudaSetDevice(ctx->device);
     rvh_server* s = new (std::nothrow) rvh_server();
     if (!s) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");

@@ -331,7 +331,7 @@ class Batch:
 class Server:
     """Continuous-batching request loop over resident characters (C++)."""
 
-    def __init__(self, ctx, max_active=16, lanes=4, pipeline_depth=2, scratch_budget_bytes=1 << 30):
+    def __init__(self, ctx, max_active=16, lanes=8, pipeline_depth=2, scratch_budget_bytes=1 << 30):
         self.ctx = ctx
         self.lib = ctx.lib
         d = ServerDesc(max_active, lanes, pipeline_depth, 0, scratch_budget_bytes)
