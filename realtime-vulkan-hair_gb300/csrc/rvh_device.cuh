@@ -349,29 +349,35 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
     f3 gv = {0.f, 0.f, 0.f};
     float rho = 0.f;
     f3 grad = {0.f, 0.f, 0.f};
+    // Branch-free corner loop: a missing corner (past the grid) or an empty cell
+    // contributes with weight 0 read from a valid cell of the point's range;
+    // adding those +-0 terms leaves every sum's bits unchanged (no sum is ever
+    // -0), so the result equals the oracle's, which skips them.
+    if (C.cnt[0] > 0 && C.cnt[1] > 0 && C.cnt[2] > 0) {
 #pragma unroll
-    for (int da = 0; da < 2; ++da) {
-        if (da >= C.cnt[0]) continue;
-        const int a = C.lo[0] + da;
+        for (int da = 0; da < 2; ++da) {
+            const bool ea = da < C.cnt[0];
+            const int a = C.lo[0] + (ea ? da : 0);
 #pragma unroll
-        for (int db = 0; db < 2; ++db) {
-            if (db >= C.cnt[1]) continue;
-            const int b = C.lo[1] + db;
-            const float wxy = M::mul(wxs[da], wys[db]);
+            for (int db = 0; db < 2; ++db) {
+                const bool eb = db < C.cnt[1];
+                const int b = C.lo[1] + (eb ? db : 0);
+                const float wxy = M::mul(wxs[da], wys[db]);
 #pragma unroll
-            for (int dc = 0; dc < 2; ++dc) {
-                if (dc >= C.cnt[2]) continue;
-                const int c = C.lo[2] + dc;
-                const CellF cf = cell(a, b, c);
-                if (cf.rcp > 0.0f) {
-                    const float w = M::mul(wxy, wzs[dc]);
+                for (int dc = 0; dc < 2; ++dc) {
+                    const bool ec = dc < C.cnt[2];
+                    const int c = C.lo[2] + (ec ? dc : 0);
+                    const CellF cf = cell(a, b, c);
+                    const bool live = ea && eb && ec && cf.rcp > 0.0f;
+                    const float w = live ? M::mul(wxy, wzs[dc]) : 0.0f;
                     const float s = M::mul(w, cf.rcp);
                     gv = v_add<M>(gv, v_scale<M>(s, f3{cf.vx, cf.vy, cf.vz}));
                     if (rep) {
-                        rho = M::add(rho, M::mul(w, cf.rc));
+                        const float rc = live ? cf.rc : 0.0f;
+                        rho = M::add(rho, M::mul(w, rc));
                         const f3 dw = {M::mul(sx[da], M::mul(wys[db], wzs[dc])),
                                        M::mul(sy[db], M::mul(wxs[da], wzs[dc])), M::mul(sz[dc], wxy)};
-                        grad = v_add<M>(grad, v_scale<M>(cf.rc, dw));
+                        grad = v_add<M>(grad, v_scale<M>(rc, dw));
                     }
                 }
             }

@@ -188,33 +188,40 @@ struct BoxWalk {
 template <class M>
 __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const BoxGeom& G,
                                                 int vol) {
+    // the corners inside the slab: x in [dlo, dhi] of {0, 1}; y, z in [0, cnt - 1]
+    const int x0 = G.lo[0] - C.lo[0];
+    const int dlo = max(0, x0), dhi = min(C.cnt[0], x0 + G.ext[0]) - 1;
+    if (dhi < dlo || C.cnt[1] <= 0 || C.cnt[2] <= 0) return;   // no corner in this slab
+    // Branch-free corner loop: a missing corner gets weight 0 at a valid cell
+    // of the point's own range, so its atomics add 0 (integer sums are unchanged).
     float wx[2], wy[2], wz[2];
+    int ox[2], oy[2], oz[2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-        wx[d] = tri_w<M>(C.g[0], C.lo[0] + d);
-        wy[d] = tri_w<M>(C.g[1], C.lo[1] + d);
-        wz[d] = tri_w<M>(C.g[2], C.lo[2] + d);
+        const bool ex = d >= dlo && d <= dhi, ey = d < C.cnt[1], ez = d < C.cnt[2];
+        wx[d] = ex ? tri_w<M>(C.g[0], C.lo[0] + d) : 0.f;
+        wy[d] = ey ? tri_w<M>(C.g[1], C.lo[1] + d) : 0.f;
+        wz[d] = ez ? tri_w<M>(C.g[2], C.lo[2] + d) : 0.f;
+        ox[d] = ex ? d : dlo;
+        oy[d] = (ey ? d : 0) * G.py;
+        oz[d] = (ez ? d : 0) * G.pz;
     }
-    const int o0 = G.offset(C.lo[0], C.lo[1], C.lo[2]);      // -1 when the first corner is left of the slab
-    const int x0 = G.lo[0] - C.lo[0], x1 = x0 + G.ext[0];   // da range of the slab
+    int* const b0 = box + G.offset(C.lo[0], C.lo[1], C.lo[2]);
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
-        if (da >= C.cnt[0] || da < x0 || da >= x1) continue;
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
-            if (db >= C.cnt[1]) continue;
             const float wxy = M::mul(wx[da], wy[db]);
 #pragma unroll
             for (int dc = 0; dc < 2; ++dc) {
-                if (dc >= C.cnt[2]) continue;
                 const float w = M::mul(wxy, wz[dc]);
-                int* cell = box + (o0 + da + G.py * db + G.pz * dc);
+                int* cell = b0 + (ox[da] + oy[db] + oz[dc]);
                 int q0, q1, q2, q3;
                 corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
-                if (q0) atomicAdd(cell, q0);
-                if (q1) atomicAdd(cell + vol, q1);
-                if (q2) atomicAdd(cell + 2 * vol, q2);
-                if (q3) atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
+                atomicAdd(cell, q0);
+                atomicAdd(cell + vol, q1);
+                atomicAdd(cell + 2 * vol, q2);
+                atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
             }
         }
     }
