@@ -163,6 +163,7 @@ DevAsset Asset::device_view(const rvh_frame& f, int g, int prev, int next) const
     A.wrap32 = params.grid_wrap32 ? 1 : 0;
     for (int i = 0; i < 3; ++i) A.origin[i] = params.grid_origin[i];
     A.h = params.grid_h;
+    A.inv_h = 1.0f / params.grid_h;
     A.nx = params.grid_dims[0];
     A.ny = params.grid_dims[1];
     A.nz = params.grid_dims[2];

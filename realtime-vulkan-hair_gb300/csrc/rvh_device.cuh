@@ -85,6 +85,7 @@ struct DevAsset {
     int32_t grid_enabled, wrap32;
     float origin[3];
     float h;
+    float inv_h;                 // 1 / h (fast math maps positions to grid space by a multiply)
     int32_t nx, ny, nz;
     // frame (rvh_frame)
     float dt_prev;               // dt of the step whose friction is pending (with grid_prev)
@@ -198,7 +199,7 @@ __device__ __forceinline__ Corners corners_of(const DevAsset& A, f3 p) {
     const int dim[3] = {A.nx, A.ny, A.nz};
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
-        const float g = M::div(M::sub(pv[ax], A.origin[ax]), A.h);
+        const float g = M::kExact ? M::div(M::sub(pv[ax], A.origin[ax]), A.h) : (pv[ax] - A.origin[ax]) * A.inv_h;
         float f = floorf(g);
         f = fminf(fmaxf(f, -2.0f), (float)dim[ax]);   // same corner set, defined conversion
         const int fi = (int)f;
@@ -336,15 +337,20 @@ __device__ __forceinline__ float grad_sign(float g, int a) {
 template <class M, class CellFn>
 __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, f3 vel, const Corners& C, CellFn cell) {
     const bool rep = A.repulsion != 0.0f;
-    float wxs[2], wys[2], wzs[2], sx[2], sy[2], sz[2];
+    float wxs[2], wys[2], wzs[2], sx[2] = {0.f, 0.f}, sy[2] = {0.f, 0.f}, sz[2] = {0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         wxs[d] = tri_w<M>(C.g[0], C.lo[0] + d);
         wys[d] = tri_w<M>(C.g[1], C.lo[1] + d);
         wzs[d] = tri_w<M>(C.g[2], C.lo[2] + d);
-        sx[d] = grad_sign<M>(C.g[0], C.lo[0] + d);
-        sy[d] = grad_sign<M>(C.g[1], C.lo[1] + d);
-        sz[d] = grad_sign<M>(C.g[2], C.lo[2] + d);
+    }
+    if (rep) {
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            sx[d] = grad_sign<M>(C.g[0], C.lo[0] + d);
+            sy[d] = grad_sign<M>(C.g[1], C.lo[1] + d);
+            sz[d] = grad_sign<M>(C.g[2], C.lo[2] + d);
+        }
     }
     f3 gv = {0.f, 0.f, 0.f};
     float rho = 0.f;

@@ -112,6 +112,7 @@ rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* d, const rvh_frame* fra
     A.wrap32 = P.grid_wrap32 ? 1 : 0;
     for (int i = 0; i < 3; ++i) A.origin[i] = P.grid_origin[i];
     A.h = P.grid_h;
+    A.inv_h = 1.0f / P.grid_h;
     A.nx = P.grid_dims[0];
     A.ny = P.grid_dims[1];
     A.nz = P.grid_dims[2];
