@@ -501,7 +501,11 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
                     const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
 #pragma unroll 1
                     for (int k = 0; k < K; ++k) {
-                        const int i = PhaseA<NFIX, L>::point(l, k);
+                        // any order works for integer sums: lanes take blocks of K points, the
+                        // block rotated by the strand's place in the warp, so the lanes of one
+                        // instruction sit K points apart and the warp's strands at different
+                        // heights (fewer lanes on one cell per shared atomic)
+                        const int i = ((l + 2 * g) % L) * K + k;
                         if (valid && i >= 1 && i < n) f(xyz(rec[i]), xyz(rec[n + i]));
                     }
                 }
