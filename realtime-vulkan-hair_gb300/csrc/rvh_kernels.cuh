@@ -185,7 +185,10 @@ struct BoxWalk {
 // one component's atomics from a warp spread over the banks.  The six
 // trilinear weights of a point are computed once.  Exact math keeps the
 // oracle's int(scale * (w * v)); fast math shares scale * w.
-template <class M>
+// Per-lane corner order (a permutation; integer sums do not depend on it).
+constexpr bool kRotateCorners = true;
+
+template <int L, class M>
 __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const BoxGeom& G,
                                                 int vol) {
     // the corners inside the slab: x in [dlo, dhi] of {0, 1}; y, z in [0, cnt - 1]
@@ -207,6 +210,25 @@ __device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners
         oz[d] = (ez ? d : 0) * G.pz;
     }
     int* const b0 = box + G.offset(C.lo[0], C.lo[1], C.lo[2]);
+    if (kRotateCorners) {
+        // corner j of this lane is corner j ^ (lane mod 8): lanes whose points share
+        // a cell then hit different corners in the same instruction
+        const int rot = (int)threadIdx.x & 7;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int q = j ^ rot;
+            const int da = q & 1, db = (q >> 1) & 1, dc = q >> 2;
+            const float w = M::mul(M::mul(da ? wx[1] : wx[0], db ? wy[1] : wy[0]), dc ? wz[1] : wz[0]);
+            int* cell = b0 + ((da ? ox[1] : ox[0]) + (db ? oy[1] : oy[0]) + (dc ? oz[1] : oz[0]));
+            int q0, q1, q2, q3;
+            corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
+            atomicAdd(cell, q0);
+            atomicAdd(cell + vol, q1);
+            atomicAdd(cell + 2 * vol, q2);
+            atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
+        }
+        return;
+    }
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
 #pragma unroll
@@ -268,7 +290,7 @@ struct LaneBounds {
 // velocity partials cannot be proven free of overflow (|partial| <= vmax *
 // (density + npts) since |int(s w v)| <= vmax * (int(s w) + 1)); the whole
 // round does when not even a one-cell-wide slab fits or npts * scale >= 4e9.
-template <class M, class Visit>
+template <int L, class M, class Visit>
 __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxShared& S, unsigned* stats, Visit visit) {
     const int npts = S.npts;
     if (npts > 0) {
@@ -288,7 +310,7 @@ __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxSha
             int4* b4 = reinterpret_cast<int4*>(box);
             for (int c = threadIdx.x; c < nv; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
             __syncthreads();
-            visit([&](f3 p, f3 v) { splat_point_box<M>(A, corners_of<M>(A, p), v, box, P, nv); });
+            visit([&](f3 p, f3 v) { splat_point_box<L, M>(A, corners_of<M>(A, p), v, box, P, nv); });
             __syncthreads();
             bool ok = true;
             for (int c = threadIdx.x; c < nv; c += kThreads)
@@ -493,7 +515,7 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
         if (A.grid_prev) __syncthreads();   // the gather box memory becomes the splat box
         if (A.grid_enabled) {   // 3. splat the group
             sb.reduce<M>(A, S);
-            splat_points<M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
+            splat_points<L, M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
 #pragma unroll 1
                 for (int r = r0; r < r1; ++r) {
                     const int strand = strand_of(r);
@@ -595,7 +617,7 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
         // 3. splat the round
         if (A.grid_enabled) {
             sb.reduce<M>(A, S);
-            splat_points<M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
+            splat_points<1, M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
                 for (int i = 1; i < np; ++i) f(xyz(rec[i]), xyz(rec[n + i]));
             });
         }
