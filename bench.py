@@ -12,7 +12,7 @@ L2 (129 MB), so no flush is needed between steps.
           stream), inputs resident in HBM.
   e2e   : the same step through the C ABI with host data every step: frame
           parameters from pinned host memory (H2D) and every curve point's
-          position back to host memory (D2H), all inside the timed region.
+          position (xyz) back to host memory (D2H), all inside the timed region.
   --impl reference : the oracle's OpenMP C++ restatement of the reference
           shader on the host cores (the reference itself is a Vulkan shader
           and has no CPU implementation), on a bounded sample of the workload.
@@ -380,9 +380,9 @@ def main():
 
     # ---- e2e through the C ABI with host buffers ----
     # every step: frame tables host->device (inside rvh_batch_step) and every
-    # curve point's position device->host (packed on the device, copied on a
-    # second stream so the copy of step k overlaps step k+1)
-    pos_bytes = pts * 16
+    # curve point's position (xyz, 12 B) device->host (packed on the device,
+    # copied on a second stream so the copy of step k overlaps step k+1)
+    pos_bytes = pts * 12
     pinned = [api.PinnedBuffer(pos_bytes) for _ in range(2)]
     h2d = batch.h2d_bytes_per_step()
     ne2e = max(3, min(args.steps, 10))

@@ -225,12 +225,14 @@ rvh_status rvh_batch_info(rvh_batch* b, int32_t* lanes, int32_t* n_items, int32_
  * the shared-memory box, rounds splatted with direct global atomics, phase-B
  * tiles gathered from the box, tiles gathered from the global grid. */
 rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]);
-/* Every asset's curvePoints (float4 per point, asset after asset in batch
- * order) copied to host memory: a packing kernel on `stream` writes a device
- * staging buffer, then a copy stream moves it while later steps run.  Two
- * staging slots alternate; host_dst should be pinned (rvh_pinned_alloc) for
- * the copy to overlap.  rvh_batch_positions_wait blocks until every copy is
- * done. */
+/* Every asset's curvePoints (asset after asset in batch order) copied to host
+ * memory: bytes = 16 * points gives the float4 records (w = 1), bytes = 12 *
+ * points the xyz triples only (the w = 1 the reference stores carries no
+ * information; a quarter fewer bytes over the host link).  A packing kernel on
+ * `stream` writes a device staging buffer, then a copy stream moves it while
+ * later steps run.  Two staging slots alternate; host_dst should be pinned
+ * (rvh_pinned_alloc) for the copy to overlap.  rvh_batch_positions_wait blocks
+ * until every copy is done. */
 rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream);
 rvh_status rvh_batch_positions_wait(rvh_batch* b);
 /* Bytes rvh_batch_step copies host->device per step (per-asset frame and collider tables). */

@@ -39,7 +39,8 @@ struct Batch {
     const void* kernel = nullptr;
     bool timing = false;
     // positions read-back: packed device staging (two slots) and a copy stream
-    DevBuf pos_stage[2], d_first;
+    DevBuf pos_stage[2], d_first;   // staging slots; d_first: the pack kernel's chunk table
+    int n_pack_chunks = 0;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t packed[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
     int pos_slot = 0;
@@ -49,22 +50,36 @@ struct Batch {
 
 // Packs the curvePoints of every asset of a batch into one contiguous float4
 // array (asset after asset): out[first[a] + s*n + i] = strands[s*3n + i].
+// Packs curvePoints of whole strands into a contiguous staging buffer.
+// Chunk c covers strands [strand0, strand0 + count) of asset `asset`, whose
+// points start at `out0` in the output; one CTA per chunk (grid-stride),
+// consecutive threads copy consecutive points (coalesced on both sides).
+struct PackChunk {
+    int asset, strand0, count, n;
+    long long out0;
+};
+
+template <bool kXyz>
 __global__ void __launch_bounds__(kThreads) k_pack_positions(const DevAsset* __restrict__ assets,
-                                                             const long long* __restrict__ first, int n_assets,
-                                                             long long total, float4* __restrict__ out) {
-    for (long long p = (long long)blockIdx.x * kThreads + threadIdx.x; p < total; p += (long long)gridDim.x * kThreads) {
-        int lo = 0, hi = n_assets - 1;  // last asset with first[a] <= p
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (first[mid] <= p) lo = mid;
-            else hi = mid - 1;
+                                                             const PackChunk* __restrict__ chunks, int n_chunks,
+                                                             void* __restrict__ out) {
+    for (int c = blockIdx.x; c < n_chunks; c += gridDim.x) {
+        const PackChunk ch = chunks[c];
+        const float4* src = assets[ch.asset].strands + (size_t)ch.strand0 * (3 * ch.n);
+        const int pts = ch.count * ch.n;
+        const FastDiv dn((unsigned)ch.n);
+        for (int q = threadIdx.x; q < pts; q += kThreads) {
+            const int s = (int)dn.div((unsigned)q), i = q - s * ch.n;
+            const float4 v = __ldcs(src + (size_t)s * (3 * ch.n) + i);
+            if (kXyz) {
+                float* o = static_cast<float*>(out) + 3 * (ch.out0 + q);
+                o[0] = v.x;
+                o[1] = v.y;
+                o[2] = v.z;
+            } else {
+                static_cast<float4*>(out)[ch.out0 + q] = v;
+            }
         }
-        const DevAsset& A = assets[lo];
-        const int n = A.n_points;
-        const long long q = p - first[lo];
-        const long long s = q / n;
-        const int i = (int)(q - s * n);
-        out[p] = __ldcs(A.strands + s * (3 * n) + i);
     }
 }
 
@@ -571,23 +586,32 @@ rvh_status rvh_batch_check(rvh_batch* b) {
 
 rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream) {
     if (!b || (!host_dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: NULL argument");
-    const size_t need = size_t(b->n_points) * 16u;
-    if (bytes != need) return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: size must be 16 * total points");
-    if (!need) return RVH_OK;
+    const size_t n4 = size_t(b->n_points) * 16u, n3 = size_t(b->n_points) * 12u;
+    if (bytes != n4 && bytes != n3)
+        return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: size must be 16 (float4) or 12 (xyz) * total points");
+    if (!bytes) return RVH_OK;
+    const bool xyz = bytes == n3 && n3 != n4;
     cudaSetDevice(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
-    if (!b->copy_stream) {  // first use: staging, offsets, copy stream
+    if (!b->copy_stream) {  // first use: staging, chunk table, copy stream
         rvh_status st;
         for (int i = 0; i < 2; ++i)
-            if ((st = b->ctx->alloc(b->pos_stage[i], need)) != RVH_OK) return st;
-        std::vector<long long> first(b->assets.size());
+            if ((st = b->ctx->alloc(b->pos_stage[i], n4)) != RVH_OK) return st;
+        std::vector<PackChunk> chunks;
         long long acc = 0;
-        for (size_t i = 0; i < b->assets.size(); ++i) {
-            first[i] = acc;
-            acc += (long long)b->assets[i]->n_strands * b->assets[i]->n_points;
+        for (size_t a = 0; a < b->assets.size(); ++a) {
+            const int ns = b->assets[a]->n_strands, n = b->assets[a]->n_points;
+            const int per = std::max(1, 8192 / n);   // strands per chunk
+            for (int s0 = 0; s0 < ns; s0 += per) {
+                const int cnt = std::min(per, ns - s0);
+                chunks.push_back(PackChunk{int(a), s0, cnt, n, acc});
+                acc += (long long)cnt * n;
+            }
         }
-        if ((st = b->ctx->alloc(b->d_first, sizeof(long long) * std::max<size_t>(1, first.size()))) != RVH_OK) return st;
-        RVH_CUDA(cudaMemcpy(b->d_first.ptr, first.data(), sizeof(long long) * first.size(), cudaMemcpyHostToDevice));
+        b->n_pack_chunks = int(chunks.size());
+        if ((st = b->ctx->alloc(b->d_first, sizeof(PackChunk) * std::max<size_t>(1, chunks.size()))) != RVH_OK) return st;
+        if (!chunks.empty())
+            RVH_CUDA(cudaMemcpy(b->d_first.ptr, chunks.data(), sizeof(PackChunk) * chunks.size(), cudaMemcpyHostToDevice));
         RVH_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
         for (int i = 0; i < 2; ++i) {
             RVH_CUDA(cudaEventCreateWithFlags(&b->packed[i], cudaEventDisableTiming));
@@ -597,19 +621,18 @@ rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t b
     const int slot = b->pos_slot;
     b->pos_slot ^= 1;
     RVH_CUDA(cudaStreamWaitEvent(s, b->copied[slot], 0));   // the copy that last read this slot is done
-    const long long total = b->n_points;
-    long long blocks = (total + kThreads - 1) / kThreads;
-    blocks = std::min<long long>(blocks, (long long)b->ctx->sm_count * 16);
+    const int blocks = std::max(1, std::min(b->n_pack_chunks, b->ctx->sm_count * 8));
     const DevAsset* assets = static_cast<const DevAsset*>(b->d_assets.ptr);
-    const long long* first = static_cast<const long long*>(b->d_first.ptr);
-    int na = int(b->assets.size());
-    float4* out = static_cast<float4*>(b->pos_stage[slot].ptr);
-    void* args[] = {&assets, &first, &na, const_cast<long long*>(&total), &out};
-    RVH_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(&k_pack_positions), dim3(unsigned(blocks)), dim3(kThreads),
-                              args, 0, s));
+    const PackChunk* chunks = static_cast<const PackChunk*>(b->d_first.ptr);
+    int nc = b->n_pack_chunks;
+    void* out = b->pos_stage[slot].ptr;
+    void* args[] = {&assets, &chunks, &nc, &out};
+    const void* fn = xyz ? reinterpret_cast<const void*>(&k_pack_positions<true>)
+                         : reinterpret_cast<const void*>(&k_pack_positions<false>);
+    RVH_CUDA(cudaLaunchKernel(fn, dim3(unsigned(blocks)), dim3(kThreads), args, 0, s));
     RVH_CUDA(cudaEventRecord(b->packed[slot], s));
     RVH_CUDA(cudaStreamWaitEvent(b->copy_stream, b->packed[slot], 0));
-    RVH_CUDA(cudaMemcpyAsync(host_dst, out, need, cudaMemcpyDeviceToHost, b->copy_stream));
+    RVH_CUDA(cudaMemcpyAsync(host_dst, out, bytes, cudaMemcpyDeviceToHost, b->copy_stream));
     RVH_CUDA(cudaEventRecord(b->copied[slot], b->copy_stream));
     return RVH_OK;
 }

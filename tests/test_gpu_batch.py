@@ -124,3 +124,25 @@ def test_streaming_kernel_fast_close_to_fp64(gpu_ctx_fast, oracle):
         mx, p99, mean = rel_pos_err(a.read(), ref64, s.n_points, L)
         assert mx <= 1e-5, (mx, p99, mean)
     b.close()
+
+
+@pytest.mark.parametrize("xyz", [False, True])
+def test_batch_positions_read_back(gpu_ctx_fast, xyz):
+    """rvh_batch_read_positions_async: every asset's curvePoints in batch order,
+    as float4 records or as xyz triples, equal to the assets' own reads."""
+    specs = configs.batched(n_assets=5, scale=0.02, seed=21)
+    assets = make_assets(gpu_ctx_fast, specs)
+    b = api.Batch(gpu_ctx_fast, assets, lanes=8)
+    pts = b.info()["points"]
+    width = 3 if xyz else 4
+    bufs = [api.PinnedBuffer(pts * 4 * width) for _ in range(2)]
+    for k in range(3):
+        b.step([s.frame(k) for s in specs])
+        b.read_positions_async(bufs[k % 2].ptr, pts * 4 * width)
+    b.positions_wait()
+    got = bufs[0].array((pts, width)).copy()   # the last step went to slot 0
+    want = np.concatenate([a.read()[:, :s.n_points, :width].reshape(-1, width) for a, s in zip(assets, specs)])
+    assert np.array_equal(got, want)
+    for p_ in bufs:
+        p_.close()
+    b.close()
