@@ -19,7 +19,10 @@ INCLUDE = os.path.join(HERE, "..", "include")
 OUT_DIR = os.path.join(HERE, "rvh", "_build")
 LIB = os.path.join(OUT_DIR, "librvh.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+# --fmad=false: no implicit multiply-add contraction, so every kernel that
+# inlines a device function computes the same bits; fast math asks for FMA
+# explicitly (fmaf in FastMath::madd).
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr", "-I", INCLUDE]
 
 

@@ -113,7 +113,7 @@ template <class M> __device__ __forceinline__ f3 v_axpy(f3 a, float s, f3 b) {
     return {M::madd(s, b.x, a.x), M::madd(s, b.y, a.y), M::madd(s, b.z, a.z)};
 }
 template <class M> __device__ __forceinline__ float v_dot(f3 a, f3 b) {
-    return M::add(M::add(M::mul(a.x, b.x), M::mul(a.y, b.y)), M::mul(a.z, b.z));
+    return M::madd(a.z, b.z, M::madd(a.y, b.y, M::mul(a.x, b.x)));   // (ax bx + ay by) + az bz
 }
 template <class M> __device__ __forceinline__ float v_len(f3 a) { return M::sqrt(v_dot<M>(a, a)); }
 // GLSL normalize: x * inversesqrt(dot(x, x))
@@ -121,15 +121,15 @@ template <class M> __device__ __forceinline__ f3 v_normalize(f3 a) { return v_sc
 
 // xyz of m * (p, 1) for a 3x4 column block: (c0 x + c1 y) + (c2 z + c3)
 template <class M> __device__ __forceinline__ f3 mat_p1(const float* m, f3 p) {
-    return {M::add(M::add(M::mul(m[0], p.x), M::mul(m[3], p.y)), M::add(M::mul(m[6], p.z), m[9])),
-            M::add(M::add(M::mul(m[1], p.x), M::mul(m[4], p.y)), M::add(M::mul(m[7], p.z), m[10])),
-            M::add(M::add(M::mul(m[2], p.x), M::mul(m[5], p.y)), M::add(M::mul(m[8], p.z), m[11]))};
+    return {M::add(M::madd(m[3], p.y, M::mul(m[0], p.x)), M::madd(m[6], p.z, m[9])),
+            M::add(M::madd(m[4], p.y, M::mul(m[1], p.x)), M::madd(m[7], p.z, m[10])),
+            M::add(M::madd(m[5], p.y, M::mul(m[2], p.x)), M::madd(m[8], p.z, m[11]))};
 }
 // xyz of m * (q, 0) for a 3x3 column block: (c0 x + c1 y) + c2 z
 template <class M> __device__ __forceinline__ f3 mat_q0(const float* m, f3 q) {
-    return {M::add(M::add(M::mul(m[0], q.x), M::mul(m[3], q.y)), M::mul(m[6], q.z)),
-            M::add(M::add(M::mul(m[1], q.x), M::mul(m[4], q.y)), M::mul(m[7], q.z)),
-            M::add(M::add(M::mul(m[2], q.x), M::mul(m[5], q.y)), M::mul(m[8], q.z))};
+    return {M::madd(m[6], q.z, M::madd(m[3], q.y, M::mul(m[0], q.x))),
+            M::madd(m[7], q.z, M::madd(m[4], q.y, M::mul(m[1], q.x))),
+            M::madd(m[8], q.z, M::madd(m[5], q.y, M::mul(m[2], q.x)))};
 }
 
 __device__ __forceinline__ f3 xyz(float4 a) { return {a.x, a.y, a.z}; }
@@ -159,7 +159,7 @@ __device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
             if (dist < c.radius) {
                 const float d = M::sub(c.radius, dist);
                 const f3 nrm = v_normalize<M>(e);
-                added = v_add<M>(added, v_scale<M>(M::mul(k, d), nrm));
+                added = v_axpy<M>(added, M::mul(k, d), nrm);
                 ++cnt;
             }
         } else {
@@ -174,7 +174,7 @@ __device__ __forceinline__ f3 collide_force(const DevAsset& A, f3 x, f3 force) {
                 const f3 surf = mat_p1<M>(c.xf, v_normalize<M>(q));
                 const float d = v_len<M>(v_sub<M>(surf, x));
                 const f3 nrm = v_normalize<M>(v_normalize<M>(mat_q0<M>(c.itr, q)));
-                added = v_add<M>(added, v_scale<M>(M::mul(k, d), nrm));
+                added = v_axpy<M>(added, M::mul(k, d), nrm);
                 ++cnt;
             }
         }
@@ -377,20 +377,20 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
                     const bool live = ea && eb && ec && cf.rcp > 0.0f;
                     const float w = live ? M::mul(wxy, wzs[dc]) : 0.0f;
                     const float s = M::mul(w, cf.rcp);
-                    gv = v_add<M>(gv, v_scale<M>(s, f3{cf.vx, cf.vy, cf.vz}));
+                    gv = v_axpy<M>(gv, s, f3{cf.vx, cf.vy, cf.vz});
                     if (rep) {
                         const float rc = live ? cf.rc : 0.0f;
-                        rho = M::add(rho, M::mul(w, rc));
+                        rho = M::madd(w, rc, rho);
                         const f3 dw = {M::mul(sx[da], M::mul(wys[db], wzs[dc])),
                                        M::mul(sy[db], M::mul(wxs[da], wzs[dc])), M::mul(sz[dc], wxy)};
-                        grad = v_add<M>(grad, v_scale<M>(rc, dw));
+                        grad = v_axpy<M>(grad, rc, dw);
                     }
                 }
             }
         }
     }
     const float fr = A.friction;
-    f3 out = v_add<M>(v_scale<M>(M::sub(1.0f, fr), vel), v_scale<M>(fr, gv));
+    f3 out = v_axpy<M>(v_scale<M>(M::sub(1.0f, fr), vel), fr, gv);
     if (rep) {
         const float coef = M::div(M::mul(A.repulsion, M::div(A.h, dt)), fmaxf(rho, 1.0f));
         out = v_sub<M>(out, v_scale<M>(coef, grad));
@@ -402,9 +402,9 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
 template <class M>
 __device__ __forceinline__ f3 head_point(const float (&h)[12], f3 p) {
     f3 o;
-    o.x = M::add(M::add(M::add(M::mul(h[0], p.x), M::mul(h[1], p.y)), M::mul(h[2], p.z)), h[3]);
-    o.y = M::add(M::add(M::add(M::mul(h[4], p.x), M::mul(h[5], p.y)), M::mul(h[6], p.z)), h[7]);
-    o.z = M::add(M::add(M::add(M::mul(h[8], p.x), M::mul(h[9], p.y)), M::mul(h[10], p.z)), h[11]);
+    o.x = M::add(M::madd(h[2], p.z, M::madd(h[1], p.y, M::mul(h[0], p.x))), h[3]);
+    o.y = M::add(M::madd(h[6], p.z, M::madd(h[5], p.y, M::mul(h[4], p.x))), h[7]);
+    o.z = M::add(M::madd(h[10], p.z, M::madd(h[9], p.y, M::mul(h[8], p.x))), h[11]);
     return o;
 }
 
@@ -488,7 +488,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
         if (valid && i >= 1 && i < n) force = collide_force<M>(A, x[k], force);
         const f3 v = vel_in[k];
         // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
-        p[k] = v_add<M>(v_add<M>(x[k], v_scale<M>(dt, v)), v_scale<M>(dt2, force));
+        p[k] = v_axpy<M>(v_axpy<M>(x[k], dt, v), dt2, force);
     }
 
     // loop 1, sequential part: FTL, newPos = parent + radius * normalize(pred - parent)
@@ -520,7 +520,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
             pi.z = __shfl_sync(FULL, p[k].z, base + own);
         }
         const f3 dir = v_normalize<M>(v_sub<M>(pi, par));
-        par = v_add<M>(par, v_scale<M>(r, dir));
+        par = v_axpy<M>(par, r, dir);
         if (L == 1 || l == own) xn[k] = par;
     }
 

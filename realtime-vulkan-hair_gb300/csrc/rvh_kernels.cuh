@@ -479,17 +479,28 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
     auto strand_of = [&](int r) { return begin + r * per_round + g * kWarps + warp; };
     for (int r0 = 0; r0 < rounds; r0 += U) {
         const int r1 = min(rounds, r0 + U);
-        if (A.grid_prev) {   // 1. the group's gather box
+        if (A.grid_prev) {   // 1. the group's gather box (all of a pair of rounds' loads in flight)
             LaneBounds lb;
-            for (int r = r0; r < r1; ++r) {
-                const int strand = strand_of(r);
-                const bool valid = g < SPW && strand < end;
-                const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+            for (int r = r0; r < r1; r += 2) {
+                f3 xs[2][K];
+                bool ok[2][K];
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const int i = PhaseA<NFIX, L>::point(l, k);
-                    if (valid && i >= 1 && i < n) lb.add(xyz(ld_cg(rec + i)));
+                for (int h = 0; h < 2; ++h) {
+                    const int strand = strand_of(r + h);
+                    const bool valid = g < SPW && r + h < r1 && strand < end;
+                    const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const int i = PhaseA<NFIX, L>::point(l, k);
+                        ok[h][k] = valid && i >= 1 && i < n;
+                        xs[h][k] = ok[h][k] ? xyz(ld_cg(rec + i)) : f3{0.f, 0.f, 0.f};
+                    }
                 }
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (ok[h][k]) lb.add(xs[h][k]);
             }
             lb.reduce<M>(A, S);
         }
@@ -521,15 +532,22 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
                     const int strand = strand_of(r);
                     const bool valid = g < SPW && strand < end;
                     const float4* rec = A.strands + (size_t)(valid ? strand : 0) * (3 * n);
-#pragma unroll 1
+                    // any order works for integer sums: lanes take blocks of K points, the
+                    // block rotated by the strand's place in the warp, so the lanes of one
+                    // instruction sit K points apart and the warp's strands at different
+                    // heights (fewer lanes on one cell per shared atomic); the round's K
+                    // points are loaded together, then splatted by a rolled loop
+                    f3 ps[K], vs[K];
+                    unsigned m = 0u;
+#pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        // any order works for integer sums: lanes take blocks of K points, the
-                        // block rotated by the strand's place in the warp, so the lanes of one
-                        // instruction sit K points apart and the warp's strands at different
-                        // heights (fewer lanes on one cell per shared atomic)
                         const int i = ((l + 2 * g) % L) * K + k;
-                        if (valid && i >= 1 && i < n) f(xyz(rec[i]), xyz(rec[n + i]));
+                        const bool ok = valid && i >= 1 && i < n;
+                        ps[k] = ok ? xyz(rec[i]) : f3{0.f, 0.f, 0.f};
+                        vs[k] = ok ? xyz(rec[n + i]) : f3{0.f, 0.f, 0.f};
+                        if (ok) m |= 1u << k;
                     }
+                    for_lane_points(ps, vs, m, [&](f3& p, f3& v) { f(p, v); });
                 }
             });
         }
@@ -590,9 +608,9 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
             if (pend_gather) v = gb.gather(x, v, A.dt_prev);
             const f3 force = collide_force<M>(A, x, f0);
             // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
-            const f3 p = v_add<M>(v_add<M>(x, v_scale<M>(dt, v)), v_scale<M>(dt2, force));
+            const f3 p = v_axpy<M>(v_axpy<M>(x, dt, v), dt2, force);
             const f3 dir = v_normalize<M>(v_sub<M>(p, par));
-            const f3 xn = v_add<M>(par, v_scale<M>(r, dir));
+            const f3 xn = v_axpy<M>(par, r, dir);
             const f3 newVel = v_div<M>(v_sub<M>(xn, x), dt);
             f3 vel = v_scale<M>(A.damping, newVel);
             if (v_len<M>(vel) > A.vmax) vel = v_scale<M>(A.vmax, v_normalize<M>(vel));
