@@ -250,6 +250,59 @@ def run_tess(ctx, api, configs, warmup=3, reps=10):
                          "bytes_per_launch": alg}}
 
 
+def run_shade(ctx, api, configs, warmup=3, reps=10):
+    """The shadow, opacity and hair passes over the tessellated 100k-strand head
+    (12 isolines x 42 segments, 51.6 M vertices) with the reference's cameras
+    and 1080 x 720 maps: device time of rvh_asset_shade by CUDA events on the
+    launching stream.  Algorithmic bytes: each vertex read by the three passes
+    (3 x 16 B), its colour written (16 B), the segment frames read once, and
+    the maps cleared, finished and read back once (depth 4 B, layers 16 B per
+    texel, three times)."""
+    import torch
+    spec = configs.full_head()
+    a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest)
+    a.set_params(spec.params)
+    a.set_colliders(spec.colliders)
+    for k in range(3):
+        a.step(spec.frame(k))
+    ctx.synchronize()
+    td, sd = api.tess_desc_reference(), api.shade_desc_reference()
+    ns, per = spec.n_strands, td.n_lines * (td.n_segments + 1)
+    vertices = ns * per
+    texels = sd.map_width * sd.map_height
+    vert = torch.empty((vertices * 4,), dtype=torch.float32, device="cuda")
+    frames = torch.empty((ns * (spec.n_points - 1) * 12,), dtype=torch.float32, device="cuda")
+    depth = torch.empty((texels,), dtype=torch.float32, device="cuda")
+    opac = torch.empty((texels * 4,), dtype=torch.float32, device="cuda")
+    col = torch.empty((vertices * 4,), dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    a.tessellate(vert.data_ptr(), frames.data_ptr(), desc=td, stream=st.cuda_stream)
+
+    def once():
+        a.shade(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), col.data_ptr(), tess_desc=td,
+                shade_desc=sd, stream=st.cuda_stream)
+
+    for _ in range(warmup):
+        once()
+    st.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        once()
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    covered = int((depth < 1).sum().item())
+    a.close()
+    alg = vertices * 64 + ns * (spec.n_points - 1) * 48 + texels * 20 * 3
+    peak, _ = load_peaks()
+    gbs = alg / (ms * 1e-3) / 1e9
+    return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments, 1080 x 720 maps",
+            "vertices": vertices, "covered_texels": covered, "ms": ms, "vertices_per_s": vertices / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "bytes_per_launch": alg}}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle's OpenMP restatement on the host cores."""
     if rank != 0:
@@ -293,6 +346,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-tess", action="store_true")
+    ap.add_argument("--no-shade", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
@@ -418,6 +472,9 @@ def main():
     tess = None
     if world == 1 and not args.no_tess:
         tess = run_tess(ctx, api, configs)
+    shade = None
+    if world == 1 and not args.no_shade:
+        shade = run_shade(ctx, api, configs)
 
     served, served_pts = None, None
     if not args.no_served and world == 1:
@@ -454,6 +511,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
+            "shading": shade,
             "served": None if served is None else {
                 "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
                             "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (

@@ -191,6 +191,53 @@ rvh_status rvh_tess_desc_reference(rvh_tess_desc* d);
  * Frisvad orthonormal basis).  Both 16-byte aligned. */
 rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vertices, void* frames, void* stream);
 
+/* ---- hair shading (src/Renderer.cpp's shadow, opacity and hair passes;
+ * src/shaders/hairOpacity.frag, src/shaders/hair.frag) ----------------------
+ * The reference draws the tessellated hair three times: into a light-space
+ * depth map, into a deep opacity map (three layers of +0.3 per fragment
+ * behind the first surface, d = 0.3, 8-bit unorm target with additive
+ * blending) and into the framebuffer with hair.frag.  Here each tessellated
+ * vertex is a fragment covering one texel (the ribbons are about a texel wide
+ * and their vertices about a texel apart at the reference's sizes); the maps
+ * and colours go to device buffers.  Matrices are column-major (glm's layout). */
+typedef struct rvh_shade_desc {
+    float camera_view[16];  /* Camera.cpp:13: lookAt((0, 1, 10), (0, 1, 0), (0, 1, 0)) */
+    float camera_proj[16];  /* Camera.cpp:14-15: perspective(45 deg, 1.5, 0.1, 50), y flipped */
+    float light_view[16];   /* Camera.cpp:28-30: lookAt(6.5 normalize((2, 0, 1) - (0, 1, 0)), (0, 1, 0), up) */
+    float light_proj[16];   /* Camera.cpp:31-32: perspective(60 deg, 1.5, 1, 10), y flipped */
+    int32_t map_width;      /* SHADOWMAP_WIDTH = 1080 (Renderer.cpp:9) */
+    int32_t map_height;     /* SHADOWMAP_HEIGHT = 720 (Renderer.cpp:10) */
+    int32_t reserved[2];
+} rvh_shade_desc;
+/* The reference's cameras and map size (glm's float arithmetic, bit for bit). */
+rvh_status rvh_shade_desc_reference(rvh_shade_desc* d);
+/* hair.frag for n caller-given fragments (replaces the fragment stage of the
+ * reference's hair pipeline, Renderer.cpp:1554-1746, whose fragment shader is
+ * hair.frag).
+ * inputs: device, n x 24 floats per fragment: in_uv (2), in_u, in_v, in_w (3
+ * each), in_viewDir (3), in_lightDir (3), in_fragPosLightSpace (4), 3 unused
+ * (hair.frag:14-20).  depth_map: map_width x map_height floats; opacity_map:
+ * the same count of float4 (layers r, g, b).  colors: n float4 (outColor).
+ * inputs, opacity_map and colors 16-byte aligned; n < 2^31. */
+rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, const void* depth_map,
+                               const void* opacity_map, int32_t map_width, int32_t map_height, void* colors,
+                               void* stream);
+/* The three passes over an asset's tessellation (vertices and frames as
+ * rvh_asset_tessellate wrote them with the same tessellation descriptor).
+ * depth_map: map_width x map_height floats (4-byte aligned), opacity_map: the
+ * same count of float4, colors: one float4 per tessellated vertex; all
+ * written.  The shadow pass's light depth map, the opacity pass's layers
+ * (min(255, 77 n) / 255 for n fragments in a layer: 0.3 as unorm8, saturating
+ * sum; alpha 0) and hair.frag's colour per vertex. */
+rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
+                           const void* frames, void* depth_map, void* opacity_map, void* colors, void* stream);
+/* A headless stand-in for the framebuffer: every vertex inside the camera's
+ * clip volume covers one pixel of a width x height float4 image; the nearest
+ * (then the lowest vertex index) wins and the pixel takes its colour; empty
+ * pixels are 0.  n_vertices < 2^32. */
+rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* vertices, const void* colors,
+                            const rvh_shade_desc* sd, int32_t width, int32_t height, void* image, void* stream);
+
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
     int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1 (one thread walks each strand), 4, 8, 16, 32 */

@@ -11,7 +11,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
-SOURCES = ["oracle_capi.cpp", "hair_oracle.hpp", "hair_adjoint.hpp"]
+SOURCES = ["oracle_capi.cpp", "hair_oracle.hpp", "hair_adjoint.hpp", "tess_oracle.hpp", "shade_oracle.hpp"]
 
 
 def _stale(out, deps):

@@ -12,6 +12,7 @@
 
 #include "hair_adjoint.hpp"
 #include "hair_oracle.hpp"
+#include "shade_oracle.hpp"
 #include "tess_oracle.hpp"
 
 namespace {
@@ -86,6 +87,63 @@ int oracle_tess(const float* records, int ns, int n, int n_lines, int n_segments
     oracle::tess::tessellate(records, ns, n, P,
                              sin_mode == 0 ? oracle::tess::RefSin::kFloat : oracle::tess::RefSin::kDouble, out,
                        frames);
+    return 0;
+}
+/* Hair shading (shade_oracle.hpp).  Fragments: in = n x 24 floats, depth =
+ * w*h floats, opacity = w*h float4, out = n float4.  sin_mode as for
+ * oracle_tess. */
+int oracle_shade_fragments(long long n, const float* in, const float* depth, const float* opacity, int w, int h,
+                           int sin_mode, float* out) {
+    if (n < 0 || (n > 0 && (!in || !depth || !opacity || !out)) || w < 1 || h < 1) return 1;
+    const oracle::shade::Maps M{depth, opacity, w, h};
+    const auto mode = sin_mode == 0 ? oracle::shade::RefSin::kFloat : oracle::shade::RefSin::kDouble;
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < n; ++i) oracle::shade::shade_fragment(in + 24 * i, M, mode, out + 4 * i);
+    return 0;
+}
+/* hairOpacity.frag's outColor for n fragments (layers 1-3, z0). */
+int oracle_opacity_fragments(long long n, const float* in, const float* depth, int w, int h, float* out) {
+    if (n < 0 || (n > 0 && (!in || !depth || !out)) || w < 1 || h < 1) return 1;
+    for (long long i = 0; i < n; ++i) oracle::shade::opacity_fragment(in + 24 * i, depth, w, h, out + 4 * i);
+    return 0;
+}
+/* Light-space projection and the eyes of the camera and light views (matrices
+ * column-major): lvp[16], cam_pos[3], light_pos[3]. */
+int oracle_shade_camera(const float* camera_view, const float* light_view, const float* light_proj, float* lvp,
+                        float* cam_pos, float* light_pos) {
+    if (!camera_view || !light_view || !light_proj || !lvp || !cam_pos || !light_pos) return 1;
+    const oracle::shade::Camera K = oracle::shade::make_camera(camera_view, light_view, light_proj);
+    for (int k = 0; k < 16; ++k) lvp[k] = K.lvp[k];
+    for (int k = 0; k < 3; ++k) {
+        cam_pos[k] = K.cam_pos[k];
+        light_pos[k] = K.light_pos[k];
+    }
+    return 0;
+}
+/* Light depth and deep opacity maps of nv vertices (float4 each). */
+int oracle_shade_maps(const float* verts, long long nv, const float* lvp, int w, int h, float* depth,
+                      float* opacity) {
+    if (nv < 0 || (nv > 0 && !verts) || !lvp || !depth || !opacity || w < 1 || h < 1) return 1;
+    oracle::shade::light_maps(verts, nv, lvp, w, h, depth, opacity);
+    return 0;
+}
+/* Fragment inputs (n_vertices x 24) of tessellated vertices and their frames. */
+int oracle_shade_vertex_inputs(const float* verts, const float* frames, int ns, int n, int n_lines, int n_segments,
+                               const float* camera_view, const float* light_view, const float* light_proj,
+                               float* in) {
+    if (!verts || !frames || !in || ns < 0 || n < 2 || n_lines < 1 || n_segments < 1) return 1;
+    const oracle::shade::Camera K = oracle::shade::make_camera(camera_view, light_view, light_proj);
+    const long long nv = (long long)ns * n_lines * (n_segments + 1);
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < nv; ++i)
+        oracle::shade::vertex_inputs(verts, frames, n, n_lines, n_segments, K, i, in + 24 * i);
+    return 0;
+}
+/* Camera image (w x h float4) of nv vertices with the given colours. */
+int oracle_render_image(const float* verts, const float* colors, long long nv, const float* view, const float* proj,
+                        int w, int h, float* image) {
+    if (nv < 0 || (nv > 0 && (!verts || !colors)) || !view || !proj || !image || w < 1 || h < 1) return 1;
+    oracle::shade::render_image(verts, colors, nv, view, proj, w, h, image);
     return 0;
 }
 /* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */

@@ -38,6 +38,16 @@ def lib():
         l.oracle_tess.argtypes = [_P(C.c_float), C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
                                   C.c_float, C.c_int, _P(C.c_float), _P(C.c_float)]
         l.oracle_tess.restype = C.c_int
+        f4 = _P(C.c_float)
+        l.oracle_shade_fragments.argtypes = [C.c_longlong, f4, f4, f4, C.c_int, C.c_int, C.c_int, f4]
+        l.oracle_shade_camera.argtypes = [f4] * 6
+        l.oracle_opacity_fragments.argtypes = [C.c_longlong, f4, f4, C.c_int, C.c_int, f4]
+        l.oracle_shade_maps.argtypes = [f4, C.c_longlong, f4, C.c_int, C.c_int, f4, f4]
+        l.oracle_shade_vertex_inputs.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4]
+        l.oracle_render_image.argtypes = [f4, f4, C.c_longlong, f4, f4, C.c_int, C.c_int, f4]
+        for f in (l.oracle_shade_fragments, l.oracle_shade_camera, l.oracle_opacity_fragments, l.oracle_shade_maps, l.oracle_shade_vertex_inputs,
+                  l.oracle_render_image):
+            f.restype = C.c_int
         l.oracle_run_head_f64.argtypes = [_P(C.c_double)] + common + [_P(C.c_float), _P(C.c_float)]
         l.oracle_run_head_f32.argtypes = [_P(C.c_float)] + common + [_P(C.c_float), _P(C.c_float)]
         adj = [_P(C.c_double), C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(T.SimParams), _P(T.Frame),
@@ -220,3 +230,86 @@ def tessellate(records, n_points, n_lines=12, n_segments=42, clump_radius=0.5, r
     if rc != 0:
         raise RuntimeError("oracle_tess failed: %d" % rc)
     return (out, fr) if frames else out
+
+
+# ---- hair shading (shade_oracle.hpp) ---------------------------------------------------------
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def _check(rc, name):
+    if rc != 0:
+        raise RuntimeError("%s failed: %d" % (name, rc))
+
+
+def shade_fragments(inputs, depth, opacity, sin_mode=1):
+    """hair.frag per fragment: inputs (n, 24), depth (h, w), opacity (h, w, 4) -> (n, 4)."""
+    inp, dep, opa = _f32(inputs), _f32(depth), _f32(opacity)
+    n = inp.shape[0]
+    h, w = dep.shape
+    out = np.zeros((n, 4), np.float32)
+    _check(lib().oracle_shade_fragments(n, _fptr(inp, C.c_float), _fptr(dep, C.c_float), _fptr(opa, C.c_float), w, h,
+                                        sin_mode, _fptr(out, C.c_float)), "oracle_shade_fragments")
+    return out
+
+
+def opacity_fragments(inputs, depth):
+    """hairOpacity.frag per fragment: (n, 4) = layers 1-3 (0 or 0.3) and z0."""
+    inp, dep = _f32(inputs), _f32(depth)
+    h, w = dep.shape
+    out = np.zeros((inp.shape[0], 4), np.float32)
+    _check(lib().oracle_opacity_fragments(inp.shape[0], _fptr(inp, C.c_float), _fptr(dep, C.c_float), w, h,
+                                          _fptr(out, C.c_float)), "oracle_opacity_fragments")
+    return out
+
+
+def _mats(desc):
+    return [_f32(np.array(list(getattr(desc, f)), np.float32)) for f in
+            ("camera_view", "camera_proj", "light_view", "light_proj")]
+
+
+def shade_camera(desc):
+    """(lvp (16,), cam_pos (3,), light_pos (3,)) of a ShadeDesc."""
+    cv, _, lv, lp = _mats(desc)
+    lvp = np.zeros(16, np.float32)
+    cam = np.zeros(3, np.float32)
+    light = np.zeros(3, np.float32)
+    _check(lib().oracle_shade_camera(*[_fptr(a, C.c_float) for a in (cv, lv, lp, lvp, cam, light)]),
+           "oracle_shade_camera")
+    return lvp, cam, light
+
+
+def shade_maps(vertices, desc):
+    """Light depth (h, w) and deep opacity (h, w, 4) maps of tessellated vertices."""
+    v = _f32(vertices).reshape(-1, 4)
+    lvp, _, _ = shade_camera(desc)
+    w, h = desc.map_width, desc.map_height
+    depth = np.zeros((h, w), np.float32)
+    opacity = np.zeros((h, w, 4), np.float32)
+    _check(lib().oracle_shade_maps(_fptr(v, C.c_float), v.shape[0], _fptr(lvp, C.c_float), w, h,
+                                   _fptr(depth, C.c_float), _fptr(opacity, C.c_float)), "oracle_shade_maps")
+    return depth, opacity
+
+
+def shade_vertex_inputs(vertices, frames, n_points, n_lines, n_segments, desc):
+    """Fragment inputs (n_vertices, 24) of tessellated vertices (ns, L, S+1, 4) and frames (ns, n-1, 3, 4)."""
+    v, fr = _f32(vertices), _f32(frames)
+    ns = v.shape[0]
+    cv, _, lv, lp = _mats(desc)
+    out = np.zeros((ns * n_lines * (n_segments + 1), 24), np.float32)
+    _check(lib().oracle_shade_vertex_inputs(_fptr(v, C.c_float), _fptr(fr, C.c_float), ns, n_points, n_lines,
+                                            n_segments, _fptr(cv, C.c_float), _fptr(lv, C.c_float),
+                                            _fptr(lp, C.c_float), _fptr(out, C.c_float)), "oracle_shade_vertex_inputs")
+    return out
+
+
+def render_image(vertices, colors, desc, width, height):
+    """Nearest-vertex camera image (height, width, 4)."""
+    v, col = _f32(vertices).reshape(-1, 4), _f32(colors).reshape(-1, 4)
+    cv, cp, _, _ = _mats(desc)
+    img = np.zeros((height, width, 4), np.float32)
+    _check(lib().oracle_render_image(_fptr(v, C.c_float), _fptr(col, C.c_float), v.shape[0], _fptr(cv, C.c_float),
+                                     _fptr(cp, C.c_float), width, height, _fptr(img, C.c_float)),
+           "oracle_render_image")
+    return img

@@ -1,0 +1,576 @@
+// rvh_shade.cu — hair shading of tessellated strands into headless buffers.
+//
+// The reference shades hair in three graphics passes (src/Renderer.cpp): the
+// hair drawn from the shadow camera into a depth map cleared to 1.0; an
+// opacity pass (hairOpacity.frag) adding 0.3 per fragment to three layers
+// behind the first surface z0, at z0 + [0, d), [d, 2d), [2d, ...) with d =
+// 0.3, into the swapchain's 8-bit unorm format with additive blending; then
+// the camera pass, hair.frag per fragment: a Marschner-style R / TT / TRT
+// single-scattering lobe in the strand's frame, a multiple-scattering term
+// damped by the opacity layer the fragment falls in, a 7x7 PCF shadow test,
+// an ambient term and a per-isoline brightness hash.  Without a graphics
+// pipeline these are CUDA kernels over the tessellated vertices
+// (rvh_asset_tessellate), each vertex one fragment covering one texel:
+//
+//   k_clear_maps      depth = 1.0, layer counts = 0
+//   k_light_depth     nearest light-space depth per texel (atomic min of the bits)
+//   k_light_opacity   each vertex counted into the layer its depth falls in,
+//                     relative to the bilinear z0 at its position
+//   k_opacity_finish  layer value = min(255, 77 count) / 255 (0.3 as unorm8,
+//                     saturating sum), in place over the counts
+//   k_shade_vertices  hair.frag's colour per vertex (k_shade_fragments: per
+//                     caller-given fragment inputs)
+//   k_image_*         optional camera image: nearest vertex per pixel
+//
+// The maps live in L2 (the reference's 1080 x 720: 3.1 MB of depth, 12.4 MB
+// of layers); the vertex passes stream the tessellated vertices from HBM.
+// Samplers are clamp-to-edge bilinear with texel centres at (i + 0.5) / size
+// (the reference's VK_FILTER_LINEAR + CLAMP_TO_EDGE samplers,
+// src/Renderer.cpp:14,1899-1902).  The brightness hash uses a correctly
+// rounded sin, as the tessellation does.  Float arithmetic is separately
+// rounded in the shader's order; acos, sin, cos, exp and pow are CUDA's, so
+// colours agree with a host evaluation to a few float ulps of those functions
+// while the maps, every comparison against them and the camera image's
+// depth test agree bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "rvh_internal.hpp"
+
+namespace rvh {
+namespace {
+
+constexpr int kShadeThreads = 256;
+constexpr float kPi = 3.14159265359f;
+constexpr float kPiOver2 = 1.57079632679f;
+constexpr float kRadToDeg = 57.2957795131f;
+constexpr float kDegToRad = 0.01745329251f;
+constexpr float kEps = 0.001f;
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return mk(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator*(V3 a, V3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float len3(V3 a) { return sqrtf(dot3(a, a)); }
+// glm normalize: v * inversesqrt(dot(v, v)), inversesqrt = 1 / sqrt
+__device__ __forceinline__ V3 nrm3(V3 a) { return a * (1.0f / sqrtf(dot3(a, a))); }
+__device__ __forceinline__ V3 cross3(V3 a, V3 b) {
+    return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+
+// ---- hair.frag's helper functions (src/shaders/hair.frag:24-124) ----------------------
+__device__ __forceinline__ bool vec3_compare(V3 a, V3 b) {
+    return fabsf(a.x - b.x) < kEps && fabsf(a.y - b.y) < kEps && fabsf(a.z - b.z) < kEps;
+}
+__device__ __forceinline__ float angle_vector_plane(V3 v, V3 n) {
+    float angle = acosf(dot3(v, n) / (len3(v) * len3(n)));
+    if (angle < kPiOver2) angle = kPiOver2 - angle;
+    else angle = -(angle - kPiOver2);
+    return angle;
+}
+__device__ __forceinline__ V3 project_onto_plane(V3 v, V3 n) { return v - dot3(v, n) * n; }
+__device__ __forceinline__ float directional_angle(V3 v1, V3 v2, V3 n) {
+    const float angle = acosf(dot3(v1, v2) / (len3(v1) * len3(v2)));
+    if (vec3_compare(nrm3(cross3(v2, v1)), n)) return angle;
+    return (2.0f * kPi) - angle;
+}
+__device__ __forceinline__ float gaussian(float alpha, float beta, float ti, float to) {
+    const float e = sinf(ti * kDegToRad) + sinf(to * kDegToRad) - alpha;
+    return (1.f / (beta * sqrtf(2.f * kPi))) * expf(-powf(e, 2.0f) / (2.f * beta * beta));
+}
+__device__ __forceinline__ float schlicks(float n, float x) {
+    const float R0 = ((1.f - n) * (1.f - n)) / ((1.f + n) * (1.f + n));
+    return R0 + (1.f - R0) * powf(1.f - x, 5.0f);
+}
+// GLSL clamp(x, 0, 1) = min(max(x, 0), 1) with max(a, b) = a < b ? b : a and
+// min(a, b) = b < a ? b : a: a NaN passes through, as in the shader.
+__device__ __forceinline__ float clamp01(float x) {
+    const float m = x < 0.f ? 0.f : x;
+    return 1.f < m ? 1.f : m;
+}
+__device__ __forceinline__ float shade_hash(float x, float y) {   // random(), correctly rounded sin
+    const float d = x * 12.9898f + y * 78.233f;
+    const float m = (float)sin((double)d) * 43758.5453123f;
+    return m - floorf(m);
+}
+
+// Clamp-to-edge bilinear sample of channel c of a (w x h x ch) float image.
+__device__ __forceinline__ float tex_texel(const float* img, int w, int h, int ch, int x, int y, int c) {
+    x = min(max(x, 0), w - 1);
+    y = min(max(y, 0), h - 1);
+    return __ldg(img + ((size_t)y * w + x) * ch + c);
+}
+__device__ __forceinline__ float tex_sample(const float* img, int w, int h, int ch, float u, float v, int c) {
+    const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    // texel indices clamped before the conversion (only the clamp to edge reads them);
+    // keeps an infinite or NaN coordinate defined
+    const int ix = (int)fminf(fmaxf(x0, -1.f), (float)w), iy = (int)fminf(fmaxf(y0, -1.f), (float)h);
+    const float t00 = tex_texel(img, w, h, ch, ix, iy, c), t10 = tex_texel(img, w, h, ch, ix + 1, iy, c);
+    const float t01 = tex_texel(img, w, h, ch, ix, iy + 1, c), t11 = tex_texel(img, w, h, ch, ix + 1, iy + 1, c);
+    const float a = t00 + fx * (t10 - t00);
+    const float b = t01 + fx * (t11 - t01);
+    return a + fy * (b - a);
+}
+
+struct Maps {
+    const float* depth;     // w x h
+    const float* opacity;   // w x h x 4 (layers r, g, b)
+    int w, h;
+};
+
+// PCFshadowCalculation (hair.frag:99-125): the shader's texel size is fixed at 1/1080 x 1/720
+__device__ float pcf_shadow(const Maps& M, float px, float py, float pz, float pw) {
+    const float x = px / pw, y = py / pw, z = pz / pw;
+    if (fabsf(x) > 1.f || fabsf(y) > 1.f || fabsf(z) > 1.f) return 0.f;
+    const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
+    const float tsx = 1.f / 1080.0f, tsy = 1.f / 720.0f;
+    float lighted = 0.f;
+    for (int dx = -3; dx <= 3; ++dx)
+        for (int dy = -3; dy <= 3; ++dy) {
+            const float cu = u + (float)dx * tsx, cv = v + (float)dy * tsy;
+            if (z > tex_sample(M.depth, M.w, M.h, 1, cu, cv, 0)) lighted += 1.f;
+        }
+    const float kernel = 2.f * 3 + 1.f;
+    return lighted / (kernel * kernel);
+}
+
+// hair.frag main (:130-261) for one fragment.  in: uv (2), u, v, w (3 each),
+// viewDir (3), lightDir (3), fragPosLightSpace (4).
+__device__ float4 shade_fragment(const float* in, const Maps& M) {
+    const float uv_x = in[0], uv_y = in[1];
+    const V3 fu = mk(in[2], in[3], in[4]), fv = mk(in[5], in[6], in[7]);
+    const V3 view = mk(in[11], in[12], in[13]), light = mk(in[14], in[15], in[16]);
+    const float px = in[17], py = in[18], pz = in[19], pw = in[20];
+    const float over255 = 1.0f / 255.0f;
+    const V3 w_i = nrm3(light);
+    const V3 w_o = nrm3(view);
+    const float n = 1.55f;
+    const V3 C = mk(101.0f, 67.0f, 33.0f) * over255;   // midBrown
+    const float roughness = 0.2f, shift = 0.01f;
+    const float theta_i = angle_vector_plane(w_i, fu) * kRadToDeg;
+    const float theta_o = angle_vector_plane(w_o, fu) * kRadToDeg;
+    const float phi_i = directional_angle(nrm3(project_onto_plane(w_i, fu)), fv, fu) * kRadToDeg;
+    const float phi_o = directional_angle(nrm3(project_onto_plane(w_o, fu)), fv, fu) * kRadToDeg;
+    const float theta_d = (theta_o - theta_i) / 2.f;
+    const float phi_d = phi_o - phi_i;
+    const float alpha_R = -2.f * shift, alpha_TT = shift, alpha_TRT = 4.f * shift;
+    const float beta_R = roughness * roughness, beta_TT = 0.5f * beta_R, beta_TRT = 2.f * beta_R;
+    const float M_R = gaussian(alpha_R, beta_R, theta_i, theta_o);
+    const float M_TT = gaussian(alpha_TT, beta_TT, theta_i, theta_o);
+    const float M_TRT = gaussian(alpha_TRT, beta_TRT, theta_i, theta_o);
+    const float cosTheta_d = cosf(theta_d * kDegToRad);
+    const float cosPhi_d = cosf(phi_d * kDegToRad);
+    const float cosPhi_dOver2 = cosf((phi_d / 2.f) * kDegToRad);
+    const float nR = schlicks(n, sqrtf(0.5f + 0.5f * dot3(w_i, w_o))) * (0.25f * sqrtf(0.5f + 0.5f * cosPhi_d));
+    const V3 N_R = mk(nR, nR, nR);
+    const float n_prime = (1.19f / cosTheta_d) + 0.36f * cosTheta_d;
+    const float a = 1.f / n_prime;
+    const float h_TT = (1.f + a * (0.6f - 0.8f * cosPhi_d)) * cosPhi_dOver2;
+    const float f_TT = schlicks(n, cosTheta_d * sqrtf(1.f - h_TT * h_TT));
+    const float Cpower_TT = sqrtf(1.f - h_TT * h_TT * a * a) / (2.f * cosTheta_d);
+    const V3 T_TT = mk(powf(C.x, Cpower_TT), powf(C.y, Cpower_TT), powf(C.z, Cpower_TT));
+    const V3 A_TT = (1.f - f_TT) * (1.f - f_TT) * T_TT;
+    const float D_TT = expf(-3.65f * cosPhi_d - 3.98f);
+    const V3 N_TT = A_TT * D_TT;
+    const V3 N_TRT = A_TT * D_TT;   // the shader reuses the TT lobe here (hair.frag:236)
+    const V3 S_single = (1.3f * N_R * M_R + 0.5f * N_TT * M_TT + N_TRT * M_TRT) / (cosTheta_d * cosTheta_d);
+    const float shadow = pcf_shadow(M, px, py, pz, pw);
+    const float x = px / pw, y = py / pw, currentDepth = pz / pw;
+    const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
+    const float z0 = tex_sample(M.depth, M.w, M.h, 1, u, v, 0);
+    const float d = 0.3f;
+    float opacity = 0.f;
+    if (currentDepth >= z0 && currentDepth < z0 + d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 0);
+    else if (currentDepth >= z0 + d && currentDepth < z0 + 2.f * d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 1);
+    else if (currentDepth >= z0 + 2.f * d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 2);
+    const V3 fakeNormal = nrm3(w_o - fu * dot3(fu, w_o));
+    const float luma = 0.3f;
+    const V3 Cexp = mk(powf(C.x / luma, 1.f - opacity), powf(C.y / luma, 1.f - opacity), powf(C.z / luma, 1.f - opacity));
+    const V3 sqrtC = mk(sqrtf(C.x), sqrtf(C.y), sqrtf(C.z));
+    const V3 S_multi = sqrtC * ((dot3(fakeNormal, w_i) + 1.f) / (4.f * kPi)) * Cexp;
+    (void)uv_y;
+    const float bright = 0.8f * fabsf(shade_hash(uv_x, uv_x)) + 0.6f;
+    const V3 col = ((S_single + S_multi) * (1.f - shadow) + 0.3f * C) * bright;
+    return make_float4(clamp01(col.x), clamp01(col.y), clamp01(col.z), 0.75f);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_shade_fragments(int n, const float* __restrict__ in, Maps M,
+                                                                   float4* __restrict__ out) {
+    for (int i = blockIdx.x * kShadeThreads + threadIdx.x; i < n; i += gridDim.x * kShadeThreads)
+        out[i] = shade_fragment(in + (size_t)i * 24, M);
+}
+
+// ---- the maps and per-vertex shading from tessellated strands ---------------------------
+struct Proj {
+    float m[16];        // column-major projection * view
+};
+struct Cam {
+    float lvp[16];      // light proj * light view (column-major)
+    float cam_pos[3];   // eye of the camera view
+    float light_pos[3]; // eye of the light view
+};
+
+__device__ __forceinline__ void mul_point(const float* m, V3 p, float& x, float& y, float& z, float& w) {
+    x = ((m[0] * p.x + m[4] * p.y) + m[8] * p.z) + m[12];
+    y = ((m[1] * p.x + m[5] * p.y) + m[9] * p.z) + m[13];
+    z = ((m[2] * p.x + m[6] * p.y) + m[10] * p.z) + m[14];
+    w = ((m[3] * p.x + m[7] * p.y) + m[11] * p.z) + m[15];
+}
+
+// The texel a vertex covers in a (w x h) target of projection m, its depth and
+// map coordinates; false outside the clip volume, where a rasteriser clips it.
+__device__ __forceinline__ bool project_texel(const float* m, V3 p, int w, int h, int& tx, int& ty, float& depth,
+                                              float& u, float& v) {
+    float x, y, z, ww;
+    mul_point(m, p, x, y, z, ww);
+    if (!(ww > 0.f)) return false;
+    x = x / ww;
+    y = y / ww;
+    z = z / ww;
+    if (fabsf(x) > 1.f || fabsf(y) > 1.f || z < 0.f || z > 1.f) return false;
+    u = x * 0.5f + 0.5f;
+    v = y * 0.5f + 0.5f;
+    tx = min((int)(u * (float)w), w - 1);
+    ty = min((int)(v * (float)h), h - 1);
+    depth = z;
+    return true;
+}
+
+// Pass 1: nearest light depth per texel (z in [0, 1]: the bits order like the values).
+__global__ void __launch_bounds__(kShadeThreads) k_light_depth(const float4* __restrict__ verts, long long nv, Cam K,
+                                                               int w, int h, unsigned* __restrict__ depth_bits) {
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
+        const float4 q = verts[i];
+        int tx, ty;
+        float z, u, v;
+        if (project_texel(K.lvp, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v))
+            atomicMin(depth_bits + (size_t)ty * w + tx, __float_as_uint(z));
+    }
+}
+
+// Pass 2: fragments per opacity layer (hairOpacity.frag:36-59), counted per texel.
+__global__ void __launch_bounds__(kShadeThreads) k_light_opacity(const float4* __restrict__ verts, long long nv, Cam K,
+                                                                 int w, int h, const float* __restrict__ depth,
+                                                                 uint4* __restrict__ counts) {
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
+        const float4 q = verts[i];
+        int tx, ty;
+        float z, u, v;
+        if (!project_texel(K.lvp, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v)) continue;
+        const float z0 = tex_sample(depth, w, h, 1, u, v, 0);
+        const float d = 0.3f;
+        unsigned* c = &counts[(size_t)ty * w + tx].x;
+        if (z >= z0 && z < z0 + d) {
+            atomicAdd(c + 0, 1u);
+            atomicAdd(c + 1, 1u);
+            atomicAdd(c + 2, 1u);
+        } else if (z >= z0 + d && z < z0 + 2.f * d) {
+            atomicAdd(c + 1, 1u);
+            atomicAdd(c + 2, 1u);
+        } else if (z >= z0 + 2.f * d) {
+            atomicAdd(c + 2, 1u);
+        }
+    }
+}
+
+// Layer counts -> the 8-bit unorm target's additive sum: 0.3 is stored as 77/255
+// and the sum saturates, min(255, 77 c) / 255.  In place: each texel's uint4 of
+// counts becomes its float4 of layers.
+__device__ __forceinline__ float layer_value(unsigned c) {
+    return (float)(c >= 4u ? 255u : min(255u, 77u * c)) / 255.0f;
+}
+__global__ void __launch_bounds__(kShadeThreads) k_opacity_finish(long long texels, uint4* map) {
+    for (long long t = (long long)blockIdx.x * kShadeThreads + threadIdx.x; t < texels; t += (long long)gridDim.x * kShadeThreads) {
+        const uint4 c = map[t];
+        reinterpret_cast<float4*>(map)[t] = make_float4(layer_value(c.x), layer_value(c.y), layer_value(c.z), 0.f);
+    }
+}
+
+// Pass 3: hair.frag's colour of every tessellated vertex, from the fragment
+// inputs the tessellation and geometry stages hand it on the ribbon's centre
+// line (hair.tese:286-330, hair.geom:43-61): uv = (isoline u, v), the frame
+// of the vertex's segment, normalize(cameraPos - pos), normalize(lightPos -
+// pos), lightProj * lightView * pos.
+__global__ void __launch_bounds__(kShadeThreads) k_shade_vertices(const float4* __restrict__ verts,
+                                                                  const float4* __restrict__ frames, int n_strands,
+                                                                  int n_points, int n_lines, int n_segments, Cam K,
+                                                                  Maps M, float4* __restrict__ out) {
+    const int S1 = n_segments + 1;
+    const long long per = (long long)n_lines * S1;
+    const long long nv = per * n_strands;
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
+        const long long s = i / per;
+        const int r = (int)(i - s * per);
+        const int j = r / S1, k = r - j * S1;
+        const float u = (float)j / (float)n_lines, v = (float)k / (float)n_segments;
+        const float x = v * (float)(n_points - 1);
+        const int sf = min((int)floorf(x), n_points - 2);
+        const float4* fr = frames + ((size_t)s * (n_points - 1) + sf) * 3;
+        const float4 q = verts[i];
+        const V3 p = mk(q.x, q.y, q.z);
+        float in[24];
+        in[0] = u;
+        in[1] = v;
+        for (int c = 0; c < 3; ++c) {
+            const float4 f = __ldg(fr + c);
+            in[2 + 3 * c] = f.x;
+            in[3 + 3 * c] = f.y;
+            in[4 + 3 * c] = f.z;
+        }
+        const V3 vd = nrm3(mk(K.cam_pos[0], K.cam_pos[1], K.cam_pos[2]) - p);
+        const V3 ld = nrm3(mk(K.light_pos[0], K.light_pos[1], K.light_pos[2]) - p);
+        in[11] = vd.x;
+        in[12] = vd.y;
+        in[13] = vd.z;
+        in[14] = ld.x;
+        in[15] = ld.y;
+        in[16] = ld.z;
+        mul_point(K.lvp, p, in[17], in[18], in[19], in[20]);
+        in[21] = in[22] = in[23] = 0.f;
+        out[i] = shade_fragment(in, M);
+    }
+}
+
+// ---- maps and image -----------------------------------------------------------------
+__global__ void __launch_bounds__(kShadeThreads) k_clear_maps(long long texels, unsigned* __restrict__ depth_bits,
+                                                              uint4* __restrict__ counts) {
+    for (long long t = (long long)blockIdx.x * kShadeThreads + threadIdx.x; t < texels; t += (long long)gridDim.x * kShadeThreads) {
+        depth_bits[t] = 0x3f800000u;   // 1.0f, the shadow pass's clear depth
+        counts[t] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// Camera image with a depth test: while splatting, the first 8 bytes of each
+// float4 pixel hold the key (depth bits << 32 | vertex index) of the nearest
+// vertex so far; the resolve pass replaces it by that vertex's colour.
+constexpr unsigned long long kNoVertex = ~0ull;
+
+__global__ void __launch_bounds__(kShadeThreads) k_image_clear(long long px, float4* __restrict__ image) {
+    for (long long t = (long long)blockIdx.x * kShadeThreads + threadIdx.x; t < px; t += (long long)gridDim.x * kShadeThreads)
+        reinterpret_cast<unsigned long long*>(image)[2 * t] = kNoVertex;
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_image_depth(const float4* __restrict__ verts, long long nv, Proj P,
+                                                               int w, int h, float4* __restrict__ image) {
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
+        const float4 q = verts[i];
+        int tx, ty;
+        float z, u, v;
+        if (!project_texel(P.m, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v)) continue;
+        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)(unsigned)i;
+        atomicMin(reinterpret_cast<unsigned long long*>(image) + 2 * ((size_t)ty * w + tx), key);
+    }
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_image_resolve(long long px, const float4* __restrict__ colors,
+                                                                 float4* __restrict__ image) {
+    for (long long t = (long long)blockIdx.x * kShadeThreads + threadIdx.x; t < px; t += (long long)gridDim.x * kShadeThreads) {
+        const unsigned long long key = reinterpret_cast<const unsigned long long*>(image)[2 * t];
+        image[t] = key == kNoVertex ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(colors + (key & 0xffffffffull));
+    }
+}
+
+// ---- host ---------------------------------------------------------------------------
+// glm's normalize, cross, lookAtRH and perspectiveRH_ZO in float, in glm's
+// operation order (glm 0.9.9 gtc/matrix_transform.inl), so the reference's
+// matrices come out bit for bit; the y flip of src/Camera.cpp:15,32.
+struct H3 {
+    float x, y, z;
+};
+H3 h_norm(H3 a) {
+    const float inv = 1.0f / std::sqrt((a.x * a.x + a.y * a.y) + a.z * a.z);
+    return H3{a.x * inv, a.y * inv, a.z * inv};
+}
+H3 h_cross(H3 a, H3 b) { return H3{a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+float h_dot(H3 a, H3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+
+void look_at(H3 eye, H3 ctr, H3 up, float* m) {
+    const H3 f = h_norm(H3{ctr.x - eye.x, ctr.y - eye.y, ctr.z - eye.z});
+    const H3 s = h_norm(h_cross(f, up));
+    const H3 u = h_cross(s, f);
+    const float cols[4][4] = {{s.x, u.x, -f.x, 0.f},
+                              {s.y, u.y, -f.y, 0.f},
+                              {s.z, u.z, -f.z, 0.f},
+                              {-h_dot(s, eye), -h_dot(u, eye), h_dot(f, eye), 1.f}};
+    std::memcpy(m, cols, sizeof cols);
+}
+
+void perspective_flipped(float fovy_deg, float aspect, float znear, float zfar, float* m) {
+    const float fovy = fovy_deg * 0.01745329251994329576923690768489f;   // glm::radians
+    const float t = std::tan(fovy / 2.0f);
+    std::memset(m, 0, 16 * sizeof(float));
+    m[0] = 1.0f / (aspect * t);
+    m[5] = -(1.0f / t);
+    m[10] = zfar / (znear - zfar);
+    m[11] = -1.0f;
+    m[14] = -(zfar * znear) / (zfar - znear);
+}
+
+// Eye of a rigid view matrix, -R^T t, in double rounded once.
+void eye_of(const float* view, float out[3]) {
+    for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc -= double(view[i * 4 + k]) * double(view[12 + k]);
+        out[i] = float(acc);
+    }
+}
+
+// Column-major a * b in double, rounded once.
+void mat_mul(const float* a, const float* b, float* o) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k) acc += double(a[k * 4 + r]) * double(b[c * 4 + k]);
+            o[c * 4 + r] = float(acc);
+        }
+}
+
+bool finite16(const float* m) {
+    for (int k = 0; k < 16; ++k)
+        if (!std::isfinite(m[k])) return false;
+    return true;
+}
+
+rvh_status check_desc(const rvh_shade_desc& d) {
+    if (d.map_width < 1 || d.map_height < 1 || d.map_width > 16384 || d.map_height > 16384)
+        return fail(RVH_ERR_INVALID_ARG, "shade: map size must be in [1, 16384]");
+    if (!finite16(d.camera_view) || !finite16(d.camera_proj) || !finite16(d.light_view) || !finite16(d.light_proj))
+        return fail(RVH_ERR_INVALID_ARG, "shade: non-finite matrix");
+    return RVH_OK;
+}
+
+Cam make_cam(const rvh_shade_desc& d) {
+    Cam K;
+    mat_mul(d.light_proj, d.light_view, K.lvp);
+    eye_of(d.camera_view, K.cam_pos);
+    eye_of(d.light_view, K.light_pos);
+    return K;
+}
+
+int grid_for(long long n, int sms) {
+    const long long b = (n + kShadeThreads - 1) / kShadeThreads;
+    return (int)std::max(1LL, std::min(b, (long long)sms * 8));
+}
+
+bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
+}  // namespace
+}  // namespace rvh
+
+using namespace rvh;
+
+extern "C" {
+
+rvh_status rvh_shade_desc_reference(rvh_shade_desc* d) {
+    if (!d) return fail(RVH_ERR_INVALID_ARG, "shade_desc_reference: NULL");
+    std::memset(d, 0, sizeof(*d));
+    const float aspect = 1080.f / 720.f;                          // src/main.cpp:162-163,188-189
+    const H3 up{0.0f, 1.0f, 0.0f}, ctr{0.0f, 1.0f, 0.0f};
+    look_at(H3{0.0f, 1.f, 10.f}, ctr, up, d->camera_view);        // src/Camera.cpp:9-15
+    perspective_flipped(45.0f, aspect, 0.1f, 50.0f, d->camera_proj);
+    const H3 nrm = h_norm(H3{2.f - 0.f, 0.f - 1.f, 1.f - 0.f});  // src/Camera.cpp:28-32
+    look_at(H3{6.5f * nrm.x, 6.5f * nrm.y, 6.5f * nrm.z}, ctr, up, d->light_view);
+    perspective_flipped(60.0f, aspect, 1.f, 10.f, d->light_proj);
+    d->map_width = 1080;                                          // SHADOWMAP_WIDTH x HEIGHT, src/Renderer.cpp:9-10
+    d->map_height = 720;
+    return RVH_OK;
+}
+
+rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, const void* depth_map,
+                               const void* opacity_map, int32_t map_width, int32_t map_height, void* colors,
+                               void* stream) {
+    if (!ctx || n < 0) return fail(RVH_ERR_INVALID_ARG, "shade_fragments: NULL context or negative count");
+    if (map_width < 1 || map_height < 1) return fail(RVH_ERR_INVALID_ARG, "shade_fragments: bad map size");
+    if (n == 0) return RVH_OK;
+    if (!inputs || !depth_map || !opacity_map || !colors)
+        return fail(RVH_ERR_INVALID_ARG, "shade_fragments: NULL buffer");
+    if (!aligned16(opacity_map) || !aligned16(colors) || !aligned16(inputs))
+        return fail(RVH_ERR_INVALID_ARG, "shade_fragments: inputs, opacity map and colors must be 16-byte aligned");
+    if (n >= (int64_t(1) << 31)) return fail(RVH_ERR_INVALID_ARG, "shade_fragments: fewer than 2^31 fragments");
+    RVH_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), map_width, map_height};
+    k_shade_fragments<<<grid_for(n, ctx->sm_count), kShadeThreads, 0, s>>>((int)n, static_cast<const float*>(inputs), M,
+                                                                              static_cast<float4*>(colors));
+    RVH_CUDA(cudaGetLastError());
+    return RVH_OK;
+}
+
+rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
+                           const void* frames, void* depth_map, void* opacity_map, void* colors, void* stream) {
+    if (!a || !td || !sd) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL argument");
+    rvh_status st = check_desc(*sd);
+    if (st != RVH_OK) return st;
+    if (td->n_lines < 1 || td->n_segments < 1) return fail(RVH_ERR_INVALID_ARG, "asset_shade: bad tessellation levels");
+    if (!depth_map || !opacity_map) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL map");
+    if (a->n_strands > 0 && (!vertices || !frames || !colors)) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL buffer");
+    if (!aligned16(vertices) || !aligned16(frames) || !aligned16(opacity_map) || !aligned16(colors) ||
+        reinterpret_cast<uintptr_t>(depth_map) % 4)
+        return fail(RVH_ERR_INVALID_ARG, "asset_shade: float4 buffers 16-byte aligned, the depth map 4-byte");
+    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->ctx->stream;
+    const Cam K = make_cam(*sd);
+    const int w = sd->map_width, h = sd->map_height;
+    const long long texels = (long long)w * h;
+    const long long nv = (long long)a->n_strands * td->n_lines * (td->n_segments + 1);
+    const int sms = a->ctx->sm_count;
+    auto* depth_bits = static_cast<unsigned*>(depth_map);
+    auto* counts = static_cast<uint4*>(opacity_map);   // layer counts in place until the finish pass
+    k_clear_maps<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, depth_bits, counts);
+    if (nv > 0) {
+        const auto* v = static_cast<const float4*>(vertices);
+        k_light_depth<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(v, nv, K, w, h, depth_bits);
+        k_light_opacity<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(v, nv, K, w, h, static_cast<const float*>(depth_map),
+                                                                    counts);
+    }
+    k_opacity_finish<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, counts);
+    if (nv > 0) {
+        const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), w, h};
+        k_shade_vertices<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(
+            static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_strands, a->n_points,
+            td->n_lines, td->n_segments, K, M, static_cast<float4*>(colors));
+    }
+    RVH_CUDA(cudaGetLastError());
+    return RVH_OK;
+}
+
+rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* vertices, const void* colors,
+                            const rvh_shade_desc* sd, int32_t width, int32_t height, void* image, void* stream) {
+    if (!ctx || !sd || n_vertices < 0) return fail(RVH_ERR_INVALID_ARG, "render_image: NULL argument");
+    if (width < 1 || height < 1 || width > 16384 || height > 16384)
+        return fail(RVH_ERR_INVALID_ARG, "render_image: size must be in [1, 16384]");
+    if (!finite16(sd->camera_view) || !finite16(sd->camera_proj))
+        return fail(RVH_ERR_INVALID_ARG, "render_image: non-finite matrix");
+    if (!image || (n_vertices > 0 && (!vertices || !colors))) return fail(RVH_ERR_INVALID_ARG, "render_image: NULL buffer");
+    if (!aligned16(image) || !aligned16(vertices) || !aligned16(colors))
+        return fail(RVH_ERR_INVALID_ARG, "render_image: buffers must be 16-byte aligned");
+    if (n_vertices > 0xffffffffLL) return fail(RVH_ERR_INVALID_ARG, "render_image: at most 2^32 - 1 vertices");
+    RVH_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    float vp[16];
+    mat_mul(sd->camera_proj, sd->camera_view, vp);
+    Proj P;
+    std::memcpy(P.m, vp, sizeof vp);
+    const long long px = (long long)width * height;
+    auto* img = static_cast<float4*>(image);
+    k_image_clear<<<grid_for(px, ctx->sm_count), kShadeThreads, 0, s>>>(px, img);
+    if (n_vertices > 0)
+        k_image_depth<<<grid_for(n_vertices, ctx->sm_count), kShadeThreads, 0, s>>>(
+            static_cast<const float4*>(vertices), n_vertices, P, width, height, img);
+    k_image_resolve<<<grid_for(px, ctx->sm_count), kShadeThreads, 0, s>>>(px, static_cast<const float4*>(colors), img);
+    RVH_CUDA(cudaGetLastError());
+    return RVH_OK;
+}
+
+}  // extern "C"

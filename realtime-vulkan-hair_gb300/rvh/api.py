@@ -216,6 +216,18 @@ class Asset:
         check(self.lib.rvh_asset_tessellate(self.h, C.byref(d), C.c_void_p(vertices_ptr),
                                             C.c_void_p(frames_ptr) if frames_ptr else None, stream))
 
+    def shade(self, vertices_ptr, frames_ptr, depth_ptr, opacity_ptr, colors_ptr, tess_desc=None, shade_desc=None,
+              stream=None):
+        """The shadow, opacity and hair passes over this asset's tessellation
+        (vertices and frames from tessellate() with the same tess_desc): writes
+        the light depth map (map_height x map_width floats), the opacity map
+        (the same count of float4) and one float4 colour per vertex."""
+        td = tess_desc if tess_desc is not None else tess_desc_reference()
+        sd = shade_desc if shade_desc is not None else shade_desc_reference()
+        check(self.lib.rvh_asset_shade(self.h, C.byref(td), C.byref(sd), C.c_void_p(vertices_ptr),
+                                       C.c_void_p(frames_ptr), C.c_void_p(depth_ptr), C.c_void_p(opacity_ptr),
+                                       C.c_void_p(colors_ptr), stream))
+
     def read(self):
         out = np.empty((self.n_strands, 3 * self.n_points, 4), np.float32)
         check(self.lib.rvh_asset_read(self.h, out.ctypes.data_as(C.c_void_p), out.nbytes))
@@ -450,6 +462,35 @@ def tess_desc_reference(**kw):
     for k, v in kw.items():
         setattr(d, k, v)
     return d
+
+
+# ---- hair shading -----------------------------------------------------------------
+class ShadeDesc(C.Structure):
+    _fields_ = [("camera_view", C.c_float * 16), ("camera_proj", C.c_float * 16), ("light_view", C.c_float * 16),
+                ("light_proj", C.c_float * 16), ("map_width", C.c_int32), ("map_height", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
+
+
+def shade_desc_reference(**kw):
+    d = ShadeDesc()
+    check(load().rvh_shade_desc_reference(C.byref(d)))
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+def shade_fragments(ctx, n, inputs_ptr, depth_ptr, opacity_ptr, map_width, map_height, colors_ptr, stream=None):
+    """hair.frag for n fragments: inputs n x 24 floats, maps as rvh_asset_shade
+    writes them, colors n float4 (all device pointers)."""
+    check(load().rvh_shade_fragments(ctx.h, n, C.c_void_p(inputs_ptr), C.c_void_p(depth_ptr),
+                                     C.c_void_p(opacity_ptr), map_width, map_height, C.c_void_p(colors_ptr), stream))
+
+
+def render_image(ctx, n_vertices, vertices_ptr, colors_ptr, width, height, image_ptr, shade_desc=None, stream=None):
+    """Nearest-vertex camera image (height x width float4) of shaded vertices."""
+    sd = shade_desc if shade_desc is not None else shade_desc_reference()
+    check(load().rvh_render_image(ctx.h, n_vertices, C.c_void_p(vertices_ptr), C.c_void_p(colors_ptr), C.byref(sd),
+                                  width, height, C.c_void_p(image_ptr), stream))
 
 
 # ---- scalp meshes and root sampling ----------------------------------------------

@@ -1,0 +1,231 @@
+"""Hair shading: the shadow, opacity and hair passes (src/Renderer.cpp,
+src/shaders/hairOpacity.frag, src/shaders/hair.frag).
+
+CPU: the oracle's restatement against the reference's own fragment shaders,
+compiled as C++ with its glm (tests/golden/shade_ref_head.npz, made by
+tests/golden/make_shade_golden.py; and live where the reference checkout
+exists), bit for bit; the library's reference cameras against glm's.
+GPU: rvh_shade_fragments against the reference's outputs, and
+rvh_asset_shade / rvh_render_image against the oracle: the light depth and
+opacity maps and the camera image's depth test bit for bit, the colours within
+COLOR_TOL — the only difference is CUDA's acos, sin, cos, exp and pow against
+the C library's (a few float ulps each; the brightness hash uses a correctly
+rounded sin on both sides).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from rvh import api
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+COLOR_TOL = 1e-4   # absolute, per colour channel in [0, 1]
+
+
+def _fixture():
+    return np.load(os.path.join(GOLDEN, "shade_ref_head.npz"))
+
+
+def _same_bits(a, b):
+    return np.array_equal(np.ascontiguousarray(a, np.float32).view(np.uint32),
+                          np.ascontiguousarray(b, np.float32).view(np.uint32))
+
+
+class _Desc:
+    def __init__(self, cams, w, h):
+        self.camera_view, self.camera_proj, self.light_view, self.light_proj = [list(c) for c in cams]
+        self.map_width, self.map_height = w, h
+
+
+def test_oracle_matches_reference_fragment_shader_golden(oracle):
+    g = _fixture()
+    out = oracle.shade_fragments(g["inputs"], g["depth"], g["opacity"], sin_mode=0)
+    assert _same_bits(out, g["rgba"])
+    # the fixture covers lit and shadowed fragments, all layers the head reaches and the clipped ones
+    assert (g["rgba"][:, :3].std(0) > 0.01).all()
+
+
+def test_oracle_matches_reference_opacity_shader_golden(oracle):
+    g = _fixture()
+    out = oracle.opacity_fragments(g["inputs"], g["depth"])
+    assert _same_bits(out, g["layers"])
+    assert (g["layers"][:, 0] > 0).any() and (g["layers"][:, 2] > 0).any() and (g["layers"][:, 2] == 0).any()
+
+
+def test_correctly_rounded_hash_agrees_on_the_reference_isolines(oracle):
+    g = _fixture()
+    out = oracle.shade_fragments(g["inputs"], g["depth"], g["opacity"], sin_mode=1)
+    assert _same_bits(out, g["rgba"])
+
+
+def test_reference_cameras_match_glm(librvh):
+    g = _fixture()
+    d = api.shade_desc_reference()
+    for k, name in enumerate(("camera_view", "camera_proj", "light_view", "light_proj")):
+        assert _same_bits(np.array(list(getattr(d, name)), np.float32), g["cameras"][k]), name
+    assert (d.map_width, d.map_height) == (1080, 720)
+
+
+def test_oracle_maps_properties(oracle):
+    g = _fixture()
+    depth, layers = g["depth"], g["opacity"][..., :3]
+    assert ((depth > 0) & (depth <= 1)).all()
+    allowed = np.array([0, 77, 154, 231, 255], np.float32) / np.float32(255)
+    assert np.isin(layers, allowed).all()
+    assert (layers[..., 0] <= layers[..., 1]).all() and (layers[..., 1] <= layers[..., 2]).all()
+    assert (g["opacity"][..., 3] == 0).all()
+
+
+def test_oracle_image_keeps_the_nearest_vertex(oracle):
+    desc = _Desc(_fixture()["cameras"], 64, 48)
+    verts = np.array([[0.0, 1.0, 0.0, 1], [0.0, 1.0, 0.5, 1], [0.0, 1.0, -0.5, 1], [50.0, 1.0, 0.0, 1]], np.float32)
+    colors = np.array([[1, 0, 0, 1], [0, 1, 0, 1], [0, 0, 1, 1], [1, 1, 1, 1]], np.float32)
+    img = oracle.render_image(verts, colors, desc, 64, 48)
+    lit = img.reshape(-1, 4)[(img.reshape(-1, 4) != 0).any(1)]
+    assert lit.shape[0] == 1 and np.array_equal(lit[0], colors[1])   # the one nearest the camera at z = 10
+
+
+def test_oracle_matches_reference_shaders_live(oracle):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_shade_golden as mk
+    lib = mk.reference_lib()
+    if lib is None:
+        pytest.skip("reference checkout not present")
+    cams = mk.ref_cameras(lib)
+    rec = np.ascontiguousarray(np.load(os.path.join(GOLDEN, "ref_head.npz"))["state_10"], np.float32)
+    verts, frames = oracle.tessellate(rec, 10, 12, 42, sin_mode=0, frames=True)
+    desc = _Desc(cams, 540, 360)
+    depth, opacity = oracle.shade_maps(verts, desc)
+    inputs = oracle.shade_vertex_inputs(verts, frames, 10, 12, 42, desc)[::3]
+    assert _same_bits(oracle.shade_fragments(inputs, depth, opacity, sin_mode=0), mk.ref_shade(lib, inputs, depth,
+                                                                                              opacity))
+    assert _same_bits(oracle.opacity_fragments(inputs, depth), mk.ref_opacity(lib, inputs, depth))
+
+
+# ---- GPU ----------------------------------------------------------------------------
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def _colors_close(got, want):
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(got), nan)
+    err = np.abs(got - want)[~nan]
+    print("colour max |diff| %.3g" % (err.max() if err.size else 0.0))
+    assert err.size == 0 or err.max() <= COLOR_TOL
+
+
+@pytest.mark.gpu
+def test_gpu_fragments_match_reference_golden(gpu_ctx, oracle):
+    import torch
+    g = _fixture()
+    inp, dep, opa = _dev(g["inputs"]), _dev(g["depth"]), _dev(g["opacity"])
+    n = g["inputs"].shape[0]
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    h, w = g["depth"].shape
+    api.shade_fragments(gpu_ctx, n, inp.data_ptr(), dep.data_ptr(), opa.data_ptr(), w, h, out.data_ptr())
+    gpu_ctx.synchronize()
+    got = out.cpu().numpy()
+    _colors_close(got, g["rgba"])
+    assert (got[:, 3] == 0.75).all()
+
+
+def _shade_on_gpu(ctx, a, ns, n, td, sd):
+    import torch
+    per = td.n_lines * (td.n_segments + 1)
+    vert = torch.zeros((ns * per * 4,), dtype=torch.float32, device="cuda")
+    fr = torch.zeros((ns * (n - 1) * 12,), dtype=torch.float32, device="cuda")
+    texels = sd.map_width * sd.map_height
+    depth = torch.full((texels,), -7.0, dtype=torch.float32, device="cuda")    # every texel is written
+    opac = torch.full((texels * 4,), -7.0, dtype=torch.float32, device="cuda")
+    col = torch.zeros((ns * per * 4,), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    a.tessellate(vert.data_ptr(), fr.data_ptr(), desc=td)
+    a.shade(vert.data_ptr(), fr.data_ptr(), depth.data_ptr(), opac.data_ptr(), col.data_ptr(), tess_desc=td,
+            shade_desc=sd)
+    ctx.synchronize()
+    return (vert.cpu().numpy().reshape(ns, td.n_lines, td.n_segments + 1, 4),
+            fr.cpu().numpy().reshape(ns, n - 1, 3, 4),
+            depth.cpu().numpy().reshape(sd.map_height, sd.map_width),
+            opac.cpu().numpy().reshape(sd.map_height, sd.map_width, 4),
+            col.cpu().numpy().reshape(-1, 4), (vert, col))
+
+
+def _head(ctx, seed, n, ns=400):
+    rec, rest, p, cols = api.generate_head(seed=seed, n_strands=ns, n_points=n, root_sampling=0, sort_roots=1,
+                                           length_min=0.3, length_max=0.9, head_collider=1, n_ellipsoids=1,
+                                           axis_min=0.2, axis_max=0.4, grid_res=0, friction=0.0, repulsion=0.0,
+                                           dftl_damping=0.9)
+    a = api.Asset(ctx, rec, n, rest=rest)
+    a.set_params(p)
+    a.set_colliders(cols)
+    for k in range(3):
+        a.step(api.T.frame(np.float32(1.0 / 60.0), np.float32((k + 1) / 60.0)))
+    return a, rec.shape[0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,lines,segs,mw,mh", [(10, 12, 42, 1080, 720), (16, 5, 17, 270, 180), (32, 8, 64, 333, 97)])
+def test_gpu_asset_shade_matches_oracle(gpu_ctx, oracle, n, lines, segs, mw, mh):
+    a, ns = _head(gpu_ctx, seed=n + lines, n=n)
+    td = api.tess_desc_reference(n_lines=lines, n_segments=segs)
+    sd = api.shade_desc_reference(map_width=mw, map_height=mh)
+    verts, frames, depth, opac, col, _ = _shade_on_gpu(gpu_ctx, a, ns, n, td, sd)
+    want_depth, want_opac = oracle.shade_maps(verts, sd)
+    assert _same_bits(depth, want_depth)
+    assert _same_bits(opac, want_opac)
+    assert (depth < 1).sum() > 100 and (opac[..., 0] > 0).sum() > 100
+    inputs = oracle.shade_vertex_inputs(verts, frames, n, lines, segs, sd)
+    want = oracle.shade_fragments(inputs, want_depth, want_opac, sin_mode=1)
+    _colors_close(col, want)
+    a.close()
+
+
+@pytest.mark.gpu
+def test_gpu_render_image_matches_oracle(gpu_ctx, oracle):
+    import torch
+    a, ns = _head(gpu_ctx, seed=3, n=10)
+    td, sd = api.tess_desc_reference(), api.shade_desc_reference()
+    verts, _, _, _, col, (vert_d, col_d) = _shade_on_gpu(gpu_ctx, a, ns, 10, td, sd)
+    w, h = 1080, 720
+    img = torch.full((w * h * 4,), -7.0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    nv = verts.reshape(-1, 4).shape[0]
+    api.render_image(gpu_ctx, nv, vert_d.data_ptr(), col_d.data_ptr(), w, h, img.data_ptr(), shade_desc=sd)
+    gpu_ctx.synchronize()
+    got = img.cpu().numpy().reshape(h, w, 4)
+    want = oracle.render_image(verts, col, sd, w, h)
+    assert _same_bits(got, want)
+    assert (got[..., 3] == 0.75).sum() > 1000
+    a.close()
+
+
+@pytest.mark.gpu
+def test_gpu_shade_rejects_bad_arguments(gpu_ctx):
+    """Every call below fails its argument checks before any launch; the buffer
+    is large enough for what a launch with those arguments would touch."""
+    import torch
+    from rvh._lib import RvhError
+    a, ns = _head(gpu_ctx, seed=1, n=8, ns=8)
+    buf = torch.zeros((400 << 20) // 4, dtype=torch.float32, device="cuda")
+    p = buf.data_ptr()
+    for kw in ({"map_width": 0}, {"map_height": 20000}):
+        with pytest.raises(RvhError):
+            a.shade(p, p, p, p, p, shade_desc=api.shade_desc_reference(**kw))
+    sd = api.shade_desc_reference()
+    sd.light_view[3] = float("nan")
+    with pytest.raises(RvhError):
+        a.shade(p, p, p, p, p, shade_desc=sd)
+    with pytest.raises(RvhError):   # misaligned colour buffer
+        a.shade(p, p, p, p, p + 4)
+    with pytest.raises(RvhError):
+        api.render_image(gpu_ctx, 10, p, p, 0, 10, p)
+    torch.cuda.synchronize()
+    a.close()
