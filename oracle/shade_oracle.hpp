@@ -13,7 +13,7 @@
  *     [z0, z0 + d), to layers 2 and 3 in [z0 + d, z0 + 2d), to layer 3 beyond
  *     (d = 0.3, hairOpacity.frag:42-59).  The target is the swapchain's
  *     B8G8R8A8_UNORM (Renderer.cpp:1939-1951) with ONE + ONE additive blending
- *     (Renderer.cpp:1475-1484): 0.3 is stored as 77/255 and the sum saturates,
+ *     (Renderer.cpp:1471-1480): 0.3 is stored as 77/255 and the sum saturates,
  *     so a layer that received c fragments reads min(255, 77 c) / 255;
  *  3. camera pass (src/shaders/hair.frag): per fragment a Marschner-style
  *     single-scattering lobe, a multiple-scattering term damped by the opacity

@@ -83,14 +83,24 @@ __device__ __forceinline__ float directional_angle(V3 v1, V3 v2, V3 n) {
     if (vec3_compare(nrm3(cross3(v2, v1)), n)) return angle;
     return (2.0f * kPi) - angle;
 }
-__device__ __forceinline__ float gaussian(float alpha, float beta, float ti, float to) {
-    const float e = sinf(ti * kDegToRad) + sinf(to * kDegToRad) - alpha;
-    return (1.f / (beta * sqrtf(2.f * kPi))) * expf(-powf(e, 2.0f) / (2.f * beta * beta));
+// gaussian(alpha, beta, theta_i, theta_o) with sin_i = sin(theta_i DEG_TO_RAD),
+// sin_o = sin(theta_o DEG_TO_RAD) computed once for the three lobes;
+// pow(e, 2) is e * e (the correctly rounded square)
+__device__ __forceinline__ float gaussian(float alpha, float beta, float sin_i, float sin_o) {
+    const float e = sin_i + sin_o - alpha;
+    return (1.f / (beta * sqrtf(2.f * kPi))) * expf(-(e * e) / (2.f * beta * beta));
 }
+// pow(1 - x, 5) as ((y^2)^2) y
 __device__ __forceinline__ float schlicks(float n, float x) {
     const float R0 = ((1.f - n) * (1.f - n)) / ((1.f + n) * (1.f + n));
-    return R0 + (1.f - R0) * powf(1.f - x, 5.0f);
+    const float y = 1.f - x, y2 = y * y;
+    return R0 + (1.f - R0) * ((y2 * y2) * y);
 }
+// GLSL's pow(x, y) = exp2(y log2(x)) for the constant bases of the hair colour:
+// log2 of midBrown / 255 and of midBrown / 255 / luma, each computed in double
+// from the float base and rounded once.
+constexpr float kLog2C[3] = {-0x1.560d64p+0f, -0x1.eda2b8p+0f, -0x1.799844p+1f};
+constexpr float kLog2CLuma[3] = {0x1.9a7186p-2f, -0x1.87c794p-3f, -0x1.3686c2p+0f};
 // GLSL clamp(x, 0, 1) = min(max(x, 0), 1) with max(a, b) = a < b ? b : a and
 // min(a, b) = b < a ? b : a: a NaN passes through, as in the shader.
 __device__ __forceinline__ float clamp01(float x) {
@@ -129,25 +139,97 @@ struct Maps {
     int w, h;
 };
 
-// PCFshadowCalculation (hair.frag:99-125): the shader's texel size is fixed at 1/1080 x 1/720
-__device__ float pcf_shadow(const Maps& M, float px, float py, float pz, float pw) {
+// PCFshadowCalculation (hair.frag:99-125): the shader's texel size is fixed at
+// 1/1080 x 1/720.  Each of the 7 x 7 taps is a bilinear sample at (u + dx ts_x,
+// v + dy ts_y); when the taps' texel columns are 7 consecutive integers and so
+// are their rows (the usual case: a tap step is one texel of a 1080 x 720 map),
+// the taps share one 8 x 8 window of texels, loaded once (64 loads instead of
+// 196) and walked two rows at a time; every tap's arithmetic is unchanged.
+// center receives the (0, 0) tap (= the shader's z0 sample) when computed.
+__device__ __forceinline__ float tap_coord(float c, int size, int& i) {
+    const float x = c * (float)size - 0.5f;
+    const float x0 = floorf(x);
+    i = (int)fminf(fmaxf(x0, -1.f), (float)size);
+    return x - x0;
+}
+
+__device__ __forceinline__ float bilerp(float t00, float t10, float t01, float t11, float fx, float fy) {
+    const float a = t00 + fx * (t10 - t00);
+    const float b = t01 + fx * (t11 - t01);
+    return a + fy * (b - a);
+}
+
+__device__ float pcf_shadow(const Maps& M, float px, float py, float pz, float pw, float& center, bool& has_center) {
+    has_center = false;
     const float x = px / pw, y = py / pw, z = pz / pw;
     if (fabsf(x) > 1.f || fabsf(y) > 1.f || fabsf(z) > 1.f) return 0.f;
     const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
     const float tsx = 1.f / 1080.0f, tsy = 1.f / 720.0f;
+    // the taps' texel columns and rows: consecutive from the first?
+    float fx[7];
+    int ix0, iy0;
+    fx[0] = tap_coord(u + (float)(-3) * tsx, M.w, ix0);
+    (void)tap_coord(v + (float)(-3) * tsy, M.h, iy0);
+    bool window = true;
+#pragma unroll
+    for (int d = 1; d < 7; ++d) {
+        int i, j;
+        fx[d] = tap_coord(u + (float)(d - 3) * tsx, M.w, i);
+        (void)tap_coord(v + (float)(d - 3) * tsy, M.h, j);
+        window = window && i == ix0 + d && j == iy0 + d;
+    }
     float lighted = 0.f;
-    for (int dx = -3; dx <= 3; ++dx)
-        for (int dy = -3; dy <= 3; ++dy) {
-            const float cu = u + (float)dx * tsx, cv = v + (float)dy * tsy;
-            if (z > tex_sample(M.depth, M.w, M.h, 1, cu, cv, 0)) lighted += 1.f;
+    if (window) {
+        // h[dx] = the horizontal lerp a = t00 + fx (t10 - t00) of row r for tap
+        // column dx; tap (dx, dy) is hprev[dx] + fy (hcur[dx] - hprev[dx]) with
+        // rows iy0 + dy and iy0 + dy + 1, the same operands as the shader's
+        // sample, so each row's lerps serve two rows of taps
+        int col[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) col[c] = min(max(ix0 + c, 0), M.w - 1);
+        float hprev[7];
+        {
+            const float* row = M.depth + (size_t)min(max(iy0, 0), M.h - 1) * M.w;
+            float t[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) t[c] = __ldg(row + col[c]);
+#pragma unroll
+            for (int dx = 0; dx < 7; ++dx) hprev[dx] = t[dx] + fx[dx] * (t[dx + 1] - t[dx]);
         }
+#pragma unroll 1
+        for (int dy = 0; dy < 7; ++dy) {
+            int iy;
+            const float fy = tap_coord(v + (float)(dy - 3) * tsy, M.h, iy);
+            const float* row = M.depth + (size_t)min(max(iy0 + dy + 1, 0), M.h - 1) * M.w;
+            float t[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) t[c] = __ldg(row + col[c]);
+#pragma unroll
+            for (int dx = 0; dx < 7; ++dx) {
+                const float hcur = t[dx] + fx[dx] * (t[dx + 1] - t[dx]);
+                const float tap = hprev[dx] + fy * (hcur - hprev[dx]);
+                if (z > tap) lighted += 1.f;
+                if (dx == 3 && dy == 3) center = tap;
+                hprev[dx] = hcur;
+            }
+        }
+        has_center = true;
+    } else {
+        for (int dx = -3; dx <= 3; ++dx)
+            for (int dy = -3; dy <= 3; ++dy) {
+                const float cu = u + (float)dx * tsx, cv = v + (float)dy * tsy;
+                if (z > tex_sample(M.depth, M.w, M.h, 1, cu, cv, 0)) lighted += 1.f;
+            }
+    }
     const float kernel = 2.f * 3 + 1.f;
     return lighted / (kernel * kernel);
 }
 
 // hair.frag main (:130-261) for one fragment.  in: uv (2), u, v, w (3 each),
 // viewDir (3), lightDir (3), fragPosLightSpace (4).
-__device__ float4 shade_fragment(const float* in, const Maps& M) {
+// bright: the brightness factor 0.8 |random(uv.x, uv.x)| + 0.6 when the caller
+// has it (a per-isoline table), else negative and computed here.
+__device__ float4 shade_fragment(const float* in, const Maps& M, float bright) {
     const float uv_x = in[0], uv_y = in[1];
     const V3 fu = mk(in[2], in[3], in[4]), fv = mk(in[5], in[6], in[7]);
     const V3 view = mk(in[11], in[12], in[13]), light = mk(in[14], in[15], in[16]);
@@ -166,9 +248,10 @@ __device__ float4 shade_fragment(const float* in, const Maps& M) {
     const float phi_d = phi_o - phi_i;
     const float alpha_R = -2.f * shift, alpha_TT = shift, alpha_TRT = 4.f * shift;
     const float beta_R = roughness * roughness, beta_TT = 0.5f * beta_R, beta_TRT = 2.f * beta_R;
-    const float M_R = gaussian(alpha_R, beta_R, theta_i, theta_o);
-    const float M_TT = gaussian(alpha_TT, beta_TT, theta_i, theta_o);
-    const float M_TRT = gaussian(alpha_TRT, beta_TRT, theta_i, theta_o);
+    const float sin_i = sinf(theta_i * kDegToRad), sin_o = sinf(theta_o * kDegToRad);
+    const float M_R = gaussian(alpha_R, beta_R, sin_i, sin_o);
+    const float M_TT = gaussian(alpha_TT, beta_TT, sin_i, sin_o);
+    const float M_TRT = gaussian(alpha_TRT, beta_TRT, sin_i, sin_o);
     const float cosTheta_d = cosf(theta_d * kDegToRad);
     const float cosPhi_d = cosf(phi_d * kDegToRad);
     const float cosPhi_dOver2 = cosf((phi_d / 2.f) * kDegToRad);
@@ -179,28 +262,30 @@ __device__ float4 shade_fragment(const float* in, const Maps& M) {
     const float h_TT = (1.f + a * (0.6f - 0.8f * cosPhi_d)) * cosPhi_dOver2;
     const float f_TT = schlicks(n, cosTheta_d * sqrtf(1.f - h_TT * h_TT));
     const float Cpower_TT = sqrtf(1.f - h_TT * h_TT * a * a) / (2.f * cosTheta_d);
-    const V3 T_TT = mk(powf(C.x, Cpower_TT), powf(C.y, Cpower_TT), powf(C.z, Cpower_TT));
+    const V3 T_TT = mk(exp2f(Cpower_TT * kLog2C[0]), exp2f(Cpower_TT * kLog2C[1]), exp2f(Cpower_TT * kLog2C[2]));
     const V3 A_TT = (1.f - f_TT) * (1.f - f_TT) * T_TT;
     const float D_TT = expf(-3.65f * cosPhi_d - 3.98f);
     const V3 N_TT = A_TT * D_TT;
     const V3 N_TRT = A_TT * D_TT;   // the shader reuses the TT lobe here (hair.frag:236)
     const V3 S_single = (1.3f * N_R * M_R + 0.5f * N_TT * M_TT + N_TRT * M_TRT) / (cosTheta_d * cosTheta_d);
-    const float shadow = pcf_shadow(M, px, py, pz, pw);
+    float z0;
+    bool has_z0;
+    const float shadow = pcf_shadow(M, px, py, pz, pw, z0, has_z0);
     const float x = px / pw, y = py / pw, currentDepth = pz / pw;
     const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
-    const float z0 = tex_sample(M.depth, M.w, M.h, 1, u, v, 0);
+    if (!has_z0) z0 = tex_sample(M.depth, M.w, M.h, 1, u, v, 0);
     const float d = 0.3f;
     float opacity = 0.f;
     if (currentDepth >= z0 && currentDepth < z0 + d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 0);
     else if (currentDepth >= z0 + d && currentDepth < z0 + 2.f * d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 1);
     else if (currentDepth >= z0 + 2.f * d) opacity = tex_sample(M.opacity, M.w, M.h, 4, u, v, 2);
     const V3 fakeNormal = nrm3(w_o - fu * dot3(fu, w_o));
-    const float luma = 0.3f;
-    const V3 Cexp = mk(powf(C.x / luma, 1.f - opacity), powf(C.y / luma, 1.f - opacity), powf(C.z / luma, 1.f - opacity));
+    const float oe = 1.f - opacity;
+    const V3 Cexp = mk(exp2f(oe * kLog2CLuma[0]), exp2f(oe * kLog2CLuma[1]), exp2f(oe * kLog2CLuma[2]));
     const V3 sqrtC = mk(sqrtf(C.x), sqrtf(C.y), sqrtf(C.z));
     const V3 S_multi = sqrtC * ((dot3(fakeNormal, w_i) + 1.f) / (4.f * kPi)) * Cexp;
     (void)uv_y;
-    const float bright = 0.8f * fabsf(shade_hash(uv_x, uv_x)) + 0.6f;
+    if (bright < 0.f) bright = 0.8f * fabsf(shade_hash(uv_x, uv_x)) + 0.6f;
     const V3 col = ((S_single + S_multi) * (1.f - shadow) + 0.3f * C) * bright;
     return make_float4(clamp01(col.x), clamp01(col.y), clamp01(col.z), 0.75f);
 }
@@ -208,12 +293,16 @@ __device__ float4 shade_fragment(const float* in, const Maps& M) {
 __global__ void __launch_bounds__(kShadeThreads) k_shade_fragments(int n, const float* __restrict__ in, Maps M,
                                                                    float4* __restrict__ out) {
     for (int i = blockIdx.x * kShadeThreads + threadIdx.x; i < n; i += gridDim.x * kShadeThreads)
-        out[i] = shade_fragment(in + (size_t)i * 24, M);
+        out[i] = shade_fragment(in + (size_t)i * 24, M, -1.f);
 }
 
 // ---- the maps and per-vertex shading from tessellated strands ---------------------------
 struct Proj {
     float m[16];        // column-major projection * view
+};
+constexpr int kMaxLines = 64;
+struct Lines {
+    float bright[kMaxLines];   // 0.8 |random(u, u)| + 0.6 of isoline u = j / n_lines
 };
 struct Cam {
     float lvp[16];      // light proj * light view (column-major)
@@ -247,53 +336,145 @@ __device__ __forceinline__ bool project_texel(const float* m, V3 p, int w, int h
     return true;
 }
 
-// Pass 1: nearest light depth per texel (z in [0, 1]: the bits order like the values).
-__global__ void __launch_bounds__(kShadeThreads) k_light_depth(const float4* __restrict__ verts, long long nv, Cam K,
-                                                               int w, int h, unsigned* __restrict__ depth_bits) {
-    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
-        const float4 q = verts[i];
-        int tx, ty;
-        float z, u, v;
-        if (project_texel(K.lvp, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v))
-            atomicMin(depth_bits + (size_t)ty * w + tx, __float_as_uint(z));
+// Passes 1 and 2 walk the vertices by (strand s, vertex k) over the isolines
+// j: a lane's vertices (s, j, k) for consecutive j are often in one texel (the
+// isolines of a strand clump together near its root), so a lane folds runs of
+// equal texels before its atomic; lanes of a warp read consecutive k of one
+// isoline at a time (coalesced).
+struct VertexWalk {
+    const float4* verts;
+    long long n_columns;   // n_strands * (n_segments + 1)
+    int n_lines, s1;
+};
+__device__ __forceinline__ const float4* column_base(const VertexWalk& W, long long q) {
+    const long long s = q / W.s1;
+    const int k = (int)(q - s * W.s1);
+    return W.verts + s * W.n_lines * W.s1 + k;
+}
+
+constexpr int kChunk = 4;   // vertices of a column loaded together
+
+// Pass 1: nearest light depth per texel (z in [0, 1]: the bits order like the
+// values).  A texel's value only decreases, so a flush whose minimum is not
+// below the value it reads has nothing to do and skips the atomic.
+__device__ __forceinline__ void flush_min(unsigned* texel, unsigned best) {
+    if (best < *reinterpret_cast<volatile unsigned*>(texel)) atomicMin(texel, best);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_light_depth(VertexWalk W, Cam K, int w, int h,
+                                                               unsigned* __restrict__ depth_bits) {
+    for (long long q = (long long)blockIdx.x * kShadeThreads + threadIdx.x; q < W.n_columns;
+         q += (long long)gridDim.x * kShadeThreads) {
+        const float4* v = column_base(W, q);
+        long long cur = -1;
+        unsigned best = 0u;
+        for (int j0 = 0; j0 < W.n_lines; j0 += kChunk) {
+            float4 p[kChunk];
+#pragma unroll
+            for (int c = 0; c < kChunk; ++c)
+                if (j0 + c < W.n_lines) p[c] = __ldg(v + (size_t)(j0 + c) * W.s1);
+#pragma unroll
+            for (int c = 0; c < kChunk; ++c) {
+                if (j0 + c >= W.n_lines) break;
+                int tx, ty;
+                float z, u, vv;
+                if (!project_texel(K.lvp, mk(p[c].x, p[c].y, p[c].z), w, h, tx, ty, z, u, vv)) continue;
+                const long long t = (long long)ty * w + tx;
+                const unsigned bits = __float_as_uint(z);
+                if (t == cur) {
+                    best = min(best, bits);
+                } else {
+                    if (cur >= 0) flush_min(depth_bits + cur, best);
+                    cur = t;
+                    best = bits;
+                }
+            }
+        }
+        if (cur >= 0) flush_min(depth_bits + cur, best);
     }
 }
 
-// Pass 2: fragments per opacity layer (hairOpacity.frag:36-59), counted per texel.
-__global__ void __launch_bounds__(kShadeThreads) k_light_opacity(const float4* __restrict__ verts, long long nv, Cam K,
-                                                                 int w, int h, const float* __restrict__ depth,
+// Pass 2: fragments per opacity layer (hairOpacity.frag:36-59), counted per
+// texel in one 64-bit word: n1, n2, n3 = fragments in [z0, z0 + d), [z0 + d,
+// z0 + 2d), [z0 + 2d, ...) in 21-bit fields.  A layer value saturates at 4
+// fragments (4 x 77 > 255), so a field only needs to reach 4: a flush adds
+// at most 4 per field and skips fields already at 4 or more, which bounds a
+// field by 4 + 4 x (flushes in flight) < 2^21.
+constexpr int kFieldBits = 21;
+constexpr unsigned long long kFieldMask = (1ull << kFieldBits) - 1ull;
+
+__device__ __forceinline__ void add_counts(unsigned long long* word, unsigned n1, unsigned n2, unsigned n3) {
+    const unsigned long long seen = *reinterpret_cast<volatile unsigned long long*>(word);
+    if ((seen & kFieldMask) >= 4u) n1 = 0u;
+    if (((seen >> kFieldBits) & kFieldMask) >= 4u) n2 = 0u;
+    if (((seen >> (2 * kFieldBits)) & kFieldMask) >= 4u) n3 = 0u;
+    const unsigned long long add = (unsigned long long)min(n1, 4u) |
+                                   ((unsigned long long)min(n2, 4u) << kFieldBits) |
+                                   ((unsigned long long)min(n3, 4u) << (2 * kFieldBits));
+    if (add) atomicAdd(word, add);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_light_opacity(VertexWalk W, Cam K, int w, int h,
+                                                                 const float* __restrict__ depth,
                                                                  uint4* __restrict__ counts) {
-    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
-        const float4 q = verts[i];
-        int tx, ty;
-        float z, u, v;
-        if (!project_texel(K.lvp, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v)) continue;
-        const float z0 = tex_sample(depth, w, h, 1, u, v, 0);
-        const float d = 0.3f;
-        unsigned* c = &counts[(size_t)ty * w + tx].x;
-        if (z >= z0 && z < z0 + d) {
-            atomicAdd(c + 0, 1u);
-            atomicAdd(c + 1, 1u);
-            atomicAdd(c + 2, 1u);
-        } else if (z >= z0 + d && z < z0 + 2.f * d) {
-            atomicAdd(c + 1, 1u);
-            atomicAdd(c + 2, 1u);
-        } else if (z >= z0 + 2.f * d) {
-            atomicAdd(c + 2, 1u);
+    auto* words = reinterpret_cast<unsigned long long*>(counts);   // texel t: words[2 t]
+    for (long long q = (long long)blockIdx.x * kShadeThreads + threadIdx.x; q < W.n_columns;
+         q += (long long)gridDim.x * kShadeThreads) {
+        const float4* v = column_base(W, q);
+        long long cur = -1;
+        unsigned n1 = 0u, n2 = 0u, n3 = 0u;
+        for (int j0 = 0; j0 < W.n_lines; j0 += kChunk) {
+            float4 p[kChunk];
+#pragma unroll
+            for (int c = 0; c < kChunk; ++c)
+                if (j0 + c < W.n_lines) p[c] = __ldg(v + (size_t)(j0 + c) * W.s1);
+            long long t[kChunk];
+            float z[kChunk], z0[kChunk];
+#pragma unroll
+            for (int c = 0; c < kChunk; ++c) {
+                t[c] = -1;
+                int tx, ty;
+                float u, vv;
+                if (j0 + c < W.n_lines && project_texel(K.lvp, mk(p[c].x, p[c].y, p[c].z), w, h, tx, ty, z[c], u, vv)) {
+                    t[c] = (long long)ty * w + tx;
+                    z0[c] = tex_sample(depth, w, h, 1, u, vv, 0);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kChunk; ++c) {
+                if (t[c] < 0) continue;
+                const float d = 0.3f;
+                const int layer = (z[c] >= z0[c] && z[c] < z0[c] + d) ? 1
+                                  : (z[c] >= z0[c] + d && z[c] < z0[c] + 2.f * d) ? 2
+                                  : (z[c] >= z0[c] + 2.f * d) ? 3 : 0;
+                if (layer == 0) continue;
+                if (t[c] != cur) {
+                    if (cur >= 0) add_counts(words + 2 * cur, n1, n2, n3);
+                    cur = t[c];
+                    n1 = n2 = n3 = 0u;
+                }
+                n1 += layer == 1;
+                n2 += layer == 2;
+                n3 += layer == 3;
+            }
         }
+        if (cur >= 0) add_counts(words + 2 * cur, n1, n2, n3);
     }
 }
 
 // Layer counts -> the 8-bit unorm target's additive sum: 0.3 is stored as 77/255
-// and the sum saturates, min(255, 77 c) / 255.  In place: each texel's uint4 of
-// counts becomes its float4 of layers.
+// and the sum saturates, min(255, 77 c) / 255 with c = n1, n1 + n2, n1 + n2 + n3
+// for layers 1, 2, 3.  In place: each texel's count word becomes its float4.
 __device__ __forceinline__ float layer_value(unsigned c) {
-    return (float)(c >= 4u ? 255u : min(255u, 77u * c)) / 255.0f;
+    return (float)(c >= 4u ? 255u : 77u * c) / 255.0f;
 }
 __global__ void __launch_bounds__(kShadeThreads) k_opacity_finish(long long texels, uint4* map) {
     for (long long t = (long long)blockIdx.x * kShadeThreads + threadIdx.x; t < texels; t += (long long)gridDim.x * kShadeThreads) {
-        const uint4 c = map[t];
-        reinterpret_cast<float4*>(map)[t] = make_float4(layer_value(c.x), layer_value(c.y), layer_value(c.z), 0.f);
+        const unsigned long long word = reinterpret_cast<const unsigned long long*>(map)[2 * t];
+        const unsigned n1 = (unsigned)(word & kFieldMask), n2 = (unsigned)((word >> kFieldBits) & kFieldMask);
+        const unsigned n3 = (unsigned)((word >> (2 * kFieldBits)) & kFieldMask);
+        reinterpret_cast<float4*>(map)[t] =
+            make_float4(layer_value(n1), layer_value(n1 + n2), layer_value(n1 + n2 + n3), 0.f);
     }
 }
 
@@ -305,14 +486,14 @@ __global__ void __launch_bounds__(kShadeThreads) k_opacity_finish(long long texe
 __global__ void __launch_bounds__(kShadeThreads) k_shade_vertices(const float4* __restrict__ verts,
                                                                   const float4* __restrict__ frames, int n_strands,
                                                                   int n_points, int n_lines, int n_segments, Cam K,
-                                                                  Maps M, float4* __restrict__ out) {
+                                                                  Maps M, Lines B, float4* __restrict__ out) {
     const int S1 = n_segments + 1;
-    const long long per = (long long)n_lines * S1;
-    const long long nv = per * n_strands;
-    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < nv; i += (long long)gridDim.x * kShadeThreads) {
-        const long long s = i / per;
-        const int r = (int)(i - s * per);
-        const int j = r / S1, k = r - j * S1;
+    const long long nv = (long long)n_lines * S1 * n_strands;   // < 2^32, checked by the caller
+    for (unsigned i = blockIdx.x * kShadeThreads + threadIdx.x; i < (unsigned)nv; i += gridDim.x * kShadeThreads) {
+        const unsigned line = i / (unsigned)S1;                 // s * n_lines + j
+        const int k = (int)(i - line * (unsigned)S1);
+        const unsigned s = line / (unsigned)n_lines;
+        const int j = (int)(line - s * (unsigned)n_lines);
         const float u = (float)j / (float)n_lines, v = (float)k / (float)n_segments;
         const float x = v * (float)(n_points - 1);
         const int sf = min((int)floorf(x), n_points - 2);
@@ -338,7 +519,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_vertices(const float4* 
         in[16] = ld.z;
         mul_point(K.lvp, p, in[17], in[18], in[19], in[20]);
         in[21] = in[22] = in[23] = 0.f;
-        out[i] = shade_fragment(in, M);
+        out[i] = shade_fragment(in, M, B.bright[j]);
     }
 }
 
@@ -369,7 +550,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_image_depth(const float4* __r
         float z, u, v;
         if (!project_texel(P.m, mk(q.x, q.y, q.z), w, h, tx, ty, z, u, v)) continue;
         const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)(unsigned)i;
-        atomicMin(reinterpret_cast<unsigned long long*>(image) + 2 * ((size_t)ty * w + tx), key);
+        unsigned long long* px = reinterpret_cast<unsigned long long*>(image) + 2 * ((size_t)ty * w + tx);
+        if (key < *reinterpret_cast<volatile unsigned long long*>(px)) atomicMin(px, key);   // keys only decrease
     }
 }
 
@@ -465,6 +647,19 @@ int grid_for(long long n, int sms) {
 
 bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
 
+// hair.frag:260's brightness factor per isoline, with the kernel's hash
+// (a correctly rounded sin: the double sin rounded once).
+Lines line_table(int n_lines) {
+    Lines B{};
+    for (int j = 0; j < n_lines; ++j) {
+        const float u = (float)j / (float)n_lines;
+        const float d = u * 12.9898f + u * 78.233f;
+        const float m = (float)std::sin((double)d) * 43758.5453123f;
+        B.bright[j] = 0.8f * std::fabs(m - std::floor(m)) + 0.6f;
+    }
+    return B;
+}
+
 }  // namespace
 }  // namespace rvh
 
@@ -512,7 +707,8 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
     if (!a || !td || !sd) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL argument");
     rvh_status st = check_desc(*sd);
     if (st != RVH_OK) return st;
-    if (td->n_lines < 1 || td->n_segments < 1) return fail(RVH_ERR_INVALID_ARG, "asset_shade: bad tessellation levels");
+    if (td->n_lines < 1 || td->n_lines > kMaxLines || td->n_segments < 1 || td->n_segments > 256)
+        return fail(RVH_ERR_INVALID_ARG, "asset_shade: n_lines must be in [1, 64], n_segments in [1, 256]");
     if (!depth_map || !opacity_map) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL map");
     if (a->n_strands > 0 && (!vertices || !frames || !colors)) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL buffer");
     if (!aligned16(vertices) || !aligned16(frames) || !aligned16(opacity_map) || !aligned16(colors) ||
@@ -524,22 +720,25 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
     const int w = sd->map_width, h = sd->map_height;
     const long long texels = (long long)w * h;
     const long long nv = (long long)a->n_strands * td->n_lines * (td->n_segments + 1);
+    if (nv >= (1LL << 32) - (long long)a->ctx->sm_count * 8 * kShadeThreads)
+        return fail(RVH_ERR_INVALID_ARG, "asset_shade: fewer than 2^32 tessellated vertices per asset");
     const int sms = a->ctx->sm_count;
     auto* depth_bits = static_cast<unsigned*>(depth_map);
     auto* counts = static_cast<uint4*>(opacity_map);   // layer counts in place until the finish pass
     k_clear_maps<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, depth_bits, counts);
     if (nv > 0) {
-        const auto* v = static_cast<const float4*>(vertices);
-        k_light_depth<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(v, nv, K, w, h, depth_bits);
-        k_light_opacity<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(v, nv, K, w, h, static_cast<const float*>(depth_map),
-                                                                    counts);
+        const VertexWalk W{static_cast<const float4*>(vertices), (long long)a->n_strands * (td->n_segments + 1),
+                           td->n_lines, td->n_segments + 1};
+        k_light_depth<<<grid_for(W.n_columns, sms), kShadeThreads, 0, s>>>(W, K, w, h, depth_bits);
+        k_light_opacity<<<grid_for(W.n_columns, sms), kShadeThreads, 0, s>>>(W, K, w, h,
+                                                                             static_cast<const float*>(depth_map), counts);
     }
     k_opacity_finish<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, counts);
     if (nv > 0) {
         const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), w, h};
         k_shade_vertices<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(
             static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_strands, a->n_points,
-            td->n_lines, td->n_segments, K, M, static_cast<float4*>(colors));
+            td->n_lines, td->n_segments, K, M, line_table(td->n_lines), static_cast<float4*>(colors));
     }
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
