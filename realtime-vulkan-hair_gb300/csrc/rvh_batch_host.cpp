@@ -46,6 +46,7 @@ struct Batch {
     int pos_slot = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs;   // recorded, not yet read
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
+    DynBatch* finisher = nullptr;   // one launch of gather-only items for rvh_batch_finish
 };
 
 // Packs the curvePoints of every asset of a batch into one contiguous float4
@@ -206,6 +207,7 @@ void destroy(Batch* b) {
     if (b->ctx) b->ctx->free(b->d_first);
     for (auto& e : b->ev_pairs) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     for (auto& e : b->ev_free) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
+    if (b->finisher) dyn_batch_free(b->finisher);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     for (int i = 0; i < 2; ++i) {
@@ -559,14 +561,27 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
     return RVH_OK;
 }
 
+// Every pending asset's loop 3 in ONE persistent launch of gather-only items
+// (the server's finish mode): the same tile code as the per-asset finish, so
+// the same bits, without a launch sequence per asset.
 rvh_status rvh_batch_finish(rvh_batch* b, void* stream) {
     if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_finish: NULL");
     cudaSetDevice(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
-    for (Asset* a : b->assets) {
-        rvh_status st = finish_pending(a, s);
-        if (st != RVH_OK) return st;
+    std::vector<Asset*> pend;
+    for (Asset* a : b->assets)
+        if (a->pending) pend.push_back(a);
+    if (pend.empty()) return RVH_OK;
+    if (!b->finisher) {
+        rvh_status st;
+        b->finisher = dyn_batch_new(b->ctx, batch_supported(b->lanes) ? b->lanes : 8, &st);
+        if (!b->finisher) return st;
     }
+    std::vector<rvh_frame> frames(pend.size());   // finish mode takes each asset's own dt of that step
+    for (size_t i = 0; i < pend.size(); ++i) frames[i].dt = pend[i]->dt_prev;
+    const std::vector<int> modes(pend.size(), MODE_FINISH);
+    rvh_status st = dyn_batch_launch(b->finisher, pend, frames, modes, s, nullptr, nullptr, nullptr);
+    if (st != RVH_OK) return st;
     return RVH_OK;
 }
 
@@ -581,6 +596,7 @@ rvh_status rvh_batch_check(rvh_batch* b) {
         RVH_CUDA(cudaMemset(b->d_error.ptr, 0, sizeof(int)));
         return fail(err, "batch: a phase-B tile gave up waiting for its asset's phase A");
     }
+    if (b->finisher) return dyn_batch_check(b->finisher);
     return RVH_OK;
 }
 

@@ -146,3 +146,59 @@ def test_batch_positions_read_back(gpu_ctx_fast, xyz):
     for p_ in bufs:
         p_.close()
     b.close()
+
+
+class _DeviceArray:
+    """A view of device memory through __cuda_array_interface__ (no copy)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False), "version": 3}
+
+
+def _raw_records(asset):
+    """The asset's device records as they are: no finish on the way (rvh_asset_device_ptr)."""
+    import torch
+    torch.cuda.synchronize()
+    n = asset.n_strands * 3 * asset.n_points * 4
+    t = torch.as_tensor(_DeviceArray(asset.device_ptr(), n), device="cuda")
+    return t.cpu().numpy().reshape(asset.n_strands, 3 * asset.n_points, 4)
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_batched_finish_equals_plain(gpu_ctx, gpu_ctx_fast, exact):
+    """rvh_batch_finish applies every asset's pending friction in one launch:
+    right after it the device records (read raw, without the finish a read
+    does) equal plain steps bit for bit; more fused steps after it, and a
+    second finish, keep that."""
+    ctx = gpu_ctx if exact else gpu_ctx_fast
+    specs = configs.batched(n_assets=9, scale=0.03, seed=31)
+    plain = make_assets(ctx, specs)
+    batched = make_assets(ctx, specs)
+    b = api.Batch(ctx, batched, lanes=8)
+
+    def advance(k0, k1):
+        for k in range(k0, k1):
+            for a, s in zip(plain, specs):
+                a.step(s.frame(k))
+            b.step([s.frame(k) for s in specs])
+
+    advance(0, 3)
+    ctx.synchronize()
+    before = [_raw_records(c) for c in batched]
+    b.finish()
+    b.check()
+    changed = 0
+    for a, c, old in zip(plain, batched, before):
+        got = _raw_records(c)
+        assert np.array_equal(a.read(), got)
+        changed += not np.array_equal(old, got)
+    assert changed > 0          # the pending friction was applied by the batched finish
+    b.finish()                  # nothing pending: no change
+    advance(3, 5)
+    b.finish()
+    b.check()
+    for a, c in zip(plain, batched):
+        assert np.array_equal(a.read(), _raw_records(c))
+    b.close()
+    for a in plain + batched:
+        a.close()
