@@ -45,7 +45,7 @@ BYTES_PER_CELL = 16         # one clear/flush pass per grid cell-step
 # step on the first 32 heads of the workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over 80 B/point + 16 B/cell); traffic grows with points
 # and cells, so the full launch's traffic is this ratio times its bytes
-TRAFFIC_PER_ALG_BYTE = 994.9 / 833.0
+TRAFFIC_PER_ALG_BYTE = 1001.8 / 833.0
 
 
 def load_peaks():
