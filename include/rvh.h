@@ -218,7 +218,7 @@ rvh_status rvh_shade_desc_reference(rvh_shade_desc* d);
  * each), in_viewDir (3), in_lightDir (3), in_fragPosLightSpace (4), 3 unused
  * (hair.frag:14-20).  depth_map: map_width x map_height floats; opacity_map:
  * the same count of float4 (layers r, g, b).  colors: n float4 (outColor).
- * inputs, opacity_map and colors 16-byte aligned; n < 2^31. */
+ * inputs, opacity_map and colors 16-byte aligned. */
 rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, const void* depth_map,
                                const void* opacity_map, int32_t map_width, int32_t map_height, void* colors,
                                void* stream);

@@ -290,9 +290,9 @@ __device__ float4 shade_fragment(const float* in, const Maps& M, float bright) {
     return make_float4(clamp01(col.x), clamp01(col.y), clamp01(col.z), 0.75f);
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_shade_fragments(int n, const float* __restrict__ in, Maps M,
+__global__ void __launch_bounds__(kShadeThreads) k_shade_fragments(long long n, const float* __restrict__ in, Maps M,
                                                                    float4* __restrict__ out) {
-    for (int i = blockIdx.x * kShadeThreads + threadIdx.x; i < n; i += gridDim.x * kShadeThreads)
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < n; i += (long long)gridDim.x * kShadeThreads)
         out[i] = shade_fragment(in + (size_t)i * 24, M, -1.f);
 }
 
@@ -692,11 +692,10 @@ rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, 
         return fail(RVH_ERR_INVALID_ARG, "shade_fragments: NULL buffer");
     if (!aligned16(opacity_map) || !aligned16(colors) || !aligned16(inputs))
         return fail(RVH_ERR_INVALID_ARG, "shade_fragments: inputs, opacity map and colors must be 16-byte aligned");
-    if (n >= (int64_t(1) << 31)) return fail(RVH_ERR_INVALID_ARG, "shade_fragments: fewer than 2^31 fragments");
     RVH_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), map_width, map_height};
-    k_shade_fragments<<<grid_for(n, ctx->sm_count), kShadeThreads, 0, s>>>((int)n, static_cast<const float*>(inputs), M,
+    k_shade_fragments<<<grid_for(n, ctx->sm_count), kShadeThreads, 0, s>>>((long long)n, static_cast<const float*>(inputs), M,
                                                                               static_cast<float4*>(colors));
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
