@@ -18,9 +18,10 @@
 //   width = mix(rootWidth, tipWidth, v)                              (:324-326)
 //   optional per-segment frames {tangent, Frisvad b1, b2}            (:289-297)
 //
-// A CTA of 256 threads takes 8 strands at a time: their points and Bezier
+// A CTA of 256 threads takes 16 strands at a time: their points and Bezier
 // control points in shared memory, their (strand, isoline) sd profiles, then
-// one thread per output vertex with coalesced float4 stores.
+// one thread per (strand, vertex column): the curve point is evaluated once and
+// offset for every isoline, with coalesced float4 stores.
 //
 // Everything that depends only on (isoline, vertex) — the clump width, the
 // direction, the five sd profiles of v, the strand width — is a table the
@@ -44,7 +45,7 @@ namespace rvh {
 namespace {
 
 constexpr int kTessThreads = 256;
-constexpr int kTessGroup = kTessThreads / RVH_MAX_POINTS;   // strands per CTA iteration (8)
+constexpr int kTessGroup = 16;   // strands per CTA iteration
 constexpr int kMaxLines = 64;
 constexpr int kMaxSegments = 256;
 
@@ -96,17 +97,18 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
     __shared__ int prof[kTessGroup][kMaxLines];
     const int n = A.n_points, L = A.n_lines, S1 = A.n_segments + 1;
     const int per_strand = L * S1;
-    const FastDiv dS1((unsigned)S1), dPer((unsigned)per_strand), dL((unsigned)L);
+    const FastDiv dS1((unsigned)S1), dL((unsigned)L);
     for (int s0 = blockIdx.x * kTessGroup; s0 < A.n_strands; s0 += gridDim.x * kTessGroup) {
         const int ng = min(kTessGroup, A.n_strands - s0);   // strands of this group
-        // the group's points: thread t loads point t % 32 of strand t / 32
-        {
-            const int g = threadIdx.x / RVH_MAX_POINTS, i = threadIdx.x % RVH_MAX_POINTS;
+        // the group's points: slot t holds point t % 32 of strand t / 32
+        for (int t = threadIdx.x; t < kTessGroup * RVH_MAX_POINTS; t += kTessThreads) {
+            const int g = t / RVH_MAX_POINTS, i = t % RVH_MAX_POINTS;
             if (g < ng && i < n) pts[g][i] = xyz(A.strands[(size_t)(s0 + g) * (3 * n) + i]);
         }
         __syncthreads();
-        {   // control points and frame of segment sf (hair.tese:45-66)
-            const int g = threadIdx.x / RVH_MAX_POINTS, sf = threadIdx.x % RVH_MAX_POINTS;
+        for (int t = threadIdx.x; t < kTessGroup * RVH_MAX_POINTS; t += kTessThreads) {
+            // control points and frame of segment sf (hair.tese:45-66)
+            const int g = t / RVH_MAX_POINTS, sf = t % RVH_MAX_POINTS;
             if (g < ng && sf + 1 < n) {
                 const f3 p1 = pts[g][sf], p2 = pts[g][sf + 1];
                 const f3 p0 = sf == 0 ? v_add<EM>(p1, v_sub<EM>(p1, p2)) : pts[g][sf - 1];
@@ -135,10 +137,13 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
             prof[g][j] = p;
         }
         __syncthreads();
+        // the curve point c(v) of (strand, vertex k) is the same for every isoline:
+        // one thread per (strand, k) evaluates it once and writes the strand's
+        // n_lines vertices of column k (consecutive threads: consecutive k of one
+        // isoline row, coalesced)
         float4* out = A.out + (size_t)s0 * per_strand;
-        for (int q = threadIdx.x; q < ng * per_strand; q += kTessThreads) {
-            const int g = (int)dPer.div((unsigned)q), r = q - g * per_strand;
-            const int j = (int)dS1.div((unsigned)r), k = r - j * S1;
+        for (int q = threadIdx.x; q < ng * S1; q += kTessThreads) {
+            const int g = (int)dS1.div((unsigned)q), k = q - g * S1;
             const float v = __ldg(A.T.v + k);
             const float x = EM::mul(v, (float)(n - 1));
             int sf = (int)floorf(x);
@@ -148,10 +153,15 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
             const f3 b01 = e_mix(b0, b1, t), b11 = e_mix(b1, b2, t), b21 = e_mix(b2, b3, t);
             const f3 b02 = e_mix(b01, b11, t), b12 = e_mix(b11, b21, t);
             const f3 c = e_mix(b02, b12, t);
-            const float sd = __ldg(A.T.sd + prof[g][j] * S1 + k);
-            const f3 dir = v_scale<EM>(sd, f3{__ldg(A.T.dir + 3 * j), __ldg(A.T.dir + 3 * j + 1), __ldg(A.T.dir + 3 * j + 2)});
-            const f3 pos = v_add<EM>(c, v_scale<EM>(__ldg(A.T.width + j * S1 + k), dir));
-            out[q] = make_float4(pos.x, pos.y, pos.z, __ldg(A.T.sw + k));
+            const float sw = __ldg(A.T.sw + k);
+            float4* col = out + (size_t)g * per_strand + k;
+            for (int j = 0; j < L; ++j) {
+                const float sd = __ldg(A.T.sd + prof[g][j] * S1 + k);
+                const f3 dir = v_scale<EM>(sd, f3{__ldg(A.T.dir + 3 * j), __ldg(A.T.dir + 3 * j + 1),
+                                                  __ldg(A.T.dir + 3 * j + 2)});
+                const f3 pos = v_add<EM>(c, v_scale<EM>(__ldg(A.T.width + j * S1 + k), dir));
+                col[(size_t)j * S1] = make_float4(pos.x, pos.y, pos.z, sw);
+            }
         }
         __syncthreads();   // pts, cb1/cb2 and prof are rewritten for the next group
     }
