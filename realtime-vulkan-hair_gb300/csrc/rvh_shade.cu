@@ -225,12 +225,12 @@ __device__ float pcf_shadow(const Maps& M, float px, float py, float pz, float p
     return lighted / (kernel * kernel);
 }
 
-// hair.frag main (:130-261) for one fragment.  in: uv (2), u, v, w (3 each),
+// hair.frag main (:133-262) for one fragment.  in: uv (2), u, v, w (3 each),
 // viewDir (3), lightDir (3), fragPosLightSpace (4).
 // bright: the brightness factor 0.8 |random(uv.x, uv.x)| + 0.6 when the caller
 // has it (a per-isoline table), else negative and computed here.
 __device__ float4 shade_fragment(const float* in, const Maps& M, float bright) {
-    const float uv_x = in[0], uv_y = in[1];
+    const float uv_x = in[0];   // in_uv.y only feeds hair.frag's unused colour gradient (:228-232)
     const V3 fu = mk(in[2], in[3], in[4]), fv = mk(in[5], in[6], in[7]);
     const V3 view = mk(in[11], in[12], in[13]), light = mk(in[14], in[15], in[16]);
     const float px = in[17], py = in[18], pz = in[19], pw = in[20];
@@ -284,7 +284,6 @@ __device__ float4 shade_fragment(const float* in, const Maps& M, float bright) {
     const V3 Cexp = mk(exp2f(oe * kLog2CLuma[0]), exp2f(oe * kLog2CLuma[1]), exp2f(oe * kLog2CLuma[2]));
     const V3 sqrtC = mk(sqrtf(C.x), sqrtf(C.y), sqrtf(C.z));
     const V3 S_multi = sqrtC * ((dot3(fakeNormal, w_i) + 1.f) / (4.f * kPi)) * Cexp;
-    (void)uv_y;
     if (bright < 0.f) bright = 0.8f * fabsf(shade_hash(uv_x, uv_x)) + 0.6f;
     const V3 col = ((S_single + S_multi) * (1.f - shadow) + 0.3f * C) * bright;
     return make_float4(clamp01(col.x), clamp01(col.y), clamp01(col.z), 0.75f);
