@@ -254,7 +254,7 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     """The shadow, opacity and hair passes over the tessellated 100k-strand head
     (12 isolines x 42 segments, 51.6 M vertices) with the reference's cameras
     and 1080 x 720 maps: device time of rvh_asset_shade by CUDA events on the
-    launching stream.  Algorithmic bytes: each vertex read by the three passes
+    launching stream; then the rasterised camera image (rvh_asset_render_hair).  Algorithmic bytes: each vertex read by the three passes
     (3 x 16 B), its colour written (16 B), the segment frames read once, and
     the maps cleared, finished and read back once (depth 4 B, layers 16 B per
     texel, three times)."""
@@ -293,6 +293,24 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
     covered = int((depth < 1).sum().item())
+    # the camera image: hair.geom's quads rasterised at the window size, 1080 x 720
+    W, H = 1080, 720
+    image = torch.empty((W * H * 4,), dtype=torch.float32, device="cuda")
+
+    def render():
+        a.render_hair(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), W, H, image.data_ptr(),
+                      tess_desc=td, shade_desc=sd, stream=st.cuda_stream)
+
+    for _ in range(warmup):
+        render()
+    st.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        render()
+    e1.record(st)
+    e1.synchronize()
+    render_ms = e0.elapsed_time(e1) / reps
+    pixels = int((image.view(-1, 4)[:, 3] > 0).sum().item())
     a.close()
     alg = vertices * 64 + ns * (spec.n_points - 1) * 48 + texels * 20 * 3
     peak, _ = load_peaks()
@@ -300,7 +318,10 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments, 1080 x 720 maps",
             "vertices": vertices, "covered_texels": covered, "ms": ms, "vertices_per_s": vertices / (ms * 1e-3),
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                         "bytes_per_launch": alg}}
+                         "bytes_per_launch": alg},
+            "render": {"workload": "hair.geom quads of every isoline segment rasterised into 1080 x 720, "
+                                   "nearest fragment shaded by hair.frag",
+                       "segments": ns * td.n_lines * td.n_segments, "ms": render_ms, "covered_pixels": pixels}}
 
 
 def run_reference(args, rank, world):

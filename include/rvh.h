@@ -235,6 +235,20 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
  * clip volume covers one pixel of a width x height float4 image; the nearest
  * (then the lowest vertex index) wins and the pixel takes its colour; empty
  * pixels are 0.  n_vertices < 2^32. */
+/* The camera image with hair.geom's geometry (src/shaders/hair.geom:41-108 and
+ * the hair pipeline, src/Renderer.cpp:1554-1746): each isoline segment of the
+ * tessellation (vertices and frames from rvh_asset_tessellate with td) becomes
+ * the geometry shader's camera-facing quad of width (|random(3.242551 u, u u)| +
+ * 0.5) * 0.075 * distance * strandWidth, rasterised with a LESS depth test; each
+ * pixel takes hair.frag's colour of its nearest fragment, with perspective-
+ * correct inputs and the maps of rvh_asset_shade (sd's light and map size).
+ * image: width x height float4 (empty pixels 0); fragment_ids (device, nullable):
+ * width x height uint32, the winning segment (s * n_lines + j) * n_segments + k
+ * or 0xffffffff.  Order-dependent alpha blending is left out; quads with a corner
+ * behind the camera or covering more than 65,536 pixels are dropped. */
+rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
+                                 const void* frames, const void* depth_map, const void* opacity_map, int32_t width,
+                                 int32_t height, void* image, void* fragment_ids, void* stream);
 rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* vertices, const void* colors,
                             const rvh_shade_desc* sd, int32_t width, int32_t height, void* image, void* stream);
 

@@ -76,7 +76,7 @@ inline void rev_strand(const double* X, const double* V, double* Xb, double* Vb,
                        const rvh_collider* cols, int ncol, const rvh_sim_params& P, double dt,
                        double& rest_bar, d3& wind_bar) {
     const double k = P.k_penalty, damp = P.damping, s = P.dftl_damping, vmax = P.vmax;
-    d3 x[RVH_MAX_POINTS], pred[RVH_MAX_POINTS], xn[RVH_MAX_POINTS], u[RVH_MAX_POINTS];
+    d3 x[RVH_MAX_POINTS] = {}, pred[RVH_MAX_POINTS], xn[RVH_MAX_POINTS], u[RVH_MAX_POINTS];
     int cnt[RVH_MAX_POINTS];
     for (int i = 0; i < n; ++i) x[i] = mk(X[3 * i], X[3 * i + 1], X[3 * i + 2]);
     xn[0] = x[0];

@@ -146,6 +146,23 @@ int oracle_render_image(const float* verts, const float* colors, long long nv, c
     oracle::shade::render_image(verts, colors, nv, view, proj, w, h, image);
     return 0;
 }
+/* Camera image of hair.geom's quads over a tessellation (shade_oracle.hpp
+ * render_hair): image w x h float4, ids (nullable) w x h uint32. */
+int oracle_render_hair(const float* verts, const float* frames, int ns, int n, int n_lines, int n_segments,
+                       const float* camera_view, const float* camera_proj, const float* light_view,
+                       const float* light_proj, const float* depth, const float* opacity, int mw, int mh, int w, int h,
+                       int sin_mode, float* image, uint32_t* ids) {
+    if (!verts || !frames || !image || !depth || !opacity || ns < 0 || n < 2 || n_lines < 1 || n_segments < 1 ||
+        w < 1 || h < 1 || mw < 1 || mh < 1)
+        return 1;
+    oracle::shade::Raster R;
+    if (!oracle::shade::make_raster(camera_view, camera_proj, light_view, light_proj, w, h, R)) return 2;
+    const oracle::shade::Maps M{depth, opacity, mw, mh};
+    oracle::shade::render_hair(verts, frames, ns, n, n_lines, n_segments, R, M,
+                               sin_mode == 0 ? oracle::shade::RefSin::kFloat : oracle::shade::RefSin::kDouble, image,
+                               ids);
+    return 0;
+}
 /* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */
 int oracle_adjoint_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,
                        const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,

@@ -45,8 +45,10 @@ def lib():
         l.oracle_shade_maps.argtypes = [f4, C.c_longlong, f4, C.c_int, C.c_int, f4, f4]
         l.oracle_shade_vertex_inputs.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4]
         l.oracle_render_image.argtypes = [f4, f4, C.c_longlong, f4, f4, C.c_int, C.c_int, f4]
+        l.oracle_render_hair.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4, f4, f4, C.c_int,
+                                         C.c_int, C.c_int, C.c_int, C.c_int, f4, _P(C.c_uint32)]
         for f in (l.oracle_shade_fragments, l.oracle_shade_camera, l.oracle_opacity_fragments, l.oracle_shade_maps, l.oracle_shade_vertex_inputs,
-                  l.oracle_render_image):
+                  l.oracle_render_image, l.oracle_render_hair):
             f.restype = C.c_int
         l.oracle_run_head_f64.argtypes = [_P(C.c_double)] + common + [_P(C.c_float), _P(C.c_float)]
         l.oracle_run_head_f32.argtypes = [_P(C.c_float)] + common + [_P(C.c_float), _P(C.c_float)]
@@ -313,3 +315,20 @@ def render_image(vertices, colors, desc, width, height):
                                      _fptr(cp, C.c_float), width, height, _fptr(img, C.c_float)),
            "oracle_render_image")
     return img
+
+
+def render_hair(vertices, frames, n_points, n_lines, n_segments, desc, depth, opacity, width, height, sin_mode=1):
+    """hair.geom's quads rasterised into a (height, width, 4) image shaded by
+    hair.frag, and the winning segment id per pixel (0xffffffff: none)."""
+    v, fr = _f32(vertices), _f32(frames)
+    dep, opa = _f32(depth), _f32(opacity)
+    ns = v.shape[0]
+    cv, cp, lv, lp = _mats(desc)
+    img = np.zeros((height, width, 4), np.float32)
+    ids = np.zeros((height, width), np.uint32)
+    mh, mw = dep.shape
+    _check(lib().oracle_render_hair(_fptr(v, C.c_float), _fptr(fr, C.c_float), ns, n_points, n_lines, n_segments,
+                                    *[_fptr(a, C.c_float) for a in (cv, cp, lv, lp, dep, opa)], mw, mh, width, height,
+                                    sin_mode, _fptr(img, C.c_float), ids.ctypes.data_as(_P(C.c_uint32))),
+           "oracle_render_hair")
+    return img, ids

@@ -166,7 +166,12 @@ inline float pcf_shadow(const Maps& M, float px, float py, float pz, float pw) {
  * shader's unused values (the transformed directions, theta_h, phi_h, the
  * colour gradient, gamma_t, the TRT lobe it computes and then replaces by the
  * TT lobe at :222) do not reach the output and are not computed. */
+inline void shade_fragment_bright(const float* in, const Maps& M, float bright, float out[4]);
 inline void shade_fragment(const float* in, const Maps& M, RefSin mode, float out[4]) {
+    shade_fragment_bright(in, M, 0.8f * std::fabs(frag_random(in[0], in[0], mode)) + 0.6f, out);
+}
+/* hair.frag with the brightness factor 0.8 |random(uv.x, uv.x)| + 0.6 given. */
+inline void shade_fragment_bright(const float* in, const Maps& M, float bright, float out[4]) {
     const V3 fu = mk(in[2], in[3], in[4]), fv = mk(in[5], in[6], in[7]);
     const V3 view = mk(in[11], in[12], in[13]), light = mk(in[14], in[15], in[16]);
     const float px = in[17], py = in[18], pz = in[19], pw = in[20];
@@ -218,7 +223,6 @@ inline void shade_fragment(const float* in, const Maps& M, RefSin mode, float ou
                        std::pow(C.z / luma, 1.f - opacity));
     const V3 sqrtC = mk(std::sqrt(C.x), std::sqrt(C.y), std::sqrt(C.z));
     const V3 S_multi = sqrtC * ((dot(fakeNormal, w_i) + 1.f) / (4.f * kPi)) * Cexp;
-    const float bright = 0.8f * std::fabs(frag_random(in[0], in[0], mode)) + 0.6f;
     const V3 col = ((S_single + S_multi) * (1.f - shadow) + 0.3f * C) * bright;
     out[0] = clamp01(col.x);
     out[1] = clamp01(col.y);
@@ -403,6 +407,304 @@ inline void render_image(const float* verts, const float* colors, long long nv, 
             for (int c = 0; c < 4; ++c) image[p * 4 + c] = colors[i * 4 + c];
         }
     }
+}
+
+
+// ---- rasterising hair.geom's quads into a camera image ------------------------------------
+/*
+ * hair.geom (:41-108) turns each isoline segment (tessellated vertices k, k+1 of
+ * isoline j of strand s) into a camera-facing quad: with P = camera proj * view,
+ * c1 = P [pos_k, 1], c2 = P [pos_k+1, 1] and the width
+ *   width1 = (|random(3.242551 u, u u)| + 0.5) * 0.075 * |cameraPos - pos_k| * strandWidth_k
+ * (width2 is computed and unused; every corner uses width1) it emits the strip
+ *   V0 = c1 - (width1, 0, 0, 0), V1 = c1 + (width1, 0, 0, 0), V2 = c2 - ..., V3 = c2 + ...
+ * with vertex k's attributes on V0, V1 and vertex k+1's on V2, V3; the light-space
+ * position of a corner is lightProj * lightView * inverse(view) * inverse(proj) * V.
+ * The hair pipeline rasterises with no culling and a LESS depth test
+ * (src/Renderer.cpp:1640-1664); its alpha blending is order dependent, so the
+ * headless image keeps, per pixel, the nearest fragment's outColor.
+ *
+ * Rasterisation (this restatement's definition of Vulkan's rules):
+ *   screen x = (x/w * 0.5 + 0.5) W, y = (y/w * 0.5 + 0.5) H, depth = z/w; pixel
+ *   centres at (px + 0.5, py + 0.5); triangles (V0, V1, V2) and (V2, V1, V3),
+ *   each reordered to positive area; a centre is covered when every edge
+ *   function is > 0, or = 0 on a top-left edge (dy < 0, or dy = 0 and dx > 0);
+ *   depth interpolated linearly in screen space and kept in [0, 1]; attributes
+ *   interpolated perspective-correctly (barycentrics over w).  Quads with a
+ *   corner at w <= 0 (no near-plane clipping), a non-finite corner or a bounding
+ *   box over 65,536 pixels are dropped.  The nearest fragment wins; ties go to
+ *   the smaller segment id = (s * n_lines + j) * n_segments + k, then to the
+ *   first triangle.  uv.x is constant along an isoline, so the brightness hash
+ *   takes the isoline's own u.
+ */
+struct Raster {
+    float vp[16];      // camera proj * view
+    float lmap[16];    // light proj * light view * inverse(view) * inverse(proj)
+    float cam_pos[3], light_pos[3];
+    int width, height;
+};
+
+inline bool invert4(const double* m, double* inv) {   // column-major, Gauss-Jordan with partial pivoting
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = m[c * 4 + r];
+            a[r][4 + c] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0) return false;
+        for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+        const double d = a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] /= d;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                const double f = a[r][c];
+                for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[c * 4 + r] = a[r][4 + c];
+    return true;
+}
+
+inline void mul4d(const double* a, const double* b, double* o) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k) acc += a[k * 4 + r] * b[c * 4 + k];
+            o[c * 4 + r] = acc;
+        }
+}
+
+inline bool make_raster(const float* cam_view, const float* cam_proj, const float* light_view, const float* light_proj,
+                        int w, int h, Raster& R) {
+    double cv[16], cp[16], lv[16], lp[16], t[16], u[16], icv[16], icp[16], vp[16];
+    for (int k = 0; k < 16; ++k) {
+        cv[k] = cam_view[k];
+        cp[k] = cam_proj[k];
+        lv[k] = light_view[k];
+        lp[k] = light_proj[k];
+    }
+    if (!invert4(cv, icv) || !invert4(cp, icp)) return false;
+    mul4d(cp, cv, vp);
+    mul4d(lp, lv, t);
+    mul4d(t, icv, u);
+    mul4d(u, icp, t);
+    for (int k = 0; k < 16; ++k) {
+        R.vp[k] = float(vp[k]);
+        R.lmap[k] = float(t[k]);
+    }
+    eye_of(cam_view, R.cam_pos);
+    eye_of(light_view, R.light_pos);
+    R.width = w;
+    R.height = h;
+    return true;
+}
+
+inline void mul_vec4(const float* m, const float v[4], float o[4]) {
+    for (int r = 0; r < 4; ++r) o[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3];
+}
+
+struct Quad {
+    float clip[4][4];   // V0..V3 clip positions
+    float sx[4], sy[4], sz[4];
+    int x0, x1, y0, y1; // covered pixel range (inclusive)
+    bool ok;
+};
+
+inline Quad make_quad(const Raster& R, const float* p_k, const float* p_k1, float width_k, float rand_u) {
+    Quad Q;
+    Q.ok = false;
+    const V3 a = mk(p_k[0], p_k[1], p_k[2]), b = mk(p_k1[0], p_k1[1], p_k1[2]);
+    const float dist = length(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - a);
+    const float scale = rand_u * 0.075f * dist;
+    const float w1 = scale * width_k;
+    float c1[4], c2[4];
+    const float pa[4] = {a.x, a.y, a.z, 1.f}, pb[4] = {b.x, b.y, b.z, 1.f};
+    mul_vec4(R.vp, pa, c1);
+    mul_vec4(R.vp, pb, c2);
+    const float* src[4] = {c1, c1, c2, c2};
+    const float off[4] = {-w1, w1, -w1, w1};
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    for (int v = 0; v < 4; ++v) {
+        Q.clip[v][0] = src[v][0] + off[v];
+        Q.clip[v][1] = src[v][1];
+        Q.clip[v][2] = src[v][2];
+        Q.clip[v][3] = src[v][3];
+        const float cw = Q.clip[v][3];
+        if (!(cw > 0.f)) return Q;
+        Q.sx[v] = (Q.clip[v][0] / cw * 0.5f + 0.5f) * (float)R.width;
+        Q.sy[v] = (Q.clip[v][1] / cw * 0.5f + 0.5f) * (float)R.height;
+        Q.sz[v] = Q.clip[v][2] / cw;
+        if (!std::isfinite(Q.sx[v]) || !std::isfinite(Q.sy[v]) || !std::isfinite(Q.sz[v])) return Q;
+        xmin = std::fmin(xmin, Q.sx[v]);
+        xmax = std::fmax(xmax, Q.sx[v]);
+        ymin = std::fmin(ymin, Q.sy[v]);
+        ymax = std::fmax(ymax, Q.sy[v]);
+    }
+    // pixel centres px + 0.5 in [xmin, xmax]
+    const float fx0 = std::ceil(xmin - 0.5f), fx1 = std::floor(xmax - 0.5f);
+    const float fy0 = std::ceil(ymin - 0.5f), fy1 = std::floor(ymax - 0.5f);
+    const float cx0 = std::fmax(fx0, 0.f), cx1 = std::fmin(fx1, (float)(R.width - 1));
+    const float cy0 = std::fmax(fy0, 0.f), cy1 = std::fmin(fy1, (float)(R.height - 1));
+    if (cx0 > cx1 || cy0 > cy1) return Q;
+    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return Q;
+    Q.x0 = (int)cx0;
+    Q.x1 = (int)cx1;
+    Q.y0 = (int)cy0;
+    Q.y1 = (int)cy1;
+    Q.ok = true;
+    return Q;
+}
+
+inline float edge_fn(float ax, float ay, float bx, float by, float px, float py) {
+    return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+inline bool top_left(float ax, float ay, float bx, float by) {
+    const float dy = by - ay, dx = bx - ax;
+    return dy < 0.f || (dy == 0.f && dx > 0.f);
+}
+
+/* Coverage of pixel centre (px, py) by triangle (i0, i1, i2) of quad Q: the
+ * barycentrics l[3] (in i0, i1, i2 order) and depth z; false when not covered. */
+inline bool cover_tri(const Quad& Q, int i0, int i1, int i2, float px, float py, int idx[3], float l[3], float& z) {
+    float area = edge_fn(Q.sx[i0], Q.sy[i0], Q.sx[i1], Q.sy[i1], Q.sx[i2], Q.sy[i2]);
+    if (area == 0.f) return false;
+    if (area < 0.f) {
+        std::swap(i1, i2);
+        area = -area;
+    }
+    const int v[3] = {i0, i1, i2};
+    float e[3];
+    for (int t = 0; t < 3; ++t) {   // edge t opposite vertex t: from v[t+1] to v[t+2]
+        const int a = v[(t + 1) % 3], b = v[(t + 2) % 3];
+        e[t] = edge_fn(Q.sx[a], Q.sy[a], Q.sx[b], Q.sy[b], px, py);
+        if (e[t] < 0.f || (e[t] == 0.f && !top_left(Q.sx[a], Q.sy[a], Q.sx[b], Q.sy[b]))) return false;
+    }
+    for (int t = 0; t < 3; ++t) {
+        l[t] = e[t] / area;
+        idx[t] = v[t];
+    }
+    z = (l[0] * Q.sz[v[0]] + l[1] * Q.sz[v[1]]) + l[2] * Q.sz[v[2]];
+    return z >= 0.f && z <= 1.f;
+}
+
+/* The nearest covering triangle of the quad at a pixel: 0 (none), 1 or 2. */
+inline int cover_quad(const Quad& Q, int px, int py, int idx[3], float l[3], float& z) {
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    int ia[3], ib[3];
+    float la[3], lb[3], za = 0.f, zb = 0.f;
+    const bool a = cover_tri(Q, 0, 1, 2, cx, cy, ia, la, za);
+    const bool b = cover_tri(Q, 2, 1, 3, cx, cy, ib, lb, zb);
+    if (a && (!b || za <= zb)) {
+        for (int t = 0; t < 3; ++t) idx[t] = ia[t], l[t] = la[t];
+        z = za;
+        return 1;
+    }
+    if (b) {
+        for (int t = 0; t < 3; ++t) idx[t] = ib[t], l[t] = lb[t];
+        z = zb;
+        return 2;
+    }
+    return 0;
+}
+
+/* hair.geom's per-isoline width factor |random(3.242551 u, u u)| + 0.5 (:46). */
+inline float geom_rand(float u, RefSin mode) { return std::fabs(frag_random(3.242551f * u, u * u, mode)) + 0.5f; }
+
+/* The camera image of a tessellation (vertices ns x L x (S+1) float4, frames
+ * ns x (n-1) x 3 float4) shaded with hair.frag over the given maps; ids (nullable)
+ * receives the winning segment id per pixel, 0xffffffff where none. */
+inline void render_hair(const float* verts, const float* frames, int ns, int n, int L, int S, const Raster& R,
+                        const Maps& M, RefSin mode, float* image, uint32_t* ids) {
+    const int W = R.width, H = R.height;
+    std::vector<uint64_t> key(size_t(W) * H, ~0ull);
+    std::vector<float> rnd(L), bright(L);
+    for (int j = 0; j < L; ++j) {
+        const float u = (float)j / (float)L;
+        rnd[j] = geom_rand(u, mode);
+        bright[j] = 0.8f * std::fabs(frag_random(u, u, mode)) + 0.6f;
+    }
+    const int S1 = S + 1;
+    auto vert = [&](int s, int j, int k) { return verts + 4 * ((size_t(s) * L + j) * S1 + k); };
+    const long long nseg = (long long)ns * L * S;
+    for (long long id = 0; id < nseg; ++id) {
+        const int k = int(id % S);
+        const long long line = id / S;
+        const int j = int(line % L), s = int(line / L);
+        const float* pk = vert(s, j, k);
+        const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
+        if (!Q.ok) continue;
+        for (int py = Q.y0; py <= Q.y1; ++py)
+            for (int px = Q.x0; px <= Q.x1; ++px) {
+                int idx[3];
+                float l[3], z;
+                if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                uint32_t zb;
+                std::memcpy(&zb, &z, 4);
+                const uint64_t kk = (uint64_t(zb) << 32) | uint64_t(uint32_t(id));
+                uint64_t& t = key[size_t(py) * W + px];
+                if (kk < t) t = kk;
+            }
+    }
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const size_t p = size_t(py) * W + px;
+            float* out = image + 4 * p;
+            if (key[p] == ~0ull) {
+                out[0] = out[1] = out[2] = out[3] = 0.f;
+                if (ids) ids[p] = 0xffffffffu;
+                continue;
+            }
+            const uint32_t id = uint32_t(key[p] & 0xffffffffu);
+            if (ids) ids[p] = id;
+            const int k = int(id % S);
+            const long long line = id / S;
+            const int j = int(line % L), s = int(line / L);
+            const float* pk = vert(s, j, k);
+            const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
+            int idx[3];
+            float l[3], z;
+            cover_quad(Q, px, py, idx, l, z);
+            // the corners' hair.frag inputs: V0, V1 take vertex k's, V2, V3 vertex k + 1's
+            float attr[4][24];
+            for (int c = 0; c < 4; ++c) {
+                const int kk = c < 2 ? k : k + 1;
+                const float* p = vert(s, j, kk);
+                const V3 pos = mk(p[0], p[1], p[2]);
+                const float u = (float)j / (float)L, v = (float)kk / (float)S;
+                const float x = v * (float)(n - 1);
+                const int sf = std::min((int)std::floor(x), n - 2);
+                const float* fr = frames + (size_t(s) * (n - 1) + sf) * 12;
+                float* a = attr[c];
+                a[0] = u;
+                a[1] = v;
+                for (int q = 0; q < 3; ++q)
+                    for (int e = 0; e < 3; ++e) a[2 + 3 * q + e] = fr[4 * q + e];
+                const V3 vd = normalize(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+                const V3 ld = normalize(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+                a[11] = vd.x;
+                a[12] = vd.y;
+                a[13] = vd.z;
+                a[14] = ld.x;
+                a[15] = ld.y;
+                a[16] = ld.z;
+                mul_vec4(R.lmap, Q.clip[c], a + 17);
+                a[21] = a[22] = a[23] = 0.f;
+            }
+            const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+            const float qs = (q0 + q1) + q2;
+            float in[24];
+            for (int e = 0; e < 24; ++e)
+                in[e] = ((q0 * attr[idx[0]][e] + q1 * attr[idx[1]][e]) + q2 * attr[idx[2]][e]) / qs;
+            in[0] = (float)j / (float)L;
+            float o[4];
+            shade_fragment_bright(in, M, bright[j], o);
+            for (int c = 0; c < 4; ++c) out[c] = o[c];
+        }
 }
 
 }  // namespace shade

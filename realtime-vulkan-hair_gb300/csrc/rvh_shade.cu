@@ -153,12 +153,6 @@ __device__ __forceinline__ float tap_coord(float c, int size, int& i) {
     return x - x0;
 }
 
-__device__ __forceinline__ float bilerp(float t00, float t10, float t01, float t11, float fx, float fy) {
-    const float a = t00 + fx * (t10 - t00);
-    const float b = t01 + fx * (t11 - t01);
-    return a + fy * (b - a);
-}
-
 __device__ float pcf_shadow(const Maps& M, float px, float py, float pz, float pw, float& center, bool& has_center) {
     has_center = false;
     const float x = px / pw, y = py / pw, z = pz / pw;
@@ -562,6 +556,275 @@ __global__ void __launch_bounds__(kShadeThreads) k_image_resolve(long long px, c
     }
 }
 
+// ---- rasterised camera image: hair.geom's quads ------------------------------------
+// hair.geom (:41-108) turns each isoline segment (vertices k, k+1 of isoline j of
+// strand s) into a camera-facing quad: with P = camera proj * view, c1 = P
+// [pos_k, 1], c2 = P [pos_k+1, 1] and width1 = (|random(3.242551 u, u u)| + 0.5)
+// * 0.075 * |cameraPos - pos_k| * strandWidth_k (every corner uses width1), the
+// strip V0 = c1 - (width1, 0, 0, 0), V1 = c1 + ..., V2 = c2 - ..., V3 = c2 + ...;
+// V0, V1 carry vertex k's attributes, V2, V3 vertex k+1's, and a corner's
+// light-space position is lightProj * lightView * inverse(view) * inverse(proj) * V.
+// Rasterisation rules (a definition of Vulkan's; the oracle restates the same
+// arithmetic): screen x = (x/w * 0.5 + 0.5) W, y likewise with H, depth z/w;
+// pixel centres at +0.5; triangles (V0, V1, V2), (V2, V1, V3) reordered to
+// positive area; covered when every edge function is > 0, or = 0 on a top-left
+// edge; depth linear in screen space, kept in [0, 1]; attributes perspective-
+// correct.  Quads with a corner at w <= 0 (no near-plane clipping), a
+// non-finite corner or a bounding box over 65,536 pixels are dropped.  The
+// nearest fragment wins (ties: the smaller segment id, then the first triangle)
+// and the pixel takes its hair.frag colour (the pipeline's order-dependent
+// alpha blending is left out).
+//   k_hair_raster   one thread per segment: the quad's pixels, depth-tested by an
+//                   atomic min of (depth bits << 32 | segment id) in the image
+//   k_hair_resolve  one thread per pixel: the winner's quad again, perspective-
+//                   correct inputs, hair.frag
+struct RasterDev {
+    float vp[16];      // camera proj * view
+    float lmap[16];    // light proj * light view * inverse(view) * inverse(proj)
+    float cam_pos[3], light_pos[3];
+    int width, height;
+    float rnd[kMaxLines];      // hair.geom's |random(3.242551 u, u u)| + 0.5 per isoline
+    float bright[kMaxLines];   // hair.frag's 0.8 |random(u, u)| + 0.6 per isoline
+};
+
+struct TessView {
+    const float4* verts;   // ns x L x (S + 1)
+    const float4* frames;  // ns x (n - 1) x 3
+    int n, L, S;
+};
+
+__device__ __forceinline__ void mul_vec4(const float* m, const float v[4], float o[4]) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) o[r] = ((m[r] * v[0] + m[4 + r] * v[1]) + m[8 + r] * v[2]) + m[12 + r] * v[3];
+}
+
+struct Quad {
+    float clip[4][4];
+    float sx[4], sy[4], sz[4];
+    int x0, x1, y0, y1;
+    bool ok;
+};
+
+__device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 pk1, float rand_u) {
+    Quad Q;
+    Q.ok = false;
+    const V3 a = mk(pk.x, pk.y, pk.z), b = mk(pk1.x, pk1.y, pk1.z);
+    const float dist = len3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - a);
+    const float scale = rand_u * 0.075f * dist;
+    const float w1 = scale * pk.w;
+    float c1[4], c2[4];
+    const float pa[4] = {a.x, a.y, a.z, 1.f}, pb[4] = {b.x, b.y, b.z, 1.f};
+    mul_vec4(R.vp, pa, c1);
+    mul_vec4(R.vp, pb, c2);
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const float* src = v < 2 ? c1 : c2;
+        Q.clip[v][0] = src[0] + ((v & 1) ? w1 : -w1);
+        Q.clip[v][1] = src[1];
+        Q.clip[v][2] = src[2];
+        Q.clip[v][3] = src[3];
+        const float cw = Q.clip[v][3];
+        if (!(cw > 0.f)) return Q;
+        Q.sx[v] = (Q.clip[v][0] / cw * 0.5f + 0.5f) * (float)R.width;
+        Q.sy[v] = (Q.clip[v][1] / cw * 0.5f + 0.5f) * (float)R.height;
+        Q.sz[v] = Q.clip[v][2] / cw;
+        if (!isfinite(Q.sx[v]) || !isfinite(Q.sy[v]) || !isfinite(Q.sz[v])) return Q;
+        xmin = fminf(xmin, Q.sx[v]);
+        xmax = fmaxf(xmax, Q.sx[v]);
+        ymin = fminf(ymin, Q.sy[v]);
+        ymax = fmaxf(ymax, Q.sy[v]);
+    }
+    const float fx0 = ceilf(xmin - 0.5f), fx1 = floorf(xmax - 0.5f);
+    const float fy0 = ceilf(ymin - 0.5f), fy1 = floorf(ymax - 0.5f);
+    const float cx0 = fmaxf(fx0, 0.f), cx1 = fminf(fx1, (float)(R.width - 1));
+    const float cy0 = fmaxf(fy0, 0.f), cy1 = fminf(fy1, (float)(R.height - 1));
+    if (cx0 > cx1 || cy0 > cy1) return Q;
+    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return Q;
+    Q.x0 = (int)cx0;
+    Q.x1 = (int)cx1;
+    Q.y0 = (int)cy0;
+    Q.y1 = (int)cy1;
+    Q.ok = true;
+    return Q;
+}
+
+__device__ __forceinline__ float edge_fn(float ax, float ay, float bx, float by, float px, float py) {
+    return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+__device__ __forceinline__ bool top_left(float ax, float ay, float bx, float by) {
+    const float dy = by - ay, dx = bx - ax;
+    return dy < 0.f || (dy == 0.f && dx > 0.f);
+}
+
+// Triangle (i0, i1, i2) of quad Q at centre (px, py): the corners' values are
+// taken into registers (no indexed local arrays) and swapped when the area is
+// negative; idx[] reports the corners in the order of l[].
+__device__ __forceinline__ bool cover_tri(const Quad& Q, int i0, int i1, int i2, float px, float py, int idx[3],
+                                          float l[3], float& z) {
+    float x0 = Q.sx[i0], y0 = Q.sy[i0], z0 = Q.sz[i0];
+    float x1 = Q.sx[i1], y1 = Q.sy[i1], z1 = Q.sz[i1];
+    float x2 = Q.sx[i2], y2 = Q.sy[i2], z2 = Q.sz[i2];
+    float area = edge_fn(x0, y0, x1, y1, x2, y2);
+    if (area == 0.f) return false;
+    if (area < 0.f) {
+        float t = x1;
+        x1 = x2;
+        x2 = t;
+        t = y1;
+        y1 = y2;
+        y2 = t;
+        t = z1;
+        z1 = z2;
+        z2 = t;
+        const int ti = i1;
+        i1 = i2;
+        i2 = ti;
+        area = -area;
+    }
+    // edge t is opposite vertex t: from vertex t+1 to vertex t+2
+    const float e0 = edge_fn(x1, y1, x2, y2, px, py);
+    if (e0 < 0.f || (e0 == 0.f && !top_left(x1, y1, x2, y2))) return false;
+    const float e1 = edge_fn(x2, y2, x0, y0, px, py);
+    if (e1 < 0.f || (e1 == 0.f && !top_left(x2, y2, x0, y0))) return false;
+    const float e2 = edge_fn(x0, y0, x1, y1, px, py);
+    if (e2 < 0.f || (e2 == 0.f && !top_left(x0, y0, x1, y1))) return false;
+    l[0] = e0 / area;
+    l[1] = e1 / area;
+    l[2] = e2 / area;
+    idx[0] = i0;
+    idx[1] = i1;
+    idx[2] = i2;
+    z = (l[0] * z0 + l[1] * z1) + l[2] * z2;
+    return z >= 0.f && z <= 1.f;
+}
+
+__device__ __forceinline__ int cover_quad(const Quad& Q, int px, int py, int idx[3], float l[3], float& z) {
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    int ia[3], ib[3];
+    float la[3], lb[3], za = 0.f, zb = 0.f;
+    const bool a = cover_tri(Q, 0, 1, 2, cx, cy, ia, la, za);
+    const bool b = cover_tri(Q, 2, 1, 3, cx, cy, ib, lb, zb);
+    if (a && (!b || za <= zb)) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) idx[t] = ia[t], l[t] = la[t];
+        z = za;
+        return 1;
+    }
+    if (b) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) idx[t] = ib[t], l[t] = lb[t];
+        z = zb;
+        return 2;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ void segment_of(const TessView& T, unsigned id, int& s, int& j, int& k) {
+    const unsigned line = id / (unsigned)T.S;
+    k = (int)(id - line * (unsigned)T.S);
+    s = (int)(line / (unsigned)T.L);
+    j = (int)(line - (unsigned)s * (unsigned)T.L);
+}
+
+__device__ __forceinline__ const float4* vert_at(const TessView& T, int s, int j, int k) {
+    return T.verts + ((size_t)s * T.L + j) * (T.S + 1) + k;
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, RasterDev R, unsigned n_seg,
+                                                               float4* __restrict__ image) {
+    auto* keys = reinterpret_cast<unsigned long long*>(image);
+    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
+        int s, j, k;
+        segment_of(T, id, s, j, k);
+        const float4* pv = vert_at(T, s, j, k);
+        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        if (!Q.ok) continue;
+        for (int py = Q.y0; py <= Q.y1; ++py)
+            for (int px = Q.x0; px <= Q.x1; ++px) {
+                int idx[3];
+                float l[3], z;
+                if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
+                unsigned long long* slot = keys + 2 * ((size_t)py * R.width + px);
+                if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
+            }
+    }
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, RasterDev R, Maps M, long long px_count,
+                                                                float4* __restrict__ image, unsigned* __restrict__ ids) {
+    for (long long p = (long long)blockIdx.x * kShadeThreads + threadIdx.x; p < px_count;
+         p += (long long)gridDim.x * kShadeThreads) {
+        const unsigned long long key = reinterpret_cast<const unsigned long long*>(image)[2 * p];
+        if (key == kNoVertex) {
+            image[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (ids) ids[p] = 0xffffffffu;
+            continue;
+        }
+        const unsigned id = (unsigned)(key & 0xffffffffull);
+        if (ids) ids[p] = id;
+        int s, j, k;
+        segment_of(T, id, s, j, k);
+        const float4* pv = vert_at(T, s, j, k);
+        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
+        int idx[3];
+        float l[3], z;
+        cover_quad(Q, px, py, idx, l, z);
+        float in[24];
+#pragma unroll
+        for (int e = 0; e < 24; ++e) in[e] = 0.f;
+        const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+        const float qs = (q0 + q1) + q2;
+        const float qc[3] = {q0, q1, q2};
+        float acc[24];
+#pragma unroll
+        for (int e = 0; e < 24; ++e) acc[e] = 0.f;
+        // the corners' hair.frag inputs, accumulated in the oracle's order (q0 a0 + q1 a1) + q2 a2
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int c = idx[t];
+            const int kk = c < 2 ? k : k + 1;
+            const float4 P4 = __ldg(vert_at(T, s, j, kk));
+            const V3 pos = mk(P4.x, P4.y, P4.z);
+            const float u = (float)j / (float)T.L, v = (float)kk / (float)T.S;
+            const float x = v * (float)(T.n - 1);
+            const int sf = min((int)floorf(x), T.n - 2);
+            const float4* fr = T.frames + ((size_t)s * (T.n - 1) + sf) * 3;
+            float a[24];
+            a[0] = u;
+            a[1] = v;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 f = __ldg(fr + q);
+                a[2 + 3 * q] = f.x;
+                a[3 + 3 * q] = f.y;
+                a[4 + 3 * q] = f.z;
+            }
+            const V3 vd = nrm3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+            const V3 ld = nrm3(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+            a[11] = vd.x;
+            a[12] = vd.y;
+            a[13] = vd.z;
+            a[14] = ld.x;
+            a[15] = ld.y;
+            a[16] = ld.z;
+            float cl[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) cl[e] = Q.clip[c][e];
+            mul_vec4(R.lmap, cl, a + 17);
+            a[21] = a[22] = a[23] = 0.f;
+#pragma unroll
+            for (int e = 0; e < 24; ++e) acc[e] = t == 0 ? qc[0] * a[e] : acc[e] + qc[t] * a[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 24; ++e) in[e] = acc[e] / qs;
+        in[0] = (float)j / (float)T.L;
+        image[p] = shade_fragment(in, M, R.bright[j]);
+    }
+}
+
 // ---- host ---------------------------------------------------------------------------
 // glm's normalize, cross, lookAtRH and perspectiveRH_ZO in float, in glm's
 // operation order (glm 0.9.9 gtc/matrix_transform.inl), so the reference's
@@ -646,6 +909,43 @@ int grid_for(long long n, int sms) {
 
 bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
 
+// Column-major 4x4 inverse by Gauss-Jordan with partial pivoting, in double (the
+// oracle's restatement uses the same steps, so both round to the same floats).
+bool invert4(const double* m, double* inv) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = m[c * 4 + r];
+            a[r][4 + c] = r == c ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0) return false;
+        for (int k = 0; k < 8; ++k) std::swap(a[c][k], a[piv][k]);
+        const double d = a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] /= d;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                const double f = a[r][c];
+                for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[c * 4 + r] = a[r][4 + c];
+    return true;
+}
+
+void mul4d(const double* a, const double* b, double* o) {
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k) acc += a[k * 4 + r] * b[c * 4 + k];
+            o[c * 4 + r] = acc;
+        }
+}
+
 // hair.frag:260's brightness factor per isoline, with the kernel's hash
 // (a correctly rounded sin: the double sin rounded once).
 Lines line_table(int n_lines) {
@@ -657,6 +957,42 @@ Lines line_table(int n_lines) {
         B.bright[j] = 0.8f * std::fabs(m - std::floor(m)) + 0.6f;
     }
     return B;
+}
+
+float hash01(float x, float y) {   // random(x, y) with the double sin rounded once
+    const float d = x * 12.9898f + y * 78.233f;
+    const float m = (float)std::sin((double)d) * 43758.5453123f;
+    return m - std::floor(m);
+}
+
+bool raster_setup(const rvh_shade_desc& d, int n_lines, int w, int h, RasterDev& R) {
+    double cv[16], cp[16], lv[16], lp[16], t[16], u[16], icv[16], icp[16], vp[16];
+    for (int k = 0; k < 16; ++k) {
+        cv[k] = d.camera_view[k];
+        cp[k] = d.camera_proj[k];
+        lv[k] = d.light_view[k];
+        lp[k] = d.light_proj[k];
+    }
+    if (!invert4(cv, icv) || !invert4(cp, icp)) return false;
+    mul4d(cp, cv, vp);
+    mul4d(lp, lv, t);
+    mul4d(t, icv, u);
+    mul4d(u, icp, t);
+    for (int k = 0; k < 16; ++k) {
+        R.vp[k] = float(vp[k]);
+        R.lmap[k] = float(t[k]);
+    }
+    eye_of(d.camera_view, R.cam_pos);
+    eye_of(d.light_view, R.light_pos);
+    R.width = w;
+    R.height = h;
+    for (int j = 0; j < kMaxLines; ++j) R.rnd[j] = R.bright[j] = 0.f;
+    for (int j = 0; j < n_lines; ++j) {
+        const float uu = (float)j / (float)n_lines;
+        R.rnd[j] = std::fabs(hash01(3.242551f * uu, uu * uu)) + 0.5f;   // hair.geom:46
+        R.bright[j] = 0.8f * std::fabs(hash01(uu, uu)) + 0.6f;         // hair.frag:260
+    }
+    return true;
 }
 
 }  // namespace
@@ -738,6 +1074,43 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
             static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_strands, a->n_points,
             td->n_lines, td->n_segments, K, M, line_table(td->n_lines), static_cast<float4*>(colors));
     }
+    RVH_CUDA(cudaGetLastError());
+    return RVH_OK;
+}
+
+rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
+                                 const void* frames, const void* depth_map, const void* opacity_map, int32_t width,
+                                 int32_t height, void* image, void* fragment_ids, void* stream) {
+    if (!a || !td || !sd) return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: NULL argument");
+    rvh_status st = check_desc(*sd);
+    if (st != RVH_OK) return st;
+    if (td->n_lines < 1 || td->n_lines > kMaxLines || td->n_segments < 1 || td->n_segments > 256)
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: n_lines must be in [1, 64], n_segments in [1, 256]");
+    if (width < 1 || height < 1 || width > 16384 || height > 16384)
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: image size must be in [1, 16384]");
+    if (!image || !depth_map || !opacity_map || (a->n_strands > 0 && (!vertices || !frames)))
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: NULL buffer");
+    if (!aligned16(image) || !aligned16(vertices) || !aligned16(frames) || !aligned16(opacity_map) ||
+        reinterpret_cast<uintptr_t>(depth_map) % 4 || reinterpret_cast<uintptr_t>(fragment_ids) % 4)
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: float4 buffers 16-byte aligned, others 4-byte");
+    const long long n_seg = (long long)a->n_strands * td->n_lines * td->n_segments;
+    if (n_seg >= (1LL << 32) - (long long)a->ctx->sm_count * 8 * kShadeThreads)
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: fewer than 2^32 segments per asset");
+    RasterDev R;
+    if (!raster_setup(*sd, td->n_lines, width, height, R))
+        return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: a camera matrix is singular");
+    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->ctx->stream;
+    const TessView T{static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_points, td->n_lines,
+                     td->n_segments};
+    const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), sd->map_width,
+                 sd->map_height};
+    const long long px = (long long)width * height;
+    const int sms = a->ctx->sm_count;
+    auto* img = static_cast<float4*>(image);
+    k_image_clear<<<grid_for(px, sms), kShadeThreads, 0, s>>>(px, img);
+    if (n_seg > 0) k_hair_raster<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, img);
+    k_hair_resolve<<<grid_for(px, sms), kShadeThreads, 0, s>>>(T, R, M, px, img, static_cast<unsigned*>(fragment_ids));
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
 }

@@ -228,6 +228,18 @@ class Asset:
                                        C.c_void_p(frames_ptr), C.c_void_p(depth_ptr), C.c_void_p(opacity_ptr),
                                        C.c_void_p(colors_ptr), stream))
 
+    def render_hair(self, vertices_ptr, frames_ptr, depth_ptr, opacity_ptr, width, height, image_ptr, ids_ptr=None,
+                    tess_desc=None, shade_desc=None, stream=None):
+        """hair.geom's quads of this asset's tessellation rasterised into a
+        height x width float4 image shaded by hair.frag (maps from shade());
+        ids_ptr (optional) receives the winning segment per pixel."""
+        td = tess_desc if tess_desc is not None else tess_desc_reference()
+        sd = shade_desc if shade_desc is not None else shade_desc_reference()
+        check(self.lib.rvh_asset_render_hair(self.h, C.byref(td), C.byref(sd), C.c_void_p(vertices_ptr),
+                                             C.c_void_p(frames_ptr), C.c_void_p(depth_ptr), C.c_void_p(opacity_ptr),
+                                             width, height, C.c_void_p(image_ptr),
+                                             C.c_void_p(ids_ptr) if ids_ptr else None, stream))
+
     def read(self):
         out = np.empty((self.n_strands, 3 * self.n_points, 4), np.float32)
         check(self.lib.rvh_asset_read(self.h, out.ctypes.data_as(C.c_void_p), out.nbytes))

@@ -208,6 +208,50 @@ def test_gpu_render_image_matches_oracle(gpu_ctx, oracle):
     a.close()
 
 
+def test_oracle_raster_image_basics(oracle):
+    """The oracle's rasterised image: covered pixels carry hair.frag's alpha and a
+    valid segment id, the rest stay empty."""
+    from oracle.oracle_ctypes import render_hair
+    rec, rest, p, cols = api.generate_head(seed=9, n_strands=40, n_points=10, root_sampling=0, sort_roots=1,
+                                           length_min=0.4, length_max=0.8, head_collider=1, n_ellipsoids=0,
+                                           grid_res=0, friction=0.0, repulsion=0.0, dftl_damping=0.9)
+    v, fr = oracle.tessellate(rec, 10, 12, 42, sin_mode=1, frames=True)
+    sd = api.shade_desc_reference(map_width=270, map_height=180)
+    d, op = oracle.shade_maps(v, sd)
+    img, ids = render_hair(v, fr, 10, 12, 42, sd, d, op, 540, 360)
+    hit = ids != 0xffffffff
+    assert hit.sum() > 500
+    assert (img[hit][:, 3] == 0.75).all() and (img[~hit] == 0).all()
+    assert ids[hit].max() < 40 * 12 * 42
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,lines,segs,w,h", [(10, 12, 42, 1080, 720), (16, 5, 17, 333, 211), (32, 8, 64, 640, 480)])
+def test_gpu_render_hair_matches_oracle(gpu_ctx, oracle, n, lines, segs, w, h):
+    """The rasterised image: the winning segment of every pixel bit for bit,
+    colours within COLOR_TOL of the oracle's."""
+    import torch
+    a, ns = _head(gpu_ctx, seed=n + 40, n=n)
+    td = api.tess_desc_reference(n_lines=lines, n_segments=segs)
+    sd = api.shade_desc_reference()
+    verts, frames, depth, opac, col, (vert_d, _) = _shade_on_gpu(gpu_ctx, a, ns, n, td, sd)
+    fr_d = _dev(frames.reshape(-1))
+    dep_d, opa_d = _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
+    img = torch.full((w * h * 4,), -7.0, dtype=torch.float32, device="cuda")
+    ids = torch.zeros((w * h,), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    a.render_hair(vert_d.data_ptr(), fr_d.data_ptr(), dep_d.data_ptr(), opa_d.data_ptr(), w, h, img.data_ptr(),
+                  ids.data_ptr(), tess_desc=td, shade_desc=sd)
+    gpu_ctx.synchronize()
+    got = img.cpu().numpy().reshape(h, w, 4)
+    got_ids = ids.cpu().numpy().view(np.uint32).reshape(h, w)
+    want, want_ids = oracle.render_hair(verts, frames, n, lines, segs, sd, depth, opac, w, h)
+    assert np.array_equal(got_ids, want_ids)
+    assert (got_ids != 0xffffffff).sum() > 1000
+    _colors_close(got.reshape(-1, 4), want.reshape(-1, 4))
+    a.close()
+
+
 @pytest.mark.gpu
 def test_gpu_shade_rejects_bad_arguments(gpu_ctx):
     """Every call below fails its argument checks before any launch; the buffer
@@ -228,5 +272,9 @@ def test_gpu_shade_rejects_bad_arguments(gpu_ctx):
         a.shade(p, p, p, p, p + 4)
     with pytest.raises(RvhError):
         api.render_image(gpu_ctx, 10, p, p, 0, 10, p)
+    with pytest.raises(RvhError):   # image too large
+        a.render_hair(p, p, p, p, 20000, 10, p)
+    with pytest.raises(RvhError):   # misaligned image
+        a.render_hair(p, p, p, p, 10, 10, p + 4)
     torch.cuda.synchronize()
     a.close()
