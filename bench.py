@@ -278,20 +278,27 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     st = torch.cuda.Stream()
     a.tessellate(vert.data_ptr(), frames.data_ptr(), desc=td, stream=st.cuda_stream)
 
-    def once():
-        a.shade(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), col.data_ptr(), tess_desc=td,
-                shade_desc=sd, stream=st.cuda_stream)
-
-    for _ in range(warmup):
-        once()
-    st.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for _ in range(reps):
-        once()
-    e1.record(st)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
+
+    def timed(desc):
+        def once():
+            a.shade(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), col.data_ptr(),
+                    tess_desc=td, shade_desc=desc, stream=st.cuda_stream)
+
+        for _ in range(warmup):
+            once()
+        st.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            once()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # the light maps as one texel per vertex (the cheap mode), then as the
+    # reference draws them (hair.geom's quads); the image uses the latter
+    ms_vertex_maps = timed(api.shade_desc_reference(map_mode=api.SHADE_MAPS_VERTICES))
+    ms = timed(sd)
     covered = int((depth < 1).sum().item())
     # the camera image: hair.geom's quads rasterised at the window size, 1080 x 720
     W, H = 1080, 720
@@ -315,8 +322,10 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     alg = vertices * 64 + ns * (spec.n_points - 1) * 48 + texels * 20 * 3
     peak, _ = load_peaks()
     gbs = alg / (ms * 1e-3) / 1e9
-    return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments, 1080 x 720 maps",
+    return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments, 1080 x 720 maps "
+                        "rasterised from hair.geom's quads in the light's view",
             "vertices": vertices, "covered_texels": covered, "ms": ms, "vertices_per_s": vertices / (ms * 1e-3),
+            "ms_vertex_maps": ms_vertex_maps,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "bytes_per_launch": alg},
             "render": {"workload": "hair.geom quads of every isoline segment rasterised into 1080 x 720, "

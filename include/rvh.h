@@ -207,8 +207,12 @@ typedef struct rvh_shade_desc {
     float light_proj[16];   /* Camera.cpp:31-32: perspective(60 deg, 1.5, 1, 10), y flipped */
     int32_t map_width;      /* SHADOWMAP_WIDTH = 1080 (Renderer.cpp:9) */
     int32_t map_height;     /* SHADOWMAP_HEIGHT = 720 (Renderer.cpp:10) */
-    int32_t reserved[2];
+    int32_t map_mode;       /* RVH_SHADE_MAPS_QUADS (reference): the light passes rasterise hair.geom's
+                               quads in the light's view; RVH_SHADE_MAPS_VERTICES: each tessellated
+                               vertex covers one texel (cheaper) */
+    int32_t reserved;
 } rvh_shade_desc;
+enum { RVH_SHADE_MAPS_VERTICES = 0, RVH_SHADE_MAPS_QUADS = 1 };
 /* The reference's cameras and map size (glm's float arithmetic, bit for bit). */
 rvh_status rvh_shade_desc_reference(rvh_shade_desc* d);
 /* hair.frag for n caller-given fragments (replaces the fragment stage of the
@@ -223,7 +227,11 @@ rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, 
                                const void* opacity_map, int32_t map_width, int32_t map_height, void* colors,
                                void* stream);
 /* The three passes over an asset's tessellation (vertices and frames as
- * rvh_asset_tessellate wrote them with the same tessellation descriptor).
+ * rvh_asset_tessellate wrote them with the same tessellation descriptor).  The
+ * light passes draw what sd->map_mode says: hair.geom's quads expanded and
+ * rasterised in the light's view (the reference's shadow and opacity passes:
+ * src/Renderer.cpp:2107-2223, the light camera bound as the geometry shader's
+ * camera), or one texel per vertex.
  * depth_map: map_width x map_height floats (4-byte aligned), opacity_map: the
  * same count of float4, colors: one float4 per tessellated vertex; all
  * written.  The shadow pass's light depth map, the opacity pass's layers

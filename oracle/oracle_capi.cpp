@@ -163,6 +163,20 @@ int oracle_render_hair(const float* verts, const float* frames, int ns, int n, i
                                ids);
     return 0;
 }
+/* Light depth and deep opacity maps rasterised from hair.geom's quads in the
+ * light's view (shade_oracle.hpp light_maps_quads). */
+int oracle_shade_maps_quads(const float* verts, int ns, int n_lines, int n_segments, const float* light_view,
+                            const float* light_proj, int w, int h, int sin_mode, float* depth, float* opacity) {
+    if (!verts || !light_view || !light_proj || !depth || !opacity || ns < 0 || n_lines < 1 || n_segments < 1 ||
+        w < 1 || h < 1)
+        return 1;
+    oracle::shade::Raster R;
+    oracle::shade::make_light_raster(light_view, light_proj, w, h, R);
+    oracle::shade::light_maps_quads(verts, ns, n_lines, n_segments, R,
+                                    sin_mode == 0 ? oracle::shade::RefSin::kFloat : oracle::shade::RefSin::kDouble,
+                                    depth, opacity);
+    return 0;
+}
 /* FP64 adjoint of the no-grid step (FTL + DFTL + collisions); see hair_adjoint.hpp. */
 int oracle_adjoint_f64(const double* state0, int ns, int n, const double* rest, const double* strand_wind,
                        const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,

@@ -45,10 +45,11 @@ def lib():
         l.oracle_shade_maps.argtypes = [f4, C.c_longlong, f4, C.c_int, C.c_int, f4, f4]
         l.oracle_shade_vertex_inputs.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4]
         l.oracle_render_image.argtypes = [f4, f4, C.c_longlong, f4, f4, C.c_int, C.c_int, f4]
+        l.oracle_shade_maps_quads.argtypes = [f4, C.c_int, C.c_int, C.c_int, f4, f4, C.c_int, C.c_int, C.c_int, f4, f4]
         l.oracle_render_hair.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4, f4, f4, C.c_int,
                                          C.c_int, C.c_int, C.c_int, C.c_int, f4, _P(C.c_uint32)]
         for f in (l.oracle_shade_fragments, l.oracle_shade_camera, l.oracle_opacity_fragments, l.oracle_shade_maps, l.oracle_shade_vertex_inputs,
-                  l.oracle_render_image, l.oracle_render_hair):
+                  l.oracle_render_image, l.oracle_render_hair, l.oracle_shade_maps_quads):
             f.restype = C.c_int
         l.oracle_run_head_f64.argtypes = [_P(C.c_double)] + common + [_P(C.c_float), _P(C.c_float)]
         l.oracle_run_head_f32.argtypes = [_P(C.c_float)] + common + [_P(C.c_float), _P(C.c_float)]
@@ -282,8 +283,21 @@ def shade_camera(desc):
     return lvp, cam, light
 
 
-def shade_maps(vertices, desc):
-    """Light depth (h, w) and deep opacity (h, w, 4) maps of tessellated vertices."""
+def shade_maps(vertices, desc, n_lines=None, n_segments=None, sin_mode=1):
+    """Light depth (h, w) and deep opacity (h, w, 4) maps of tessellated vertices,
+    as desc.map_mode says: hair.geom's quads rasterised in the light's view
+    (vertices shaped (ns, n_lines, n_segments + 1, 4)), or one texel per vertex."""
+    if getattr(desc, "map_mode", 0) == 1:
+        v = _f32(vertices)
+        ns, L, S1 = v.shape[0], v.shape[1], v.shape[2]
+        _, _, lv, lp = _mats(desc)
+        w, h = desc.map_width, desc.map_height
+        depth = np.zeros((h, w), np.float32)
+        opacity = np.zeros((h, w, 4), np.float32)
+        _check(lib().oracle_shade_maps_quads(_fptr(v, C.c_float), ns, L, S1 - 1, _fptr(lv, C.c_float),
+                                             _fptr(lp, C.c_float), w, h, sin_mode, _fptr(depth, C.c_float),
+                                             _fptr(opacity, C.c_float)), "oracle_shade_maps_quads")
+        return depth, opacity
     v = _f32(vertices).reshape(-1, 4)
     lvp, _, _ = shade_camera(desc)
     w, h = desc.map_width, desc.map_height

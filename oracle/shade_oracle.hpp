@@ -707,5 +707,89 @@ inline void render_hair(const float* verts, const float* frames, int ns, int n, 
         }
 }
 
+
+/* The light camera as the geometry shader's camera: the shadow and opacity passes
+ * bind it at set 0 (src/Renderer.cpp:2147-2160, 2203-2216), so quads are expanded
+ * with the light's projection and the distance to the light, and a fragment's
+ * light-space position lightProj * lightView * inverse(lightView) *
+ * inverse(lightProj) * V is V itself (taken exactly). */
+inline bool make_light_raster(const float* light_view, const float* light_proj, int w, int h, Raster& R) {
+    double lv[16], lp[16], vp[16];
+    for (int k = 0; k < 16; ++k) {
+        lv[k] = light_view[k];
+        lp[k] = light_proj[k];
+    }
+    mul4d(lp, lv, vp);
+    for (int k = 0; k < 16; ++k) {
+        R.vp[k] = float(vp[k]);
+        R.lmap[k] = (k % 5 == 0) ? 1.f : 0.f;
+    }
+    eye_of(light_view, R.cam_pos);
+    eye_of(light_view, R.light_pos);
+    R.width = w;
+    R.height = h;
+    return true;
+}
+
+/* Light depth and deep opacity maps from hair.geom's quads rasterised in the
+ * light's view: the depth pass keeps each texel's nearest fragment
+ * (LESS_OR_EQUAL, cleared to 1.0); the opacity pass has no depth attachment, so
+ * every fragment adds to the layer its depth falls in relative to the depth map
+ * sampled at its light-space position (hairOpacity.frag:36-59), saturating as in
+ * light_maps. */
+inline void light_maps_quads(const float* verts, int ns, int L, int S, const Raster& R, RefSin mode, float* depth,
+                             float* opacity) {
+    const int W = R.width, H = R.height;
+    const size_t texels = size_t(W) * H;
+    std::fill(depth, depth + texels, 1.0f);
+    std::vector<float> rnd(L);
+    for (int j = 0; j < L; ++j) rnd[j] = geom_rand((float)j / (float)L, mode);
+    const int S1 = S + 1;
+    auto vert = [&](int s, int j, int k) { return verts + 4 * ((size_t(s) * L + j) * S1 + k); };
+    const long long nseg = (long long)ns * L * S;
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<uint32_t> count(pass == 1 ? texels * 3 : 0, 0);
+        for (long long id = 0; id < nseg; ++id) {
+            const int k = int(id % S);
+            const long long line = id / S;
+            const int j = int(line % L), s = int(line / L);
+            const float* pk = vert(s, j, k);
+            const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
+            if (!Q.ok) continue;
+            for (int py = Q.y0; py <= Q.y1; ++py)
+                for (int px = Q.x0; px <= Q.x1; ++px) {
+                    int idx[3];
+                    float l[3], z;
+                    if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                    const size_t t = size_t(py) * W + px;
+                    if (pass == 0) {
+                        if (z < depth[t]) depth[t] = z;
+                        continue;
+                    }
+                    const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+                    const float qs = (q0 + q1) + q2;
+                    float c[4];
+                    for (int e = 0; e < 4; ++e)
+                        c[e] = ((q0 * Q.clip[idx[0]][e] + q1 * Q.clip[idx[1]][e]) + q2 * Q.clip[idx[2]][e]) / qs;
+                    const float x = c[0] / c[3], y = c[1] / c[3], cz = c[2] / c[3];
+                    const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
+                    const int layer = opacity_layer(cz, sample(depth, W, H, 1, u, v, 0));
+                    uint32_t* cnt = count.data() + t * 3;
+                    if (layer == 1) cnt[0]++;
+                    if (layer == 1 || layer == 2) cnt[1]++;
+                    if (layer != 0) cnt[2]++;
+                }
+        }
+        if (pass == 1)
+            for (size_t t = 0; t < texels; ++t) {
+                for (int l = 0; l < 3; ++l) {
+                    const uint32_t c = count[t * 3 + l];
+                    opacity[t * 4 + l] = (float)(c >= 4 ? 255u : (uint32_t)kLayerUnit * c) / 255.0f;
+                }
+                opacity[t * 4 + 3] = 0.f;
+            }
+    }
+}
+
 }  // namespace shade
 }  // namespace oracle

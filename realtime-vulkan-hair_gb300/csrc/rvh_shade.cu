@@ -752,6 +752,64 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, Raste
     }
 }
 
+// Light maps from hair.geom's quads, the light camera bound as the geometry
+// shader's camera (the reference's shadow and opacity passes): the depth pass
+// keeps each texel's nearest fragment (LESS_OR_EQUAL, cleared to 1.0); the
+// opacity pass has no depth test, so every fragment adds to the layer its depth
+// falls in relative to the depth map at its light-space position, which is the
+// fragment's own interpolated clip position (lightProj * lightView *
+// inverse(lightView) * inverse(lightProj) taken as the identity).
+__global__ void __launch_bounds__(kShadeThreads) k_light_quads_depth(TessView T, RasterDev R, unsigned n_seg,
+                                                                     unsigned* __restrict__ depth_bits) {
+    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
+        int s, j, k;
+        segment_of(T, id, s, j, k);
+        const float4* pv = vert_at(T, s, j, k);
+        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        if (!Q.ok) continue;
+        for (int py = Q.y0; py <= Q.y1; ++py)
+            for (int px = Q.x0; px <= Q.x1; ++px) {
+                int idx[3];
+                float l[3], z;
+                if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                flush_min(depth_bits + (size_t)py * R.width + px, __float_as_uint(z));
+            }
+    }
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_light_quads_opacity(TessView T, RasterDev R, unsigned n_seg,
+                                                                       const float* __restrict__ depth,
+                                                                       uint4* __restrict__ counts) {
+    auto* words = reinterpret_cast<unsigned long long*>(counts);
+    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
+        int s, j, k;
+        segment_of(T, id, s, j, k);
+        const float4* pv = vert_at(T, s, j, k);
+        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        if (!Q.ok) continue;
+        for (int py = Q.y0; py <= Q.y1; ++py)
+            for (int px = Q.x0; px <= Q.x1; ++px) {
+                int idx[3];
+                float l[3], z;
+                if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+                const float qs = (q0 + q1) + q2;
+                float c[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    c[e] = ((q0 * Q.clip[idx[0]][e] + q1 * Q.clip[idx[1]][e]) + q2 * Q.clip[idx[2]][e]) / qs;
+                const float x = c[0] / c[3], y = c[1] / c[3], cz = c[2] / c[3];
+                const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
+                const float z0 = tex_sample(depth, R.width, R.height, 1, u, v, 0);
+                const float d = 0.3f;
+                const int layer = (cz >= z0 && cz < z0 + d) ? 1 : (cz >= z0 + d && cz < z0 + 2.f * d) ? 2
+                                                                  : (cz >= z0 + 2.f * d) ? 3 : 0;
+                if (layer == 0) continue;
+                add_counts(words + 2 * ((size_t)py * R.width + px), layer == 1, layer == 2, layer == 3);
+            }
+    }
+}
+
 __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, RasterDev R, Maps M, long long px_count,
                                                                 float4* __restrict__ image, unsigned* __restrict__ ids) {
     for (long long p = (long long)blockIdx.x * kShadeThreads + threadIdx.x; p < px_count;
@@ -889,6 +947,8 @@ bool finite16(const float* m) {
 rvh_status check_desc(const rvh_shade_desc& d) {
     if (d.map_width < 1 || d.map_height < 1 || d.map_width > 16384 || d.map_height > 16384)
         return fail(RVH_ERR_INVALID_ARG, "shade: map size must be in [1, 16384]");
+    if (d.map_mode != RVH_SHADE_MAPS_VERTICES && d.map_mode != RVH_SHADE_MAPS_QUADS)
+        return fail(RVH_ERR_INVALID_ARG, "shade: map_mode must be RVH_SHADE_MAPS_VERTICES or RVH_SHADE_MAPS_QUADS");
     if (!finite16(d.camera_view) || !finite16(d.camera_proj) || !finite16(d.light_view) || !finite16(d.light_proj))
         return fail(RVH_ERR_INVALID_ARG, "shade: non-finite matrix");
     return RVH_OK;
@@ -965,6 +1025,15 @@ float hash01(float x, float y) {   // random(x, y) with the double sin rounded o
     return m - std::floor(m);
 }
 
+void set_line_tables(RasterDev& R, int n_lines) {
+    for (int j = 0; j < kMaxLines; ++j) R.rnd[j] = R.bright[j] = 0.f;
+    for (int j = 0; j < n_lines; ++j) {
+        const float uu = (float)j / (float)n_lines;
+        R.rnd[j] = std::fabs(hash01(3.242551f * uu, uu * uu)) + 0.5f;   // hair.geom:46
+        R.bright[j] = 0.8f * std::fabs(hash01(uu, uu)) + 0.6f;         // hair.frag:260
+    }
+}
+
 bool raster_setup(const rvh_shade_desc& d, int n_lines, int w, int h, RasterDev& R) {
     double cv[16], cp[16], lv[16], lp[16], t[16], u[16], icv[16], icp[16], vp[16];
     for (int k = 0; k < 16; ++k) {
@@ -986,12 +1055,7 @@ bool raster_setup(const rvh_shade_desc& d, int n_lines, int w, int h, RasterDev&
     eye_of(d.light_view, R.light_pos);
     R.width = w;
     R.height = h;
-    for (int j = 0; j < kMaxLines; ++j) R.rnd[j] = R.bright[j] = 0.f;
-    for (int j = 0; j < n_lines; ++j) {
-        const float uu = (float)j / (float)n_lines;
-        R.rnd[j] = std::fabs(hash01(3.242551f * uu, uu * uu)) + 0.5f;   // hair.geom:46
-        R.bright[j] = 0.8f * std::fabs(hash01(uu, uu)) + 0.6f;         // hair.frag:260
-    }
+    set_line_tables(R, n_lines);
     return true;
 }
 
@@ -1014,6 +1078,7 @@ rvh_status rvh_shade_desc_reference(rvh_shade_desc* d) {
     perspective_flipped(60.0f, aspect, 1.f, 10.f, d->light_proj);
     d->map_width = 1080;                                          // SHADOWMAP_WIDTH x HEIGHT, src/Renderer.cpp:9-10
     d->map_height = 720;
+    d->map_mode = RVH_SHADE_MAPS_QUADS;                           // the passes draw hair.geom's quads
     return RVH_OK;
 }
 
@@ -1060,7 +1125,21 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
     auto* depth_bits = static_cast<unsigned*>(depth_map);
     auto* counts = static_cast<uint4*>(opacity_map);   // layer counts in place until the finish pass
     k_clear_maps<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, depth_bits, counts);
-    if (nv > 0) {
+    if (nv > 0 && sd->map_mode == RVH_SHADE_MAPS_QUADS) {
+        RasterDev R;   // the light camera as the geometry shader's camera
+        std::memcpy(R.vp, K.lvp, sizeof R.vp);
+        for (int q = 0; q < 16; ++q) R.lmap[q] = (q % 5 == 0) ? 1.f : 0.f;
+        for (int q = 0; q < 3; ++q) R.cam_pos[q] = R.light_pos[q] = K.light_pos[q];
+        R.width = w;
+        R.height = h;
+        set_line_tables(R, td->n_lines);
+        const TessView T{static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_points,
+                         td->n_lines, td->n_segments};
+        const long long n_seg = (long long)a->n_strands * td->n_lines * td->n_segments;
+        k_light_quads_depth<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, depth_bits);
+        k_light_quads_opacity<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg,
+                                                                            static_cast<const float*>(depth_map), counts);
+    } else if (nv > 0) {
         const VertexWalk W{static_cast<const float4*>(vertices), (long long)a->n_strands * (td->n_segments + 1),
                            td->n_lines, td->n_segments + 1};
         k_light_depth<<<grid_for(W.n_columns, sms), kShadeThreads, 0, s>>>(W, K, w, h, depth_bits);

@@ -480,7 +480,11 @@ def tess_desc_reference(**kw):
 class ShadeDesc(C.Structure):
     _fields_ = [("camera_view", C.c_float * 16), ("camera_proj", C.c_float * 16), ("light_view", C.c_float * 16),
                 ("light_proj", C.c_float * 16), ("map_width", C.c_int32), ("map_height", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("map_mode", C.c_int32), ("reserved", C.c_int32)]
+
+
+SHADE_MAPS_VERTICES = 0
+SHADE_MAPS_QUADS = 1
 
 
 def shade_desc_reference(**kw):

@@ -52,7 +52,7 @@ int main(void) {
   S(rvh_tune_desc) S(rvh_tune_result) S(rvh_server_desc) S(rvh_request) S(rvh_request_result) S(rvh_server_stats)
   S(rvh_mesh_roots_desc) O(rvh_mesh_roots_desc, seed) O(rvh_mesh_roots_desc, normal_mode)
   S(rvh_tess_desc) O(rvh_tess_desc, tip_width)
-  S(rvh_shade_desc) O(rvh_shade_desc, light_proj) O(rvh_shade_desc, map_height)
+  S(rvh_shade_desc) O(rvh_shade_desc, light_proj) O(rvh_shade_desc, map_height) O(rvh_shade_desc, map_mode)
   O(rvh_collider, kind) O(rvh_collider, radius) O(rvh_sim_params, grid_enabled) O(rvh_sim_params, grid_dims)
   O(rvh_frame, wind) O(rvh_asset_desc, strands) O(rvh_asset_desc, rest_lengths) O(rvh_asset_desc, lanes_per_strand)
   O(rvh_head_desc, grid_res) O(rvh_head_desc, dftl_damping) O(rvh_wind_desc, seed)
