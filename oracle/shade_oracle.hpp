@@ -736,7 +736,8 @@ inline bool make_light_raster(const float* light_view, const float* light_proj, 
  * (LESS_OR_EQUAL, cleared to 1.0); the opacity pass has no depth attachment, so
  * every fragment adds to the layer its depth falls in relative to the depth map
  * sampled at its light-space position (hairOpacity.frag:36-59), saturating as in
- * light_maps. */
+ * light_maps.  That position is the fragment's own (the light camera is the
+ * geometry shader's camera here): its pixel centre and its rasterised depth. */
 inline void light_maps_quads(const float* verts, int ns, int L, int S, const Raster& R, RefSin mode, float* depth,
                              float* opacity) {
     const int W = R.width, H = R.height;
@@ -766,14 +767,11 @@ inline void light_maps_quads(const float* verts, int ns, int L, int S, const Ras
                         if (z < depth[t]) depth[t] = z;
                         continue;
                     }
-                    const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
-                    const float qs = (q0 + q1) + q2;
-                    float c[4];
-                    for (int e = 0; e < 4; ++e)
-                        c[e] = ((q0 * Q.clip[idx[0]][e] + q1 * Q.clip[idx[1]][e]) + q2 * Q.clip[idx[2]][e]) / qs;
-                    const float x = c[0] / c[3], y = c[1] / c[3], cz = c[2] / c[3];
-                    const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
-                    const int layer = opacity_layer(cz, sample(depth, W, H, 1, u, v, 0));
+                    // the fragment's light-space position is its own: texture coordinates at the
+                    // pixel centre, depth the rasterised one (what the perspective-correct
+                    // interpolation of V and the divide by w give in exact arithmetic)
+                    const float u = ((float)px + 0.5f) / (float)W, v = ((float)py + 0.5f) / (float)H;
+                    const int layer = opacity_layer(z, sample(depth, W, H, 1, u, v, 0));
                     uint32_t* cnt = count.data() + t * 3;
                     if (layer == 1) cnt[0]++;
                     if (layer == 1 || layer == 2) cnt[1]++;

@@ -606,7 +606,7 @@ struct Quad {
 };
 
 __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 pk1, float rand_u) {
-    Quad Q;
+    Quad Q{};   // every field defined, also for a dropped quad (its box is shuffled but never used)
     Q.ok = false;
     const V3 a = mk(pk.x, pk.y, pk.z), b = mk(pk1.x, pk1.y, pk1.z);
     const float dist = len3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - a);
@@ -731,25 +731,83 @@ __device__ __forceinline__ const float4* vert_at(const TessView& T, int s, int j
     return T.verts + ((size_t)s * T.L + j) * (T.S + 1) + k;
 }
 
+// Warp-cooperative rasterisation: a lane per quad leaves most lanes idle while
+// one walks a larger pixel box (about 8 of 32 lanes active per instruction).  A
+// warp instead takes 32 consecutive segments, prefix-sums their boxes' pixel
+// counts and hands the (segment, pixel) jobs out 32 at a time: a lane finds the
+// job's quad by a shuffle search over the prefix sums and fetches its corners by
+// shuffles.  Each (segment, pixel) test is the same function on the same values
+// as before, so the results do not change.
+// The screen-space corners of lane `lane`'s quad (all the coverage test reads).
+__device__ __forceinline__ void shfl_quad(const Quad& src, Quad& dst, int lane) {
+    const unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        dst.sx[v] = __shfl_sync(FULL, src.sx[v], lane);
+        dst.sy[v] = __shfl_sync(FULL, src.sy[v], lane);
+        dst.sz[v] = __shfl_sync(FULL, src.sz[v], lane);
+    }
+}
+
+// frag(Q, id, j, px, py) for every pixel of every quad of segments [0, n_seg);
+// called by all threads of the grid (whole warps).
+template <class Frag>
+__device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& R, unsigned n_seg, Frag frag) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned warp0 = (blockIdx.x * kShadeThreads + (threadIdx.x & ~31u));
+    for (unsigned base = warp0; base < n_seg; base += gridDim.x * kShadeThreads) {   // warp-uniform
+        const unsigned id = base + lane;
+        Quad Q{};
+        int j = 0;
+        if (id < n_seg) {
+            int s, k;
+            segment_of(T, id, s, j, k);
+            const float4* pv = vert_at(T, s, j, k);
+            Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        }
+        const int bw = Q.ok ? Q.x1 - Q.x0 + 1 : 0;
+        const int cnt = Q.ok ? bw * (Q.y1 - Q.y0 + 1) : 0;   // <= 65,536 per quad
+        int incl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, off);
+            if (lane >= off) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        for (int t0 = 0; t0 < total; t0 += 32) {
+            const int t = t0 + lane;
+            int o = 0;   // the job's quad: the number of lanes whose prefix ends at or before t
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int v = __shfl_sync(FULL, incl, o + step - 1);
+                if (v <= t) o += step;
+            }
+            o = min(o, 31);
+            Quad Qo{};
+            shfl_quad(Q, Qo, o);
+            const int o_incl = __shfl_sync(FULL, incl, o), o_cnt = __shfl_sync(FULL, cnt, o);
+            const int o_bw = __shfl_sync(FULL, bw, o), o_x0 = __shfl_sync(FULL, Q.x0, o);
+            const int o_y0 = __shfl_sync(FULL, Q.y0, o), o_j = __shfl_sync(FULL, j, o);
+            if (t >= total) continue;
+            const int local = t - (o_incl - o_cnt);
+            const int ry = local / o_bw;
+            frag(Qo, base + (unsigned)o, o_j, o_x0 + (local - ry * o_bw), o_y0 + ry);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, RasterDev R, unsigned n_seg,
                                                                float4* __restrict__ image) {
     auto* keys = reinterpret_cast<unsigned long long*>(image);
-    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
-        int s, j, k;
-        segment_of(T, id, s, j, k);
-        const float4* pv = vert_at(T, s, j, k);
-        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
-        if (!Q.ok) continue;
-        for (int py = Q.y0; py <= Q.y1; ++py)
-            for (int px = Q.x0; px <= Q.x1; ++px) {
-                int idx[3];
-                float l[3], z;
-                if (!cover_quad(Q, px, py, idx, l, z)) continue;
-                const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-                unsigned long long* slot = keys + 2 * ((size_t)py * R.width + px);
-                if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
-            }
-    }
+    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned id, int, int px, int py) {
+        int idx[3];
+        float l[3], z;
+        if (!cover_quad(Q, px, py, idx, l, z)) return;
+        const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
+        unsigned long long* slot = keys + 2 * ((size_t)py * R.width + px);
+        if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
+    });
 }
 
 // Light maps from hair.geom's quads, the light camera bound as the geometry
@@ -757,57 +815,35 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, Raste
 // keeps each texel's nearest fragment (LESS_OR_EQUAL, cleared to 1.0); the
 // opacity pass has no depth test, so every fragment adds to the layer its depth
 // falls in relative to the depth map at its light-space position, which is the
-// fragment's own interpolated clip position (lightProj * lightView *
-// inverse(lightView) * inverse(lightProj) taken as the identity).
+// fragment's own (lightProj * lightView * inverse(lightView) * inverse(lightProj)
+// is the identity): its pixel centre and its rasterised depth.
 __global__ void __launch_bounds__(kShadeThreads) k_light_quads_depth(TessView T, RasterDev R, unsigned n_seg,
                                                                      unsigned* __restrict__ depth_bits) {
-    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
-        int s, j, k;
-        segment_of(T, id, s, j, k);
-        const float4* pv = vert_at(T, s, j, k);
-        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
-        if (!Q.ok) continue;
-        for (int py = Q.y0; py <= Q.y1; ++py)
-            for (int px = Q.x0; px <= Q.x1; ++px) {
-                int idx[3];
-                float l[3], z;
-                if (!cover_quad(Q, px, py, idx, l, z)) continue;
-                flush_min(depth_bits + (size_t)py * R.width + px, __float_as_uint(z));
-            }
-    }
+    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
+        int idx[3];
+        float l[3], z;
+        if (!cover_quad(Q, px, py, idx, l, z)) return;
+        flush_min(depth_bits + (size_t)py * R.width + px, __float_as_uint(z));
+    });
 }
 
 __global__ void __launch_bounds__(kShadeThreads) k_light_quads_opacity(TessView T, RasterDev R, unsigned n_seg,
                                                                        const float* __restrict__ depth,
                                                                        uint4* __restrict__ counts) {
     auto* words = reinterpret_cast<unsigned long long*>(counts);
-    for (unsigned id = blockIdx.x * kShadeThreads + threadIdx.x; id < n_seg; id += gridDim.x * kShadeThreads) {
-        int s, j, k;
-        segment_of(T, id, s, j, k);
-        const float4* pv = vert_at(T, s, j, k);
-        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
-        if (!Q.ok) continue;
-        for (int py = Q.y0; py <= Q.y1; ++py)
-            for (int px = Q.x0; px <= Q.x1; ++px) {
-                int idx[3];
-                float l[3], z;
-                if (!cover_quad(Q, px, py, idx, l, z)) continue;
-                const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
-                const float qs = (q0 + q1) + q2;
-                float c[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    c[e] = ((q0 * Q.clip[idx[0]][e] + q1 * Q.clip[idx[1]][e]) + q2 * Q.clip[idx[2]][e]) / qs;
-                const float x = c[0] / c[3], y = c[1] / c[3], cz = c[2] / c[3];
-                const float u = x * 0.5f + 0.5f, v = y * 0.5f + 0.5f;
-                const float z0 = tex_sample(depth, R.width, R.height, 1, u, v, 0);
-                const float d = 0.3f;
-                const int layer = (cz >= z0 && cz < z0 + d) ? 1 : (cz >= z0 + d && cz < z0 + 2.f * d) ? 2
-                                                                  : (cz >= z0 + 2.f * d) ? 3 : 0;
-                if (layer == 0) continue;
-                add_counts(words + 2 * ((size_t)py * R.width + px), layer == 1, layer == 2, layer == 3);
-            }
-    }
+    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
+        int idx[3];
+        float l[3], cz;
+        if (!cover_quad(Q, px, py, idx, l, cz)) return;
+        // the fragment's light-space position: its pixel centre and rasterised depth
+        const float u = ((float)px + 0.5f) / (float)R.width, v = ((float)py + 0.5f) / (float)R.height;
+        const float z0 = tex_sample(depth, R.width, R.height, 1, u, v, 0);
+        const float d = 0.3f;
+        const int layer = (cz >= z0 && cz < z0 + d) ? 1 : (cz >= z0 + d && cz < z0 + 2.f * d) ? 2
+                                                          : (cz >= z0 + 2.f * d) ? 3 : 0;
+        if (layer == 0) return;
+        add_counts(words + 2 * ((size_t)py * R.width + px), layer == 1, layer == 2, layer == 3);
+    });
 }
 
 __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, RasterDev R, Maps M, long long px_count,
