@@ -258,6 +258,76 @@ def test_gpu_render_hair_matches_oracle(gpu_ctx, oracle, n, lines, segs, w, h):
     a.close()
 
 
+def _look_at(eye, ctr, up):
+    """glm::lookAt (right-handed), column-major float32."""
+    eye, ctr, up = (np.asarray(x, np.float64) for x in (eye, ctr, up))
+    f = (ctr - eye) / np.linalg.norm(ctr - eye)
+    s_ = np.cross(f, up)
+    s_ /= np.linalg.norm(s_)
+    u = np.cross(s_, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s_, u, -f
+    m[:3, 3] = [-s_ @ eye, -u @ eye, f @ eye]
+    return m.T.astype(np.float32).reshape(-1)   # column-major
+
+
+def _desc_with_camera(eye, ctr):
+    sd = api.shade_desc_reference()
+    for k, v in enumerate(_look_at(eye, ctr, (0.0, 1.0, 0.0))):
+        sd.camera_view[k] = float(v)
+    return sd
+
+
+def test_oracle_raster_quad_area(oracle):
+    """One straight segment seen from the front covers about its screen area in
+    pixel centres: length x width, both from the projection."""
+    from oracle.oracle_ctypes import render_hair
+    n, L, S = 2, 1, 1
+    verts = np.array([[[[-0.5, 1.0, 0.0, 0.02], [0.5, 1.0, 0.0, 0.02]]]], np.float32)   # (1, L, S+1, 4)
+    frames = np.zeros((1, n - 1, 3, 4), np.float32)
+    frames[0, 0, 0, :3] = (1, 0, 0)
+    frames[0, 0, 1, :3] = (0, 1, 0)
+    frames[0, 0, 2, :3] = (0, 0, 1)
+    sd = api.shade_desc_reference(map_width=64, map_height=64)
+    d, op = oracle.shade_maps(verts, sd)
+    W, H = 1080, 720
+    img, ids = render_hair(verts, frames, n, L, S, sd, d, op, W, H)
+    hit = int((ids != 0xffffffff).sum())
+    P = np.array(list(sd.camera_proj), np.float64).reshape(4, 4).T @ np.array(list(sd.camera_view),
+                                                                             np.float64).reshape(4, 4).T
+    c = [P @ np.array([x, 1.0, 0.0, 1.0]) for x in (-0.5, 0.5)]
+    length_px = abs(c[1][0] / c[1][3] - c[0][0] / c[0][3]) * 0.5 * W
+    rand = abs(np.float32(np.modf(np.sin(0.0) * 43758.5453123)[0])) + 0.5   # u = 0: random(0, 0) = 0
+    width_clip = rand * 0.075 * np.linalg.norm(np.array([0.0, 1.0, 10.0]) - [-0.5, 1.0, 0.0]) * 0.02
+    width_px = 2 * width_clip / c[0][3] * 0.5 * W
+    assert abs(hit - length_px * width_px) <= 2 * length_px + 4, (hit, length_px, width_px)
+
+
+@pytest.mark.gpu
+def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle):
+    """A camera among the strands: quads behind it (w <= 0) and near ones over
+    65,536 pixels are dropped the same way on both sides; the rest match."""
+    import torch
+    a, ns = _head(gpu_ctx, seed=77, n=16)
+    td = api.tess_desc_reference()
+    sd = _desc_with_camera((0.0, 0.9, 0.6), (0.0, 0.2, -1.0))
+    verts, frames, depth, opac, col, (vert_d, _) = _shade_on_gpu(gpu_ctx, a, ns, 16, td, sd)
+    fr_d, dep_d, opa_d = _dev(frames.reshape(-1)), _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
+    w, h = 640, 480
+    img = torch.zeros((w * h * 4,), dtype=torch.float32, device="cuda")
+    ids = torch.zeros((w * h,), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    a.render_hair(vert_d.data_ptr(), fr_d.data_ptr(), dep_d.data_ptr(), opa_d.data_ptr(), w, h, img.data_ptr(),
+                  ids.data_ptr(), tess_desc=td, shade_desc=sd)
+    gpu_ctx.synchronize()
+    got_ids = ids.cpu().numpy().view(np.uint32).reshape(h, w)
+    want, want_ids = oracle.render_hair(verts, frames, 16, td.n_lines, td.n_segments, sd, depth, opac, w, h)
+    assert np.array_equal(got_ids, want_ids)
+    assert (got_ids != 0xffffffff).sum() > 1000
+    _colors_close(img.cpu().numpy().reshape(-1, 4), want.reshape(-1, 4))
+    a.close()
+
+
 @pytest.mark.gpu
 def test_gpu_shade_rejects_bad_arguments(gpu_ctx):
     """Every call below fails its argument checks before any launch; the buffer
