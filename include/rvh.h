@@ -260,6 +260,37 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
 rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* vertices, const void* colors,
                             const rvh_shade_desc* sd, int32_t width, int32_t height, void* image, void* stream);
 
+/* ---- checkpoint / resume ---------------------------------------------------
+ * The reference's state lives only in its VkBuffers (Strand.cpp:186-191,
+ * Scene.cpp:4-20).  A snapshot is the whole simulation state of one asset in
+ * a flat host buffer: this header, then 16-byte aligned sections: rest lengths
+ * (n_strands floats), strand wind (n_strands float4, flag RVH_SNAPSHOT_WIND),
+ * the rest roots of a head motion (n_strands float4, flag RVH_SNAPSHOT_ROOTS),
+ * the Strand records (48 * n_points bytes per strand).  A pending friction is
+ * finished first, so a restored asset continues with the same bits. */
+enum { RVH_SNAPSHOT_WIND = 1, RVH_SNAPSHOT_ROOTS = 2, RVH_SNAPSHOT_HEAD_ACTIVE = 4 };
+typedef struct rvh_snapshot_header {
+    char magic[8];                /* "RVHSNAP" */
+    uint32_t version;             /* 1 */
+    uint32_t header_bytes;        /* sizeof(rvh_snapshot_header) */
+    uint64_t total_bytes;
+    int32_t n_strands;
+    int32_t n_points;
+    uint32_t flags;
+    int32_t n_colliders;
+    int32_t lanes_per_strand;
+    int32_t reserved;
+    rvh_sim_params params;
+    rvh_collider colliders[RVH_MAX_COLLIDERS];
+    float head[16];               /* head pose (column-major) when RVH_SNAPSHOT_HEAD_ACTIVE */
+} rvh_snapshot_header;
+rvh_status rvh_asset_snapshot_bytes(rvh_asset* a, uint64_t* bytes);
+/* Synchronous; bytes must equal rvh_asset_snapshot_bytes. */
+rvh_status rvh_asset_snapshot(rvh_asset* a, void* host_dst, uint64_t bytes);
+/* A new asset in ctx from a snapshot (lanes_per_strand 0: the snapshot's). */
+rvh_status rvh_asset_restore(rvh_context* ctx, const void* host_src, uint64_t bytes, int32_t lanes_per_strand,
+                             rvh_asset** out);
+
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
     int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1 (one thread walks each strand), 4, 8, 16, 32 */

@@ -22,6 +22,13 @@ class AssetDesc(C.Structure):
                 ("lanes_per_strand", C.c_int32), ("reserved", C.c_int32)]
 
 
+class SnapshotHeader(C.Structure):
+    _fields_ = [("magic", C.c_char * 8), ("version", C.c_uint32), ("header_bytes", C.c_uint32),
+                ("total_bytes", C.c_uint64), ("n_strands", C.c_int32), ("n_points", C.c_int32), ("flags", C.c_uint32),
+                ("n_colliders", C.c_int32), ("lanes_per_strand", C.c_int32), ("reserved", C.c_int32),
+                ("params", T.SimParams), ("colliders", T.Collider * 8), ("head", C.c_float * 16)]
+
+
 class BatchDesc(C.Structure):
     _fields_ = [("lanes_per_strand", C.c_int32), ("strands_per_tile", C.c_int32), ("ctas_per_sm", C.c_int32),
                 ("use_graph", C.c_int32), ("full_steps", C.c_int32), ("reserved", C.c_int32)]
@@ -190,6 +197,27 @@ class Asset:
         if self.h:
             self.lib.rvh_asset_destroy(self.h)
             self.h = None
+
+    def snapshot(self):
+        """The asset's whole simulation state as bytes (rvh_asset_snapshot)."""
+        n = C.c_uint64()
+        check(self.lib.rvh_asset_snapshot_bytes(self.h, C.byref(n)))
+        buf = (C.c_ubyte * n.value)()
+        check(self.lib.rvh_asset_snapshot(self.h, buf, n.value))
+        return bytes(buf)
+
+    @classmethod
+    def restore(cls, ctx, data, lanes=0):
+        """A new asset in ctx from snapshot bytes (rvh_asset_restore)."""
+        buf = (C.c_ubyte * len(data)).from_buffer_copy(data)
+        h = C.c_void_p()
+        check(ctx.lib.rvh_asset_restore(ctx.h, buf, len(data), lanes, C.byref(h)))
+        self = cls.__new__(cls)
+        self.ctx, self.lib, self.h = ctx, ctx.lib, h
+        ns, npts = C.c_int32(), C.c_int32()
+        check(ctx.lib.rvh_asset_strand_count(h, C.byref(ns), C.byref(npts)))
+        self.n_strands, self.n_points = ns.value, npts.value
+        return self
 
     def set_params(self, p):
         check(self.lib.rvh_asset_set_params(self.h, C.byref(p)))
