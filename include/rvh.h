@@ -260,6 +260,21 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
 rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* vertices, const void* colors,
                             const rvh_shade_desc* sd, int32_t width, int32_t height, void* image, void* stream);
 
+/* ---- failure detection ------------------------------------------------------
+ * The reference has none.  A scan of the asset's records (after finishing a
+ * pending friction; synchronous): non-finite position or velocity components
+ * (the root's velocity included), the largest |v| (the step clamps it to vmax,
+ * compute.comp:198-200), and the largest |segment - rest| / (rest * (n - 1))
+ * with its strand (FTL keeps it near rounding, compute.comp:191-192). */
+typedef struct rvh_health {
+    uint64_t nonfinite;
+    float max_speed;
+    float max_length_error;
+    int32_t worst_strand;     /* strand of max_length_error, -1 for an empty asset */
+    int32_t reserved;
+} rvh_health;
+rvh_status rvh_asset_health(rvh_asset* a, rvh_health* out);
+
 /* ---- checkpoint / resume ---------------------------------------------------
  * The reference's state lives only in its VkBuffers (Strand.cpp:186-191,
  * Scene.cpp:4-20).  A snapshot is the whole simulation state of one asset in

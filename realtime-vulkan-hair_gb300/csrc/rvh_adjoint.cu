@@ -267,6 +267,7 @@ extern "C" {
 
 rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, int32_t checkpoint_every,
                        const float* targets, double* loss, float* d_wind, float* d_rest, float* d_v0) {
+    TraceRange trace("rvh_adjoint");
     if (!a || !frames || !targets || !loss) return fail(RVH_ERR_INVALID_ARG, "adjoint: NULL argument");
     if (n_steps < 1) return fail(RVH_ERR_INVALID_ARG, "adjoint: n_steps must be >= 1");
     if (checkpoint_every < 1) checkpoint_every = 10;

@@ -517,6 +517,7 @@ rvh_status rvh_batch_destroy(rvh_batch* b) {
 }
 
 rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
+    TraceRange trace("rvh_batch_step");
     if (!b || (!frames && !b->assets.empty())) return fail(RVH_ERR_INVALID_ARG, "batch_step: NULL argument");
     for (size_t i = 0; i < b->assets.size(); ++i) {
         rvh_status s = validate_frame(frames[i]);
@@ -565,6 +566,7 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
 // (the server's finish mode): the same tile code as the per-asset finish, so
 // the same bits, without a launch sequence per asset.
 rvh_status rvh_batch_finish(rvh_batch* b, void* stream) {
+    TraceRange trace("rvh_batch_finish");
     if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_finish: NULL");
     cudaSetDevice(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;

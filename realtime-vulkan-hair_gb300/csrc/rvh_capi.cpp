@@ -778,6 +778,7 @@ rvh_status rvh_asset_read_grid(rvh_asset* a, int64_t* dst, size_t bytes) {
 }
 
 rvh_status rvh_step(rvh_asset* a, const rvh_frame* frame, void* stream) {
+    TraceRange trace("rvh_step");
     if (!a || !frame) return fail(RVH_ERR_INVALID_ARG, "step: NULL argument");
     rvh_status s = validate_frame(*frame);
     if (s != RVH_OK) return s;

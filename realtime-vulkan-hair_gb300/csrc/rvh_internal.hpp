@@ -12,6 +12,13 @@
 #include "../../include/rvh.h"
 #include "rvh_kernels.cuh"
 
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>   // header-only NVTX v3: a no-op unless a profiler is attached
+#define RVH_HAVE_NVTX 1
+#else
+#define RVH_HAVE_NVTX 0
+#endif
+
 namespace rvh {
 
 // ---- errors -------------------------------------------------------------------
@@ -49,6 +56,24 @@ private:
 };
 
 struct Context;
+
+// An NVTX range around a public entry point, for timeline tools (nsys, ncu --nvtx).
+struct TraceRange {
+    explicit TraceRange(const char* name) {
+#if RVH_HAVE_NVTX
+        nvtxRangePushA(name);
+#else
+        (void)name;
+#endif
+    }
+    ~TraceRange() {
+#if RVH_HAVE_NVTX
+        nvtxRangePop();
+#endif
+    }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 
 // A device allocation charged to a context's budget.
 struct DevBuf {

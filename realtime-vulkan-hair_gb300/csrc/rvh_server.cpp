@@ -213,6 +213,7 @@ rvh_status rvh_server_character_steps(rvh_server* s, int32_t id, int64_t* steps)
 
 rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh_request_result* results,
                           rvh_server_stats* stats) {
+    TraceRange trace("rvh_server_run");
     if (!s || (n > 0 && (!reqs || !results))) return fail(RVH_ERR_INVALID_ARG, "server_run: NULL argument");
     cudaSetDevice(s->ctx->device);
     using clk = std::chrono::steady_clock;

@@ -1139,6 +1139,7 @@ rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, 
 
 rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
                            const void* frames, void* depth_map, void* opacity_map, void* colors, void* stream) {
+    TraceRange trace("rvh_asset_shade");
     if (!a || !td || !sd) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL argument");
     rvh_status st = check_desc(*sd);
     if (st != RVH_OK) return st;
@@ -1196,6 +1197,7 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
 rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
                                  const void* frames, const void* depth_map, const void* opacity_map, int32_t width,
                                  int32_t height, void* image, void* fragment_ids, void* stream) {
+    TraceRange trace("rvh_asset_render_hair");
     if (!a || !td || !sd) return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: NULL argument");
     rvh_status st = check_desc(*sd);
     if (st != RVH_OK) return st;

@@ -70,6 +70,7 @@ rvh_status rvh_asset_snapshot_bytes(rvh_asset* a, uint64_t* bytes) {
 }
 
 rvh_status rvh_asset_snapshot(rvh_asset* a, void* host_dst, uint64_t bytes) {
+    TraceRange trace("rvh_asset_snapshot");
     if (!a || !host_dst) return fail(RVH_ERR_INVALID_ARG, "snapshot: NULL argument");
     const uint32_t flags = flags_of(a);
     const Layout L = layout_of(a->n_strands, a->n_points, flags);

@@ -242,6 +242,7 @@ rvh_status rvh_tess_desc_reference(rvh_tess_desc* d) {
 }
 
 rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vertices, void* frames, void* stream) {
+    TraceRange trace("rvh_asset_tessellate");
     if (!a || !d) return fail(RVH_ERR_INVALID_ARG, "asset_tessellate: NULL argument");
     if (d->n_lines < 1 || d->n_lines > kMaxLines || d->n_segments < 1 || d->n_segments > kMaxSegments)
         return fail(RVH_ERR_INVALID_ARG, "asset_tessellate: n_lines must be in [1, 64], n_segments in [1, 256]");

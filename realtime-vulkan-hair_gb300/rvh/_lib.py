@@ -81,6 +81,7 @@ PROTOTYPES = [
     ("rvh_shade_fragments", _st, [_vp, C.c_int64, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
     ("rvh_asset_shade", _st, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("rvh_render_image", _st, [_vp, C.c_int64, _vp, _vp, _vp, C.c_int32, C.c_int32, _vp, _vp]),
+    ("rvh_asset_health", _st, [_vp, _vp]),
     ("rvh_asset_snapshot_bytes", _st, [_vp, _P(C.c_uint64)]),
     ("rvh_asset_snapshot", _st, [_vp, _vp, C.c_uint64]),
     ("rvh_asset_restore", _st, [_vp, _vp, C.c_uint64, C.c_int32, _P(_vp)]),

@@ -22,6 +22,11 @@ class AssetDesc(C.Structure):
                 ("lanes_per_strand", C.c_int32), ("reserved", C.c_int32)]
 
 
+class Health(C.Structure):
+    _fields_ = [("nonfinite", C.c_uint64), ("max_speed", C.c_float), ("max_length_error", C.c_float),
+                ("worst_strand", C.c_int32), ("reserved", C.c_int32)]
+
+
 class SnapshotHeader(C.Structure):
     _fields_ = [("magic", C.c_char * 8), ("version", C.c_uint32), ("header_bytes", C.c_uint32),
                 ("total_bytes", C.c_uint64), ("n_strands", C.c_int32), ("n_points", C.c_int32), ("flags", C.c_uint32),
@@ -197,6 +202,12 @@ class Asset:
         if self.h:
             self.lib.rvh_asset_destroy(self.h)
             self.h = None
+
+    def health(self):
+        """Non-finite count, largest speed and inextensibility error (rvh_asset_health)."""
+        h = Health()
+        check(self.lib.rvh_asset_health(self.h, C.byref(h)))
+        return h
 
     def snapshot(self):
         """The asset's whole simulation state as bytes (rvh_asset_snapshot)."""

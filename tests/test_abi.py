@@ -53,6 +53,7 @@ int main(void) {
   S(rvh_mesh_roots_desc) O(rvh_mesh_roots_desc, seed) O(rvh_mesh_roots_desc, normal_mode)
   S(rvh_tess_desc) O(rvh_tess_desc, tip_width)
   S(rvh_shade_desc) O(rvh_shade_desc, light_proj) O(rvh_shade_desc, map_height) O(rvh_shade_desc, map_mode)
+  S(rvh_health) O(rvh_health, worst_strand)
   S(rvh_snapshot_header) O(rvh_snapshot_header, params) O(rvh_snapshot_header, colliders) O(rvh_snapshot_header, head)
   O(rvh_collider, kind) O(rvh_collider, radius) O(rvh_sim_params, grid_enabled) O(rvh_sim_params, grid_dims)
   O(rvh_frame, wind) O(rvh_asset_desc, strands) O(rvh_asset_desc, rest_lengths) O(rvh_asset_desc, lanes_per_strand)
@@ -77,7 +78,7 @@ def test_struct_layouts_match_ctypes():
         "rvh_orbit": api.Orbit, "rvh_tune_desc": api.TuneDesc, "rvh_tune_result": api.TuneResult,
         "rvh_server_desc": api.ServerDesc, "rvh_request": api.Request, "rvh_request_result": api.RequestResult,
         "rvh_server_stats": api.ServerStats, "rvh_mesh_roots_desc": api.MeshRootsDesc,
-        "rvh_tess_desc": api.TessDesc, "rvh_shade_desc": api.ShadeDesc, "rvh_snapshot_header": api.SnapshotHeader,
+        "rvh_tess_desc": api.TessDesc, "rvh_shade_desc": api.ShadeDesc, "rvh_snapshot_header": api.SnapshotHeader, "rvh_health": api.Health,
     }
     for name, cls in py.items():
         assert int(c_vals[name]) == C.sizeof(cls), name

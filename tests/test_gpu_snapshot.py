@@ -1,4 +1,5 @@
-"""Checkpoint / resume (rvh_asset_snapshot, rvh_asset_restore).
+"""Checkpoint / resume (rvh_asset_snapshot, rvh_asset_restore) and failure
+detection (rvh_asset_health).
 
 A restored asset continues with the same bits as the original: plain steps
 with a grid, colliders, per-strand wind and a moving head; and an asset whose
@@ -101,3 +102,23 @@ def test_corrupt_snapshots_are_rejected(gpu_ctx):
     h = api.SnapshotHeader.from_buffer_copy(bytes(snap[:api.C.sizeof(api.SnapshotHeader)]))
     assert h.magic == b"RVHSNAP" and h.version == 1 and h.n_points == 16
     assert h.flags == 7   # wind, rest roots, head active
+
+
+def test_health_of_a_running_and_a_corrupted_asset(gpu_ctx_fast):
+    """A stepped asset is healthy (finite, |v| <= vmax, segments at rest length);
+    NaN and a stretched segment written into its records are reported."""
+    a = _head_asset(gpu_ctx_fast, seed=6)
+    for k in range(5):
+        a.step(_frame(k))
+    h = a.health()
+    assert h.nonfinite == 0 and 0 < h.max_speed <= 10.0 * (1 + 1e-6)
+    assert h.max_length_error <= 1e-6 and 0 <= h.worst_strand < a.n_strands
+    rec = a.read()
+    rec[7, 3, 0] = np.nan               # strand 7: a position component
+    rec[11, 16 + 2, 1] = np.inf         # strand 11: a velocity component
+    rec[42, 5, :3] += np.float32(0.5)    # strand 42: a stretched segment
+    a.write(rec)
+    h = a.health()
+    assert h.nonfinite == 2
+    assert h.worst_strand == 42 and h.max_length_error > 0.1
+    a.close()
