@@ -445,6 +445,11 @@ def main():
     batch.finish()
     ctx.synchronize()
     finish_ms = (time.perf_counter() - t0) * 1e3
+    # the benchmarked state after every step of this run: finite, clamped, inextensible
+    hs = [a.health() for a in assets]
+    health = {"assets": len(hs), "nonfinite": int(sum(h.nonfinite for h in hs)),
+              "max_speed": float(max(h.max_speed for h in hs)) if hs else 0.0,
+              "max_length_error": float(max(h.max_length_error for h in hs)) if hs else 0.0}
 
     # ---- plain step: one launch sequence per asset, no graph ----
     plain_value, plain_ms = None, None
@@ -529,7 +534,7 @@ def main():
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (pts * 48 / 1e9),
                        "math": "fast"},
             "p50_step_ms": lat_sorted[len(lat_sorted) // 2], "p99_step_ms": lat_sorted[-1],
-            "finish_ms": finish_ms, "tuner": tuned,
+            "finish_ms": finish_ms, "health": health, "tuner": tuned,
             "plain": {"value": plain_value, "ms_per_step": plain_ms,
                       "speedup_batched_vs_plain": (value / plain_value) if plain_value else None},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
