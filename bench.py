@@ -18,8 +18,9 @@ L2 (129 MB), so no flush is needed between steps.
           and has no CPU implementation), on a bounded sample of the workload.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-Under torchrun (N>1) assets are sharded across ranks (no collective on the
-data path); timing is max over ranks after a barrier.
+Under torchrun (N>1) every rank steps its own 256-head shard of an N x 256-head
+workload (weak scaling, no collective on the data path); timing is max over
+ranks after a barrier and value sums the ranks' points.
 """
 import argparse
 import json
@@ -113,8 +114,12 @@ def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
         backend = os.environ.get("RVH_DIST_BACKEND", "nccl")
+        if backend == "nccl" and torch.cuda.is_available():
+            # one GPU per rank: NCCL's barrier and the max-over-ranks tensor live on this rank's GPU
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group(backend)
     return rank, world
 
@@ -133,6 +138,17 @@ def max_over_ranks(x, world):
     dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
     t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 
@@ -391,7 +407,9 @@ def main():
     from rvh import api, configs
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
-    all_specs = configs.batched(n_assets=args.assets)
+    # weak scaling: every rank steps a full workload of args.assets heads (rank r takes
+    # heads r, r + N, ... of N * args.assets), with no collective on the data path
+    all_specs = configs.batched(n_assets=args.assets * world)
     specs = shard(all_specs, rank, world)
     ctx = api.Context(device=dev, math=api.MATH_FAST)
     assets = make_assets(ctx, specs)
@@ -428,7 +446,7 @@ def main():
     batch.check()
     step_ms = dev_ms / max(1, launches)
     step_ms = max_over_ranks(step_ms, world)
-    total_pts = int(max_over_ranks(pts, world)) * world if world > 1 else pts  # weak scaling: ~equal shards
+    total_pts = int(sum_over_ranks(pts, world))   # every rank's points of one step
     value = total_pts / (step_ms * 1e-3)
 
     # per-step latency distribution (each launch timed separately)
@@ -527,8 +545,9 @@ def main():
             "metric": METRIC, "value": value, "unit": "point-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generators, no dataset)",
-            "config": {"workload": "batched: %d heads, strands log-uniform 512..65536, points {8,16,24,32}, "
-                                   "lengths U(0.2,1), grids 32^3..64^3, 0-4 ellipsoids" % args.assets,
+            "config": {"workload": "batched: %d heads per GPU (%d in all), strands log-uniform 512..65536, "
+                                   "points {8,16,24,32}, lengths U(0.2,1), grids 32^3..64^3, 0-4 ellipsoids"
+                                   % (args.assets, args.assets * world),
                        "points_per_step": total_pts, "grid_cells": cells, "lanes_per_strand": info["lanes"],
                        "work_items": info["items"], "ctas": info["ctas"],
                        "l2": "inputs (%.1f GB) larger than L2; no flush" % (pts * 48 / 1e9),
