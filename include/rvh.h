@@ -263,8 +263,9 @@ rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* ve
 /* ---- failure detection ------------------------------------------------------
  * The reference has none.  A scan of the asset's records (after finishing a
  * pending friction; synchronous): non-finite position or velocity components
- * (the root's velocity included), the largest |v| (the step clamps it to vmax,
- * compute.comp:198-200), and the largest |segment - rest| / (rest * (n - 1))
+ * (the root's velocity included), the largest |v| (clamped to vmax before the
+ * DFTL correction and the friction blend, compute.comp:198-215, so it can exceed
+ * vmax), and the largest |segment - rest| / (rest * (n - 1))
  * with its strand (FTL keeps it near rounding, compute.comp:191-192). */
 typedef struct rvh_health {
     uint64_t nonfinite;

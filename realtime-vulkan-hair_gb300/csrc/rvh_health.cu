@@ -3,7 +3,8 @@
 // The reference has none (its state is only ever drawn).  rvh_asset_health
 // scans an asset's Strand records on the device and reports what a blown-up
 // or corrupted simulation shows first: non-finite positions or velocities, the
-// largest speed (the step clamps it to vmax, compute.comp:198-200), and the
+// largest speed (clamped to vmax before the DFTL correction and the friction
+// blend, compute.comp:198-215, so a healthy state can exceed vmax), and the
 // largest inextensibility error |segment - rest| / (rest * (n - 1)) that FTL
 // keeps near rounding (compute.comp:191-192).  One thread per strand; the
 // maxima are atomic maxima of the float bits (non-negative values order like

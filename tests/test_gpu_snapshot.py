@@ -105,13 +105,13 @@ def test_corrupt_snapshots_are_rejected(gpu_ctx):
 
 
 def test_health_of_a_running_and_a_corrupted_asset(gpu_ctx_fast):
-    """A stepped asset is healthy (finite, |v| <= vmax, segments at rest length);
-    NaN and a stretched segment written into its records are reported."""
+    """A stepped asset is healthy (finite, segments at rest length); NaN, Inf and a
+    stretched segment written into its records are reported."""
     a = _head_asset(gpu_ctx_fast, seed=6)
     for k in range(5):
         a.step(_frame(k))
     h = a.health()
-    assert h.nonfinite == 0 and 0 < h.max_speed <= 10.0 * (1 + 1e-6)
+    assert h.nonfinite == 0 and 0 < h.max_speed < 1e3
     assert h.max_length_error <= 1e-6 and 0 <= h.worst_strand < a.n_strands
     rec = a.read()
     rec[7, 3, 0] = np.nan               # strand 7: a position component
