@@ -129,6 +129,33 @@ def test_gpu_tessellation_after_batched_steps(gpu_ctx, oracle):
 
 
 @pytest.mark.gpu
+def test_gpu_tessellation_after_head_motion(gpu_ctx, oracle):
+    """A moving head moves the roots, which pick each isoline's sd profile
+    (randomChoice hashes the root): the tessellation still equals the oracle's."""
+    rec, rest, p, cols = api.generate_head(seed=23, n_strands=300, n_points=12, root_sampling=0, sort_roots=1,
+                                           length_min=0.3, length_max=0.9, head_collider=1, n_ellipsoids=0,
+                                           grid_res=0, friction=0.0, repulsion=0.0, dftl_damping=0.9)
+    a = api.Asset(gpu_ctx, rec, 12, rest=rest)
+    a.set_params(p)
+    a.set_colliders(cols)
+    for k in range(4):
+        m = np.eye(4, dtype=np.float32)
+        t = 0.05 * (k + 1)
+        m[0, 0], m[0, 1], m[1, 0], m[1, 1] = np.cos(t), -np.sin(t), np.sin(t), np.cos(t)
+        m[0, 3] = 0.1 * (k + 1)
+        a.set_head_transform(m)
+        a.step(api.T.frame(np.float32(1.0 / 60.0), np.float32((k + 1) / 60.0)))
+    state = a.read()
+    assert not np.array_equal(state[:, 0], rec[:, 0])   # the roots moved
+    desc = api.tess_desc_reference()
+    got, gfr = _gpu_tess(gpu_ctx, a, rec.shape[0], 12, desc)
+    want, wfr = oracle.tessellate(state, 12, desc.n_lines, desc.n_segments, sin_mode=1, frames=True)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(gfr.view(np.uint32), wfr.view(np.uint32))
+    a.close()
+
+
+@pytest.mark.gpu
 def test_gpu_tessellation_rejects_bad_descriptors(gpu_ctx):
     from rvh._lib import RvhError
     rec, rest, p, cols = api.generate_head(seed=1, n_strands=8, n_points=8, root_sampling=0, sort_roots=0,
