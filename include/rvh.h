@@ -233,8 +233,8 @@ rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, 
  * src/Renderer.cpp:2107-2223, the light camera bound as the geometry shader's
  * camera), or one texel per vertex.
  * depth_map: map_width x map_height floats (4-byte aligned), opacity_map: the
- * same count of float4, colors: one float4 per tessellated vertex; all
- * written.  The shadow pass's light depth map, the opacity pass's layers
+ * same count of float4, colors: one float4 per tessellated vertex, or NULL to
+ * skip the per-vertex hair.frag (the maps alone feed rvh_asset_render_hair).  The shadow pass's light depth map, the opacity pass's layers
  * (min(255, 77 n) / 255 for n fragments in a layer: 0.3 as unorm8, saturating
  * sum; alpha 0) and hair.frag's colour per vertex. */
 rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,

@@ -1146,7 +1146,7 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
     if (td->n_lines < 1 || td->n_lines > kMaxLines || td->n_segments < 1 || td->n_segments > 256)
         return fail(RVH_ERR_INVALID_ARG, "asset_shade: n_lines must be in [1, 64], n_segments in [1, 256]");
     if (!depth_map || !opacity_map) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL map");
-    if (a->n_strands > 0 && (!vertices || !frames || !colors)) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL buffer");
+    if (a->n_strands > 0 && (!vertices || !frames)) return fail(RVH_ERR_INVALID_ARG, "asset_shade: NULL buffer");
     if (!aligned16(vertices) || !aligned16(frames) || !aligned16(opacity_map) || !aligned16(colors) ||
         reinterpret_cast<uintptr_t>(depth_map) % 4)
         return fail(RVH_ERR_INVALID_ARG, "asset_shade: float4 buffers 16-byte aligned, the depth map 4-byte");
@@ -1184,7 +1184,7 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
                                                                              static_cast<const float*>(depth_map), counts);
     }
     k_opacity_finish<<<grid_for(texels, sms), kShadeThreads, 0, s>>>(texels, counts);
-    if (nv > 0) {
+    if (nv > 0 && colors) {   // colours are optional: the maps alone feed rvh_asset_render_hair
         const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), w, h};
         k_shade_vertices<<<grid_for(nv, sms), kShadeThreads, 0, s>>>(
             static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_strands, a->n_points,

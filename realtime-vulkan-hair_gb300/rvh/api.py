@@ -265,7 +265,7 @@ class Asset:
         sd = shade_desc if shade_desc is not None else shade_desc_reference()
         check(self.lib.rvh_asset_shade(self.h, C.byref(td), C.byref(sd), C.c_void_p(vertices_ptr),
                                        C.c_void_p(frames_ptr), C.c_void_p(depth_ptr), C.c_void_p(opacity_ptr),
-                                       C.c_void_p(colors_ptr), stream))
+                                       C.c_void_p(colors_ptr) if colors_ptr else None, stream))
 
     def render_hair(self, vertices_ptr, frames_ptr, depth_ptr, opacity_ptr, width, height, image_ptr, ids_ptr=None,
                     tess_desc=None, shade_desc=None, stream=None):

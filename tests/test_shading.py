@@ -329,6 +329,28 @@ def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle):
 
 
 @pytest.mark.gpu
+def test_gpu_shade_maps_without_colours(gpu_ctx, oracle):
+    """colors = NULL: only the two light passes run; the maps are unchanged."""
+    import torch
+    a, ns = _head(gpu_ctx, seed=19, n=10)
+    td, sd = api.tess_desc_reference(), api.shade_desc_reference()
+    per = td.n_lines * (td.n_segments + 1)
+    vert = torch.zeros((ns * per * 4,), dtype=torch.float32, device="cuda")
+    fr = torch.zeros((ns * 9 * 12,), dtype=torch.float32, device="cuda")
+    depth = torch.zeros((1080 * 720,), dtype=torch.float32, device="cuda")
+    opac = torch.zeros((1080 * 720 * 4,), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    a.tessellate(vert.data_ptr(), fr.data_ptr(), desc=td)
+    a.shade(vert.data_ptr(), fr.data_ptr(), depth.data_ptr(), opac.data_ptr(), None, tess_desc=td, shade_desc=sd)
+    gpu_ctx.synchronize()
+    v = vert.cpu().numpy().reshape(ns, td.n_lines, td.n_segments + 1, 4)
+    want_d, want_o = oracle.shade_maps(v, sd)
+    assert _same_bits(depth.cpu().numpy().reshape(720, 1080), want_d)
+    assert _same_bits(opac.cpu().numpy().reshape(720, 1080, 4), want_o)
+    a.close()
+
+
+@pytest.mark.gpu
 def test_gpu_shade_rejects_bad_arguments(gpu_ctx):
     """Every call below fails its argument checks before any launch; the buffer
     is large enough for what a launch with those arguments would touch."""
