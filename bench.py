@@ -366,6 +366,27 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
             "frame_ms": frame_ms}
 
 
+def run_adjoint(ctx, api, configs, reps=3):
+    """The differentiable step: 4,096 strands x 32 points over 60 steps, the FP32
+    adjoint of the tip loss with checkpoints every 10 steps (forward, per-segment
+    recompute, reverse), wall time per call (synchronous) and per step."""
+    spec, targets = configs.adjoint_case(n_strands=4096, n_points=32)
+    a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest, strand_wind=spec.strand_wind)
+    a.set_params(spec.params)
+    a.set_colliders(spec.colliders)
+    frames = [spec.frame(k) for k in range(60)]
+    a.adjoint(frames, targets)   # warm-up
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        a.write(spec.records)
+        a.adjoint(frames, targets)
+    ms = (time.perf_counter() - t0) * 1e3 / reps
+    a.close()
+    pts = spec.n_strands * spec.n_points
+    return {"workload": "%d strands x 32 points, 60 steps, checkpoints every 10, tip loss" % spec.n_strands,
+            "ms": ms, "ms_per_step": ms / 60, "point_steps_per_s": pts * 60 / (ms * 1e-3)}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle's OpenMP restatement on the host cores."""
     if rank != 0:
@@ -410,6 +431,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-tess", action="store_true")
     ap.add_argument("--no-shade", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
@@ -545,6 +567,9 @@ def main():
     shade = None
     if world == 1 and not args.no_shade:
         shade = run_shade(ctx, api, configs)
+    adjoint = None
+    if world == 1 and not args.no_adjoint:
+        adjoint = run_adjoint(ctx, api, configs)
 
     served, served_pts = None, None
     if not args.no_served and world == 1:
@@ -582,7 +607,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
-            "shading": shade,
+            "shading": shade, "adjoint": adjoint,
             "served": None if served is None else {
                 "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
                             "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (
