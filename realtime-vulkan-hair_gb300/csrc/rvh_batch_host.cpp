@@ -87,11 +87,14 @@ __global__ void __launch_bounds__(kThreads) k_pack_positions(const DevAsset* __r
 namespace {
 
 constexpr int kTargetPointsA = 4096;   // points per phase-A item
+constexpr int kMinTilePoints = 1024;   // smallest phase-A item of a request-server launch
 constexpr int kTargetPointsB = kTileB;  // points per phase-B item (one shared-memory box)
 constexpr int kClearChunk = 1 << 16;   // 16-B units per clear item (1 MiB)
 constexpr uint32_t kSpinLimit = 1u << 22;  // ~1 s of 256-ns sleeps before a wait gives up
 
-void plan(Batch& b, int strands_per_tile) {
+// strands_per_tile > 0 fixes the phase-A tile; else a tile holds about
+// target_points points (rounded to whole CTA rounds).
+void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     const int S = 32 / b.lanes;
     const int quantum = kWarps * S;
     std::vector<int> order(b.assets.size());
@@ -132,7 +135,7 @@ void plan(Batch& b, int strands_per_tile) {
             emit_b(ai);
             continue;
         }
-        int ta = strands_per_tile > 0 ? strands_per_tile : kTargetPointsA / a->n_points;
+        int ta = strands_per_tile > 0 ? strands_per_tile : target_points / a->n_points;
         ta = std::max(quantum, (ta + quantum - 1) / quantum * quantum);
         for (int s = 0; s < a->n_strands; s += ta) {
             b.items.push_back({ITEM_A, ai, s, std::min(a->n_strands, s + ta)});
@@ -346,7 +349,12 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     Batch& b = d->b;
     b.assets = assets;
     b.modes = modes;
-    plan(b, 0);
+    // a launch carries what the requests of the moment need: tiles sized so every CTA
+    // gets about two (small launches would otherwise leave most CTAs idle)
+    int64_t launch_pts = 0;
+    for (Asset* a : assets) launch_pts += int64_t(a->n_strands) * a->n_points;
+    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 2 * int64_t(b.n_ctas));
+    plan(b, 0, int(std::min<int64_t>(kTargetPointsA, std::max<int64_t>(kMinTilePoints, per_tile))));
     b.dev.n_items = int32_t(b.items.size());
     int64_t pts = 0;
     for (Asset* a : assets) pts += int64_t(a->n_strands) * a->n_points;
