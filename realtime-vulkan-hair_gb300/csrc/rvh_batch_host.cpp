@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kThreads) k_pack_positions(const DevAsset* __r
 namespace {
 
 constexpr int kTargetPointsA = 4096;   // points per phase-A item
-constexpr int kMinTilePoints = 1024;   // smallest phase-A item of a request-server launch
+constexpr int kMinTilePoints = 512;   // smallest phase-A item of a request-server launch
 constexpr int kTargetPointsB = kTileB;  // points per phase-B item (one shared-memory box)
 constexpr int kClearChunk = 1 << 16;   // 16-B units per clear item (1 MiB)
 constexpr uint32_t kSpinLimit = 1u << 22;  // ~1 s of 256-ns sleeps before a wait gives up
@@ -350,10 +350,11 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     b.assets = assets;
     b.modes = modes;
     // a launch carries what the requests of the moment need: tiles sized so every CTA
-    // gets about two (small launches would otherwise leave most CTAs idle)
+    // gets about eight (small launches would otherwise leave most CTAs idle, and a
+    // few large tiles leave a tail; measured against two and four per CTA)
     int64_t launch_pts = 0;
     for (Asset* a : assets) launch_pts += int64_t(a->n_strands) * a->n_points;
-    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 2 * int64_t(b.n_ctas));
+    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 8 * int64_t(b.n_ctas));
     plan(b, 0, int(std::min<int64_t>(kTargetPointsA, std::max<int64_t>(kMinTilePoints, per_tile))));
     b.dev.n_items = int32_t(b.items.size());
     int64_t pts = 0;
