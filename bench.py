@@ -12,7 +12,8 @@ L2 (129 MB), so no flush is needed between steps.
           stream), inputs resident in HBM.
   e2e   : the same step through the C ABI with host data every step: frame
           parameters from pinned host memory (H2D) and every curve point's
-          position (xyz) back to host memory (D2H), all inside the timed region.
+          position (xyz) back to host memory (D2H), all inside the timed region
+          (rvh_batch_step_read_positions: the step kernel stages the positions).
   --impl reference : the oracle's OpenMP C++ restatement of the reference
           shader on the host cores (the reference itself is a Vulkan shader
           and has no CPU implementation), on a bounded sample of the workload.
@@ -525,26 +526,38 @@ def main():
         plain_value = total_pts / (plain_ms * 1e-3)
 
     # ---- e2e through the C ABI with host buffers ----
-    # every step: frame tables host->device (inside rvh_batch_step) and every
-    # curve point's position (xyz, 12 B) device->host (packed on the device,
-    # copied on a second stream so the copy of step k overlaps step k+1)
+    # every step: frame tables host->device (inside the step call) and every
+    # curve point's position (xyz, 12 B) device->host.  rvh_batch_step_read_positions:
+    # the step kernel writes each new position into a staging slot as it stores the
+    # record, and a second stream copies it so the copy of step k overlaps step k+1.
+    # For comparison, the same with a separate packing pass after each step
+    # (rvh_batch_step + rvh_batch_read_positions_async).
     pos_bytes = pts * 12
     pinned = [api.PinnedBuffer(pos_bytes) for _ in range(2)]
     h2d = batch.h2d_bytes_per_step()
     ne2e = max(3, min(args.steps, 10))
-    for k in range(2):
-        batch.step(frames[k])
-        batch.read_positions_async(pinned[k % 2].ptr, pos_bytes)
-    batch.positions_wait()
-    ctx.synchronize()
-    barrier(world)
-    t0 = time.perf_counter()
-    for k in range(ne2e):
-        batch.step(frames[k])
-        batch.read_positions_async(pinned[k % 2].ptr, pos_bytes)
-    batch.positions_wait()
-    ctx.synchronize()
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / ne2e, world)
+
+    def e2e_run(fused):
+        def one(k):
+            if fused:
+                batch.step_read_positions(frames[k], pinned[k % 2].ptr, pos_bytes)
+            else:
+                batch.step(frames[k])
+                batch.read_positions_async(pinned[k % 2].ptr, pos_bytes)
+        for k in range(2):
+            one(k)
+        batch.positions_wait()
+        ctx.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for k in range(ne2e):
+            one(k)
+        batch.positions_wait()
+        ctx.synchronize()
+        return max_over_ranks((time.perf_counter() - t0) * 1e3 / ne2e, world)
+
+    e2e_pack_ms = e2e_run(False)
+    e2e_ms = e2e_run(True)
     e2e_value = total_pts / (e2e_ms * 1e-3)
     d2h = pos_bytes
     for p_ in pinned:
@@ -605,7 +618,8 @@ def main():
                          "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                          "fallback 6.8 TB/s"},
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+                    "d2h_bytes_per_step": d2h, "api": "rvh_batch_step_read_positions",
+                    "ms_per_step_with_packing_pass": e2e_pack_ms},
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
             "shading": shade, "adjoint": adjoint,
             "served": None if served is None else {

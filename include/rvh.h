@@ -350,6 +350,14 @@ rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]);
  * (rvh_pinned_alloc) for the copy to overlap.  rvh_batch_positions_wait blocks
  * until every copy is done. */
 rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream);
+/* rvh_batch_step, then that step's curvePoints to host memory as xyz triples
+ * (bytes = 12 * points, the layout of rvh_batch_read_positions_async): the
+ * step kernel itself writes each new position into a staging slot beside the
+ * Strand record it stores, so no separate pass reads the records again.  The
+ * copy runs on the copy stream; rvh_batch_positions_wait blocks until it is
+ * done. */
+rvh_status rvh_batch_step_read_positions(rvh_batch* b, const rvh_frame* frames, void* host_dst, size_t bytes,
+                                         void* stream);
 rvh_status rvh_batch_positions_wait(rvh_batch* b);
 /* Bytes rvh_batch_step copies host->device per step (per-asset frame and collider tables). */
 rvh_status rvh_batch_h2d_bytes(rvh_batch* b, uint64_t* bytes);

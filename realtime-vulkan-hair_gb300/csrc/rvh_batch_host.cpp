@@ -47,6 +47,7 @@ struct Batch {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pairs;   // recorded, not yet read
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
     DynBatch* finisher = nullptr;   // one launch of gather-only items for rvh_batch_finish
+    std::vector<int64_t> first_point;   // per asset: its first point in the batch's position order
 };
 
 // Packs the curvePoints of every asset of a batch into one contiguous float4
@@ -444,6 +445,7 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
             }
         b->assets.push_back(assets[i]);
         b->modes.push_back(d.full_steps ? MODE_FULL : MODE_FUSED);
+        b->first_point.push_back(b->n_points);
         b->n_points += int64_t(assets[i]->n_strands) * assets[i]->n_points;
     }
     b->kernel = batch_kernel(lanes, b->exact);
@@ -525,8 +527,14 @@ rvh_status rvh_batch_destroy(rvh_batch* b) {
     return RVH_OK;
 }
 
-rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
-    TraceRange trace("rvh_batch_step");
+}  // extern "C"
+
+namespace rvh {
+namespace {
+
+// One batched step; with xyz set, every point's new position is also written
+// there (asset after asset, xyz per point) by the step itself.
+rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, float* xyz) {
     if (!b || (!frames && !b->assets.empty())) return fail(RVH_ERR_INVALID_ARG, "batch_step: NULL argument");
     for (size_t i = 0; i < b->assets.size(); ++i) {
         rvh_status s = validate_frame(frames[i]);
@@ -534,7 +542,6 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
     }
     if (b->items.empty()) return RVH_OK;
     cudaSetDevice(b->ctx->device);
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
     const int slot = b->slot;
     b->slot ^= 1;
     RVH_CUDA(cudaEventSynchronize(b->staged[slot]));  // the copy that last read this staging buffer is done
@@ -543,6 +550,7 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
     for (size_t i = 0; i < b->assets.size(); ++i) {
         rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i]);
         if (ps != RVH_OK) return ps;
+        st[i].pos_xyz = xyz ? xyz + 3 * b->first_point[i] : nullptr;
     }
     RVH_CUDA(cudaMemcpyAsync(b->d_assets.ptr, st, sizeof(DevAsset) * b->assets.size(), cudaMemcpyHostToDevice, s));
     RVH_CUDA(cudaEventRecord(b->staged[slot], s));
@@ -569,6 +577,17 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
     }
     for (size_t i = 0; i < b->assets.size(); ++i) commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt);
     return RVH_OK;
+}
+
+}  // namespace
+}  // namespace rvh
+
+extern "C" {
+
+rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
+    TraceRange trace("rvh_batch_step");
+    if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_step: NULL argument");
+    return batch_step(b, frames, stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream, nullptr);
 }
 
 // Every pending asset's loop 3 in ONE persistent launch of gather-only items
@@ -611,6 +630,57 @@ rvh_status rvh_batch_check(rvh_batch* b) {
     return RVH_OK;
 }
 
+}  // extern "C"
+
+namespace rvh {
+namespace {
+
+// First use of a batch's position read-back: two staging slots, the pack
+// kernel's chunk table, the copy stream and its events.
+rvh_status ensure_staging(rvh_batch* b) {
+    if (b->copy_stream) return RVH_OK;
+    const size_t n4 = size_t(b->n_points) * 16u;
+    rvh_status st;
+    for (int i = 0; i < 2; ++i)
+        if ((st = b->ctx->alloc(b->pos_stage[i], n4)) != RVH_OK) return st;
+    std::vector<PackChunk> chunks;
+    long long acc = 0;
+    for (size_t a = 0; a < b->assets.size(); ++a) {
+        const int ns = b->assets[a]->n_strands, n = b->assets[a]->n_points;
+        const int per = std::max(1, 8192 / n);   // strands per chunk
+        for (int s0 = 0; s0 < ns; s0 += per) {
+            const int cnt = std::min(per, ns - s0);
+            chunks.push_back(PackChunk{int(a), s0, cnt, n, acc});
+            acc += (long long)cnt * n;
+        }
+    }
+    b->n_pack_chunks = int(chunks.size());
+    if ((st = b->ctx->alloc(b->d_first, sizeof(PackChunk) * std::max<size_t>(1, chunks.size()))) != RVH_OK) return st;
+    if (!chunks.empty())
+        RVH_CUDA(cudaMemcpy(b->d_first.ptr, chunks.data(), sizeof(PackChunk) * chunks.size(), cudaMemcpyHostToDevice));
+    RVH_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        RVH_CUDA(cudaEventCreateWithFlags(&b->packed[i], cudaEventDisableTiming));
+        RVH_CUDA(cudaEventCreateWithFlags(&b->copied[i], cudaEventDisableTiming));
+    }
+    return RVH_OK;
+}
+
+// The staged positions of `slot` are complete on stream s: copy them to the
+// host on the copy stream.
+rvh_status copy_out(rvh_batch* b, int slot, cudaStream_t s, void* host_dst, size_t bytes) {
+    RVH_CUDA(cudaEventRecord(b->packed[slot], s));
+    RVH_CUDA(cudaStreamWaitEvent(b->copy_stream, b->packed[slot], 0));
+    RVH_CUDA(cudaMemcpyAsync(host_dst, b->pos_stage[slot].ptr, bytes, cudaMemcpyDeviceToHost, b->copy_stream));
+    RVH_CUDA(cudaEventRecord(b->copied[slot], b->copy_stream));
+    return RVH_OK;
+}
+
+}  // namespace
+}  // namespace rvh
+
+extern "C" {
+
 rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t bytes, void* stream) {
     if (!b || (!host_dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: NULL argument");
     const size_t n4 = size_t(b->n_points) * 16u, n3 = size_t(b->n_points) * 12u;
@@ -620,31 +690,8 @@ rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t b
     const bool xyz = bytes == n3 && n3 != n4;
     cudaSetDevice(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
-    if (!b->copy_stream) {  // first use: staging, chunk table, copy stream
-        rvh_status st;
-        for (int i = 0; i < 2; ++i)
-            if ((st = b->ctx->alloc(b->pos_stage[i], n4)) != RVH_OK) return st;
-        std::vector<PackChunk> chunks;
-        long long acc = 0;
-        for (size_t a = 0; a < b->assets.size(); ++a) {
-            const int ns = b->assets[a]->n_strands, n = b->assets[a]->n_points;
-            const int per = std::max(1, 8192 / n);   // strands per chunk
-            for (int s0 = 0; s0 < ns; s0 += per) {
-                const int cnt = std::min(per, ns - s0);
-                chunks.push_back(PackChunk{int(a), s0, cnt, n, acc});
-                acc += (long long)cnt * n;
-            }
-        }
-        b->n_pack_chunks = int(chunks.size());
-        if ((st = b->ctx->alloc(b->d_first, sizeof(PackChunk) * std::max<size_t>(1, chunks.size()))) != RVH_OK) return st;
-        if (!chunks.empty())
-            RVH_CUDA(cudaMemcpy(b->d_first.ptr, chunks.data(), sizeof(PackChunk) * chunks.size(), cudaMemcpyHostToDevice));
-        RVH_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
-        for (int i = 0; i < 2; ++i) {
-            RVH_CUDA(cudaEventCreateWithFlags(&b->packed[i], cudaEventDisableTiming));
-            RVH_CUDA(cudaEventCreateWithFlags(&b->copied[i], cudaEventDisableTiming));
-        }
-    }
+    rvh_status st = ensure_staging(b);
+    if (st != RVH_OK) return st;
     const int slot = b->pos_slot;
     b->pos_slot ^= 1;
     RVH_CUDA(cudaStreamWaitEvent(s, b->copied[slot], 0));   // the copy that last read this slot is done
@@ -657,11 +704,25 @@ rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t b
     const void* fn = xyz ? reinterpret_cast<const void*>(&k_pack_positions<true>)
                          : reinterpret_cast<const void*>(&k_pack_positions<false>);
     RVH_CUDA(cudaLaunchKernel(fn, dim3(unsigned(blocks)), dim3(kThreads), args, 0, s));
-    RVH_CUDA(cudaEventRecord(b->packed[slot], s));
-    RVH_CUDA(cudaStreamWaitEvent(b->copy_stream, b->packed[slot], 0));
-    RVH_CUDA(cudaMemcpyAsync(host_dst, out, bytes, cudaMemcpyDeviceToHost, b->copy_stream));
-    RVH_CUDA(cudaEventRecord(b->copied[slot], b->copy_stream));
-    return RVH_OK;
+    return copy_out(b, slot, s, host_dst, bytes);
+}
+
+rvh_status rvh_batch_step_read_positions(rvh_batch* b, const rvh_frame* frames, void* host_dst, size_t bytes,
+                                         void* stream) {
+    TraceRange trace("rvh_batch_step_read_positions");
+    if (!b || (!host_dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "batch_step_read_positions: NULL argument");
+    if (bytes != size_t(b->n_points) * 12u)
+        return fail(RVH_ERR_INVALID_ARG, "batch_step_read_positions: size must be 12 (xyz) * total points");
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
+    if (!bytes) return batch_step(b, frames, s, nullptr);
+    cudaSetDevice(b->ctx->device);
+    rvh_status st = ensure_staging(b);
+    if (st != RVH_OK) return st;
+    const int slot = b->pos_slot;
+    b->pos_slot ^= 1;
+    RVH_CUDA(cudaStreamWaitEvent(s, b->copied[slot], 0));   // the copy that last read this slot is done
+    if ((st = batch_step(b, frames, s, static_cast<float*>(b->pos_stage[slot].ptr))) != RVH_OK) return st;
+    return copy_out(b, slot, s, host_dst, bytes);
 }
 
 rvh_status rvh_batch_positions_wait(rvh_batch* b) {

@@ -98,6 +98,9 @@ struct DevAsset {
     // (head: row-major 3 x 4 affine) before the FTL chain
     const float4* root_rest;
     float head[12];
+    // optional: the step also writes every point's new position (xyz, the root
+    // included) to pos_xyz[3 * (strand * n + i)], for a device-to-host copy
+    float* pos_xyz;
 };
 
 struct f3 {
@@ -559,6 +562,18 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
 
     // store x', v, corr for points 1..n-1 (the root is written only when a head moves it)
     if (moving && valid && l == 0) st_f4(rec, xn[0], 1.0f);
+    if (A.pos_xyz != nullptr && valid) {   // every point's position, the root included
+        float* o = A.pos_xyz + 3 * ((size_t)strand * n);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int i = PhaseA<NFIX, L>::point(l, k);
+            if (i < n) {
+                o[3 * i] = xn[k].x;
+                o[3 * i + 1] = xn[k].y;
+                o[3 * i + 2] = xn[k].z;
+            }
+        }
+    }
     unsigned mask = 0u;
 #pragma unroll
     for (int k = 0; k < K; ++k) {

@@ -58,6 +58,7 @@ PROTOTYPES = [
     ("rvh_batch_finish", _st, [_vp, _vp]),
     ("rvh_batch_info", _st, [_vp, _P(C.c_int32), _P(C.c_int32), _P(C.c_int32), _P(C.c_int64)]),
     ("rvh_batch_read_positions_async", _st, [_vp, _vp, C.c_size_t, _vp]),
+    ("rvh_batch_step_read_positions", _st, [_vp, _vp, _vp, C.c_size_t, _vp]),
     ("rvh_batch_positions_wait", _st, [_vp]),
     ("rvh_batch_box_stats", _st, [_vp, _P(C.c_uint32)]),
     ("rvh_batch_h2d_bytes", _st, [_vp, _P(C.c_uint64)]),

@@ -364,6 +364,12 @@ class Batch:
     def read_positions_async(self, host_ptr, nbytes, stream=None):
         check(self.lib.rvh_batch_read_positions_async(self.h, C.c_void_p(host_ptr), nbytes, stream))
 
+    def step_read_positions(self, frames, host_ptr, nbytes, stream=None):
+        """One step, then its positions (xyz per point) copied to host_ptr by the
+        step's own staging writes; positions_wait() blocks until the copy is done."""
+        arr = (T.Frame * max(1, len(frames)))(*frames)
+        check(self.lib.rvh_batch_step_read_positions(self.h, arr, C.c_void_p(host_ptr), nbytes, stream))
+
     def positions_wait(self):
         check(self.lib.rvh_batch_positions_wait(self.h))
 

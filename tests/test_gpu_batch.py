@@ -148,6 +148,42 @@ def test_batch_positions_read_back(gpu_ctx_fast, xyz):
     b.close()
 
 
+@pytest.mark.parametrize("exact", [True, False])
+@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+def test_step_read_positions(gpu_ctx, gpu_ctx_fast, exact, lanes):
+    """rvh_batch_step_read_positions: the step kernel's own xyz copy of every
+    point (a moving head's roots included) equals the assets' reads, and the
+    records equal those of a twin batch stepped without the copy."""
+    ctx = gpu_ctx if exact else gpu_ctx_fast
+    specs = configs.batched(n_assets=4, scale=0.02, seed=23)
+    twin = make_assets(ctx, specs)
+    assets = make_assets(ctx, specs)
+    pose = np.eye(4, dtype=np.float32)
+    pose[0, 3], pose[1, 3] = 0.05, -0.02
+    for a in (twin[1], assets[1]):
+        a.set_head_transform(pose)
+    b = api.Batch(ctx, assets, lanes=lanes)
+    bt = api.Batch(ctx, twin, lanes=lanes)
+    pts = b.info()["points"]
+    bufs = [api.PinnedBuffer(pts * 12) for _ in range(2)]
+    for k in range(3):
+        b.step_read_positions([s.frame(k) for s in specs], bufs[k % 2].ptr, pts * 12)
+        bt.step([s.frame(k) for s in specs])
+    b.positions_wait()
+    got = bufs[0].array((pts, 3)).copy()   # the last step went to slot 0
+    want = np.concatenate([a.read()[:, :s.n_points, :3].reshape(-1, 3) for a, s in zip(assets, specs)])
+    assert np.array_equal(got, want)
+    for a, t in zip(assets, twin):
+        assert np.array_equal(a.read(), t.read())
+    from rvh._lib import RvhError
+    with pytest.raises(RvhError):
+        b.step_read_positions([s.frame(3) for s in specs], bufs[0].ptr, pts * 16)   # xyz only
+    for p_ in bufs:
+        p_.close()
+    b.close()
+    bt.close()
+
+
 class _DeviceArray:
     """A view of device memory through __cuda_array_interface__ (no copy)."""
 
