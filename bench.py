@@ -233,7 +233,9 @@ def run_served(ctx, args, rank, lanes):
 def run_tess(ctx, api, configs, warmup=3, reps=10):
     """Strand tessellation of the 100k-strand head (32 points) after a few
     steps, with the reference's levels (12 isolines x 42 segments): device
-    time by CUDA events on the launching stream."""
+    time by CUDA events on the launching stream.  `ms`: pinned roots (the
+    reference's case), so the per-strand sd profiles come from the cache;
+    `ms_roots_moving`: a head motion before every call, every profile recomputed."""
     import torch
     spec = configs.full_head()
     a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest)
@@ -256,6 +258,21 @@ def run_tess(ctx, api, configs, warmup=3, reps=10):
     e1.record(st)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    # the same with the roots moving before every call (a head motion and a step
+    # in between): no cached sd profile applies, each call recomputes them all
+    pose = np.eye(4, dtype=np.float32)
+    moving = []
+    for k in range(warmup + reps):
+        pose[1, 3] = np.float32(0.001 * (k + 1))
+        a.set_head_transform(pose)
+        a.step(spec.frame(3 + k), stream=st.cuda_stream)
+        e0.record(st)
+        a.tessellate(out.data_ptr(), None, desc=d, stream=st.cuda_stream)
+        e1.record(st)
+        e1.synchronize()
+        if k >= warmup:
+            moving.append(e0.elapsed_time(e1))
+    ms_moving = sum(moving) / len(moving)
     a.close()
     vertices = ns * per
     alg = vertices * 16 + ns * spec.n_points * 16      # vertex writes + position reads
@@ -263,6 +280,7 @@ def run_tess(ctx, api, configs, warmup=3, reps=10):
     gbs = alg / (ms * 1e-3) / 1e9
     return {"workload": "100k strands x 32 points (the full head), 12 isolines x 42 segments per strand",
             "vertices": vertices, "ms": ms, "vertices_per_s": vertices / (ms * 1e-3),
+            "ms_roots_moving": ms_moving,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "bytes_per_launch": alg}}
 

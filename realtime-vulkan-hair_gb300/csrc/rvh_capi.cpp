@@ -619,6 +619,7 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     c->free(a->draw);
     c->free(a->root_rest);
     c->free(a->tess_tables);
+    c->free(a->tess_cache);
     delete a;
     return RVH_OK;
 }

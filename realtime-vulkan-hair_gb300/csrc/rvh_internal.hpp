@@ -125,6 +125,7 @@ struct Asset {
     DevBuf root_rest;   // float4 per strand, captured at the first head transform
     // tessellation tables of the last descriptor (rvh_asset_tessellate)
     DevBuf tess_tables;
+    DevBuf tess_cache;   // per strand: root bits and the sd profiles computed from them
     rvh_tess_desc tess_desc{};
     size_t tess_off[6] = {0, 0, 0, 0, 0, 0};
 

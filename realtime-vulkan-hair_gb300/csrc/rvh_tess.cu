@@ -29,7 +29,8 @@
 // The per-strand hash random(st) = fract(sin(dot(st, (12.9898, 78.233))) *
 // 43758.5453123) (:29-31) picks the sd profile; its sin is evaluated in double
 // and rounded once (a correctly rounded float sin), so every host and the GPU
-// agree.  All float arithmetic is separately rounded, in the shader's order.
+// agree.  The profiles are cached per strand with the root bits they came from
+// and recomputed only for strands whose root moved.  All float arithmetic is separately rounded, in the shader's order.
 // Two definitions where the shader is undefined: at v = 1 it reads point n
 // (out of bounds) — here the curve ends at the tip (last segment, t = 1); and
 // n is the asset's point count (the shader fixes 10).
@@ -83,13 +84,31 @@ struct TessTablesDev {
     const float* sw;
 };
 
+// Profile cache: the sd profile of (strand, isoline) depends only on the
+// strand's root and the isoline, and roots move only with a head motion (or a
+// write of the records).  Each strand keeps the root bits its cached profiles
+// were computed from; a strand whose root bits are unchanged reuses them, any
+// other strand recomputes (the same function, so the bits never differ).
+struct TessCacheDev {
+    uint4* roots;            // per strand: root x, y, z bits (w unused); all ones before the first call
+    unsigned char* prof;     // per strand: n_lines profiles
+};
+
 struct TessArgs {
     const float4* strands;
     int n_strands, n_points, n_lines, n_segments;
     TessTablesDev T;
+    TessCacheDev C;          // roots == nullptr: no cache
     float4* out;
     float4* frames;
 };
+
+__device__ __forceinline__ int tess_profile(float u, f3 root) {
+    const float choice = EM::mul(tess_random_dev(u, root.x), tess_random_dev(root.y, root.z));
+    int p = 0;
+    if (choice > 0.5f) p = choice > 0.9f ? 1 : choice > 0.8f ? 2 : choice > 0.7f ? 3 : choice > 0.6f ? 4 : 5;
+    return p;
+}
 
 __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_constant__ TessArgs A) {
     __shared__ f3 pts[kTessGroup][RVH_MAX_POINTS];
@@ -127,16 +146,33 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
                 }
             }
         }
-        // sd profile of (strand, isoline): randomChoice (hair.tese:253-283)
+        // sd profile of (strand, isoline): randomChoice (hair.tese:253-283), from
+        // the cache when the strand's root bits are those it was computed from
         for (int q = threadIdx.x; q < ng * L; q += kTessThreads) {
             const int g = (int)dL.div((unsigned)q), j = q - g * L;
             const f3 root = pts[g][0];
-            const float choice = EM::mul(tess_random_dev(A.T.u[j], root.x), tess_random_dev(root.y, root.z));
-            int p = 0;
-            if (choice > 0.5f) p = choice > 0.9f ? 1 : choice > 0.8f ? 2 : choice > 0.7f ? 3 : choice > 0.6f ? 4 : 5;
+            int p;
+            if (A.C.roots != nullptr) {
+                const uint4 cr = A.C.roots[s0 + g];
+                unsigned char* cp = A.C.prof + (size_t)(s0 + g) * L + j;
+                if (cr.x == __float_as_uint(root.x) && cr.y == __float_as_uint(root.y) &&
+                    cr.z == __float_as_uint(root.z)) {
+                    p = *cp;
+                } else {
+                    p = tess_profile(A.T.u[j], root);
+                    *cp = (unsigned char)p;
+                }
+            } else {
+                p = tess_profile(A.T.u[j], root);
+            }
             prof[g][j] = p;
         }
         __syncthreads();
+        if (A.C.roots != nullptr && threadIdx.x < ng) {   // every comparison above is done
+            const f3 root = pts[threadIdx.x][0];
+            A.C.roots[s0 + threadIdx.x] =
+                make_uint4(__float_as_uint(root.x), __float_as_uint(root.y), __float_as_uint(root.z), 0u);
+        }
         // the curve point c(v) of (strand, vertex k) is the same for every isoline:
         // one thread per (strand, k) evaluates it once and writes the strand's
         // n_lines vertices of column k (consecutive threads: consecutive k of one
@@ -265,6 +301,14 @@ rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vert
         RVH_CUDA(cudaMemcpy(a->tess_tables.ptr, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
         a->tess_desc = *d;
         std::memcpy(a->tess_off, off, sizeof off);
+        // a new descriptor: the profile cache starts empty (roots all ones, profiles 0);
+        // without room for it every call recomputes the profiles
+        a->ctx->free(a->tess_cache);
+        const size_t rb = size_t(a->n_strands) * 16u, pb = size_t(a->n_strands) * size_t(d->n_lines);
+        if (a->ctx->alloc(a->tess_cache, rb + ((pb + 15u) & ~size_t(15))) == RVH_OK) {
+            RVH_CUDA(cudaMemsetAsync(a->tess_cache.ptr, 0xff, rb, s));
+            RVH_CUDA(cudaMemsetAsync(static_cast<unsigned char*>(a->tess_cache.ptr) + rb, 0, pb, s));
+        }
     }
     const float* base = static_cast<const float*>(a->tess_tables.ptr);
     TessArgs A{};
@@ -275,6 +319,10 @@ rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vert
     A.n_segments = d->n_segments;
     A.T = TessTablesDev{base + a->tess_off[0], base + a->tess_off[1], base + a->tess_off[2],
                         base + a->tess_off[3], base + a->tess_off[4], base + a->tess_off[5]};
+    if (a->tess_cache.ptr) {
+        A.C.roots = static_cast<uint4*>(a->tess_cache.ptr);
+        A.C.prof = static_cast<unsigned char*>(a->tess_cache.ptr) + size_t(a->n_strands) * 16u;
+    }
     A.out = static_cast<float4*>(vertices);
     A.frames = static_cast<float4*>(frames);
     const long long groups = (a->n_strands + kTessGroup - 1) / kTessGroup;

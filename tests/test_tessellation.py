@@ -156,6 +156,46 @@ def test_gpu_tessellation_after_head_motion(gpu_ctx, oracle):
 
 
 @pytest.mark.gpu
+def test_gpu_tessellation_profile_cache_follows_the_roots(gpu_ctx, oracle):
+    """The sd profiles are cached per strand with the root bits they were
+    computed from.  Across calls, a moving head, a write that moves a few roots
+    and descriptor changes, every call still equals the oracle bit for bit."""
+    rec, rest, p, cols = api.generate_head(seed=29, n_strands=400, n_points=10, root_sampling=0, sort_roots=1,
+                                           length_min=0.3, length_max=0.9, head_collider=1, n_ellipsoids=0,
+                                           grid_res=0, friction=0.0, repulsion=0.0, dftl_damping=0.9)
+    a = api.Asset(gpu_ctx, rec, 10, rest=rest)
+    a.set_params(p)
+    a.set_colliders(cols)
+    ref = api.tess_desc_reference()
+    few = api.tess_desc_reference(n_lines=5, n_segments=17)
+
+    def check(desc):
+        got, _ = _gpu_tess(gpu_ctx, a, rec.shape[0], 10, desc, frames=False)
+        want = oracle.tessellate(a.read(), 10, desc.n_lines, desc.n_segments, sin_mode=1)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        return got
+
+    first = check(ref)
+    assert np.array_equal(check(ref).view(np.uint32), first.view(np.uint32))   # cached: same bits
+    for k in range(2):
+        m = np.eye(4, dtype=np.float32)
+        m[1, 3] = 0.07 * (k + 1)
+        a.set_head_transform(m)
+        a.step(api.T.frame(np.float32(1.0 / 60.0), np.float32((k + 1) / 60.0)))
+        check(ref)
+    a.set_head_transform(None)
+    state = a.read()
+    state[5, 0, :3] += np.float32(0.3)
+    state[17, 0, 0] = np.float32(5.0)
+    state[200, 0, 2] = np.float32(-1.25)
+    a.write(state)
+    check(ref)
+    check(few)
+    check(ref)
+    a.close()
+
+
+@pytest.mark.gpu
 def test_gpu_tessellation_rejects_bad_descriptors(gpu_ctx):
     from rvh._lib import RvhError
     rec, rest, p, cols = api.generate_head(seed=1, n_strands=8, n_points=8, root_sampling=0, sort_roots=0,
