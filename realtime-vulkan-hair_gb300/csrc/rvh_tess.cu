@@ -117,12 +117,28 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
     const int n = A.n_points, L = A.n_lines, S1 = A.n_segments + 1;
     const int per_strand = L * S1;
     const FastDiv dS1((unsigned)S1), dL((unsigned)L);
-    for (int s0 = blockIdx.x * kTessGroup; s0 < A.n_strands; s0 += gridDim.x * kTessGroup) {
+    // the group's points: slot t = threadIdx.x + m * kTessThreads holds point t % 32
+    // of strand t / 32; a thread's slots of the next group are loaded into
+    // registers while the current group's vertices are written
+    constexpr int kSlots = kTessGroup * RVH_MAX_POINTS / kTessThreads;
+    static_assert(kSlots * kTessThreads == kTessGroup * RVH_MAX_POINTS, "slots per thread");
+    const int stride = gridDim.x * kTessGroup;
+    float4 next[kSlots];
+    auto load_group = [&](int s) {
+        const int ngs = min(kTessGroup, A.n_strands - s);
+#pragma unroll
+        for (int m = 0; m < kSlots; ++m) {
+            const int t = threadIdx.x + m * kTessThreads, g = t / RVH_MAX_POINTS, i = t % RVH_MAX_POINTS;
+            if (s < A.n_strands && g < ngs && i < n) next[m] = A.strands[(size_t)(s + g) * (3 * n) + i];
+        }
+    };
+    load_group(blockIdx.x * kTessGroup);
+    for (int s0 = blockIdx.x * kTessGroup; s0 < A.n_strands; s0 += stride) {
         const int ng = min(kTessGroup, A.n_strands - s0);   // strands of this group
-        // the group's points: slot t holds point t % 32 of strand t / 32
-        for (int t = threadIdx.x; t < kTessGroup * RVH_MAX_POINTS; t += kTessThreads) {
-            const int g = t / RVH_MAX_POINTS, i = t % RVH_MAX_POINTS;
-            if (g < ng && i < n) pts[g][i] = xyz(A.strands[(size_t)(s0 + g) * (3 * n) + i]);
+#pragma unroll
+        for (int m = 0; m < kSlots; ++m) {
+            const int t = threadIdx.x + m * kTessThreads, g = t / RVH_MAX_POINTS, i = t % RVH_MAX_POINTS;
+            if (g < ng && i < n) pts[g][i] = xyz(next[m]);
         }
         __syncthreads();
         for (int t = threadIdx.x; t < kTessGroup * RVH_MAX_POINTS; t += kTessThreads) {
@@ -173,6 +189,7 @@ __global__ void __launch_bounds__(kTessThreads) k_tessellate(const __grid_consta
             A.C.roots[s0 + threadIdx.x] =
                 make_uint4(__float_as_uint(root.x), __float_as_uint(root.y), __float_as_uint(root.z), 0u);
         }
+        load_group(s0 + stride);   // in flight during the stores below
         // the curve point c(v) of (strand, vertex k) is the same for every isoline:
         // one thread per (strand, k) evaluates it once and writes the strand's
         // n_lines vertices of column k (consecutive threads: consecutive k of one
@@ -325,8 +342,15 @@ rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vert
     }
     A.out = static_cast<float4*>(vertices);
     A.frames = static_cast<float4*>(frames);
+    // one wave of resident CTAs, each walking its groups
+    static int per_sm = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tessellate, kTessThreads, 0) != cudaSuccess)
+            per_sm = 0;
+    });
     const long long groups = (a->n_strands + kTessGroup - 1) / kTessGroup;
-    const int blocks = (int)std::min<long long>(groups, (long long)a->ctx->sm_count * 8);
+    const int blocks = (int)std::min<long long>(groups, (long long)a->ctx->sm_count * std::max(1, per_sm));
     void* args[] = {&A};
     RVH_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(&k_tessellate), dim3(blocks), dim3(kTessThreads), args, 0, s));
     return RVH_OK;
