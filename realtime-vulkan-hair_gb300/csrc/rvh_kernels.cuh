@@ -600,6 +600,13 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
             par = head_point<M>(A.head, xyz(A.root_rest[strand]));
             st_f4(rec, par, 1.0f);
         }
+        // optional copy of every new position (the root included) for the host
+        float* const pxyz = A.pos_xyz != nullptr && valid ? A.pos_xyz + 3 * ((size_t)strand * n) : nullptr;
+        if (pxyz) {
+            pxyz[0] = par.x;
+            pxyz[1] = par.y;
+            pxyz[2] = par.z;
+        }
         LaneBounds sb;
         f3 vprev = {0.f, 0.f, 0.f};
         for (int i = 1; i < np; ++i) {
@@ -617,6 +624,11 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
             const f3 cor = v_scale<M>(A.dftl, v_sub<M>(xn, p));
             st_f4(rec + i, xn, 1.0f);
             st_f4(rec + 2 * n + i, cor, 0.0f);
+            if (pxyz) {
+                pxyz[3 * i] = xn.x;
+                pxyz[3 * i + 1] = xn.y;
+                pxyz[3 * i + 2] = xn.z;
+            }
             if (i >= 2) {   // point i-1: v -= corr_i / dt (compute.comp:213-215)
                 vprev = v_sub<M>(vprev, v_div<M>(cor, dt));
                 st_f4(rec + n + i - 1, vprev, 0.0f);

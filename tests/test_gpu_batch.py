@@ -149,7 +149,7 @@ def test_batch_positions_read_back(gpu_ctx_fast, xyz):
 
 
 @pytest.mark.parametrize("exact", [True, False])
-@pytest.mark.parametrize("lanes", [4, 8, 16, 32])
+@pytest.mark.parametrize("lanes", [1, 4, 8, 16, 32])
 def test_step_read_positions(gpu_ctx, gpu_ctx_fast, exact, lanes):
     """rvh_batch_step_read_positions: the step kernel's own xyz copy of every
     point (a moving head's roots included) equals the assets' reads, and the
