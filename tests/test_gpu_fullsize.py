@@ -6,8 +6,9 @@ batched workload (74.2 M points).  An FP64 oracle run of those sizes does not
 finish in seconds, so the checks are what holds at any size: one step against
 the FP64 oracle (1e-5 of strand length), inextensibility (segment length =
 rest length within 1e-6 of strand length), the root pinned, finite state,
-bitwise repeatability, and batch = per-asset plain steps (fast math: every
-kernel inlines the same device functions without implicit contraction).
+bitwise repeatability, batch = per-asset plain steps (fast math: every
+kernel inlines the same device functions without implicit contraction), and
+the positions a batched step stages for the host = the records it stored.
 """
 import numpy as np
 import pytest
@@ -70,10 +71,21 @@ def test_batched_workload_full_size(gpu_ctx_fast):
     assets = [_asset(gpu_ctx_fast, s) for s in specs]
     b = api.Batch(gpu_ctx_fast, assets, lanes=8)
     steps = 4
-    for k in range(steps):
+    pts = b.info()["points"]
+    assert pts == 74171408
+    host = api.PinnedBuffer(pts * 12)
+    for k in range(steps - 1):
         b.step([s.frame(k) for s in specs])
+    b.step_read_positions([s.frame(steps - 1) for s in specs], host.ptr, pts * 12)   # the step stages its xyz
+    b.positions_wait()
     b.check()
-    assert b.info()["points"] == 74171408
+    staged = host.array((pts, 3))
+    at = 0
+    for a, s in zip(assets, specs):
+        cnt = s.n_strands * s.n_points
+        assert np.array_equal(staged[at:at + cnt], a.read()[:, :s.n_points, :3].reshape(-1, 3))
+        at += cnt
+    host.close()
     picks = [0, 17, 128, 255]                   # plain steps of a few assets give the same bits
     for i in picks:
         s = specs[i]
