@@ -14,6 +14,8 @@ L2 (129 MB), so no flush is needed between steps.
           parameters from pinned host memory (H2D) and every curve point's
           position (xyz) back to host memory (D2H), all inside the timed region
           (rvh_batch_step_read_positions: the step kernel stages the positions).
+  full_head : the 100k-strand x 32-point head alone (plain step, and a
+          one-asset batch at 8, 16 and 32 lanes per strand), CUDA events.
   --impl reference : the oracle's OpenMP C++ restatement of the reference
           shader on the host cores (the reference itself is a Vulkan shader
           and has no CPU implementation), on a bounded sample of the workload.
@@ -228,6 +230,72 @@ def run_served(ctx, args, rank, lanes):
     for a in assets:
         a.close()
     return out, pts
+
+
+def run_full_head(ctx, api, configs, warmup=5, reps=20):
+    """The full single head (100,000 strands x 32 points, 64^3 grid, 4
+    ellipsoids + the head sphere, wind with gusts): per-step device time by
+    CUDA events on the launching stream, through the plain step (rvh_step:
+    one launch sequence) and through a one-asset batch (persistent launch in a
+    CUDA graph).  The records (154 MB) are a little larger than L2 (129 MB)."""
+    import torch
+    spec = configs.full_head()
+    st = torch.cuda.Stream()
+    n_pts = spec.n_strands * spec.n_points
+    cells = int(np.prod(list(spec.params.grid_dims)))
+    alg = 80 * n_pts + 16 * cells
+    peak, _ = load_peaks()
+    out = {"workload": "100k strands x 32 points, 64^3 grid, 4 ellipsoids + head sphere, wind with gusts",
+           "points_per_step": n_pts, "grid_cells": cells}
+
+    def timed(step_fn):
+        for k in range(warmup):
+            step_fn(k)
+        st.synchronize()
+        per = []
+        for k in range(warmup, warmup + reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            step_fn(k)
+            e1.record(st)
+            e1.synchronize()
+            per.append(e0.elapsed_time(e1))
+        per.sort()
+        ms = sum(per) / len(per)
+        gbs = alg / (ms * 1e-3) / 1e9
+        return {"ms_per_step": ms, "p50_step_ms": per[len(per) // 2], "p99_step_ms": per[-1],
+                "point_steps_per_s": n_pts / (ms * 1e-3),
+                "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                             "bytes_per_step": alg}}
+
+    def make():
+        a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest, strand_wind=spec.strand_wind)
+        a.set_params(spec.params)
+        a.set_colliders(spec.colliders_at(0))
+        return a
+
+    a = make()
+
+    def plain(k):
+        a.set_colliders(spec.colliders_at(k))
+        a.step(spec.frame(k), stream=st.cuda_stream)
+    out["plain"] = timed(plain)
+    a.close()
+    by_lanes = {}
+    for lanes in (8, 16, 32):   # every strand has 32 points: the lane count is tried, not assumed
+        a = make()
+        b = api.Batch(ctx, [a], lanes=lanes)
+
+        def batched(k):
+            a.set_colliders(spec.colliders_at(k))
+            b.step([spec.frame(k)], stream=st.cuda_stream)
+        by_lanes[lanes] = timed(batched)
+        b.close()
+        a.close()
+    best = min(by_lanes, key=lambda x: by_lanes[x]["ms_per_step"])
+    out["batched"] = dict(by_lanes[best], lanes_per_strand=best)
+    out["batched_ms_by_lanes"] = {str(k): v["ms_per_step"] for k, v in by_lanes.items()}
+    return out
 
 
 def run_tess(ctx, api, configs, warmup=3, reps=10):
@@ -449,6 +517,7 @@ def main():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-tess", action="store_true")
+    ap.add_argument("--no-full-head", action="store_true")
     ap.add_argument("--no-shade", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
@@ -592,6 +661,9 @@ def main():
                "sample": "first %d assets (%d points) of the workload, 3 steps, FP32 OpenMP restatement "
                          "of the reference shader" % (len(sample), spts)}
 
+    full = None
+    if world == 1 and not args.no_full_head:
+        full = run_full_head(ctx, api, configs)
     tess = None
     if world == 1 and not args.no_tess:
         tess = run_tess(ctx, api, configs)
@@ -639,7 +711,7 @@ def main():
                     "d2h_bytes_per_step": d2h, "api": "rvh_batch_step_read_positions",
                     "ms_per_step_with_packing_pass": e2e_pack_ms},
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
-            "shading": shade, "adjoint": adjoint,
+            "shading": shade, "adjoint": adjoint, "full_head": full,
             "served": None if served is None else {
                 "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
                             "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (
