@@ -268,19 +268,23 @@ def run_full_head(ctx, api, configs, warmup=5, reps=20):
                 "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                              "bytes_per_step": alg}}
 
-    def make():
-        a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest, strand_wind=spec.strand_wind)
+    def make(lanes=0):
+        a = api.Asset(ctx, spec.records, spec.n_points, rest=spec.rest, strand_wind=spec.strand_wind, lanes=lanes)
         a.set_params(spec.params)
         a.set_colliders(spec.colliders_at(0))
         return a
 
-    a = make()
+    plain_by_lanes = {}
+    for lanes in (0, 4, 8, 16, 32):   # 0: the asset's default for its point count
+        a = make(lanes)
 
-    def plain(k):
-        a.set_colliders(spec.colliders_at(k))
-        a.step(spec.frame(k), stream=st.cuda_stream)
-    out["plain"] = timed(plain)
-    a.close()
+        def plain(k):
+            a.set_colliders(spec.colliders_at(k))
+            a.step(spec.frame(k), stream=st.cuda_stream)
+        plain_by_lanes[lanes] = timed(plain)
+        a.close()
+    out["plain"] = plain_by_lanes[0]
+    out["plain_ms_by_lanes"] = {str(k): v["ms_per_step"] for k, v in plain_by_lanes.items() if k}
     by_lanes = {}
     for lanes in (8, 16, 32):   # every strand has 32 points: the lane count is tried, not assumed
         a = make()

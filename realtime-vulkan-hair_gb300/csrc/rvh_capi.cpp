@@ -120,9 +120,11 @@ DevCollider pack_collider(const rvh_collider& c) {
 
 // Fewest lanes per strand with a compiled phase-A kernel, starting from the
 // preferred count for n (point counts without a fixed-size kernel use the
-// generic one, which needs >= 4 lanes).
+// generic one, which needs >= 4 lanes).  Longer strands prefer 8 lanes: the
+// 100k-strand x 32-point head's plain step measured 0.41 / 0.28 / 0.30 / 0.37 ms
+// with 4 / 8 / 16 / 32 lanes per strand.
 int default_lanes(int n) {
-    const int pref = n <= 10 ? 1 : n <= 16 ? 2 : 4;
+    const int pref = n <= 10 ? 1 : n <= 16 ? 2 : 8;
     for (int l = pref; l <= 32; l *= 2)
         if (plain_a_supported(n, l)) return l;
     return pref;
