@@ -46,7 +46,8 @@ typedef struct rvh_asset_desc {
     float uniform_rest_length;    /* used when rest_lengths is NULL (reference 2.5/(n-1), compute.comp:139-140) */
     const float* rest_lengths;    /* optional host array: rest segment length per strand */
     const float* strand_wind;     /* optional host array: wind acceleration per strand (3 floats) */
-    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1,2,4,8,16,32 (strands per warp = 32/lanes) */
+    int32_t lanes_per_strand;     /* 0 = by point count: 1 up to 10 points, 2 up to 16, 8 above (or the next
+                                     compiled count); else 1,2,4,8,16,32 (strands per warp = 32/lanes) */
     int32_t reserved;
 } rvh_asset_desc;
 
@@ -309,7 +310,8 @@ rvh_status rvh_asset_restore(rvh_context* ctx, const void* host_src, uint64_t by
 
 /* ---- batching: many assets, one persistent launch in a CUDA graph ---------- */
 typedef struct rvh_batch_desc {
-    int32_t lanes_per_strand;     /* 0 = tuner's choice; else 1 (one thread walks each strand), 4, 8, 16, 32 */
+    int32_t lanes_per_strand;     /* 0 = tuner's choice (8 without a tuned record); else 1 (one thread walks
+                                     each strand), 4, 8, 16, 32 */
     int32_t strands_per_tile;     /* phase-A tile size; 0 = tuner's choice */
     int32_t ctas_per_sm;          /* 0 = occupancy limit */
     int32_t use_graph;            /* 1 = capture the launch in a CUDA graph (default) */

@@ -421,11 +421,11 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
             lanes = tr.lanes_per_strand;
             if (d.strands_per_tile == 0) d.strands_per_tile = tr.strands_per_tile;
         } else {
-            lanes = 4;
+            lanes = 8;   // the tuner's pick on the 256-head workload (4 lanes: 7.3-7.5 ms a step against 5.4 ms)
         }
         set_error(keep);
     }
-    if (!batch_supported(lanes)) return fail(RVH_ERR_UNSUPPORTED, "batch: lanes_per_strand must be 4, 8, 16 or 32");
+    if (!batch_supported(lanes)) return fail(RVH_ERR_UNSUPPORTED, "batch: lanes_per_strand must be 1, 4, 8, 16 or 32");
     cudaSetDevice(ctx->device);
     rvh_batch* b = new (std::nothrow) rvh_batch();
     if (!b) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");

@@ -322,9 +322,12 @@ rvh_status rvh_asset_tessellate(rvh_asset* a, const rvh_tess_desc* d, void* vert
         // without room for it every call recomputes the profiles
         a->ctx->free(a->tess_cache);
         const size_t rb = size_t(a->n_strands) * 16u, pb = size_t(a->n_strands) * size_t(d->n_lines);
+        const std::string keep = last_error_cstr();   // a cache that does not fit is not an error
         if (a->ctx->alloc(a->tess_cache, rb + ((pb + 15u) & ~size_t(15))) == RVH_OK) {
             RVH_CUDA(cudaMemsetAsync(a->tess_cache.ptr, 0xff, rb, s));
             RVH_CUDA(cudaMemsetAsync(static_cast<unsigned char*>(a->tess_cache.ptr) + rb, 0, pb, s));
+        } else {
+            set_error(keep);
         }
     }
     const float* base = static_cast<const float*>(a->tess_tables.ptr);
