@@ -537,8 +537,8 @@ namespace {
 rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, float* xyz) {
     if (!b || (!frames && !b->assets.empty())) return fail(RVH_ERR_INVALID_ARG, "batch_step: NULL argument");
     for (size_t i = 0; i < b->assets.size(); ++i) {
-        rvh_status s = validate_frame(frames[i]);
-        if (s != RVH_OK) return s;
+        const rvh_status vs = validate_frame(frames[i]);
+        if (vs != RVH_OK) return vs;
     }
     if (b->items.empty()) return RVH_OK;
     cudaSetDevice(b->ctx->device);
