@@ -177,7 +177,10 @@ def algorithmic_bytes(specs):
     return pts * BYTES_PER_POINT + cells * BYTES_PER_CELL, pts, cells
 
 
-def cpu_sample(specs, budget_points=3_000_000):
+CPU_SAMPLE_POINTS = 1_500_000   # points of the CPU legs' sample (about 10-30 s of CPU work in all)
+
+
+def cpu_sample(specs, budget_points=CPU_SAMPLE_POINTS):
     """A bounded sample of the workload for the CPU leg: whole assets taken in
     order until ~budget_points points."""
     out, pts = [], 0
@@ -457,6 +460,54 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
             "frame_ms": frame_ms}
 
 
+def run_error(ctx, api, specs, lanes, steps=120):
+    """FP64 error of the benchmarked step: the CPU legs' sample of the batched
+    workload (its leading assets), fresh from the generator, stepped `steps`
+    times through the batched launch (fast math, the timed lane count), then
+    compared with the FP64 oracle over the same frames.  The FP32 twin (the
+    reference shader's own arithmetic) is reported beside it, and both again
+    over the well-conditioned strands (oracle/errors.py)."""
+    from oracle import errors as E
+    from oracle import oracle_ctypes as O
+    sample, pts = cpu_sample(specs)
+    assets = make_assets(ctx, sample)
+    b = api.Batch(ctx, assets, lanes=lanes)
+    for k in range(steps):
+        b.step([s.frame(k) for s in sample])
+    b.finish()
+    b.check()
+    got = [a.read() for a in assets]
+    b.close()
+    for a in assets:
+        a.close()
+    thr = O.max_threads()
+    ef, et, wf, wt = [], [], [], []
+    seg, n_well, n_all = 0.0, 0, 0
+    for g, s in zip(got, sample):
+        L = E.lengths(s.rest, s.n_points)
+        ref = E.run_spec(s, steps, np.float64, thr)
+        twin = E.run_spec(s, steps, np.float32, thr)
+        well = E.spread(s, steps, ref, thr) <= 1e-4
+        e_f, e_t = E.point_errors(g, ref, s.n_points, L), E.point_errors(twin, ref, s.n_points, L)
+        ef.append(e_f.reshape(-1))
+        et.append(e_t.reshape(-1))
+        wf.append(e_f[well].reshape(-1))
+        wt.append(e_t[well].reshape(-1))
+        seg = max(seg, E.segment_error(g, s.rest, s.n_points))
+        n_well += int(well.sum())
+        n_all += s.n_strands
+    cat = np.concatenate
+    return {"steps": steps, "vs": "FP64 oracle", "unit": "|x - x_fp64| / strand length, per curve point",
+            "sample": "first %d assets (%d points) of the workload, batched launch, fast math, lanes %d"
+                      % (len(sample), pts, lanes),
+            "fast": E.summary(cat(ef)), "reference_fp32": E.summary(cat(et)),
+            "well_conditioned": {"strands": n_well, "of": n_all, "fast": E.summary(cat(wf)),
+                                 "reference_fp32": E.summary(cat(wt))},
+            "seg_len_max": seg,
+            "note": "reference_fp32 = the oracle's FP32 twin, bit-identical to the reference shader's arithmetic; "
+                    "well-conditioned = FP64 spread of a 1e-7 L initial perturbation <= 1e-4 L after the same steps"}
+
+
 def run_adjoint(ctx, api, configs, reps=3):
     """The differentiable step: 4,096 strands x 32 points over 60 steps, the FP32
     adjoint of the tip loss with checkpoints every 10 steps (forward, per-segment
@@ -478,16 +529,30 @@ def run_adjoint(ctx, api, configs, reps=3):
             "ms": ms, "ms_per_step": ms / 60, "point_steps_per_s": pts * 60 / (ms * 1e-3)}
 
 
+def cpu_sample_count(n_assets, budget_points=CPU_SAMPLE_POINTS):
+    """How many leading assets of the batched workload cpu_sample takes."""
+    from rvh import configs
+    pts = 0
+    for i, (ns, n, _, _) in enumerate(configs.batched_sizes(n_assets)):
+        pts += ns * n
+        if pts >= budget_points:
+            return i + 1
+    return n_assets
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the oracle's OpenMP restatement on the host cores."""
+    """--impl reference: the oracle's OpenMP restatement on the host cores.
+    The workload sample comes from the oracle's own statement of the seeded
+    generator (oracle/scene_oracle.hpp), so this process never maps the CUDA
+    library; it is byte for byte the sample the GPU arm's cpu_baseline times."""
     if rank != 0:
         return
-    import __graft_entry__
-    __graft_entry__.build()   # the scene generator (host C++) makes the inputs
+    from oracle import build as oracle_build
+    oracle_build.build()
     from oracle import oracle_ctypes as O
     from rvh import configs
-    specs = configs.batched()
-    sample, pts = cpu_sample(specs, 1_500_000)
+    specs = configs.batched(n_assets=args.assets, gen=O.SceneGen(), indices=range(cpu_sample_count(args.assets)))
+    sample, pts = cpu_sample(specs)
     threads = O.max_threads()
     time_cpu(sample, 1, threads)  # warm-up
     per_step = []
@@ -524,6 +589,7 @@ def main():
     ap.add_argument("--no-full-head", action="store_true")
     ap.add_argument("--no-shade", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
     args = ap.parse_args()
@@ -658,12 +724,16 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle import oracle_ctypes as O
-        sample, spts = cpu_sample(specs, 1_500_000)
+        sample, spts = cpu_sample(specs)
         threads = O.max_threads()
         v, dt = time_cpu(sample, 3, threads)
         cpu = {"value": v, "unit": "point-steps/s", "cores": threads, "kind": "port",
                "sample": "first %d assets (%d points) of the workload, 3 steps, FP32 OpenMP restatement "
                          "of the reference shader" % (len(sample), spts)}
+
+    err = None
+    if rank == 0 and world == 1 and not args.no_error:
+        err = run_error(ctx, api, specs, info["lanes"])
 
     full = None
     if world == 1 and not args.no_full_head:
@@ -714,6 +784,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "point-steps/s", "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "rvh_batch_step_read_positions",
                     "ms_per_step_with_packing_pass": e2e_pack_ms},
+            "error": err,
             "cpu_baseline": cpu, "clocks": clk, "gpu_launches": int(launches), "tessellation": tess,
             "shading": shade, "adjoint": adjoint, "full_head": full,
             "served": None if served is None else {

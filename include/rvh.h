@@ -146,9 +146,11 @@ rvh_status rvh_step(rvh_asset* a, const rvh_frame* frame, void* stream);
  * (8 MiB per GPU that loads the library, held until exit).  Larger grids are
  * rejected with RVH_ERR_INVALID_ARG.  Each call clears the grid cells it
  * uses; calls on one device whose work overlaps on the GPU race on the shared
- * array.  The first call on a device looks up the array's address and should
+ * array.  The first call on a device (and the first after its context was
+ * torn down, e.g. by cudaDeviceReset) looks up the array's address and should
  * come before any stream capture.  Same results as rvh_step on an asset with
- * the same state, params, colliders and math mode. */
+ * the same state, params, colliders and math mode; with n_strands = 0 it only
+ * writes the draw record (vertex_count 0). */
 #define RVH_NOALLOC_MAX_GRID_CELLS (64 * 64 * 64)
 typedef struct rvh_noalloc_step_desc {
     void* strands;                /* device: n_strands Strand records, updated in place */

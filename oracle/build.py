@@ -11,7 +11,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
-SOURCES = ["oracle_capi.cpp", "hair_oracle.hpp", "hair_adjoint.hpp", "tess_oracle.hpp", "shade_oracle.hpp"]
+SOURCES = ["oracle_capi.cpp", "hair_oracle.hpp", "hair_adjoint.hpp", "tess_oracle.hpp", "shade_oracle.hpp",
+           "scene_oracle.hpp"]
 
 
 def _stale(out, deps):
@@ -23,7 +24,7 @@ def _stale(out, deps):
 
 def build(force=False, verbose=False):
     deps = [os.path.join(HERE, s) for s in SOURCES]
-    deps.append(os.path.join(HERE, "..", "include", "rvh_types.h"))
+    deps += [os.path.join(HERE, "..", "include", h) for h in ("rvh_types.h", "rvh_scene.h")]
     if not force and not _stale(LIB, deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)

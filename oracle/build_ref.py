@@ -1,7 +1,7 @@
 """Compile the REFERENCE's own compute shader as C++ (TEST INFRASTRUCTURE ONLY).
 
 Reads src/shaders/compute.comp where it lies (under the reference checkout,
-default /root/reference, or $RVH_REFERENCE_DIR), rewrites only the GLSL-only
+the directory $RVH_REFERENCE_DIR names), rewrites only the GLSL-only
 declarations into C++ in memory, and pipes the result to g++ together with
 oracle/ref_harness.hpp (prelude) and oracle/ref_driver.inc (dispatch loop),
 against the reference's vendored glm (external/glm).  No rewritten copy of the
@@ -31,12 +31,13 @@ LIB = os.path.join(OUT_DIR, "libref_shader.so")
 
 
 def reference_dir():
-    return os.environ.get("RVH_REFERENCE_DIR", "/root/reference")
+    """The reference checkout named by $RVH_REFERENCE_DIR, or None."""
+    return os.environ.get("RVH_REFERENCE_DIR") or None
 
 
 def available():
     r = reference_dir()
-    return (os.path.isfile(os.path.join(r, "src", "shaders", "compute.comp"))
+    return r is not None and (os.path.isfile(os.path.join(r, "src", "shaders", "compute.comp"))
             and os.path.isdir(os.path.join(r, "external", "glm", "glm")))
 
 

@@ -2,7 +2,7 @@
 
 GeneratePointsOnMesh (src/Strand.cpp:11-146: generateRandomFloat,
 generateRandomInt and the sampler) is read where it lies under the reference
-checkout (default /root/reference, or $RVH_REFERENCE_DIR), cut out of
+checkout (the directory $RVH_REFERENCE_DIR names), cut out of
 Strand.cpp in memory (the rest of that file needs Vulkan), and piped to g++
 together with the reference's vendored tiny_obj_loader (src/tiny_obj_loader.h)
 and glm (external/glm).  NUM_STRANDS becomes a variable the wrapper sets.  No
@@ -24,7 +24,8 @@ LIB = os.path.join(OUT_DIR, "libref_roots.so")
 
 
 def reference_dir():
-    return os.environ.get("RVH_REFERENCE_DIR", "/root/reference")
+    """The reference checkout named by $RVH_REFERENCE_DIR, or None."""
+    return os.environ.get("RVH_REFERENCE_DIR") or None
 
 
 def _paths():
@@ -34,6 +35,8 @@ def _paths():
 
 
 def available():
+    if reference_dir() is None:
+        return False
     strand, tinyobj, glm = _paths()
     return os.path.isfile(strand) and os.path.isfile(tinyobj) and os.path.isdir(os.path.join(glm, "glm"))
 

@@ -2,7 +2,7 @@
 
 Reads src/shaders/hair.frag and src/shaders/hairOpacity.frag where they lie
 (under the reference checkout,
-default /root/reference, or $RVH_REFERENCE_DIR), rewrites only the GLSL-only
+the directory $RVH_REFERENCE_DIR names), rewrites only the GLSL-only
 declarations into C++ in memory and pipes the result to g++ against the
 reference's vendored glm (external/glm), with the float literal and swizzle
 rewrites of oracle/build_ref.py plus:
@@ -59,7 +59,7 @@ def _shader(name="hair.frag"):
 
 
 def available():
-    return os.path.isfile(_shader()) and os.path.isfile(_shader("hairOpacity.frag")) and os.path.isdir(os.path.join(reference_dir(), "external", "glm", "glm"))
+    return reference_dir() is not None and os.path.isfile(_shader()) and os.path.isfile(_shader("hairOpacity.frag")) and os.path.isdir(os.path.join(reference_dir(), "external", "glm", "glm"))
 
 
 PRELUDE = r"""

@@ -1,7 +1,7 @@
 """Compile the REFERENCE's own tessellation shader as C++ (TEST INFRASTRUCTURE ONLY).
 
 Reads src/shaders/hair.tese where it lies (under the reference checkout,
-default /root/reference, or $RVH_REFERENCE_DIR), rewrites only the GLSL-only
+the directory $RVH_REFERENCE_DIR names), rewrites only the GLSL-only
 declarations into C++ in memory and pipes the result to g++ against the
 reference's vendored glm (external/glm), with the float literal, swizzle and
 uniform-block rewrites of oracle/build_ref.py plus:
@@ -45,7 +45,7 @@ def _shader():
 
 
 def available():
-    return os.path.isfile(_shader()) and os.path.isdir(os.path.join(reference_dir(), "external", "glm", "glm"))
+    return reference_dir() is not None and os.path.isfile(_shader()) and os.path.isdir(os.path.join(reference_dir(), "external", "glm", "glm"))
 
 
 PRELUDE = r"""

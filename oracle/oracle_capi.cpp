@@ -12,6 +12,7 @@
 
 #include "hair_adjoint.hpp"
 #include "hair_oracle.hpp"
+#include "scene_oracle.hpp"
 #include "shade_oracle.hpp"
 #include "tess_oracle.hpp"
 
@@ -207,5 +208,20 @@ int oracle_loss_f64(const double* state0, int ns, int n, const double* rest, con
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+/* The seeded synthetic head of include/rvh_scene.h, from scene_oracle.hpp:
+ * records = ns*12*n floats, rest = ns floats, params and up to
+ * RVH_MAX_COLLIDERS colliders (either may be NULL). */
+int oracle_generate_head(const rvh_head_desc* d, float* records, float* rest, rvh_sim_params* params,
+                         rvh_collider* colliders, int32_t* n_colliders) {
+    return oracle::scene::head(d, records, rest, params, colliders, n_colliders);
+}
+
+/* Wind of frame `step` at time t (scene_oracle.hpp). */
+int oracle_wind_at(const rvh_wind_desc* w, int64_t step, float t, float* out) {
+    if (!w || !out) return 1;
+    oracle::scene::wind(w, step, t, out);
+    return 0;
+}
 
 }  // extern "C"

@@ -61,6 +61,11 @@ def lib():
                   l.oracle_adjoint_f64, l.oracle_loss_f64):
             f.restype = C.c_int
         l.oracle_max_threads.restype = C.c_int
+        l.oracle_generate_head.argtypes = [_P(T.HeadDesc), C.c_void_p, _P(C.c_float), _P(T.SimParams),
+                                           _P(T.Collider), _P(C.c_int32)]
+        l.oracle_generate_head.restype = C.c_int
+        l.oracle_wind_at.argtypes = [_P(T.WindDesc), C.c_int64, C.c_float, _P(C.c_float)]
+        l.oracle_wind_at.restype = C.c_int
         _lib = l
     return _lib
 
@@ -162,6 +167,35 @@ def loss(state0, n_points, rest, params, frames, colliders, n_steps, targets, st
     if rc != 0:
         raise RuntimeError("oracle_loss failed: %d" % rc)
     return out[0]
+
+
+class SceneGen:
+    """The seeded synthetic inputs (include/rvh_scene.h) from the oracle's own
+    statement of them (scene_oracle.hpp): rvh.configs builds a workload with
+    it when given gen=SceneGen(), so the CPU timing arm of bench.py never
+    maps the CUDA library.  Same calls and results as rvh.api's."""
+
+    @staticmethod
+    def generate_head(**kw):
+        d = T.head_desc(**kw)
+        ns, n = d.n_strands, d.n_points
+        rec = np.empty((ns, 3 * n, 4), np.float32)
+        rest = np.empty(max(ns, 1), np.float32)
+        p = T.SimParams()
+        cols = (T.Collider * T.MAX_COLLIDERS)()
+        nc = C.c_int32()
+        rc = lib().oracle_generate_head(C.byref(d), rec.ctypes.data_as(C.c_void_p), _fptr(rest, C.c_float),
+                                        C.byref(p), cols, C.byref(nc))
+        if rc != 0:
+            raise RuntimeError("oracle_generate_head failed: %d" % rc)
+        return rec, rest[:ns], p, [cols[i] for i in range(nc.value)]
+
+    @staticmethod
+    def wind_at(desc, step, t):
+        out = (C.c_float * 3)()
+        if lib().oracle_wind_at(C.byref(desc), step, t, out) != 0:
+            raise RuntimeError("oracle_wind_at failed")
+        return tuple(out)
 
 
 def max_threads():

@@ -279,7 +279,7 @@ rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, i
         if (st != RVH_OK) return st;
     }
     Context* ctx = a->ctx;
-    cudaSetDevice(ctx->device);
+    RVH_DEVICE(ctx->device);
     const int ns = a->n_strands, n = a->n_points;
     if (ns == 0) {
         *loss = 0.0;

@@ -426,7 +426,7 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
         set_error(keep);
     }
     if (!batch_supported(lanes)) return fail(RVH_ERR_UNSUPPORTED, "batch: lanes_per_strand must be 1, 4, 8, 16 or 32");
-    cudaSetDevice(ctx->device);
+    RVH_DEVICE(ctx->device);
     rvh_batch* b = new (std::nothrow) rvh_batch();
     if (!b) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->ctx = ctx;
@@ -541,7 +541,7 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
         if (vs != RVH_OK) return vs;
     }
     if (b->items.empty()) return RVH_OK;
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     const int slot = b->slot;
     b->slot ^= 1;
     RVH_CUDA(cudaEventSynchronize(b->staged[slot]));  // the copy that last read this staging buffer is done
@@ -596,7 +596,7 @@ rvh_status rvh_batch_step(rvh_batch* b, const rvh_frame* frames, void* stream) {
 rvh_status rvh_batch_finish(rvh_batch* b, void* stream) {
     TraceRange trace("rvh_batch_finish");
     if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_finish: NULL");
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
     std::vector<Asset*> pend;
     for (Asset* a : b->assets)
@@ -617,7 +617,7 @@ rvh_status rvh_batch_finish(rvh_batch* b, void* stream) {
 
 rvh_status rvh_batch_check(rvh_batch* b) {
     if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_check: NULL");
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(b->ctx->stream));
     RVH_CUDA(cudaDeviceSynchronize());
     int err = 0;
@@ -688,7 +688,7 @@ rvh_status rvh_batch_read_positions_async(rvh_batch* b, void* host_dst, size_t b
         return fail(RVH_ERR_INVALID_ARG, "batch_read_positions: size must be 16 (float4) or 12 (xyz) * total points");
     if (!bytes) return RVH_OK;
     const bool xyz = bytes == n3 && n3 != n4;
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
     rvh_status st = ensure_staging(b);
     if (st != RVH_OK) return st;
@@ -715,7 +715,7 @@ rvh_status rvh_batch_step_read_positions(rvh_batch* b, const rvh_frame* frames, 
         return fail(RVH_ERR_INVALID_ARG, "batch_step_read_positions: size must be 12 (xyz) * total points");
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : b->ctx->stream;
     if (!bytes) return batch_step(b, frames, s, nullptr);
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     rvh_status st = ensure_staging(b);
     if (st != RVH_OK) return st;
     const int slot = b->pos_slot;
@@ -728,7 +728,7 @@ rvh_status rvh_batch_step_read_positions(rvh_batch* b, const rvh_frame* frames, 
 rvh_status rvh_batch_positions_wait(rvh_batch* b) {
     if (!b) return fail(RVH_ERR_INVALID_ARG, "batch_positions_wait: NULL");
     if (!b->copy_stream) return RVH_OK;
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(b->copy_stream));
     return RVH_OK;
 }
@@ -763,7 +763,7 @@ rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launch
 
 rvh_status rvh_batch_box_stats(rvh_batch* b, uint32_t out[4]) {
     if (!b || !out) return fail(RVH_ERR_INVALID_ARG, "batch_box_stats: NULL");
-    cudaSetDevice(b->ctx->device);
+    RVH_DEVICE(b->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(b->ctx->stream));
     RVH_CUDA(cudaMemcpy(out, b->d_stats.ptr, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost));
     RVH_CUDA(cudaMemset(b->d_stats.ptr, 0, 4 * sizeof(unsigned)));

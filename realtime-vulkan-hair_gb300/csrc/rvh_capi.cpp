@@ -265,18 +265,6 @@ using namespace rvh;
 namespace {
 cudaStream_t pick_stream(rvh_asset* a, void* s) { return s ? static_cast<cudaStream_t>(s) : a->ctx->stream; }
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 // 4x4 column-major float matrices as used by the reference (glm).
 struct M4 {
@@ -418,7 +406,7 @@ rvh_status rvh_context_create(const rvh_context_desc* desc, rvh_context** out) {
 
 rvh_status rvh_context_destroy(rvh_context* ctx) {
     if (!ctx) return RVH_OK;
-    DeviceGuard g(ctx->device);
+    RVH_DEVICE(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -427,7 +415,7 @@ rvh_status rvh_context_destroy(rvh_context* ctx) {
 
 rvh_status rvh_context_synchronize(rvh_context* ctx) {
     if (!ctx) return fail(RVH_ERR_INVALID_ARG, "ctx is NULL");
-    DeviceGuard g(ctx->device);
+    RVH_DEVICE(ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
     return RVH_OK;
 }
@@ -552,7 +540,7 @@ rvh_status rvh_asset_create(rvh_context* ctx, const rvh_asset_desc* desc, rvh_as
     const int lanes = d.lanes_per_strand ? d.lanes_per_strand : default_lanes(d.n_points);
     if (!plain_a_supported(d.n_points, lanes))
         return fail(RVH_ERR_UNSUPPORTED, "asset_create: lanes_per_strand not supported for this n_points");
-    DeviceGuard g(ctx->device);
+    RVH_DEVICE(ctx->device);
     rvh_asset* a = new (std::nothrow) rvh_asset();
     if (!a) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");
     a->ctx = ctx;
@@ -611,7 +599,7 @@ rvh_status rvh_asset_create(rvh_context* ctx, const rvh_asset_desc* desc, rvh_as
 
 rvh_status rvh_asset_destroy(rvh_asset* a) {
     if (!a) return RVH_OK;
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     cudaStreamSynchronize(a->ctx->stream);
     Context* c = a->ctx;
     c->free(a->strands);
@@ -630,7 +618,7 @@ rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p) {
     if (!a || !p) return fail(RVH_ERR_INVALID_ARG, "set_params: NULL argument");
     rvh_status s = validate_params(*p);
     if (s != RVH_OK) return s;
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     s = finish_pending(a, a->ctx->stream);  // the pending gather uses the old grid geometry
     if (s != RVH_OK) return s;
     a->params = *p;
@@ -662,7 +650,7 @@ rvh_status rvh_asset_set_head_transform(rvh_asset* a, const float m[16]) {
     if (!affine_finite(m)) return fail(RVH_ERR_INVALID_ARG, "set_head_transform: m must be a finite affine matrix");
     if (!a->root_rest.ptr && a->n_strands > 0) {
         // the roots now are the rest pose of m = identity (roots never move without a head motion)
-        DeviceGuard g(a->ctx->device);
+        RVH_DEVICE(a->ctx->device);
         rvh_status s = a->ctx->alloc(a->root_rest, size_t(a->n_strands) * 16u);
         if (s != RVH_OK) return s;
         RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
@@ -679,7 +667,7 @@ rvh_status rvh_asset_set_rest_lengths(rvh_asset* a, const float* rest) {
     for (int i = 0; i < a->n_strands; ++i)
         if (!std::isfinite(rest[i]) || rest[i] < 0.f) return fail(RVH_ERR_INVALID_ARG, "set_rest_lengths: bad value");
     if (!a->n_strands) return RVH_OK;
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
     RVH_CUDA(cudaMemcpy(a->rest.ptr, rest, sizeof(float) * a->n_strands, cudaMemcpyHostToDevice));
     return RVH_OK;
@@ -687,7 +675,7 @@ rvh_status rvh_asset_set_rest_lengths(rvh_asset* a, const float* rest) {
 
 rvh_status rvh_asset_set_strand_wind(rvh_asset* a, const float* wind3) {
     if (!a) return fail(RVH_ERR_INVALID_ARG, "set_strand_wind: NULL asset");
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
     if (!wind3 || !a->n_strands) {
         a->has_wind = false;
@@ -730,7 +718,7 @@ rvh_status rvh_asset_strand_count(rvh_asset* a, int32_t* ns, int32_t* n) {
 rvh_status rvh_asset_read(rvh_asset* a, void* dst, size_t bytes) {
     if (!a || (!dst && bytes)) return fail(RVH_ERR_INVALID_ARG, "asset_read: NULL argument");
     if (bytes != a->record_bytes()) return fail(RVH_ERR_INVALID_ARG, "asset_read: size must be 48*n_points*n_strands");
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     rvh_status fs = finish_pending(a, a->ctx->stream);
     if (fs != RVH_OK) return fs;
     RVH_CUDA(cudaDeviceSynchronize());
@@ -741,7 +729,7 @@ rvh_status rvh_asset_read(rvh_asset* a, void* dst, size_t bytes) {
 rvh_status rvh_asset_write(rvh_asset* a, const void* src, size_t bytes) {
     if (!a || (!src && bytes)) return fail(RVH_ERR_INVALID_ARG, "asset_write: NULL argument");
     if (bytes != a->record_bytes()) return fail(RVH_ERR_INVALID_ARG, "asset_write: size must be 48*n_points*n_strands");
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
     a->pending = false;  // the new state carries no pending friction
     if (bytes) RVH_CUDA(cudaMemcpy(a->strands.ptr, src, bytes, cudaMemcpyHostToDevice));
@@ -753,7 +741,7 @@ rvh_status rvh_asset_read_positions_async(rvh_asset* a, void* dst, size_t bytes,
     const size_t need = size_t(a->n_strands) * a->n_points * 16u;
     if (bytes != need) return fail(RVH_ERR_INVALID_ARG, "read_positions: size must be 16*n_points*n_strands");
     if (!need) return RVH_OK;
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     cudaStream_t s = pick_stream(a, stream);
     // curvePoints[n] is the first 16*n bytes of each 48*n-byte record: one strided 2-D copy.
     RVH_CUDA(cudaMemcpy2DAsync(dst, 16u * a->n_points, a->strands.ptr, 48u * a->n_points, 16u * a->n_points,
@@ -763,7 +751,7 @@ rvh_status rvh_asset_read_positions_async(rvh_asset* a, void* dst, size_t bytes,
 
 rvh_status rvh_asset_read_draw(rvh_asset* a, rvh_draw_indirect* out) {
     if (!a || !out) return fail(RVH_ERR_INVALID_ARG, "read_draw: NULL argument");
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
     RVH_CUDA(cudaMemcpy(out, a->draw.ptr, sizeof(*out), cudaMemcpyDeviceToHost));
     return RVH_OK;
@@ -773,7 +761,7 @@ rvh_status rvh_asset_read_grid(rvh_asset* a, int64_t* dst, size_t bytes) {
     if (!a || !dst) return fail(RVH_ERR_INVALID_ARG, "read_grid: NULL argument");
     if (!a->params.grid_enabled) return fail(RVH_ERR_STATE, "read_grid: the grid is disabled");
     if (bytes != a->grid_bytes()) return fail(RVH_ERR_INVALID_ARG, "read_grid: size must be 32*cells");
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
     if (a->last_grid < 0) return fail(RVH_ERR_STATE, "read_grid: no step has splatted yet");
     RVH_CUDA(cudaMemcpy(dst, a->grid[a->last_grid].ptr, bytes, cudaMemcpyDeviceToHost));
@@ -786,7 +774,7 @@ rvh_status rvh_step(rvh_asset* a, const rvh_frame* frame, void* stream) {
     rvh_status s = validate_frame(*frame);
     if (s != RVH_OK) return s;
     if (a->n_strands == 0) return RVH_OK;
-    DeviceGuard g(a->ctx->device);
+    RVH_DEVICE(a->ctx->device);
     return launch_plain(a, *frame, pick_stream(a, stream));
 }
 

@@ -88,7 +88,7 @@ rvh_status rvh_asset_health(rvh_asset* a, rvh_health* out) {
     *out = rvh_health{};
     out->worst_strand = -1;
     if (a->n_strands == 0) return RVH_OK;
-    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    RVH_DEVICE(a->ctx->device);
     rvh_status st = finish_pending(a, a->ctx->stream);
     if (st != RVH_OK) return st;
     DevBuf buf;

@@ -32,6 +32,28 @@ rvh_status cuda_fail(cudaError_t e, const char* what);
         if (e_ != cudaSuccess) return ::rvh::cuda_fail(e_, #call);  \
     } while (0)
 
+// Makes `dev` current for the guard's lifetime and puts the caller's device
+// back afterwards, so no entry point leaks a device switch into host code
+// that drives several GPUs.  RVH_DEVICE(dev) declares one and returns the
+// CUDA error when the switch fails.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+#define RVH_DEVICE(dev)                                                                         \
+    ::rvh::DeviceGuard rvh_device_guard_(dev);                                                  \
+    if (rvh_device_guard_.err != cudaSuccess) return ::rvh::cuda_fail(rvh_device_guard_.err, "cudaSetDevice")
+
 // ---- HBM admission accounting --------------------------------------------------
 // Every device allocation a context makes is admitted against its budget
 // first; a request that would exceed it fails with RVH_ERR_BUDGET and

@@ -87,6 +87,34 @@ bool fix_index(long idx, size_t n, int* out) {
     return true;
 }
 
+// ---- in_triangle and triangulate: derived from tiny_obj_loader 2.0 ----------
+// They restate the polygon triangulation of tiny_obj_loader 2.0 (the loader
+// the reference vendors, src/tiny_obj_loader.h:1314-1326 and :1380-1500), so
+// that triangle t of a mesh is the reference's triangle t.  That code is
+// distributed under the MIT License:
+//
+//   The MIT License (MIT)
+//
+//   Copyright (c) 2012-2018 Syoyo Fujita and many contributors.
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a copy
+//   of this software and associated documentation files (the "Software"), to deal
+//   in the Software without restriction, including without limitation the rights
+//   to use, copy, modify, merge, publish, distribute, sublicense, and/or sell
+//   copies of the Software, and to permit persons to whom the Software is
+//   furnished to do so, subject to the following conditions:
+//
+//   The above copyright notice and this permission notice shall be included in
+//   all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR
+//   IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY,
+//   FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE
+//   AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY CLAIM, DAMAGES OR OTHER
+//   LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR OTHERWISE, ARISING FROM,
+//   OUT OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN
+//   THE SOFTWARE.
+
 // tiny_obj_loader's pnpoly (W. R. Franklin's crossing test) on three vertices.
 bool in_triangle(const float* vx, const float* vy, float tx, float ty) {
     bool c = false;

@@ -15,8 +15,11 @@
 // calls on one device share that device's copy: each call clears the cells it
 // uses before splatting, and calls whose work overlaps on the GPU (for
 // example on two streams) race on it, so a caller must order them.  The first
-// call on a device looks up the array's device address; make that first call
-// before any stream capture.
+// call on a device (and the first after that device's context was torn down,
+// e.g. by cudaDeviceReset) looks up the array's device address; make that
+// first call before any stream capture.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "rvh_internal.hpp"
@@ -27,22 +30,66 @@ namespace {
 
 static __device__ __align__(256) unsigned long long g_noalloc_grid[size_t(RVH_NOALLOC_MAX_GRID_CELLS) * 4];
 
+// Writes the draw record of an empty step (no strands): vertexCount 0.
+__global__ void k_noalloc_empty_draw(rvh_draw_indirect* d) {
+    d->vertex_count = 0u;
+    d->instance_count = 1u;
+    d->first_vertex = 0u;
+    d->first_instance = 0u;
+}
+
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void* g_addr[kMaxDevices] = {};
+struct ScratchAddr {
+    void* ptr = nullptr;
+    unsigned long long ctx_id = 0;   // the context the address belongs to (0: unknown)
+};
+ScratchAddr g_addr[kMaxDevices];
 
-// Device address of the scratch array on the current device; looked up once
-// per device (with that device current) on its first call.
+// Unique id of the calling thread's current context, or 0 when there is none
+// or the driver cannot say (then the address is looked up on every call).
+// cuCtxGetId ids are never reused within a process, so a context that was
+// torn down and created again gets a new one.
+unsigned long long current_context_id() {
+    using GetCurrent = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device `dev`, looked up
+// with that device current on its first call and again whenever the current
+// context is not the one the cached address was taken in.
 rvh_status scratch_address(int dev, void** out) {
     if (dev < 0 || dev >= kMaxDevices) return fail(RVH_ERR_UNSUPPORTED, "step_noalloc: device ordinal too large");
     std::lock_guard<std::mutex> g(g_mu);
-    if (!g_addr[dev]) {
+    ScratchAddr& a = g_addr[dev];
+    const unsigned long long id = current_context_id();
+    if (!a.ptr || id == 0 || id != a.ctx_id) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_grid);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc grid)");
-        g_addr[dev] = p;
+        a.ptr = p;
+        a.ctx_id = current_context_id();   // the lookup has made the device's context current
     }
-    *out = g_addr[dev];
+    *out = a.ptr;
     return RVH_OK;
 }
 
@@ -84,7 +131,14 @@ rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* d, const rvh_frame* fra
     const void* ka = plain_a_kernel(d->n_points, lanes, exact);
     const void* kb = plain_b_kernel(exact);
     if (!ka) return fail(RVH_ERR_UNSUPPORTED, "step_noalloc: no phase-A kernel for this (n_points, lanes_per_strand)");
-    if (d->n_strands == 0) return RVH_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (d->n_strands == 0) {   // nothing to step; the draw record still reports zero strands
+        if (d->draw_indirect) {
+            k_noalloc_empty_draw<<<1, 1, 0, s>>>(static_cast<rvh_draw_indirect*>(d->draw_indirect));
+            RVH_CUDA(cudaGetLastError());
+        }
+        return RVH_OK;
+    }
     int dev = 0;
     RVH_CUDA(cudaGetDevice(&dev));
     void* grid = nullptr;
@@ -122,7 +176,6 @@ rvh_status rvh_step_noalloc(const rvh_noalloc_step_desc* d, const rvh_frame* fra
     A.n_colliders = d->n_colliders;
     for (int j = 0; j < d->n_colliders; ++j) A.col[j] = pack_collider(d->colliders[j]);
 
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the shared scratch keeps the previous call's sums: clear the cells this call uses
     if (P.grid_enabled) RVH_CUDA(cudaMemsetAsync(grid, 0, cells * 32u, s));
     void* args[] = {&A};

@@ -1,23 +1,19 @@
 // rvh_registry.cu — lookup of the compiled step kernels by shape; the
 // phase-B kernel's instantiations.
-#include <mutex>
-#include <set>
-
 #include "rvh_kernels.cuh"
+#include "rvh_optin.hpp"
 #include "rvh_registry.h"
 
 namespace rvh {
 
 bool prepare_kernel(const void* fn) {
-    static std::mutex mu;
-    static std::set<const void*> done;
-    std::lock_guard<std::mutex> g(mu);
+    static OptInRecord record;
     if (!fn) return false;
-    if (done.count(fn)) return true;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) != cudaSuccess)
-        return false;
-    done.insert(fn);
-    return true;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    return record.ensure(dev, fn, [&] {
+        return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes) == cudaSuccess;
+    });
 }
 
 namespace {

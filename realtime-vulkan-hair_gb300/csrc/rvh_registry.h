@@ -19,7 +19,8 @@ template <int L, bool EXACT>
 const void* batch_kernel_inst();
 template <int NFIX, bool EXACT>
 const void* plain_a_inst(int lanes);
-// Opts a kernel into kSmemBytes of dynamic shared memory (once per kernel).
+// Opts a kernel into kSmemBytes of dynamic shared memory on the current
+// device (once per device and kernel).
 bool prepare_kernel(const void* fn);
 
 }  // namespace rvh

@@ -135,7 +135,7 @@ rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_
     if (d.max_active < 1 || d.max_active > 4096) return fail(RVH_ERR_INVALID_ARG, "server: max_active in [1, 4096]");
     if (d.pipeline_depth < 1 || d.pipeline_depth > 8) return fail(RVH_ERR_INVALID_ARG, "server: pipeline_depth in [1, 8]");
     if (!d.lanes_per_strand) d.lanes_per_strand = 8;
-    cudaSetDevice(ctx->device);
+    RVH_DEVICE(ctx->device);
     rvh_server* s = new (std::nothrow) rvh_server();
     if (!s) return fail(RVH_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->ctx = ctx;
@@ -160,7 +160,7 @@ rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_
 
 rvh_status rvh_server_destroy(rvh_server* s) {
     if (!s) return RVH_OK;
-    cudaSetDevice(s->ctx->device);
+    RVH_DEVICE(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     for (auto& e : s->events) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     for (Character& c : s->chars) {
@@ -184,7 +184,7 @@ rvh_status rvh_server_add_character(rvh_server* s, rvh_asset* a, const rvh_wind_
         if (c.asset == a) return fail(RVH_ERR_INVALID_ARG, "server_add_character: asset already registered");
     if (a->params.grid_enabled && !s->slab.ptr)
         return fail(RVH_ERR_BUDGET, "server_add_character: the server has no scratch budget for grids");
-    cudaSetDevice(s->ctx->device);
+    RVH_DEVICE(s->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(s->ctx->stream));
     // the grids become per-request scratch lent from the server's pool
     rvh_status fs = finish_pending(a, s->ctx->stream);
@@ -215,7 +215,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
                           rvh_server_stats* stats) {
     TraceRange trace("rvh_server_run");
     if (!s || (n > 0 && (!reqs || !results))) return fail(RVH_ERR_INVALID_ARG, "server_run: NULL argument");
-    cudaSetDevice(s->ctx->device);
+    RVH_DEVICE(s->ctx->device);
     using clk = std::chrono::steady_clock;
     const cudaStream_t stream = s->ctx->stream;
     std::vector<int> order(n);

@@ -1128,7 +1128,7 @@ rvh_status rvh_shade_fragments(rvh_context* ctx, int64_t n, const void* inputs, 
         return fail(RVH_ERR_INVALID_ARG, "shade_fragments: NULL buffer");
     if (!aligned16(opacity_map) || !aligned16(colors) || !aligned16(inputs))
         return fail(RVH_ERR_INVALID_ARG, "shade_fragments: inputs, opacity map and colors must be 16-byte aligned");
-    RVH_CUDA(cudaSetDevice(ctx->device));
+    RVH_DEVICE(ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     const Maps M{static_cast<const float*>(depth_map), static_cast<const float*>(opacity_map), map_width, map_height};
     k_shade_fragments<<<grid_for(n, ctx->sm_count), kShadeThreads, 0, s>>>((long long)n, static_cast<const float*>(inputs), M,
@@ -1150,7 +1150,7 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
     if (!aligned16(vertices) || !aligned16(frames) || !aligned16(opacity_map) || !aligned16(colors) ||
         reinterpret_cast<uintptr_t>(depth_map) % 4)
         return fail(RVH_ERR_INVALID_ARG, "asset_shade: float4 buffers 16-byte aligned, the depth map 4-byte");
-    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    RVH_DEVICE(a->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->ctx->stream;
     const Cam K = make_cam(*sd);
     const int w = sd->map_width, h = sd->map_height;
@@ -1216,7 +1216,7 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
     RasterDev R;
     if (!raster_setup(*sd, td->n_lines, width, height, R))
         return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: a camera matrix is singular");
-    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    RVH_DEVICE(a->ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : a->ctx->stream;
     const TessView T{static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_points, td->n_lines,
                      td->n_segments};
@@ -1243,7 +1243,7 @@ rvh_status rvh_render_image(rvh_context* ctx, int64_t n_vertices, const void* ve
     if (!aligned16(image) || !aligned16(vertices) || !aligned16(colors))
         return fail(RVH_ERR_INVALID_ARG, "render_image: buffers must be 16-byte aligned");
     if (n_vertices > 0xffffffffLL) return fail(RVH_ERR_INVALID_ARG, "render_image: at most 2^32 - 1 vertices");
-    RVH_CUDA(cudaSetDevice(ctx->device));
+    RVH_DEVICE(ctx->device);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     float vp[16];
     mat_mul(sd->camera_proj, sd->camera_view, vp);

@@ -76,7 +76,7 @@ rvh_status rvh_asset_snapshot(rvh_asset* a, void* host_dst, uint64_t bytes) {
     const Layout L = layout_of(a->n_strands, a->n_points, flags);
     if (bytes != L.total) return fail(RVH_ERR_INVALID_ARG, "snapshot: size must be rvh_asset_snapshot_bytes");
     if (a->colliders.size() > RVH_MAX_COLLIDERS) return fail(RVH_ERR_STATE, "snapshot: too many colliders");
-    RVH_CUDA(cudaSetDevice(a->ctx->device));
+    RVH_DEVICE(a->ctx->device);
     rvh_status st = finish_pending(a, a->ctx->stream);
     if (st != RVH_OK) return st;
     RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));

@@ -78,7 +78,7 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
             return RVH_OK;
         }
     }
-    cudaSetDevice(ctx->device);
+    RVH_DEVICE(ctx->device);
     RVH_CUDA(cudaDeviceSynchronize());
     // snapshot the records of every asset
     std::vector<DevBuf> snap(n);

@@ -39,18 +39,8 @@ class BatchDesc(C.Structure):
                 ("use_graph", C.c_int32), ("full_steps", C.c_int32), ("reserved", C.c_int32)]
 
 
-class HeadDesc(C.Structure):
-    _fields_ = [("seed", C.c_uint64), ("n_strands", C.c_int32), ("n_points", C.c_int32),
-                ("head_radius", C.c_float), ("head_center", C.c_float * 3), ("root_sampling", C.c_int32),
-                ("sort_roots", C.c_int32), ("length_min", C.c_float), ("length_max", C.c_float),
-                ("head_collider", C.c_int32), ("n_ellipsoids", C.c_int32), ("axis_min", C.c_float),
-                ("axis_max", C.c_float), ("grid_res", C.c_int32), ("friction", C.c_float),
-                ("repulsion", C.c_float), ("dftl_damping", C.c_float)]
-
-
-class WindDesc(C.Structure):
-    _fields_ = [("amplitude", C.c_float), ("omega", C.c_float), ("dir", C.c_float * 3), ("gust_sigma", C.c_float),
-                ("seed", C.c_uint64)]
+HeadDesc = T.HeadDesc   # layouts in rvh/types.py (shared with the oracle)
+WindDesc = T.WindDesc
 
 
 class TuneDesc(C.Structure):
@@ -476,14 +466,7 @@ def init_strands_reference(roots, normals, n_points, seg, dir_offset=(0.05, 5.0,
 
 def generate_head(**kw):
     """Returns (records (ns, 3n, 4) f32, rest (ns,), SimParams, [Collider])."""
-    d = HeadDesc()
-    d.head_radius = 1.0
-    d.dftl_damping = 0.0
-    for k, v in kw.items():
-        if k == "head_center":
-            d.head_center[:] = v
-        else:
-            setattr(d, k, v)
+    d = T.head_desc(**kw)
     ns, n = d.n_strands, d.n_points
     rec = np.empty((ns, 3 * n, 4), np.float32)
     rest = np.empty(max(ns, 1), np.float32)

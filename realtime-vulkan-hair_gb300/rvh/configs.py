@@ -13,6 +13,11 @@
   adjoint       4,096 strands x 32 points, 60 steps, no grid.
 The head sphere is collider 0 in every workload (the reference makes
 colliders[0] a sphere, compute.comp:160-169), so hair rests on the head.
+
+`gen` (optional, every builder): where the inputs come from, an object with
+generate_head(**desc) and wind_at(desc, step, t) -- rvh.api (the library,
+the default) or any other statement of include/rvh_scene.h with the same
+results.
 """
 import math
 
@@ -25,7 +30,8 @@ DT = np.float32(1.0 / 60.0)
 
 
 class AssetSpec:
-    def __init__(self, records, rest, params, colliders, n_points, orbit=None, strand_wind=None, wind=None):
+    def __init__(self, records, rest, params, colliders, n_points, orbit=None, strand_wind=None, wind=None,
+                 gen=None):
         self.records = records
         self.rest = rest
         self.params = params
@@ -34,6 +40,7 @@ class AssetSpec:
         self.orbit = orbit            # optional api.Orbit appended as the last collider each frame
         self.strand_wind = strand_wind
         self.wind = wind              # api.WindDesc
+        self.gen = api if gen is None else gen
 
     @property
     def n_strands(self):
@@ -49,7 +56,7 @@ class AssetSpec:
 
     def frame(self, step):
         t = self.time(step)
-        w = api.wind_at(self.wind, step, t) if self.wind is not None else (0.0, 0.0, 0.0)
+        w = self.gen.wind_at(self.wind, step, t) if self.wind is not None else (0.0, 0.0, 0.0)
         return T.frame(DT, t, w)
 
     def colliders_at(self, step):
@@ -60,7 +67,7 @@ class AssetSpec:
 
 
 def _wind(seed, gust):
-    w = api.WindDesc()
+    w = T.WindDesc()
     w.amplitude = 2.0
     w.omega = 0.5
     w.dir[:] = (1.0, 0.0, 0.0)
@@ -104,16 +111,20 @@ def batched_sizes(n_assets=256, seed=2, smin=512, smax=65536):
     return out
 
 
-def batched(n_assets=256, seed=2, scale=1.0, smin=512, smax=65536):
-    """`scale` shrinks every asset's strand count (parity tests use small batches)."""
+def batched(n_assets=256, seed=2, scale=1.0, smin=512, smax=65536, gen=None, indices=None):
+    """`scale` shrinks every asset's strand count (parity tests use small batches);
+    `indices` builds only those assets of the workload, in that order."""
+    gen = api if gen is None else gen
+    sizes = batched_sizes(n_assets, seed, smin, smax)
     specs = []
-    for i, (ns, n, res, ne) in enumerate(batched_sizes(n_assets, seed, smin, smax)):
+    for i in (range(n_assets) if indices is None else indices):
+        ns, n, res, ne = sizes[i]
         ns = max(1, int(ns * scale))
-        rec, rest, p, cols = api.generate_head(seed=seed * 100003 + i, n_strands=ns, n_points=n,
+        rec, rest, p, cols = gen.generate_head(seed=seed * 100003 + i, n_strands=ns, n_points=n,
                                                root_sampling=0, sort_roots=1, length_min=0.2, length_max=1.0,
                                                head_collider=1, n_ellipsoids=ne, axis_min=0.2, axis_max=0.5,
                                                grid_res=res, friction=0.05, repulsion=0.02, dftl_damping=0.9)
-        specs.append(AssetSpec(rec, rest, p, cols, n, wind=_wind(seed * 7919 + i, 0.5)))
+        specs.append(AssetSpec(rec, rest, p, cols, n, wind=_wind(seed * 7919 + i, 0.5), gen=gen))
     return specs
 
 

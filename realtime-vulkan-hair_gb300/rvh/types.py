@@ -56,6 +56,35 @@ class DrawIndirect(C.Structure):
                 ("first_vertex", C.c_uint32), ("first_instance", C.c_uint32)]
 
 
+class HeadDesc(C.Structure):
+    """rvh_head_desc (include/rvh_scene.h): a seeded synthetic head."""
+    _fields_ = [("seed", C.c_uint64), ("n_strands", C.c_int32), ("n_points", C.c_int32),
+                ("head_radius", C.c_float), ("head_center", C.c_float * 3), ("root_sampling", C.c_int32),
+                ("sort_roots", C.c_int32), ("length_min", C.c_float), ("length_max", C.c_float),
+                ("head_collider", C.c_int32), ("n_ellipsoids", C.c_int32), ("axis_min", C.c_float),
+                ("axis_max", C.c_float), ("grid_res", C.c_int32), ("friction", C.c_float),
+                ("repulsion", C.c_float), ("dftl_damping", C.c_float)]
+
+
+class WindDesc(C.Structure):
+    """rvh_wind_desc (include/rvh_scene.h): closed-form wind plus seeded gusts."""
+    _fields_ = [("amplitude", C.c_float), ("omega", C.c_float), ("dir", C.c_float * 3), ("gust_sigma", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+def head_desc(**kw):
+    """A HeadDesc with head radius 1 and the reference's DFTL damping unless given."""
+    d = HeadDesc()
+    d.head_radius = 1.0
+    d.dftl_damping = 0.0
+    for k, v in kw.items():
+        if k == "head_center":
+            d.head_center[:] = v
+        else:
+            setattr(d, k, v)
+    return d
+
+
 def reference_params():
     """The constants hard-coded in src/shaders/compute.comp (lines cited in rvh_types.h)."""
     p = SimParams()

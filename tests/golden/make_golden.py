@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the REFERENCE's own code.
 
 Runs src/shaders/compute.comp (compiled as C++ against the reference's glm by
-oracle/build_ref.py; needs the reference checkout, default /root/reference)
+oracle/build_ref.py; needs the reference checkout, named by $RVH_REFERENCE_DIR)
 on seeded reference-mode scenes, and records inputs and outputs:
 
   ref_head.npz   96 strands x 10 points rooted on the reference's head

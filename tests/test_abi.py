@@ -106,3 +106,30 @@ def test_status_strings_and_version(librvh):
     assert librvh.rvh_abi_version() == 1
     for s in range(9):
         assert librvh.rvh_status_string(s)
+
+
+def test_kernel_opt_in_is_recorded_per_device(tmp_path):
+    """cudaFuncSetAttribute applies to the current device only: the record of
+    opted-in kernels must key on (device, kernel), so a second device runs the
+    opt-in again for a kernel the first already has.  Compiled alone (host C++)."""
+    src = tmp_path / "optin.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "rvh_optin.hpp"
+int main() {
+    rvh::OptInRecord r;
+    int calls = 0, k1 = 0, k2 = 0;
+    auto ok = [&] { ++calls; return true; };
+    auto bad = [&] { ++calls; return false; };
+    bool a = r.ensure(0, &k1, ok), b = r.ensure(0, &k1, ok);   // once per (device, kernel)
+    bool c = r.ensure(1, &k1, ok);                             // another device: again
+    bool d = r.ensure(1, &k2, bad), e = r.ensure(1, &k2, ok);  // a failure is not recorded
+    std::printf("%d %d %d %d %d %d %zu\n", a, b, c, d, e, calls, r.size());
+    return 0;
+}
+''')
+    exe = tmp_path / "optin"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "realtime-vulkan-hair_gb300", "csrc"), str(src),
+                    "-o", str(exe), "-lpthread"], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["1", "1", "1", "0", "1", "4", "3"], out

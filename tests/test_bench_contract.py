@@ -1,6 +1,7 @@
 """bench.py's JSON line: the reference arm (the oracle's OpenMP restatement on
 the host cores, the one arm that runs without a GPU) prints every field of the
-contract, with the reference arm's own e2e and cpu_baseline."""
+contract, with the reference arm's own e2e and cpu_baseline, and never maps
+the CUDA library (its workload sample comes from the oracle's generator)."""
 import json
 import os
 import subprocess
@@ -11,9 +12,16 @@ from conftest import ROOT
 
 def test_reference_arm_prints_the_contract_line():
     env = dict(os.environ, OMP_NUM_THREADS=os.environ.get("OMP_NUM_THREADS", "4"))
-    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                          "--warmup", "3"], capture_output=True, text=True, env=env, timeout=600, check=True).stdout
-    line = json.loads(out.strip().splitlines()[-1])
+    prog = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '3']; "
+            "runpy.run_path(%r, run_name='__main__'); "
+            "print('MAPS', [l.split()[-1] for l in open('/proc/self/maps') if l.rstrip().endswith('.so')])"
+            % os.path.join(ROOT, "bench.py"))
+    out = subprocess.run([sys.executable, "-c", prog], capture_output=True, text=True, env=env, timeout=600,
+                         check=True, cwd=ROOT).stdout
+    lines = out.strip().splitlines()
+    maps = [l for l in lines if l.startswith("MAPS")][0]
+    assert "librvh" not in maps and "liboracle" in maps, maps
+    line = json.loads([l for l in lines if l.startswith("{")][-1])
     for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in line, key

@@ -119,3 +119,25 @@ def test_rng_is_counter_based(librvh):
     assert a == b and len(set(a)) == 5
     u = np.array([librvh.rvh_rng_uniform(9, i) for i in range(10000)])
     assert 0 <= u.min() and u.max() < 1 and abs(u.mean() - 0.5) < 0.02
+
+
+def test_oracle_scene_generator_gives_the_library_bytes(librvh, oracle):
+    """The CPU timing arm of bench.py builds its workload sample with the
+    oracle's statement of the seeded generator, never mapping the CUDA
+    library; it must be the same workload, byte for byte."""
+    gen = oracle.SceneGen()
+    lib_specs = configs.batched(indices=range(6))
+    ora_specs = configs.batched(indices=range(6), gen=gen)
+    for a, b in zip(lib_specs, ora_specs):
+        assert a.records.tobytes() == b.records.tobytes()
+        assert a.rest.tobytes() == b.rest.tobytes()
+        assert bytes(a.params) == bytes(b.params)
+        assert [bytes(c) for c in a.colliders] == [bytes(c) for c in b.colliders]
+        for k in (0, 1, 57):
+            assert bytes(a.frame(k)) == bytes(b.frame(k))
+    kw = dict(seed=11, n_strands=3000, n_points=12, root_sampling=1, sort_roots=1, length_min=0.4,
+              length_max=0.8, head_collider=1, n_ellipsoids=4, axis_min=0.2, axis_max=0.5, grid_res=40,
+              friction=0.05, repulsion=0.02, dftl_damping=0.9, head_center=(0.5, -1.0, 2.0))
+    x, y = api.generate_head(**kw), gen.generate_head(**kw)
+    assert x[0].tobytes() == y[0].tobytes() and x[1].tobytes() == y[1].tobytes()
+    assert bytes(x[2]) == bytes(y[2]) and [bytes(c) for c in x[3]] == [bytes(c) for c in y[3]]
