@@ -3,10 +3,16 @@
 // predict, FTL, velocity damping/clamp, DFTL correction), with checkpointed
 // recomputation.
 //
-// One thread owns one strand for the whole run (strands are independent when
-// the grid is off).  The forward keeps (x, v) every C steps; the reverse walks
-// the checkpoints backwards, recomputes each segment's step inputs into a
-// per-strand tape, then back-propagates through those steps tip-to-root.
+// One warp owns one strand for the whole run (strands are independent when
+// the grid is off) and lane i owns curve point i (n <= 32): every per-point
+// term runs in parallel across the lanes, and only the two chains along the
+// strand are sequential -- the FTL chain of the forward step (run in every
+// lane, the predicted points broadcast by shuffles, as the step kernel does)
+// and its reverse, the tip-to-root accumulation of the FTL adjoint.  The
+// forward keeps (x, v) every C steps; the reverse walks the checkpoints
+// backwards, recomputes each segment's step inputs into a per-strand tape,
+// then back-propagates through those steps.  Checkpoints and tape are stored
+// point-major per strand, so a warp's loads and stores are contiguous.
 //
 // Loss: L = 1/ns * sum_s |x_tip,s(T) - target_s|^2.  Outputs dL/d(strand
 // wind), dL/d(rest segment length), dL/d(initial velocity).  The contact set
@@ -19,7 +25,7 @@
 
 namespace rvh {
 
-constexpr int kAdjThreads = 32;   // one warp per CTA: 4,096 strands spread over 128 SMs (64-thread CTAs: 14 % slower)
+constexpr int kAdjThreads = 256;   // 8 strands (warps) per CTA
 
 struct AdjDev {
     DevAsset A;                 // asset view: params, colliders, strands (initial state), rest, wind
@@ -36,31 +42,37 @@ struct AdjDev {
     float4* d_v0;               // per point (xyz)
 };
 
+__device__ __forceinline__ f3 shfl3(f3 a, int src) {
+    const unsigned FULL = 0xffffffffu;
+    return {__shfl_sync(FULL, a.x, src), __shfl_sync(FULL, a.y, src), __shfl_sync(FULL, a.z, src)};
+}
+
+// One forward step of the warp's strand (lane i = point i): the step kernel's
+// arithmetic (strand_phase_a with one point per lane), so exact math gives
+// its bits.  Lanes i >= n carry zeros; the root (lane 0) never moves.
 template <class M>
-__device__ void fwd_local(f3* X, f3* V, int n, float r, f3 f0, const DevAsset& A, float dt) {
-    f3 P[RVH_MAX_POINTS], XN[RVH_MAX_POINTS];
+__device__ __forceinline__ void fwd_warp(f3& X, f3& V, int n, float r, f3 f0, const DevAsset& A, float dt) {
+    const int i = threadIdx.x & 31;
+    const bool moving = i >= 1 && i < n;
     const float dt2 = M::mul(dt, dt);
-    for (int i = 1; i < n; ++i) {
-        const f3 force = collide_force<M>(A, X[i], f0);
-        P[i] = v_add<M>(v_add<M>(X[i], v_scale<M>(dt, V[i])), v_scale<M>(dt2, force));
+    const f3 force = moving ? collide_force<M>(A, X, f0) : f0;
+    // predictedPos = currentPos + dt * currentVel + dt * dt * force   (compute.comp:187)
+    const f3 P = v_axpy<M>(v_axpy<M>(X, dt, V), dt2, force);
+    f3 par = shfl3(X, 0), XN = X;
+    for (int j = 1; j < n; ++j) {   // FTL (compute.comp:191-192), the same chain in every lane
+        const f3 pj = shfl3(P, j);
+        par = v_axpy<M>(par, r, v_normalize<M>(v_sub<M>(pj, par)));
+        if (i == j) XN = par;
     }
-    f3 par = X[0];
-    XN[0] = X[0];
-    for (int i = 1; i < n; ++i) {
-        const f3 dir = v_normalize<M>(v_sub<M>(P[i], par));
-        par = v_add<M>(par, v_scale<M>(r, dir));
-        XN[i] = par;
+    f3 v = v_scale<M>(A.damping, v_div<M>(v_sub<M>(XN, X), dt));
+    if (v_len<M>(v) > A.vmax) v = v_scale<M>(A.vmax, v_normalize<M>(v));
+    const f3 cor = v_scale<M>(A.dftl, v_sub<M>(XN, P));
+    const f3 cn = shfl3(cor, (i + 1) & 31);   // DFTL: v_i -= corr_{i+1} / dt for i < n-1 (compute.comp:213-215)
+    if (i >= 1 && i < n - 1) v = v_sub<M>(v, v_div<M>(cn, dt));
+    if (moving) {
+        X = XN;
+        V = v;
     }
-    f3 cor[RVH_MAX_POINTS];
-    for (int i = 1; i < n; ++i) {
-        const f3 newVel = v_div<M>(v_sub<M>(XN[i], X[i]), dt);
-        f3 v = v_scale<M>(A.damping, newVel);
-        if (v_len<M>(v) > A.vmax) v = v_scale<M>(A.vmax, v_normalize<M>(v));
-        V[i] = v;
-        cor[i] = v_scale<M>(A.dftl, v_sub<M>(XN[i], P[i]));
-    }
-    for (int i = 1; i < n - 1; ++i) V[i] = v_sub<M>(V[i], v_div<M>(cor[i + 1], dt));
-    for (int i = 1; i < n; ++i) X[i] = XN[i];
 }
 
 // plain IEEE float helpers for the reverse sweep
@@ -81,113 +93,114 @@ __device__ __forceinline__ f3 matT(const float* m, f3 v) {
             m[6] * v.x + m[7] * v.y + m[8] * v.z};
 }
 
-// Reverse of one step: X, V = step inputs; Xb, Vb in: adjoints of the outputs,
-// out: adjoints of the inputs.
+// Reverse of one step for the warp's strand (lane i = point i).  X, V: the
+// step's inputs; Xb, Vb in: adjoints of its outputs, out: adjoints of its
+// inputs.  rest_bar and wind_bar collect this lane's terms (summed over the
+// warp at the end of the run).
 template <class M>
-__device__ void rev_local(const f3* X, const f3* V, f3* Xb, f3* Vb, int n, float r, f3 f0, const DevAsset& A,
-                          float dt, float& rest_bar, f3& wind_bar) {
+__device__ __forceinline__ void rev_warp(f3 X, f3 V, f3& Xb, f3& Vb, int n, float r, f3 f0, const DevAsset& A,
+                                         float dt, float& rest_bar, f3& wind_bar) {
+    const int i = threadIdx.x & 31;
+    const bool moving = i >= 1 && i < n;
     const float k = A.k_penalty, damp = A.damping, s = A.dftl, vmax = A.vmax;
-    f3 P[RVH_MAX_POINTS], XN[RVH_MAX_POINTS], U[RVH_MAX_POINTS];
-    int cnt[RVH_MAX_POINTS];
     const float dt2 = M::mul(dt, dt);
-    for (int i = 1; i < n; ++i) {
-        int c_n = 0;
-        const int nc = A.n_colliders;
-        for (int j = 0; j < nc; ++j) {
+    // recompute the step: contact count, prediction, FTL, undamped-clamp input
+    int cnt = 0;
+    if (moving) {
+        for (int j = 0; j < A.n_colliders; ++j) {
             const DevCollider& c = A.col[j];
             if (c.kind == RVH_COLLIDER_SPHERE) {
-                if (v_len<M>(v_sub<M>(X[i], f3{c.c[0], c.c[1], c.c[2]})) < c.radius) ++c_n;
+                if (v_len<M>(v_sub<M>(X, f3{c.c[0], c.c[1], c.c[2]})) < c.radius) ++cnt;
             } else {
-                if (v_len<M>(mat_p1<M>(c.inv, X[i])) <= 1.0f) ++c_n;
+                if (v_len<M>(mat_p1<M>(c.inv, X)) <= 1.0f) ++cnt;
             }
         }
-        cnt[i] = c_n;
-        const f3 force = collide_force<M>(A, X[i], f0);
-        P[i] = v_add<M>(v_add<M>(X[i], v_scale<M>(dt, V[i])), v_scale<M>(dt2, force));
     }
-    f3 par = X[0];
-    XN[0] = X[0];
-    for (int i = 1; i < n; ++i) {
-        par = v_add<M>(par, v_scale<M>(r, v_normalize<M>(v_sub<M>(P[i], par))));
-        XN[i] = par;
-        U[i] = v_scale<M>(damp, v_div<M>(v_sub<M>(XN[i], X[i]), dt));
+    const f3 force = moving ? collide_force<M>(A, X, f0) : f0;
+    const f3 P = v_axpy<M>(v_axpy<M>(X, dt, V), dt2, force);
+    f3 par = shfl3(X, 0), XN = X;
+    for (int j = 1; j < n; ++j) {
+        const f3 pj = shfl3(P, j);
+        par = v_axpy<M>(par, r, v_normalize<M>(v_sub<M>(pj, par)));
+        if (i == j) XN = par;
     }
-    f3 xnb[RVH_MAX_POINTS], cb[RVH_MAX_POINTS], xb[RVH_MAX_POINTS], vb[RVH_MAX_POINTS], pb[RVH_MAX_POINTS];
+    const f3 U = v_scale<M>(damp, v_div<M>(v_sub<M>(XN, X), dt));
+    const f3 XNm = shfl3(XN, (i + 31) & 31);   // XN_{i-1}
+
+    // velocity outputs: DFTL (corr_{i+1} of lane i+1 gets -Vb_i / dt), clamp, damping
     const f3 z = {0.f, 0.f, 0.f};
-    for (int i = 0; i < n; ++i) {
-        xnb[i] = Xb[i];
-        cb[i] = xb[i] = vb[i] = pb[i] = z;
-    }
-    for (int i = 1; i < n; ++i) {
-        const f3 vob = Vb[i];
-        if (i != n - 1) cb[i + 1] = s3(cb[i + 1], m3(1.0f / dt, vob));
-        f3 ub = vob;
-        const float ul = l3(U[i]);
+    const f3 vb_prev = shfl3(Vb, (i + 31) & 31);   // Vb_{i-1}
+    f3 cb = (i >= 2 && i < n) ? m3(-1.0f, m3(1.0f / dt, vb_prev)) : z;
+    f3 xnb = Xb, xb = z, vb = z, pb = z;
+    if (moving) {
+        f3 ub = Vb;
+        const float ul = l3(U);
         if (ul > vmax) {
-            const f3 uh = m3(1.0f / ul, U[i]);
-            ub = m3(vmax / ul, s3(vob, m3(d3(uh, vob), uh)));
+            const f3 uh = m3(1.0f / ul, U);
+            ub = m3(vmax / ul, s3(Vb, m3(d3(uh, Vb), uh)));
         }
-        xnb[i] = a3(xnb[i], m3(damp / dt, ub));
-        xb[i] = s3(xb[i], m3(damp / dt, ub));
+        xnb = a3(xnb, m3(damp / dt, ub));
+        xb = s3(xb, m3(damp / dt, ub));
+        xnb = a3(xnb, m3(s, cb));
+        pb = s3(pb, m3(s, cb));
     }
-    for (int i = 1; i < n; ++i) {
-        xnb[i] = a3(xnb[i], m3(s, cb[i]));
-        pb[i] = s3(pb[i], m3(s, cb[i]));
+    // FTL adjoint, tip to root: lane j's finished xnb_j gives its pb term and
+    // passes xnb_j - db_j on to lane j - 1
+    const f3 dv = s3(P, XNm);
+    for (int j = n - 1; j >= 1; --j) {
+        f3 carry = z;
+        if (i == j) {
+            const f3 nh = m3(1.0f / l3(dv), dv);
+            rest_bar += d3(xnb, nh);
+            const f3 db = nvjp(dv, m3(r, xnb));
+            carry = s3(xnb, db);
+            pb = a3(pb, db);
+        }
+        carry = shfl3(carry, j);
+        if (i == j - 1) xnb = a3(xnb, carry);
     }
-    for (int i = n - 1; i >= 1; --i) {
-        const f3 dv = s3(P[i], XN[i - 1]);
-        const f3 nh = m3(1.0f / l3(dv), dv);
-        rest_bar += d3(xnb[i], nh);
-        const f3 db = nvjp(dv, m3(r, xnb[i]));
-        xnb[i - 1] = s3(a3(xnb[i - 1], xnb[i]), db);
-        pb[i] = a3(pb[i], db);
-    }
-    for (int i = 1; i < n; ++i) {
-        xb[i] = a3(xb[i], pb[i]);
-        vb[i] = a3(vb[i], m3(dt, pb[i]));
-        const f3 fb = m3(dt * dt, pb[i]);
+    // prediction and penalty-force adjoints
+    if (moving) {
+        xb = a3(xb, pb);
+        vb = a3(vb, m3(dt, pb));
+        const f3 fb = m3(dt * dt, pb);
         wind_bar = a3(wind_bar, fb);
-        if (cnt[i] == 0) continue;
-        const f3 g = m3(1.0f / (float)cnt[i], fb);
-        const f3 x = X[i];
-        const int nc = A.n_colliders;
-        for (int j = 0; j < nc; ++j) {
-            const DevCollider& c = A.col[j];
-            if (c.kind == RVH_COLLIDER_SPHERE) {
-                const f3 e0 = s3(x, f3{c.c[0], c.c[1], c.c[2]});
-                const float rho = l3(e0);
-                if (!(v_len<M>(v_sub<M>(x, f3{c.c[0], c.c[1], c.c[2]})) < c.radius)) continue;
-                const f3 e = m3(1.0f / rho, e0);
-                const float eg = d3(e, g);
-                xb[i] = a3(xb[i], m3(k, a3(m3(-eg, e), m3((c.radius - rho) / rho, s3(g, m3(eg, e))))));
-            } else {
-                const f3 q = mat_p1<M>(c.inv, x);
-                if (!(v_len<M>(q) <= 1.0f)) continue;
-                const f3 uh = m3(1.0f / l3(q), q);
-                const f3 surf = mat_p1<M>(c.xf, uh);
-                const f3 e = s3(surf, x);
-                const float d = l3(e);
-                const f3 m = mat_q0<M>(c.itr, q);
-                const f3 nt = m3(1.0f / l3(m), m);
-                const float dbar = k * d3(nt, g);
-                const f3 ntb = m3(k * d, g);
-                f3 qb = z;
-                if (d > 0.f) {
-                    const f3 eb = m3(dbar / d, e);
-                    xb[i] = s3(xb[i], eb);
-                    qb = a3(qb, nvjp(q, matT(c.xf, eb)));
+        if (cnt > 0) {
+            const f3 g = m3(1.0f / (float)cnt, fb);
+            for (int j = 0; j < A.n_colliders; ++j) {
+                const DevCollider& c = A.col[j];
+                if (c.kind == RVH_COLLIDER_SPHERE) {
+                    const f3 e0 = s3(X, f3{c.c[0], c.c[1], c.c[2]});
+                    const float rho = l3(e0);
+                    if (!(v_len<M>(v_sub<M>(X, f3{c.c[0], c.c[1], c.c[2]})) < c.radius)) continue;
+                    const f3 e = m3(1.0f / rho, e0);
+                    const float eg = d3(e, g);
+                    xb = a3(xb, m3(k, a3(m3(-eg, e), m3((c.radius - rho) / rho, s3(g, m3(eg, e))))));
+                } else {
+                    const f3 q = mat_p1<M>(c.inv, X);
+                    if (!(v_len<M>(q) <= 1.0f)) continue;
+                    const f3 uh = m3(1.0f / l3(q), q);
+                    const f3 surf = mat_p1<M>(c.xf, uh);
+                    const f3 e = s3(surf, X);
+                    const float d = l3(e);
+                    const f3 m = mat_q0<M>(c.itr, q);
+                    const f3 nt = m3(1.0f / l3(m), m);
+                    const float dbar = k * d3(nt, g);
+                    const f3 ntb = m3(k * d, g);
+                    f3 qb = z;
+                    if (d > 0.f) {
+                        const f3 eb = m3(dbar / d, e);
+                        xb = s3(xb, eb);
+                        qb = a3(qb, nvjp(q, matT(c.xf, eb)));
+                    }
+                    qb = a3(qb, matT(c.itr, nvjp(m, ntb)));
+                    xb = a3(xb, matT(c.inv, qb));
                 }
-                qb = a3(qb, matT(c.itr, nvjp(m, ntb)));
-                xb[i] = a3(xb[i], matT(c.inv, qb));
             }
         }
     }
-    Xb[0] = z;
-    Vb[0] = z;
-    for (int i = 1; i < n; ++i) {
-        Xb[i] = xb[i];
-        Vb[i] = vb[i];
-    }
+    Xb = moving ? xb : z;
+    Vb = moving ? vb : z;
 }
 
 __device__ __forceinline__ f3 strand_f0(const DevAsset& A, const rvh_frame& F, int s) {
@@ -201,44 +214,43 @@ __device__ __forceinline__ f3 strand_f0(const DevAsset& A, const rvh_frame& F, i
 
 template <class M>
 __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const __grid_constant__ AdjDev D) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const DevAsset& A = D.A;
-    if (s >= A.n_strands) return;
+    const int s = (int)((blockIdx.x * (unsigned)kAdjThreads + threadIdx.x) >> 5);   // the warp's strand
+    if (s >= A.n_strands) return;   // uniform across the warp
     const int n = A.n_points;
+    const int i = threadIdx.x & 31;
+    const bool live = i < n;
     const float r = A.rest[s];
-    f3 X[RVH_MAX_POINTS], V[RVH_MAX_POINTS];
     const float4* rec = A.strands + (size_t)s * 3 * n;
-    for (int i = 0; i < n; ++i) {
-        X[i] = xyz(rec[i]);
-        V[i] = xyz(rec[n + i]);
-    }
+    f3 X = live ? xyz(rec[i]) : f3{0.f, 0.f, 0.f};
+    f3 V = live ? xyz(rec[n + i]) : f3{0.f, 0.f, 0.f};
     const size_t stride = (size_t)2 * n;  // float4 per strand per saved state
     auto save = [&](float4* base, int slot) {
+        if (!live) return;
         float4* p = base + ((size_t)slot * A.n_strands + s) * stride;
-        for (int i = 0; i < n; ++i) {
-            p[i] = make_float4(X[i].x, X[i].y, X[i].z, 0.f);
-            p[n + i] = make_float4(V[i].x, V[i].y, V[i].z, 0.f);
-        }
+        p[i] = make_float4(X.x, X.y, X.z, 0.f);
+        p[n + i] = make_float4(V.x, V.y, V.z, 0.f);
     };
-    auto load = [&](const float4* base, int slot, f3* Xo, f3* Vo) {
+    auto load = [&](const float4* base, int slot, f3& Xo, f3& Vo) {
+        if (!live) return;
         const float4* p = base + ((size_t)slot * A.n_strands + s) * stride;
-        for (int i = 0; i < n; ++i) {
-            Xo[i] = xyz(p[i]);
-            Vo[i] = xyz(p[n + i]);
-        }
+        Xo = xyz(p[i]);
+        Vo = xyz(p[n + i]);
     };
     for (int t = 0; t < D.n_steps; ++t) {
         if (t % D.ckpt == 0) save(D.ck, t / D.ckpt);
-        fwd_local<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
+        fwd_warp<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
     }
     const float4 tg = D.targets[s];
-    const double ex = (double)X[n - 1].x - (double)tg.x, ey = (double)X[n - 1].y - (double)tg.y,
-                 ez = (double)X[n - 1].z - (double)tg.z;
-    D.loss_parts[s] = ex * ex + ey * ey + ez * ez;
-    f3 Xb[RVH_MAX_POINTS], Vb[RVH_MAX_POINTS];
-    for (int i = 0; i < n; ++i) Xb[i] = Vb[i] = f3{0.f, 0.f, 0.f};
+    const f3 tip = shfl3(X, n - 1);
+    if (i == 0) {
+        const double ex = (double)tip.x - (double)tg.x, ey = (double)tip.y - (double)tg.y,
+                     ez = (double)tip.z - (double)tg.z;
+        D.loss_parts[s] = ex * ex + ey * ey + ez * ez;
+    }
     const float g2 = 2.0f / (float)A.n_strands;
-    Xb[n - 1] = {g2 * (X[n - 1].x - tg.x), g2 * (X[n - 1].y - tg.y), g2 * (X[n - 1].z - tg.z)};
+    f3 Xb = {0.f, 0.f, 0.f}, Vb = {0.f, 0.f, 0.f};
+    if (i == n - 1) Xb = {g2 * (X.x - tg.x), g2 * (X.y - tg.y), g2 * (X.z - tg.z)};
     float rest_bar = 0.f;
     f3 wind_bar = {0.f, 0.f, 0.f};
     for (int k = D.n_ckpt - 1; k >= 0; --k) {
@@ -246,17 +258,26 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(const __grid_constant__
         load(D.ck, k, X, V);
         for (int t = t0; t < t1; ++t) {
             save(D.tape, t - t0);
-            if (t + 1 < t1) fwd_local<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
+            if (t + 1 < t1) fwd_warp<M>(X, V, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt);
         }
         for (int t = t1 - 1; t >= t0; --t) {
-            f3 Xi[RVH_MAX_POINTS], Vi[RVH_MAX_POINTS];
+            f3 Xi = {0.f, 0.f, 0.f}, Vi = {0.f, 0.f, 0.f};
             load(D.tape, t - t0, Xi, Vi);
-            rev_local<M>(Xi, Vi, Xb, Vb, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt, rest_bar, wind_bar);
+            rev_warp<M>(Xi, Vi, Xb, Vb, n, r, strand_f0(A, D.frames[t], s), A, D.frames[t].dt, rest_bar, wind_bar);
         }
     }
-    D.d_rest[s] = rest_bar;
-    D.d_wind[s] = make_float4(wind_bar.x, wind_bar.y, wind_bar.z, 0.f);
-    for (int i = 0; i < n; ++i) D.d_v0[(size_t)s * n + i] = make_float4(Vb[i].x, Vb[i].y, Vb[i].z, 0.f);
+    const unsigned FULL = 0xffffffffu;
+    for (int o = 16; o > 0; o >>= 1) {   // the lanes' rest and wind terms
+        rest_bar += __shfl_xor_sync(FULL, rest_bar, o);
+        wind_bar.x += __shfl_xor_sync(FULL, wind_bar.x, o);
+        wind_bar.y += __shfl_xor_sync(FULL, wind_bar.y, o);
+        wind_bar.z += __shfl_xor_sync(FULL, wind_bar.z, o);
+    }
+    if (i == 0) {
+        D.d_rest[s] = rest_bar;
+        D.d_wind[s] = make_float4(wind_bar.x, wind_bar.y, wind_bar.z, 0.f);
+    }
+    if (live) D.d_v0[(size_t)s * n + i] = make_float4(Vb.x, Vb.y, Vb.z, 0.f);
 }
 
 }  // namespace rvh
@@ -324,8 +345,8 @@ rvh_status rvh_adjoint(rvh_asset* a, const rvh_frame* frames, int32_t n_steps, i
     void* args[] = {&D};
     const void* kern = ctx->math == RVH_MATH_EXACT ? reinterpret_cast<const void*>(&k_adjoint<ExactMath>)
                                                    : reinterpret_cast<const void*>(&k_adjoint<FastMath>);
-    e = cudaLaunchKernel(kern, dim3(unsigned((ns + kAdjThreads - 1) / kAdjThreads)), dim3(kAdjThreads), args, 0,
-                         ctx->stream);
+    const int per_cta = kAdjThreads / 32;   // one warp per strand
+    e = cudaLaunchKernel(kern, dim3(unsigned((ns + per_cta - 1) / per_cta)), dim3(kAdjThreads), args, 0, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     std::vector<double> parts(ns);
     std::vector<float4> w4(ns), v4(size_t(ns) * n);

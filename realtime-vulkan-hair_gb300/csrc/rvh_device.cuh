@@ -101,6 +101,15 @@ struct DevAsset {
     // optional: the step also writes every point's new position (xyz, the root
     // included) to pos_xyz[3 * (strand * n + i)], for a device-to-host copy
     float* pos_xyz;
+    // Cell boxes of the phase-A groups (two int4 per group, indexed by the
+    // group's first round: {lo xyz, tag}, {hi xyz, points}).  A fused step
+    // writes each group's splat box under box_tag_write; the next fused step
+    // of the same grouping finds there the box of the positions its pending
+    // gather reads (the same points, unmoved since) when the tag equals
+    // box_tag_read, and skips recomputing it.  Null or tag 0: not used.
+    int4* group_box;
+    uint32_t box_tag_read;
+    uint32_t box_tag_write;
 };
 
 struct f3 {
@@ -193,6 +202,7 @@ struct Corners {
     float g[3];    // grid-space coordinates
     int lo[3];     // first corner per axis
     int cnt[3];    // 0, 1 or 2 corners per axis
+    float flo[3];  // lo as a float (exact: small integers), so weights need no conversion
 };
 
 template <class M>
@@ -211,13 +221,15 @@ __device__ __forceinline__ Corners corners_of(const DevAsset& A, f3 p) {
         C.g[ax] = g;
         C.lo[ax] = lo;
         C.cnt[ax] = max(hi - lo + 1, 0);
+        C.flo[ax] = fmaxf(f, 0.0f);
     }
     return C;
 }
 
+// clamp(1 - abs(g - a), 0, 1) for corner coordinate a (a float holding an integer)
 template <class M>
-__device__ __forceinline__ float tri_w(float g, int a) {  // clamp(1 - abs(g - a), 0, 1)
-    return fminf(fmaxf(M::sub(1.0f, fabsf(M::sub(g, (float)a))), 0.0f), 1.0f);
+__device__ __forceinline__ float tri_w(float g, float a) {
+    return fminf(fmaxf(M::sub(1.0f, fabsf(M::sub(g, a))), 0.0f), 1.0f);
 }
 
 __device__ __forceinline__ long long fixed_of(float scale_times_x) {
@@ -259,18 +271,18 @@ __device__ __forceinline__ void splat_point(const DevAsset& A, f3 pos, f3 vel, i
         if (da >= C.cnt[0]) continue;
         const int a = C.lo[0] + da;
         if (a < xlo || a >= xhi) continue;
-        const float wx = tri_w<M>(C.g[0], a);
+        const float wx = tri_w<M>(C.g[0], C.flo[0] + (float)da);
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
             if (db >= C.cnt[1]) continue;
             const int b = C.lo[1] + db;
-            const float wy = tri_w<M>(C.g[1], b);
+            const float wy = tri_w<M>(C.g[1], C.flo[1] + (float)db);
             const float wxy = M::mul(wx, wy);
 #pragma unroll
             for (int dc = 0; dc < 2; ++dc) {
                 if (dc >= C.cnt[2]) continue;
                 const int c = C.lo[2] + dc;
-                const float w = M::mul(wxy, tri_w<M>(C.g[2], c));
+                const float w = M::mul(wxy, tri_w<M>(C.g[2], C.flo[2] + (float)dc));
                 unsigned long long* cell = A.grid + 4ull * (unsigned)(a + b * A.nx + c * nxny);
                 int q0, q1, q2, q3;
                 corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
@@ -327,8 +339,8 @@ __device__ __forceinline__ CellF cell_from_global(const DevAsset& A, const unsig
 // d(weight)/d(g) sign of corner a on one axis: -1 left of the point, +1 right
 // of it, 0 outside the unit support (compute.comp repulsion extension).
 template <class M>
-__device__ __forceinline__ float grad_sign(float g, int a) {
-    const float ga = M::sub(g, (float)a);
+__device__ __forceinline__ float grad_sign(float g, float a) {
+    const float ga = M::sub(g, a);
     return fabsf(ga) < 1.0f ? (ga >= 0.0f ? -1.0f : 1.0f) : 0.0f;
 }
 
@@ -343,16 +355,16 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
     float wxs[2], wys[2], wzs[2], sx[2] = {0.f, 0.f}, sy[2] = {0.f, 0.f}, sz[2] = {0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-        wxs[d] = tri_w<M>(C.g[0], C.lo[0] + d);
-        wys[d] = tri_w<M>(C.g[1], C.lo[1] + d);
-        wzs[d] = tri_w<M>(C.g[2], C.lo[2] + d);
+        wxs[d] = tri_w<M>(C.g[0], C.flo[0] + (float)d);
+        wys[d] = tri_w<M>(C.g[1], C.flo[1] + (float)d);
+        wzs[d] = tri_w<M>(C.g[2], C.flo[2] + (float)d);
     }
     if (rep) {
 #pragma unroll
         for (int d = 0; d < 2; ++d) {
-            sx[d] = grad_sign<M>(C.g[0], C.lo[0] + d);
-            sy[d] = grad_sign<M>(C.g[1], C.lo[1] + d);
-            sz[d] = grad_sign<M>(C.g[2], C.lo[2] + d);
+            sx[d] = grad_sign<M>(C.g[0], C.flo[0] + (float)d);
+            sy[d] = grad_sign<M>(C.g[1], C.flo[1] + (float)d);
+            sz[d] = grad_sign<M>(C.g[2], C.flo[2] + (float)d);
         }
     }
     f3 gv = {0.f, 0.f, 0.f};
@@ -390,6 +402,103 @@ __device__ __forceinline__ f3 gather_point(const DevAsset& A, float dt, f3 pos, 
                     }
                 }
             }
+        }
+    }
+    const float fr = A.friction;
+    f3 out = v_axpy<M>(v_scale<M>(M::sub(1.0f, fr), vel), fr, gv);
+    if (rep) {
+        const float coef = M::div(M::mul(A.repulsion, M::div(A.h, dt)), fmaxf(rho, 1.0f));
+        out = v_sub<M>(out, v_scale<M>(coef, grad));
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Fast-math gather.  A cell is 16 B: its mean velocity v_sum * (1/density)
+// and rc = density / scale (all zero for an empty cell), and the trilinear
+// sums are taken axis by axis: over z, then y, then x, so the eight corners
+// cost 4 + 2 + 1 weighted float4 sums instead of eight weight products, and
+// the repulsion gradient reuses the partial sums.  Same quantities as
+// gather_point (compute.comp:280-297 plus the repulsion extension), in a
+// different order of rounding.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 cellq_from_sums(long long vx, long long vy, long long vz, long long dens, float scale) {
+    const float fd = i64_to_f32(dens);
+    const float r = FastMath::rcp(fd);
+    return make_float4(i64_to_f32(vx) * r, i64_to_f32(vy) * r, i64_to_f32(vz) * r, FastMath::div(fd, scale));
+}
+
+__device__ __forceinline__ float4 cellq_from_global(const DevAsset& A, const unsigned long long* grid, unsigned idx) {
+    const ulonglong2* cell = reinterpret_cast<const ulonglong2*>(grid + 4ull * idx);
+    const bool wrap = A.wrap32 != 0;
+    const ulonglong2 zw = __ldcg(cell + 1);
+    const long long dens = grid_val(zw.y, wrap);
+    if (dens <= 0) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const ulonglong2 xy = __ldcg(cell);
+    return cellq_from_sums(grid_val(xy.x, wrap), grid_val(xy.y, wrap), grid_val(zw.x, wrap), dens, A.scale);
+}
+
+__device__ __forceinline__ float4 f4_axpy(float4 acc, float w, float4 q) {
+    return make_float4(fmaf(w, q.x, acc.x), fmaf(w, q.y, acc.y), fmaf(w, q.z, acc.z), fmaf(w, q.w, acc.w));
+}
+__device__ __forceinline__ float4 f4_lerp(float w0, float4 q0, float w1, float4 q1) {
+    return f4_axpy(make_float4(w0 * q0.x, w0 * q0.y, w0 * q0.z, w0 * q0.w), w1, q1);
+}
+
+// cellq(i) returns the 16-B cell at linear index i of the array it reads;
+// base is corner (lo, lo, lo)'s index and sy, sz the array's row and slab
+// pitches.  A corner past the grid gets weight and gradient sign 0 and reads
+// a valid cell of the point's own range.
+template <class CellFn>
+__device__ __forceinline__ f3 gather_point_fast(const DevAsset& A, float dt, f3 vel, const Corners& C, int base, int sy,
+                                                int sz, CellFn cellq) {
+    using M = FastMath;
+    const bool rep = A.repulsion != 0.0f;
+    f3 gv = {0.f, 0.f, 0.f}, grad = {0.f, 0.f, 0.f};
+    float rho = 0.f;
+    if (C.cnt[0] > 0 && C.cnt[1] > 0 && C.cnt[2] > 0) {
+        float w[3][2];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+            for (int d = 0; d < 2; ++d)
+                w[ax][d] = d < C.cnt[ax] ? tri_w<M>(C.g[ax], C.flo[ax] + (float)d) : 0.f;
+        const int ox = C.cnt[0] > 1 ? 1 : 0, oy = C.cnt[1] > 1 ? sy : 0, oz = C.cnt[2] > 1 ? sz : 0;
+        // corner (a, b, c): z sums Zab first, then y sums Y[a], then the x sum; the
+        // repulsion gradient's y and z terms (ty over a and c, tz over a and b)
+        // accumulate as the corners stream by
+        float4 Y[2];
+        float ty[2] = {0.f, 0.f}, tz[2] = {0.f, 0.f};
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                const int i0 = base + (a ? ox : 0) + (b ? oy : 0);
+                const float4 q0 = cellq(i0);
+                const float4 q1 = cellq(i0 + oz);
+                const float4 Zab = f4_lerp(w[2][0], q0, w[2][1], q1);
+                Y[a] = b == 0 ? make_float4(w[1][0] * Zab.x, w[1][0] * Zab.y, w[1][0] * Zab.z, w[1][0] * Zab.w)
+                              : f4_axpy(Y[a], w[1][1], Zab);
+                if (rep) {
+                    ty[b] = fmaf(w[0][a], Zab.w, ty[b]);
+                    const float wab = w[0][a] * w[1][b];
+                    tz[0] = fmaf(wab, q0.w, tz[0]);
+                    tz[1] = fmaf(wab, q1.w, tz[1]);
+                }
+            }
+        const float4 X = f4_lerp(w[0][0], Y[0], w[0][1], Y[1]);
+        gv = f3{X.x, X.y, X.z};
+        if (rep) {
+            float sg[3][2];   // d(weight)/d(g) signs; 0 for a corner past the grid
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                for (int d = 0; d < 2; ++d)
+                    sg[ax][d] = d < C.cnt[ax] ? grad_sign<M>(C.g[ax], C.flo[ax] + (float)d) : 0.f;
+            rho = X.w;
+            grad.x = fmaf(sg[0][1], Y[1].w, sg[0][0] * Y[0].w);
+            grad.y = fmaf(sg[1][1], ty[1], sg[1][0] * ty[0]);
+            grad.z = fmaf(sg[2][1], tz[1], sg[2][0] * tz[0]);
         }
     }
     const float fr = A.friction;

@@ -23,7 +23,8 @@ constexpr int kSmemBytes = 72 * 1024;  // dynamic shared memory per CTA (grid bo
 constexpr int kMinCtasPerSm = 3;       // 3 x 72 KB of boxes and <= 80 registers per thread per SM
 constexpr int kUnionRounds = 4;        // rounds sharing one gather box and one splat box
 constexpr int kBoxCellsA = kSmemBytes / 16;   // phase A: 4 x int32 partial sums per cell
-constexpr int kBoxCellsB = kSmemBytes / 20;   // phase B: CellF without padding (float4 + rcp)
+// gather boxes: exact math keeps CellF (float4 + rcp, 20 B), fast math a 16-B normalised cell
+template <class M> constexpr int box_cells_b() { return M::kExact ? kSmemBytes / 20 : kSmemBytes / 16; }
 constexpr int kTileB = 2048;           // points per phase-B tile
 constexpr int kPtsB = kTileB / kThreads;
 
@@ -180,70 +181,65 @@ struct BoxWalk {
 };
 
 // Splat one point into the shared box (int32 partial sums): its corners with
-// x index in [G.lo[0], G.lo[0] + G.ext[0]).
-// The box is laid out as four arrays (vx, vy, vz, density) of `vol` cells, so
-// one component's atomics from a warp spread over the banks.  The six
-// trilinear weights of a point are computed once.  Exact math keeps the
-// oracle's int(scale * (w * v)); fast math shares scale * w.
-// Per-lane corner order (a permutation; integer sums do not depend on it).
-constexpr bool kRotateCorners = true;
-
+// x index in [G.lo[0], G.lo[0] + G.ext[0]).  The box holds four component
+// arrays (vx, vy, vz, density) kBoxCellsA cells apart, so each component's
+// address is the cell's plus a constant, and one component's atomics from a
+// warp spread over the banks.  The six trilinear weights of a point are
+// computed once.  Exact math keeps the oracle's int(scale * (w * v)); fast
+// math shares scale * w.
+// Per-lane corner order (integer sums do not depend on it): in step j lane l
+// adds corner j ^ (l mod 8), so lanes whose points share a cell hit different
+// corners in the same instruction.  The order is set once per point by
+// swapping the two corners of each axis whose bit is set in l mod 8; every
+// step then has compile-time corner indices, and each corner's weight is
+// still (wx * wy) * wz.
 template <int L, class M>
-__device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const BoxGeom& G,
-                                                int vol) {
+__device__ __forceinline__ void splat_point_box(const DevAsset& A, const Corners& C, f3 vel, int* box, const BoxGeom& G) {
     // the corners inside the slab: x in [dlo, dhi] of {0, 1}; y, z in [0, cnt - 1]
     const int x0 = G.lo[0] - C.lo[0];
     const int dlo = max(0, x0), dhi = min(C.cnt[0], x0 + G.ext[0]) - 1;
     if (dhi < dlo || C.cnt[1] <= 0 || C.cnt[2] <= 0) return;   // no corner in this slab
     // Branch-free corner loop: a missing corner gets weight 0 at a valid cell
     // of the point's own range, so its atomics add 0 (integer sums are unchanged).
-    float wx[2], wy[2], wz[2];
-    int ox[2], oy[2], oz[2];
+    float w[3][2];
+    int o[3][2];
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
         const bool ex = d >= dlo && d <= dhi, ey = d < C.cnt[1], ez = d < C.cnt[2];
-        wx[d] = ex ? tri_w<M>(C.g[0], C.lo[0] + d) : 0.f;
-        wy[d] = ey ? tri_w<M>(C.g[1], C.lo[1] + d) : 0.f;
-        wz[d] = ez ? tri_w<M>(C.g[2], C.lo[2] + d) : 0.f;
-        ox[d] = ex ? d : dlo;
-        oy[d] = (ey ? d : 0) * G.py;
-        oz[d] = (ez ? d : 0) * G.pz;
+        w[0][d] = ex ? tri_w<M>(C.g[0], C.flo[0] + (float)d) : 0.f;
+        w[1][d] = ey ? tri_w<M>(C.g[1], C.flo[1] + (float)d) : 0.f;
+        w[2][d] = ez ? tri_w<M>(C.g[2], C.flo[2] + (float)d) : 0.f;
+        o[0][d] = ex ? d : dlo;
+        o[1][d] = (ey ? d : 0) * G.py;
+        o[2][d] = (ez ? d : 0) * G.pz;
+    }
+    const int rot = (int)threadIdx.x & 7;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const bool sw = (rot >> ax) & 1;
+        const float w0 = w[ax][0], w1 = w[ax][1];
+        const int o0 = o[ax][0], o1 = o[ax][1];
+        w[ax][0] = sw ? w1 : w0;
+        w[ax][1] = sw ? w0 : w1;
+        o[ax][0] = sw ? o1 : o0;
+        o[ax][1] = sw ? o0 : o1;
     }
     int* const b0 = box + G.offset(C.lo[0], C.lo[1], C.lo[2]);
-    if (kRotateCorners) {
-        // corner j of this lane is corner j ^ (lane mod 8): lanes whose points share
-        // a cell then hit different corners in the same instruction
-        const int rot = (int)threadIdx.x & 7;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int q = j ^ rot;
-            const int da = q & 1, db = (q >> 1) & 1, dc = q >> 2;
-            const float w = M::mul(M::mul(da ? wx[1] : wx[0], db ? wy[1] : wy[0]), dc ? wz[1] : wz[0]);
-            int* cell = b0 + ((da ? ox[1] : ox[0]) + (db ? oy[1] : oy[0]) + (dc ? oz[1] : oz[0]));
-            int q0, q1, q2, q3;
-            corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
-            atomicAdd(cell, q0);
-            atomicAdd(cell + vol, q1);
-            atomicAdd(cell + 2 * vol, q2);
-            atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
-        }
-        return;
-    }
 #pragma unroll
     for (int da = 0; da < 2; ++da) {
 #pragma unroll
         for (int db = 0; db < 2; ++db) {
-            const float wxy = M::mul(wx[da], wy[db]);
+            const float wxy = M::mul(w[0][da], w[1][db]);
+            int* const bxy = b0 + (o[0][da] + o[1][db]);
 #pragma unroll
             for (int dc = 0; dc < 2; ++dc) {
-                const float w = M::mul(wxy, wz[dc]);
-                int* cell = b0 + (ox[da] + oy[db] + oz[dc]);
+                int* cell = bxy + o[2][dc];
                 int q0, q1, q2, q3;
-                corner_contribs<M>(A.scale, w, vel, q0, q1, q2, q3);
+                corner_contribs<M>(A.scale, M::mul(wxy, w[2][dc]), vel, q0, q1, q2, q3);
                 atomicAdd(cell, q0);
-                atomicAdd(cell + vol, q1);
-                atomicAdd(cell + 2 * vol, q2);
-                atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * vol), (unsigned)q3);
+                atomicAdd(cell + kBoxCellsA, q1);
+                atomicAdd(cell + 2 * kBoxCellsA, q2);
+                atomicAdd(reinterpret_cast<unsigned*>(cell + 3 * kBoxCellsA), (unsigned)q3);
             }
         }
     }
@@ -307,18 +303,24 @@ __device__ __forceinline__ void splat_points(const DevAsset& A, int* box, BoxSha
             P.py = P.ext[0] | 1;
             P.pz = (P.py * P.ext[1]) | 1;
             const int nv = P.pz * P.ext[2];
-            int4* b4 = reinterpret_cast<int4*>(box);
-            for (int c = threadIdx.x; c < nv; c += kThreads) b4[c] = make_int4(0, 0, 0, 0);
+            int4* b4 = reinterpret_cast<int4*>(box);   // four component arrays, kBoxCellsA cells apart
+            constexpr int kQ = kBoxCellsA / 4;
+            for (int c = threadIdx.x; c < (nv + 3) / 4; c += kThreads) {
+                b4[c] = make_int4(0, 0, 0, 0);
+                b4[kQ + c] = make_int4(0, 0, 0, 0);
+                b4[2 * kQ + c] = make_int4(0, 0, 0, 0);
+                b4[3 * kQ + c] = make_int4(0, 0, 0, 0);
+            }
             __syncthreads();
-            visit([&](f3 p, f3 v) { splat_point_box<L, M>(A, corners_of<M>(A, p), v, box, P, nv); });
+            visit([&](f3 p, f3 v) { splat_point_box<L, M>(A, corners_of<M>(A, p), v, box, P); });
             __syncthreads();
             bool ok = true;
             for (int c = threadIdx.x; c < nv; c += kThreads)
-                ok = ok && vmax * ((float)(unsigned)box[3 * nv + c] + (float)npts) < 2.0e9f;
+                ok = ok && vmax * ((float)(unsigned)box[3 * kBoxCellsA + c] + (float)npts) < 2.0e9f;
             if (__syncthreads_and(ok)) {
                 const BoxWalk W(P);
                 for (int c = threadIdx.x; c < nv; c += kThreads) {
-                    const int4 v = make_int4(box[c], box[nv + c], box[2 * nv + c], box[3 * nv + c]);
+                    const int4 v = make_int4(box[c], box[kBoxCellsA + c], box[2 * kBoxCellsA + c], box[3 * kBoxCellsA + c]);
                     if (!(v.x | v.y | v.z | v.w)) continue;   // untouched (padding cells always are)
                     int a, b, cc;
                     W.cell(P, c, a, b, cc);
@@ -374,10 +376,11 @@ __device__ __forceinline__ void for_lane_points(f3 (&x)[K], f3 (&v)[K], unsigned
     }
 }
 
-// Copies the box's cells of grid G into shared memory as CellF (float4
-// {vx, vy, vz, rc} at bf[c], rcp at br[c]).  Padding cells are skipped, and so
-// are cells past the grid's last layer: a point beyond the grid has no corner
-// on that axis but still widens the box there.
+// Copies the box's cells of grid G into shared memory: exact math as CellF
+// (float4 {vx, vy, vz, rc} at bf[c], rcp at br[c]), fast math as the 16-B
+// normalised cell at bf[c].  Padding cells are skipped, and so are cells past
+// the grid's last layer: a point beyond the grid has no corner on that axis
+// but still widens the box there.
 template <class M>
 __device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigned long long* grid, const BoxGeom& G,
                                                 float4* bf, float* br) {
@@ -387,9 +390,14 @@ __device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigne
     for (int c = threadIdx.x; c < vol; c += kThreads) {
         int a, b, cc;
         if (!W.cell(G, c, a, b, cc) || a >= A.nx || b >= A.ny || cc >= A.nz) continue;
-        const CellF cf = cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + cc * nxny));
-        bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.rc);
-        br[c] = cf.rcp;
+        const unsigned idx = (unsigned)(a + b * A.nx + cc * nxny);
+        if constexpr (M::kExact) {
+            const CellF cf = cell_from_global<M>(A, grid, idx);
+            bf[c] = make_float4(cf.vx, cf.vy, cf.vz, cf.rc);
+            br[c] = cf.rcp;
+        } else {
+            bf[c] = cellq_from_global(A, grid, idx);
+        }
     }
 }
 
@@ -398,9 +406,15 @@ __device__ __forceinline__ void load_gather_box(const DevAsset& A, const unsigne
 template <class M>
 __device__ __forceinline__ f3 gather_point_direct(const DevAsset& A, const unsigned long long* grid, float dt, f3 x, f3 v) {
     const int nxny = A.nx * A.ny;
-    return gather_point<M>(A, dt, x, v, corners_of<M>(A, x), [&](int a, int b, int c) {
-        return cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + c * nxny));
-    });
+    if constexpr (M::kExact) {
+        return gather_point<M>(A, dt, x, v, corners_of<M>(A, x), [&](int a, int b, int c) {
+            return cell_from_global<M>(A, grid, (unsigned)(a + b * A.nx + c * nxny));
+        });
+    } else {
+        const Corners C = corners_of<M>(A, x);
+        return gather_point_fast(A, dt, v, C, C.lo[0] + C.lo[1] * A.nx + C.lo[2] * nxny, A.nx, nxny,
+                                 [&](int i) { return cellq_from_global(A, grid, (unsigned)i); });
+    }
 }
 
 // The CTA's gather box over grid `grid` (after LaneBounds::reduce of the
@@ -420,14 +434,15 @@ struct GatherBox {
     const unsigned long long* grid;
     const GatherShared& GS;
     unsigned char* smem;
+    static constexpr int kCap = box_cells_b<M>();
     __device__ __forceinline__ GatherBox(const DevAsset& a, const unsigned long long* g, unsigned char* sm,
                                          const BoxShared& S, GatherShared& gs, unsigned* stats)
         : A(a), grid(g), GS(gs), smem(sm) {
         if (!grid) return;   // nothing to gather (uniform across the CTA)
         const int npts = S.npts;
         const BoxGeom G = box_geom(S);
-        const bool use = npts > 0 && G.vol <= kBoxCellsB;
-        if (use) load_gather_box<M>(A, grid, G, reinterpret_cast<float4*>(smem), reinterpret_cast<float*>(smem + 16 * kBoxCellsB));
+        const bool use = npts > 0 && G.vol <= kCap;
+        if (use) load_gather_box<M>(A, grid, G, reinterpret_cast<float4*>(smem), reinterpret_cast<float*>(smem + 16 * kCap));
         if (threadIdx.x == 0) {
             gs.G = G;
             gs.use = use ? 1 : 0;
@@ -439,13 +454,18 @@ struct GatherBox {
         const Corners C = corners_of<M>(A, x);
         if (GS.use) {
             const float4* bf = reinterpret_cast<const float4*>(smem);
-            const float* br = reinterpret_cast<const float*>(smem + 16 * kBoxCellsB);
             const BoxGeom& G = GS.G;
-            return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
-                const int li = G.offset(a, b, c);
-                const float4 q = bf[li];
-                return CellF{q.x, q.y, q.z, q.w, br[li]};
-            });
+            if constexpr (M::kExact) {
+                const float* br = reinterpret_cast<const float*>(smem + 16 * kCap);
+                return gather_point<M>(A, dt, x, v, C, [&](int a, int b, int c) {
+                    const int li = G.offset(a, b, c);
+                    const float4 q = bf[li];
+                    return CellF{q.x, q.y, q.z, q.w, br[li]};
+                });
+            } else {
+                return gather_point_fast(A, dt, v, C, G.offset(C.lo[0], C.lo[1], C.lo[2]), G.py, G.pz,
+                                         [&](int i) { return bf[i]; });
+            }
         }
         return gather_point_direct<M>(A, grid, dt, x, v);
     }
