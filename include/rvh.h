@@ -213,9 +213,12 @@ typedef struct rvh_shade_desc {
     int32_t map_mode;       /* RVH_SHADE_MAPS_QUADS (reference): the light passes rasterise hair.geom's
                                quads in the light's view; RVH_SHADE_MAPS_VERTICES: each tessellated
                                vertex covers one texel (cheaper) */
-    int32_t reserved;
+    int32_t image_mode;     /* rvh_asset_render_hair: RVH_IMAGE_BLEND (reference): the hair pipeline's
+                               in-order alpha blending (Renderer.cpp:1657-1679); RVH_IMAGE_NEAREST: each
+                               pixel takes its nearest fragment's colour (cheaper) */
 } rvh_shade_desc;
 enum { RVH_SHADE_MAPS_VERTICES = 0, RVH_SHADE_MAPS_QUADS = 1 };
+enum { RVH_IMAGE_NEAREST = 0, RVH_IMAGE_BLEND = 1 };
 /* The reference's cameras and map size (glm's float arithmetic, bit for bit). */
 rvh_status rvh_shade_desc_reference(rvh_shade_desc* d);
 /* hair.frag for n caller-given fragments (replaces the fragment stage of the
@@ -250,13 +253,24 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
  * the hair pipeline, src/Renderer.cpp:1554-1746): each isoline segment of the
  * tessellation (vertices and frames from rvh_asset_tessellate with td) becomes
  * the geometry shader's camera-facing quad of width (|random(3.242551 u, u u)| +
- * 0.5) * 0.075 * distance * strandWidth, rasterised with a LESS depth test; each
- * pixel takes hair.frag's colour of its nearest fragment, with perspective-
- * correct inputs and the maps of rvh_asset_shade (sd's light and map size).
- * image: width x height float4 (empty pixels 0); fragment_ids (device, nullable):
- * width x height uint32, the winning segment (s * n_lines + j) * n_segments + k
- * or 0xffffffff.  Order-dependent alpha blending is left out; quads with a corner
- * behind the camera or covering more than 65,536 pixels are dropped. */
+ * 0.5) * 0.075 * distance * strandWidth, rasterised with a LESS depth test and
+ * shaded by hair.frag with perspective-correct inputs and the maps of
+ * rvh_asset_shade (sd's light and map size).
+ * sd->image_mode RVH_IMAGE_BLEND (the reference pipeline): quads in segment
+ * order, each quad's triangles (V0, V1, V2) then (V2, V1, V3); a fragment that
+ * passes the depth test against the earlier fragments (depth cleared to 1.0)
+ * writes its depth and blends SRC_ALPHA / ONE_MINUS_SRC_ALPHA into the colour and
+ * ONE / ONE into the alpha (clamped to 1); the image starts at the reference's
+ * clear colour (101, 129, 140, 255) / 255 (the head mesh the reference draws
+ * first is not drawn) and is kept in float (the reference's 8-bit swapchain
+ * rounds each write).  Fewer than 2^31 segments.  Uses device scratch of 12 B
+ * per pixel and 8 B per fragment, admitted against the context's budget.
+ * RVH_IMAGE_NEAREST: each pixel takes its nearest fragment's colour (empty
+ * pixels 0).
+ * image: width x height float4; fragment_ids (device, nullable): width x height
+ * uint32, the nearest fragment's segment (s * n_lines + j) * n_segments + k (in
+ * blend mode the last one written, which is the same), or 0xffffffff.  Quads with
+ * a corner behind the camera or covering more than 65,536 pixels are dropped. */
 rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
                                  const void* frames, const void* depth_map, const void* opacity_map, int32_t width,
                                  int32_t height, void* image, void* fragment_ids, void* stream);
@@ -314,7 +328,8 @@ rvh_status rvh_asset_restore(rvh_context* ctx, const void* host_src, uint64_t by
 typedef struct rvh_batch_desc {
     int32_t lanes_per_strand;     /* 0 = tuner's choice (8 without a tuned record); else 1 (one thread walks
                                      each strand), 4, 8, 16, 32 */
-    int32_t strands_per_tile;     /* phase-A tile size; 0 = tuner's choice */
+    int32_t strands_per_tile;     /* phase-A tile size in strands; 0 = the tuner's choice with lanes_per_strand 0,
+                                     else whole groups of rounds (the kernel's box span) near 4,096 points */
     int32_t ctas_per_sm;          /* 0 = occupancy limit */
     int32_t use_graph;            /* 1 = capture the launch in a CUDA graph (default) */
     int32_t full_steps;           /* 0 (default): fused steps - each launch first applies the previous
@@ -370,8 +385,8 @@ rvh_status rvh_batch_timing_read(rvh_batch* b, double* total_ms, int32_t* launch
 
 /* ---- autotuning -------------------------------------------------------------
  * Times real batched steps of `assets` for every candidate: lanes per strand
- * {1, 4, 8, 16, 32} (strands per warp 32, 8, 4, 2, 1) x phase-A tile {1, 2, 4}
- * rounds, and with tune_grid also each listed grid resolution (every
+ * {1, 4, 8, 16, 32} (strands per warp 32, 8, 4, 2, 1) x phase-A tile {whole
+ * groups near 4,096 points, 1, 2, 4 rounds}, and with tune_grid also each listed grid resolution (every
  * grid-enabled asset re-gridded over the same bounds).  The strand records
  * are restored after every trial.  The winner is cached per workload
  * signature; rvh_batch_create with lanes_per_strand = 0 uses it. */

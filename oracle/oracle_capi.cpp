@@ -164,6 +164,23 @@ int oracle_render_hair(const float* verts, const float* frames, int ns, int n, i
                                ids);
     return 0;
 }
+/* The hair pass with the pipeline's in-order blending (shade_oracle.hpp
+ * render_hair_blend), from clear colour clear_rgba. */
+int oracle_render_hair_blend(const float* verts, const float* frames, int ns, int n, int n_lines, int n_segments,
+                             const float* camera_view, const float* camera_proj, const float* light_view,
+                             const float* light_proj, const float* depth, const float* opacity, int mw, int mh, int w,
+                             int h, int sin_mode, const float* clear_rgba, float* image, uint32_t* ids) {
+    if (!verts || !frames || !image || !depth || !opacity || !clear_rgba || ns < 0 || n < 2 || n_lines < 1 ||
+        n_segments < 1 || w < 1 || h < 1 || mw < 1 || mh < 1)
+        return 1;
+    oracle::shade::Raster R;
+    if (!oracle::shade::make_raster(camera_view, camera_proj, light_view, light_proj, w, h, R)) return 2;
+    const oracle::shade::Maps M{depth, opacity, mw, mh};
+    oracle::shade::render_hair_blend(verts, frames, ns, n, n_lines, n_segments, R, M,
+                                     sin_mode == 0 ? oracle::shade::RefSin::kFloat : oracle::shade::RefSin::kDouble,
+                                     clear_rgba, image, ids);
+    return 0;
+}
 /* Light depth and deep opacity maps rasterised from hair.geom's quads in the
  * light's view (shade_oracle.hpp light_maps_quads). */
 int oracle_shade_maps_quads(const float* verts, int ns, int n_lines, int n_segments, const float* light_view,

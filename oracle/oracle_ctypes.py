@@ -48,6 +48,9 @@ def lib():
         l.oracle_shade_maps_quads.argtypes = [f4, C.c_int, C.c_int, C.c_int, f4, f4, C.c_int, C.c_int, C.c_int, f4, f4]
         l.oracle_render_hair.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4, f4, f4, C.c_int,
                                          C.c_int, C.c_int, C.c_int, C.c_int, f4, _P(C.c_uint32)]
+        l.oracle_render_hair_blend.argtypes = [f4, f4, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, f4, f4, f4, f4,
+                                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, f4, f4, _P(C.c_uint32)]
+        l.oracle_render_hair_blend.restype = C.c_int
         for f in (l.oracle_shade_fragments, l.oracle_shade_camera, l.oracle_opacity_fragments, l.oracle_shade_maps, l.oracle_shade_vertex_inputs,
                   l.oracle_render_image, l.oracle_render_hair, l.oracle_shade_maps_quads):
             f.restype = C.c_int
@@ -365,9 +368,15 @@ def render_image(vertices, colors, desc, width, height):
     return img
 
 
+# the reference framebuffer's clear colour (src/Renderer.cpp:2235)
+CLEAR_RGBA = np.array([101.0 / 255.0, 129.0 / 255.0, 140.0 / 255.0, 1.0], np.float32)
+
+
 def render_hair(vertices, frames, n_points, n_lines, n_segments, desc, depth, opacity, width, height, sin_mode=1):
     """hair.geom's quads rasterised into a (height, width, 4) image shaded by
-    hair.frag, and the winning segment id per pixel (0xffffffff: none)."""
+    hair.frag, and per pixel the nearest fragment's segment id (0xffffffff:
+    none).  desc.image_mode 1 (blend): the pipeline's in-order blending from the
+    reference's clear colour; 0: the nearest fragment's colour."""
     v, fr = _f32(vertices), _f32(frames)
     dep, opa = _f32(depth), _f32(opacity)
     ns = v.shape[0]
@@ -375,8 +384,12 @@ def render_hair(vertices, frames, n_points, n_lines, n_segments, desc, depth, op
     img = np.zeros((height, width, 4), np.float32)
     ids = np.zeros((height, width), np.uint32)
     mh, mw = dep.shape
-    _check(lib().oracle_render_hair(_fptr(v, C.c_float), _fptr(fr, C.c_float), ns, n_points, n_lines, n_segments,
-                                    *[_fptr(a, C.c_float) for a in (cv, cp, lv, lp, dep, opa)], mw, mh, width, height,
-                                    sin_mode, _fptr(img, C.c_float), ids.ctypes.data_as(_P(C.c_uint32))),
-           "oracle_render_hair")
+    args = [_fptr(v, C.c_float), _fptr(fr, C.c_float), ns, n_points, n_lines, n_segments,
+            *[_fptr(a, C.c_float) for a in (cv, cp, lv, lp, dep, opa)], mw, mh, width, height, sin_mode]
+    if getattr(desc, "image_mode", 0) == 1:
+        _check(lib().oracle_render_hair_blend(*args, _fptr(CLEAR_RGBA, C.c_float), _fptr(img, C.c_float),
+                                              ids.ctypes.data_as(_P(C.c_uint32))), "oracle_render_hair_blend")
+    else:
+        _check(lib().oracle_render_hair(*args, _fptr(img, C.c_float), ids.ctypes.data_as(_P(C.c_uint32))),
+               "oracle_render_hair")
     return img, ids

@@ -615,6 +615,59 @@ inline int cover_quad(const Quad& Q, int px, int py, int idx[3], float l[3], flo
 /* hair.geom's per-isoline width factor |random(3.242551 u, u u)| + 0.5 (:46). */
 inline float geom_rand(float u, RefSin mode) { return std::fabs(frag_random(3.242551f * u, u * u, mode)) + 0.5f; }
 
+/* hair.frag's outColor for the fragment of segment (s, j, k)'s quad Q at a
+ * pixel, covered by the quad's triangle with corners idx[] and barycentrics
+ * l[]: the corners' inputs (V0, V1 take vertex k's, V2, V3 vertex k + 1's)
+ * interpolated perspective-correctly. */
+inline void segment_fragment(const float* verts, const float* frames, int n, int L, int S, const Raster& R,
+                             const Maps& M, float bright, int s, int j, int k, const Quad& Q, const int idx[3],
+                             const float l[3], float o[4]) {
+    const int S1 = S + 1;
+    auto vert = [&](int kk) { return verts + 4 * ((size_t(s) * L + j) * S1 + kk); };
+    float attr[4][24];
+    for (int c = 0; c < 4; ++c) {
+        const int kk = c < 2 ? k : k + 1;
+        const float* p = vert(kk);
+        const V3 pos = mk(p[0], p[1], p[2]);
+        const float u = (float)j / (float)L, v = (float)kk / (float)S;
+        const float x = v * (float)(n - 1);
+        const int sf = std::min((int)std::floor(x), n - 2);
+        const float* fr = frames + (size_t(s) * (n - 1) + sf) * 12;
+        float* a = attr[c];
+        a[0] = u;
+        a[1] = v;
+        for (int q = 0; q < 3; ++q)
+            for (int e = 0; e < 3; ++e) a[2 + 3 * q + e] = fr[4 * q + e];
+        const V3 vd = normalize(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+        const V3 ld = normalize(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+        a[11] = vd.x;
+        a[12] = vd.y;
+        a[13] = vd.z;
+        a[14] = ld.x;
+        a[15] = ld.y;
+        a[16] = ld.z;
+        mul_vec4(R.lmap, Q.clip[c], a + 17);
+        a[21] = a[22] = a[23] = 0.f;
+    }
+    const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+    const float qs = (q0 + q1) + q2;
+    float in[24];
+    for (int e = 0; e < 24; ++e) in[e] = ((q0 * attr[idx[0]][e] + q1 * attr[idx[1]][e]) + q2 * attr[idx[2]][e]) / qs;
+    in[0] = (float)j / (float)L;
+    shade_fragment_bright(in, M, bright, o);
+}
+
+/* Per-isoline factors: hair.geom's width factor and hair.frag's brightness. */
+inline void isoline_factors(int L, RefSin mode, std::vector<float>& rnd, std::vector<float>& bright) {
+    rnd.resize(L);
+    bright.resize(L);
+    for (int j = 0; j < L; ++j) {
+        const float u = (float)j / (float)L;
+        rnd[j] = geom_rand(u, mode);
+        bright[j] = 0.8f * std::fabs(frag_random(u, u, mode)) + 0.6f;
+    }
+}
+
 /* The camera image of a tessellation (vertices ns x L x (S+1) float4, frames
  * ns x (n-1) x 3 float4) shaded with hair.frag over the given maps; ids (nullable)
  * receives the winning segment id per pixel, 0xffffffff where none. */
@@ -622,12 +675,8 @@ inline void render_hair(const float* verts, const float* frames, int ns, int n, 
                         const Maps& M, RefSin mode, float* image, uint32_t* ids) {
     const int W = R.width, H = R.height;
     std::vector<uint64_t> key(size_t(W) * H, ~0ull);
-    std::vector<float> rnd(L), bright(L);
-    for (int j = 0; j < L; ++j) {
-        const float u = (float)j / (float)L;
-        rnd[j] = geom_rand(u, mode);
-        bright[j] = 0.8f * std::fabs(frag_random(u, u, mode)) + 0.6f;
-    }
+    std::vector<float> rnd, bright;
+    isoline_factors(L, mode, rnd, bright);
     const int S1 = S + 1;
     auto vert = [&](int s, int j, int k) { return verts + 4 * ((size_t(s) * L + j) * S1 + k); };
     const long long nseg = (long long)ns * L * S;
@@ -669,42 +718,61 @@ inline void render_hair(const float* verts, const float* frames, int ns, int n, 
             int idx[3];
             float l[3], z;
             cover_quad(Q, px, py, idx, l, z);
-            // the corners' hair.frag inputs: V0, V1 take vertex k's, V2, V3 vertex k + 1's
-            float attr[4][24];
-            for (int c = 0; c < 4; ++c) {
-                const int kk = c < 2 ? k : k + 1;
-                const float* p = vert(s, j, kk);
-                const V3 pos = mk(p[0], p[1], p[2]);
-                const float u = (float)j / (float)L, v = (float)kk / (float)S;
-                const float x = v * (float)(n - 1);
-                const int sf = std::min((int)std::floor(x), n - 2);
-                const float* fr = frames + (size_t(s) * (n - 1) + sf) * 12;
-                float* a = attr[c];
-                a[0] = u;
-                a[1] = v;
-                for (int q = 0; q < 3; ++q)
-                    for (int e = 0; e < 3; ++e) a[2 + 3 * q + e] = fr[4 * q + e];
-                const V3 vd = normalize(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
-                const V3 ld = normalize(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
-                a[11] = vd.x;
-                a[12] = vd.y;
-                a[13] = vd.z;
-                a[14] = ld.x;
-                a[15] = ld.y;
-                a[16] = ld.z;
-                mul_vec4(R.lmap, Q.clip[c], a + 17);
-                a[21] = a[22] = a[23] = 0.f;
-            }
-            const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
-            const float qs = (q0 + q1) + q2;
-            float in[24];
-            for (int e = 0; e < 24; ++e)
-                in[e] = ((q0 * attr[idx[0]][e] + q1 * attr[idx[1]][e]) + q2 * attr[idx[2]][e]) / qs;
-            in[0] = (float)j / (float)L;
-            float o[4];
-            shade_fragment_bright(in, M, bright[j], o);
-            for (int c = 0; c < 4; ++c) out[c] = o[c];
+            segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, out);
         }
+}
+
+/* The hair pass as the reference's pipeline draws it (src/Renderer.cpp:1657-1679):
+ * segments in order, each quad's triangles (V0, V1, V2) then (V2, V1, V3); a
+ * fragment passes the LESS depth test against the depth the fragments before it
+ * wrote (cleared to 1.0, Renderer.cpp:2236), writes its depth and blends
+ * SRC_ALPHA / ONE_MINUS_SRC_ALPHA into the colour, ONE / ONE into the alpha
+ * (clamped to 1, as the unorm target clamps), hair.frag's alpha being 0.75.
+ * The colour starts at clear_rgba (the reference clears to (101, 129, 140,
+ * 255) / 255 and draws the head mesh first; here the hair alone is drawn) and
+ * is kept in float (the reference's 8-bit swapchain rounds every write).
+ * ids (nullable): the last fragment written per pixel (its nearest), or
+ * 0xffffffff. */
+inline void render_hair_blend(const float* verts, const float* frames, int ns, int n, int L, int S, const Raster& R,
+                              const Maps& M, RefSin mode, const float clear_rgba[4], float* image, uint32_t* ids) {
+    const int W = R.width, H = R.height;
+    std::vector<float> depth(size_t(W) * H, 1.0f);
+    for (size_t p = 0; p < size_t(W) * H; ++p) {
+        for (int c = 0; c < 4; ++c) image[4 * p + c] = clear_rgba[c];
+        if (ids) ids[p] = 0xffffffffu;
+    }
+    std::vector<float> rnd, bright;
+    isoline_factors(L, mode, rnd, bright);
+    const int S1 = S + 1;
+    auto vert = [&](int s, int j, int k) { return verts + 4 * ((size_t(s) * L + j) * S1 + k); };
+    const long long nseg = (long long)ns * L * S;
+    for (long long id = 0; id < nseg; ++id) {
+        const int k = int(id % S);
+        const long long line = id / S;
+        const int j = int(line % L), s = int(line / L);
+        const float* pk = vert(s, j, k);
+        const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
+        if (!Q.ok) continue;
+        for (int tri = 0; tri < 2; ++tri)
+            for (int py = Q.y0; py <= Q.y1; ++py)
+                for (int px = Q.x0; px <= Q.x1; ++px) {
+                    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+                    int idx[3];
+                    float l[3], z;
+                    const bool cov = tri == 0 ? cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z)
+                                              : cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
+                    const size_t p = size_t(py) * W + px;
+                    if (!cov || !(z < depth[p])) continue;
+                    depth[p] = z;
+                    float c[4];
+                    segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, c);
+                    float* out = image + 4 * p;
+                    const float ia = 1.0f - c[3];
+                    for (int e = 0; e < 3; ++e) out[e] = c[e] * c[3] + out[e] * ia;
+                    out[3] = std::min(1.0f, c[3] + out[3]);
+                    if (ids) ids[p] = uint32_t(id);
+                }
+    }
 }
 
 

@@ -22,6 +22,7 @@ struct Batch {
     Context* ctx = nullptr;
     std::vector<Asset*> assets;
     std::vector<int> modes;   // per asset: MODE_FUSED (loop 3 left pending), MODE_FULL, MODE_FINISH
+    std::vector<int> tile_strands;   // per asset: strands per phase-A item of the current plan
     int lanes = 4;
     bool exact = false;
     bool use_graph = true;
@@ -110,6 +111,7 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     });
     b.items.clear();
     b.need_a.assign(b.assets.size(), 0u);
+    b.tile_strands.assign(b.assets.size(), 0);
     const size_t lag = size_t(2) * size_t(std::max(1, b.n_ctas));
     struct Pending {
         int asset;
@@ -136,8 +138,18 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
             emit_b(ai);
             continue;
         }
-        int ta = strands_per_tile > 0 ? strands_per_tile : target_points / a->n_points;
-        ta = std::max(quantum, (ta + quantum - 1) / quantum * quantum);
+        int ta;
+        if (strands_per_tile > 0) {
+            ta = std::max(quantum, (strands_per_tile + quantum - 1) / quantum * quantum);
+        } else {
+            // whole groups of rounds (the kernel's boxes span a group: at most kUnionRounds rounds and
+            // fewer than 4e9 / scale points), the nearest to target_points
+            const float cap = 4.0e9f / (a->params.grid_scale * float(quantum * a->n_points));
+            const int group = quantum * std::max(1, std::min(kUnionRounds, int(cap)));
+            const int want = std::max(1, target_points / a->n_points);
+            ta = std::max(1, (want + group / 2) / group) * group;
+        }
+        b.tile_strands[ai] = ta;
         for (int s = 0; s < a->n_strands; s += ta) {
             b.items.push_back({ITEM_A, ai, s, std::min(a->n_strands, s + ta)});
             b.need_a[ai]++;
@@ -156,11 +168,21 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
 
 // Grid choice of one asset for one batched step: gather the pending friction from
 // grid[prev], splat into grid[t] (cleared first if dirty), clear grid[u] in-kernel.
+// box_tag: the group-box tag this launch writes (0: none).
 struct GridUse {
     int prev = -1, t = -1, u = -1;
+    uint32_t box_tag = 0;
 };
 
-rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s, DevAsset* view, GridUse* gu) {
+// The grouping of an asset's phase-A rounds in a launch: lanes per strand and
+// strands per item (groups are counted from each item's first round).  One
+// thread per strand (lanes 1) keeps no group boxes: 0.
+uint32_t box_layout_of(int lanes, int tile_strands) {
+    return lanes > 1 ? (uint32_t(lanes) << 24) | uint32_t(tile_strands) : 0u;
+}
+
+rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s, DevAsset* view, GridUse* gu,
+                         uint32_t layout) {
     *gu = GridUse{};
     if (!a->params.grid_enabled) {
         *view = a->device_view(f, -1);
@@ -180,10 +202,22 @@ rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s,
     if (a->grid_dirty[gu->t]) RVH_CUDA(cudaMemsetAsync(a->grid[gu->t].ptr, 0, a->grid_bytes(), s));
     gu->u = a->pick_grid(gu->prev, gu->t);
     *view = a->device_view(f, gu->t, gu->prev, gu->u);
+    // group boxes: one record pair per round of 8 strands at most (32 lanes per strand)
+    if (layout && !a->group_boxes.ptr && a->n_strands > 0) {
+        const size_t groups = (size_t(a->n_strands) + 7) / 8;
+        // optional: without it every fused step recomputes its gather boxes
+        if (a->ctx->alloc(a->group_boxes, groups * 2 * sizeof(int4)) != RVH_OK) set_error("");
+    }
+    if (layout && a->group_boxes.ptr) {
+        view->group_box = static_cast<int4*>(a->group_boxes.ptr);
+        view->box_tag_read = (a->pending && a->box_layout == layout) ? a->box_tag : 0u;
+        gu->box_tag = a->box_tag + 1u ? a->box_tag + 1u : 1u;
+        view->box_tag_write = gu->box_tag;
+    }
     return RVH_OK;
 }
 
-void commit_asset(Asset* a, int mode, const GridUse& gu, float dt) {
+void commit_asset(Asset* a, int mode, const GridUse& gu, float dt, uint32_t layout) {
     if (!a->params.grid_enabled) return;
     if (mode == MODE_FINISH) {
         a->pending = false;
@@ -197,6 +231,8 @@ void commit_asset(Asset* a, int mode, const GridUse& gu, float dt) {
     a->pending = mode == MODE_FUSED;
     a->pend = gu.t;
     a->dt_prev = dt;
+    a->box_tag = gu.box_tag ? gu.box_tag : a->box_tag;
+    a->box_layout = gu.box_tag ? layout : 0u;
 }
 
 void destroy(Batch* b) {
@@ -369,7 +405,8 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     RVH_CUDA(cudaEventSynchronize(b.staged[slot]));
     std::vector<GridUse> gus(assets.size());
     for (size_t i = 0; i < assets.size(); ++i) {
-        rvh_status ps = prepare_asset(assets[i], modes[i], frames[i], s, &b.h_stage[slot][i], &gus[i]);
+        rvh_status ps = prepare_asset(assets[i], modes[i], frames[i], s, &b.h_stage[slot][i], &gus[i],
+                                      box_layout_of(b.lanes, b.tile_strands[i]));
         if (ps != RVH_OK) return ps;
         d->h_need[slot][i] = b.need_a[i];
     }
@@ -382,7 +419,8 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     rvh_status ls = enqueue_launch(&b, s);
     if (ls != RVH_OK) return ls;
     if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
-    for (size_t i = 0; i < assets.size(); ++i) commit_asset(assets[i], modes[i], gus[i], frames[i].dt);
+    for (size_t i = 0; i < assets.size(); ++i)
+        commit_asset(assets[i], modes[i], gus[i], frames[i].dt, box_layout_of(b.lanes, b.tile_strands[i]));
     return RVH_OK;
 }
 
@@ -523,6 +561,8 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
 }
 
 rvh_status rvh_batch_destroy(rvh_batch* b) {
+    if (!b) return RVH_OK;
+    DeviceGuard g(b->ctx ? b->ctx->device : 0);   // releases even if the switch fails
     destroy(b);
     return RVH_OK;
 }
@@ -548,7 +588,8 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
     DevAsset* st = b->h_stage[slot];
     std::vector<GridUse> gus(b->assets.size());
     for (size_t i = 0; i < b->assets.size(); ++i) {
-        rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i]);
+        rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i],
+                                      box_layout_of(b->lanes, b->tile_strands[i]));
         if (ps != RVH_OK) return ps;
         st[i].pos_xyz = xyz ? xyz + 3 * b->first_point[i] : nullptr;
     }
@@ -575,7 +616,8 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
         RVH_CUDA(cudaEventRecord(ev.second, s));
         b->ev_pairs.push_back(ev);
     }
-    for (size_t i = 0; i < b->assets.size(); ++i) commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt);
+    for (size_t i = 0; i < b->assets.size(); ++i)
+        commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt, box_layout_of(b->lanes, b->tile_strands[i]));
     return RVH_OK;
 }
 

@@ -406,7 +406,7 @@ rvh_status rvh_context_create(const rvh_context_desc* desc, rvh_context** out) {
 
 rvh_status rvh_context_destroy(rvh_context* ctx) {
     if (!ctx) return RVH_OK;
-    RVH_DEVICE(ctx->device);
+    DeviceGuard g(ctx->device);   // releases even if the switch fails
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -599,7 +599,7 @@ rvh_status rvh_asset_create(rvh_context* ctx, const rvh_asset_desc* desc, rvh_as
 
 rvh_status rvh_asset_destroy(rvh_asset* a) {
     if (!a) return RVH_OK;
-    RVH_DEVICE(a->ctx->device);
+    DeviceGuard g(a->ctx->device);   // releases even if the switch fails
     cudaStreamSynchronize(a->ctx->stream);
     Context* c = a->ctx;
     c->free(a->strands);
@@ -608,8 +608,11 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     for (int i = 0; i < 3; ++i) c->free(a->grid[i]);
     c->free(a->draw);
     c->free(a->root_rest);
+    c->free(a->group_boxes);
     c->free(a->tess_tables);
     c->free(a->tess_cache);
+    c->free(a->raster_px);
+    c->free(a->raster_frags);
     delete a;
     return RVH_OK;
 }

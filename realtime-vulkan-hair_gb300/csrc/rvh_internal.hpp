@@ -145,9 +145,17 @@ struct Asset {
     bool head_active = false;
     float head[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};   // column-major
     DevBuf root_rest;   // float4 per strand, captured at the first head transform
+    // phase-A group boxes a fused batched step leaves for the next one (DevAsset::group_box):
+    // the tag of the last write and the grouping (lanes, strands per tile) it was written with
+    DevBuf group_boxes;
+    uint32_t box_tag = 0;
+    uint32_t box_layout = 0;
     // tessellation tables of the last descriptor (rvh_asset_tessellate)
     DevBuf tess_tables;
     DevBuf tess_cache;   // per strand: root bits and the sd profiles computed from them
+    // rvh_asset_render_hair's blending scratch: per-pixel counts, offsets, cursors and tile sums;
+    // the per-pixel fragment lists
+    DevBuf raster_px, raster_frags;
     rvh_tess_desc tess_desc{};
     size_t tess_off[6] = {0, 0, 0, 0, 0, 0};
 

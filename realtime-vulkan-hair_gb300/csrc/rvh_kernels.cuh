@@ -471,6 +471,23 @@ struct GatherBox {
     }
 };
 
+// ---- L2 prefetch ----------------------------------------------------------------
+// Asks L2 to fetch `bytes` (a multiple of 16) at p (16-byte aligned); the
+// thread does not wait.  L2 is the GPU's point of coherence, so a prefetch
+// never returns stale data.
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Positions and velocities (adjacent in the record, 32 n bytes per strand) and
+// rest lengths of strands [s0, s1), s0 a multiple of 8 (an item's first strand).  The rest buffer is
+// allocated in 256-B units, so rounding its range up to 16 B stays inside.
+__device__ __forceinline__ void prefetch_strands(const float4* strands, const float* rest, int n, int s0, int s1) {
+    for (int s = s0 + (int)threadIdx.x; s < s1; s += kThreads)
+        prefetch_l2(strands + (size_t)s * (3 * n), 32u * (unsigned)n);
+    if (threadIdx.x == kThreads - 1 && s1 > s0) prefetch_l2(rest + s0, ((unsigned)(s1 - s0) * 4u + 15u) & ~15u);
+}
+
 // Strands [begin, end) of one asset in rounds of kWarps * (32/L) strands,
 // handled in groups of U consecutive rounds that share one gather box and one
 // splat box (fewer box loads, flushes and barriers than a box per round; a
@@ -497,9 +514,31 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
     const int U = max(1, min(kUnionRounds, (int)cap));
     // a warp's strands are spread over the round (neighbouring strands share cells)
     auto strand_of = [&](int r) { return begin + r * per_round + g * kWarps + warp; };
+    const int first_round = begin / per_round;   // tiles start on round boundaries
     for (int r0 = 0; r0 < rounds; r0 += U) {
         const int r1 = min(rounds, r0 + U);
-        if (A.grid_prev) {   // 1. the group's gather box (all of a pair of rounds' loads in flight)
+        int4* const gbox = A.group_box ? A.group_box + 2 * (first_round + r0) : nullptr;
+        bool stored = false;   // the previous fused step left this group's box (uniform across the CTA)
+        if (A.grid_prev && gbox && A.box_tag_read) {
+            __shared__ int s_stored;
+            if (threadIdx.x == 0) {
+                const int4 lo = __ldcg(gbox), hi = __ldcg(gbox + 1);
+                s_stored = (unsigned)lo.w == A.box_tag_read;
+                if (s_stored) {
+                    S.lo[0] = lo.x;
+                    S.lo[1] = lo.y;
+                    S.lo[2] = lo.z;
+                    S.hi[0] = hi.x;
+                    S.hi[1] = hi.y;
+                    S.hi[2] = hi.z;
+                    S.npts = hi.w;
+                }
+            }
+            __syncthreads();
+            stored = s_stored != 0;
+            __syncthreads();   // s_stored is read by every thread before the next group writes it
+        }
+        if (A.grid_prev && !stored) {   // 1. the group's gather box (all of a pair of rounds' loads in flight)
             LaneBounds lb;
             for (int r = r0; r < r1; r += 2) {
                 f3 xs[2][K];
@@ -546,6 +585,10 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
         if (A.grid_prev) __syncthreads();   // the gather box memory becomes the splat box
         if (A.grid_enabled) {   // 3. splat the group
             sb.reduce<M>(A, S);
+            if (gbox && A.box_tag_write && threadIdx.x == 0) {   // the next fused step's gather box
+                gbox[0] = make_int4(S.lo[0], S.lo[1], S.lo[2], (int)A.box_tag_write);
+                gbox[1] = make_int4(S.hi[0], S.hi[1], S.hi[2], S.npts);
+            }
             splat_points<L, M>(A, reinterpret_cast<int*>(smem), S, stats, [&](auto&& f) {
 #pragma unroll 1
                 for (int r = r0; r < r1; ++r) {
@@ -763,17 +806,34 @@ template <int L, class M>
 __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_constant__ BatchDev B) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ BoxShared S;
-    __shared__ int s_item;
+    __shared__ int s_item, s_next;
     __shared__ int s_asset;
     // The current item's asset, copied once into shared memory: reads of its
     // fields then cannot alias the global stores of the step.
     __shared__ __align__(16) DevAsset A;
-    if (threadIdx.x == 0) s_asset = -1;
+    // Each CTA holds the item after its current one (taken from the queue in
+    // order, so every wait is still on an earlier item) and, when it is a
+    // phase-A item, asks L2 for its strands while the current one runs.
+    if (threadIdx.x == 0) {
+        s_asset = -1;
+        s_next = (int)atomicAdd(B.head, 1u);
+    }
     for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(B.head, 1u);
+        __syncthreads();   // the previous item is done and s_next is visible
+        if (threadIdx.x == 0) {
+            s_item = s_next;
+            s_next = s_item < B.n_items ? (int)atomicAdd(B.head, 1u) : B.n_items;
+        }
         __syncthreads();
         const int it = s_item;
         if (it >= B.n_items) break;
+        if (s_next < B.n_items) {
+            const WorkItem wn = B.items[s_next];
+            if (wn.kind == ITEM_A) {
+                const DevAsset* N = B.assets + wn.asset;
+                prefetch_strands(N->strands, N->rest, N->n_points, wn.begin, wn.end);
+            }
+        }
         const WorkItem w = B.items[it];
         if (w.asset != s_asset) {
             constexpr int words = (int)(sizeof(DevAsset) / 4);
@@ -811,7 +871,6 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_
             uint4* g = reinterpret_cast<uint4*>(A.grid_next);
             for (int c = w.begin + threadIdx.x; c < w.end; c += kThreads) g[c] = make_uint4(0u, 0u, 0u, 0u);
         }
-        __syncthreads();  // s_item is rewritten only after every thread has read it
     }
 }
 

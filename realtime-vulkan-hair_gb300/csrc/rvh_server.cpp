@@ -160,7 +160,7 @@ rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_
 
 rvh_status rvh_server_destroy(rvh_server* s) {
     if (!s) return RVH_OK;
-    RVH_DEVICE(s->ctx->device);
+    DeviceGuard g(s->ctx->device);   // releases even if the switch fails
     cudaStreamSynchronize(s->ctx->stream);
     for (auto& e : s->events) cudaEventDestroy(e.first), cudaEventDestroy(e.second);
     for (Character& c : s->chars) {

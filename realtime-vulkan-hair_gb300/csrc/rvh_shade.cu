@@ -846,6 +846,63 @@ __global__ void __launch_bounds__(kShadeThreads) k_light_quads_opacity(TessView 
     });
 }
 
+// hair.frag's outColor for the fragment of segment (s, j, k)'s quad Q at
+// pixel (px, py), covered by the triangle with corners idx[] and barycentrics
+// l[]: the corners' inputs interpolated perspective-correctly.
+__device__ __forceinline__ float4 segment_fragment(const TessView& T, const RasterDev& R, const Maps& M, int s, int j,
+                                                   int k, const Quad& Q, const int idx[3], const float l[3]) {
+    float in[24];
+#pragma unroll
+    for (int e = 0; e < 24; ++e) in[e] = 0.f;
+    const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
+    const float qs = (q0 + q1) + q2;
+    const float qc[3] = {q0, q1, q2};
+    float acc[24];
+#pragma unroll
+    for (int e = 0; e < 24; ++e) acc[e] = 0.f;
+    // the corners' hair.frag inputs, accumulated in the oracle's order (q0 a0 + q1 a1) + q2 a2
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        const int c = idx[t];
+        const int kk = c < 2 ? k : k + 1;
+        const float4 P4 = __ldg(vert_at(T, s, j, kk));
+        const V3 pos = mk(P4.x, P4.y, P4.z);
+        const float u = (float)j / (float)T.L, v = (float)kk / (float)T.S;
+        const float x = v * (float)(T.n - 1);
+        const int sf = min((int)floorf(x), T.n - 2);
+        const float4* fr = T.frames + ((size_t)s * (T.n - 1) + sf) * 3;
+        float a[24];
+        a[0] = u;
+        a[1] = v;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float4 f = __ldg(fr + q);
+            a[2 + 3 * q] = f.x;
+            a[3 + 3 * q] = f.y;
+            a[4 + 3 * q] = f.z;
+        }
+        const V3 vd = nrm3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+        const V3 ld = nrm3(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+        a[11] = vd.x;
+        a[12] = vd.y;
+        a[13] = vd.z;
+        a[14] = ld.x;
+        a[15] = ld.y;
+        a[16] = ld.z;
+        float cl[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) cl[e] = Q.clip[c][e];
+        mul_vec4(R.lmap, cl, a + 17);
+        a[21] = a[22] = a[23] = 0.f;
+#pragma unroll
+        for (int e = 0; e < 24; ++e) acc[e] = t == 0 ? qc[0] * a[e] : acc[e] + qc[t] * a[e];
+    }
+#pragma unroll
+    for (int e = 0; e < 24; ++e) in[e] = acc[e] / qs;
+    in[0] = (float)j / (float)T.L;
+    return shade_fragment(in, M, R.bright[j]);
+}
+
 __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, RasterDev R, Maps M, long long px_count,
                                                                 float4* __restrict__ image, unsigned* __restrict__ ids) {
     for (long long p = (long long)blockIdx.x * kShadeThreads + threadIdx.x; p < px_count;
@@ -866,56 +923,194 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, Rast
         int idx[3];
         float l[3], z;
         cover_quad(Q, px, py, idx, l, z);
-        float in[24];
+        image[p] = segment_fragment(T, R, M, s, j, k, Q, idx, l);
+    }
+}
+
+// ---- the hair pass with the pipeline's in-order blending (RVH_IMAGE_BLEND) -----------
+// The reference's hair pipeline (src/Renderer.cpp:1657-1679) draws the quads in
+// segment order, each quad's triangles (V0, V1, V2) then (V2, V1, V3); a
+// fragment passes a LESS depth test against the depth the earlier fragments
+// wrote (cleared to 1.0), writes its depth and blends SRC_ALPHA /
+// ONE_MINUS_SRC_ALPHA into the colour, ONE / ONE into the alpha (clamped to 1).
+// So a pixel's colour is the fold, in primitive order, over the fragments whose
+// depth is below every earlier fragment's.  Here every fragment is listed per
+// pixel (count, scan, scatter) as (primitive key << 32 | depth bits), primitive
+// key = 2 * segment + triangle + 1; a warp per pixel then walks the passing
+// fragments in primitive order (each the smallest key above the last one with a
+// depth below the last one's), shades up to 32 of them in parallel and folds.
+
+// Calls f(t, idx, l, z) for each of quad Q's triangles t (0, 1) covering pixel (px, py).
+template <class F>
+__device__ __forceinline__ void for_covering_triangles(const Quad& Q, int px, int py, F f) {
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    int idx[3];
+    float l[3], z;
+    if (cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z)) f(0, idx, l, z);
+    if (cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z)) f(1, idx, l, z);
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_blend_count(TessView T, RasterDev R, unsigned n_seg,
+                                                               unsigned* __restrict__ counts) {
+    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
+        for_covering_triangles(Q, px, py, [&](int, const int*, const float*, float) {
+            atomicAdd(counts + (size_t)py * R.width + px, 1u);
+        });
+    });
+}
+
+// Exclusive scan of counts[0, n) into offs[0, n] (offs[n] = the total) and
+// cursor[0, n), in tiles of kScanTile: local scans, a scan of the tile totals,
+// then the tile offsets added.
+constexpr int kScanTile = 4 * kShadeThreads;
+__global__ void __launch_bounds__(kShadeThreads) k_scan_tiles(const unsigned* __restrict__ counts, long long n,
+                                                              unsigned* __restrict__ offs, unsigned* __restrict__ sums) {
+    __shared__ unsigned warp_tot[kShadeThreads / 32];
+    const long long base = (long long)blockIdx.x * kScanTile + 4 * threadIdx.x;
+    unsigned v[4], run = 0;
 #pragma unroll
-        for (int e = 0; e < 24; ++e) in[e] = 0.f;
-        const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
-        const float qs = (q0 + q1) + q2;
-        const float qc[3] = {q0, q1, q2};
-        float acc[24];
+    for (int q = 0; q < 4; ++q) {
+        v[q] = base + q < n ? counts[base + q] : 0u;
+        run += v[q];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = run;
 #pragma unroll
-        for (int e = 0; e < 24; ++e) acc[e] = 0.f;
-        // the corners' hair.frag inputs, accumulated in the oracle's order (q0 a0 + q1 a1) + q2 a2
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    unsigned before = 0;
+    for (int w = 0; w < warp; ++w) before += warp_tot[w];
+    unsigned acc = before + incl - run;
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            const int c = idx[t];
-            const int kk = c < 2 ? k : k + 1;
-            const float4 P4 = __ldg(vert_at(T, s, j, kk));
-            const V3 pos = mk(P4.x, P4.y, P4.z);
-            const float u = (float)j / (float)T.L, v = (float)kk / (float)T.S;
-            const float x = v * (float)(T.n - 1);
-            const int sf = min((int)floorf(x), T.n - 2);
-            const float4* fr = T.frames + ((size_t)s * (T.n - 1) + sf) * 3;
-            float a[24];
-            a[0] = u;
-            a[1] = v;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const float4 f = __ldg(fr + q);
-                a[2 + 3 * q] = f.x;
-                a[3 + 3 * q] = f.y;
-                a[4 + 3 * q] = f.z;
-            }
-            const V3 vd = nrm3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
-            const V3 ld = nrm3(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
-            a[11] = vd.x;
-            a[12] = vd.y;
-            a[13] = vd.z;
-            a[14] = ld.x;
-            a[15] = ld.y;
-            a[16] = ld.z;
-            float cl[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) cl[e] = Q.clip[c][e];
-            mul_vec4(R.lmap, cl, a + 17);
-            a[21] = a[22] = a[23] = 0.f;
-#pragma unroll
-            for (int e = 0; e < 24; ++e) acc[e] = t == 0 ? qc[0] * a[e] : acc[e] + qc[t] * a[e];
+    for (int q = 0; q < 4; ++q) {
+        if (base + q < n) offs[base + q] = acc;
+        acc += v[q];
+    }
+    if (threadIdx.x == kShadeThreads - 1) sums[blockIdx.x] = before + incl;
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_scan_sums(unsigned* __restrict__ sums, int n_tiles) {
+    // one CTA: each thread scans a contiguous run of tiles, then the runs are offset
+    __shared__ unsigned part[kShadeThreads];
+    const int per = (n_tiles + kShadeThreads - 1) / kShadeThreads;
+    const int t0 = threadIdx.x * per, t1 = min(n_tiles, t0 + per);
+    unsigned run = 0;
+    for (int t = t0; t < t1; ++t) run += sums[t];
+    part[threadIdx.x] = run;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned acc = 0;
+        for (int i = 0; i < kShadeThreads; ++i) {
+            const unsigned x = part[i];
+            part[i] = acc;
+            acc += x;
         }
+    }
+    __syncthreads();
+    unsigned acc = part[threadIdx.x];
+    for (int t = t0; t < t1; ++t) {
+        const unsigned x = sums[t];
+        sums[t] = acc;
+        acc += x;
+    }
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_scan_add(const unsigned* __restrict__ counts, long long n,
+                                                            const unsigned* __restrict__ sums, unsigned* __restrict__ offs,
+                                                            unsigned* __restrict__ cursor) {
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kShadeThreads) {
+        const unsigned o = offs[i] + sums[i / kScanTile];
+        offs[i] = o;
+        cursor[i] = o;
+        if (i == n - 1) offs[n] = o + counts[i];
+    }
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, RasterDev R, unsigned n_seg,
+                                                                 unsigned* __restrict__ cursor,
+                                                                 unsigned long long* __restrict__ frags,
+                                                                 unsigned long long capacity) {
+    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned id, int, int px, int py) {
+        for_covering_triangles(Q, px, py, [&](int t, const int*, const float*, float z) {
+            const unsigned slot = atomicAdd(cursor + (size_t)py * R.width + px, 1u);
+            if (slot < capacity)   // the count pass sized the list; this never fails
+                frags[slot] = ((unsigned long long)(2u * id + (unsigned)t + 1u) << 32) | __float_as_uint(z);
+        });
+    });
+}
+
+__global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, RasterDev R, Maps M, long long px_count,
+                                                                 const unsigned* __restrict__ offs,
+                                                                 const unsigned long long* __restrict__ frags,
+                                                                 float4 clear, float4* __restrict__ image,
+                                                                 unsigned* __restrict__ ids) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (kShadeThreads / 32);
+    for (long long p = ((long long)blockIdx.x * kShadeThreads + threadIdx.x) >> 5; p < px_count; p += warps) {
+        const unsigned lo = offs[p], hi = offs[p + 1];
+        const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
+        float3 rgb = make_float3(clear.x, clear.y, clear.z);
+        float alpha = clear.w;
+        unsigned last = 0xffffffffu;
+        unsigned cur_key = 0u;
+        float cur_z = 1.0f;
+        for (;;) {
+            // the next (up to) 32 passing fragments, in primitive order: lane i holds the i-th
+            unsigned long long mine = ~0ull;
+            int npass = 0;
+            while (npass < 32) {
+                unsigned long long best = ~0ull;
+                for (unsigned f = lo + lane; f < hi; f += 32) {
+                    const unsigned long long v = __ldg(frags + f);
+                    if ((unsigned)(v >> 32) > cur_key && __uint_as_float((unsigned)v) < cur_z && v < best) best = v;
+                }
 #pragma unroll
-        for (int e = 0; e < 24; ++e) in[e] = acc[e] / qs;
-        in[0] = (float)j / (float)T.L;
-        image[p] = shade_fragment(in, M, R.bright[j]);
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long t = __shfl_xor_sync(FULL, best, o);
+                    best = t < best ? t : best;
+                }
+                if (best == ~0ull) break;
+                if (lane == npass) mine = best;
+                cur_key = (unsigned)(best >> 32);
+                cur_z = __uint_as_float((unsigned)best);
+                ++npass;
+            }
+            if (npass == 0) break;
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < npass) {
+                const unsigned key = (unsigned)(mine >> 32) - 1u;
+                const unsigned id = key >> 1;
+                int s, j, k;
+                segment_of(T, id, s, j, k);
+                const float4* pv = vert_at(T, s, j, k);
+                const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+                const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+                int idx[3];
+                float l[3], z;
+                if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
+                else cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z);
+                c = segment_fragment(T, R, M, s, j, k, Q, idx, l);
+            }
+            for (int t = 0; t < npass; ++t) {   // SRC_ALPHA / ONE_MINUS_SRC_ALPHA, alpha ONE / ONE
+                const float cr = __shfl_sync(FULL, c.x, t), cg = __shfl_sync(FULL, c.y, t);
+                const float cb = __shfl_sync(FULL, c.z, t), ca = __shfl_sync(FULL, c.w, t);
+                const float ia = 1.0f - ca;
+                rgb = make_float3(cr * ca + rgb.x * ia, cg * ca + rgb.y * ia, cb * ca + rgb.z * ia);
+                alpha = fminf(1.0f, ca + alpha);
+            }
+            last = ((unsigned)(__shfl_sync(FULL, mine, npass - 1) >> 32) - 1u) >> 1;
+            if (npass < 32) break;
+        }
+        if (lane == 0) {
+            image[p] = make_float4(rgb.x, rgb.y, rgb.z, alpha);
+            if (ids) ids[p] = last;
+        }
     }
 }
 
@@ -985,6 +1180,8 @@ rvh_status check_desc(const rvh_shade_desc& d) {
         return fail(RVH_ERR_INVALID_ARG, "shade: map size must be in [1, 16384]");
     if (d.map_mode != RVH_SHADE_MAPS_VERTICES && d.map_mode != RVH_SHADE_MAPS_QUADS)
         return fail(RVH_ERR_INVALID_ARG, "shade: map_mode must be RVH_SHADE_MAPS_VERTICES or RVH_SHADE_MAPS_QUADS");
+    if (d.image_mode != RVH_IMAGE_NEAREST && d.image_mode != RVH_IMAGE_BLEND)
+        return fail(RVH_ERR_INVALID_ARG, "shade: image_mode must be RVH_IMAGE_NEAREST or RVH_IMAGE_BLEND");
     if (!finite16(d.camera_view) || !finite16(d.camera_proj) || !finite16(d.light_view) || !finite16(d.light_proj))
         return fail(RVH_ERR_INVALID_ARG, "shade: non-finite matrix");
     return RVH_OK;
@@ -1002,6 +1199,51 @@ int grid_for(long long n, int sms) {
     const long long b = (n + kShadeThreads - 1) / kShadeThreads;
     return (int)std::max(1LL, std::min(b, (long long)sms * 8));
 }
+
+// The hair pass with in-order blending: count the fragments per pixel, scan,
+// list them, resolve per pixel.  Scratch (counts, offsets, cursors, tile sums,
+// fragment list) lives in the asset, grown as needed; the fragment total is
+// read back once to size the list.
+rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const Maps& M, long long n_seg, long long px,
+                        float4* img, unsigned* ids, cudaStream_t s) {
+    if (n_seg >= (1LL << 31)) return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: blending needs fewer than 2^31 segments");
+    const int sms = a->ctx->sm_count;
+    const long long tiles = (px + kScanTile - 1) / kScanTile;
+    const size_t need_px = size_t(px) * 4 * 3 + 4 + size_t(tiles) * 4;   // counts, offs (+1), cursor, tile sums
+    if (a->raster_px.bytes < need_px) {
+        a->ctx->free(a->raster_px);
+        rvh_status st = a->ctx->alloc(a->raster_px, need_px);
+        if (st != RVH_OK) return st;
+    }
+    unsigned* counts = static_cast<unsigned*>(a->raster_px.ptr);
+    unsigned* offs = counts + px;
+    unsigned* cursor = offs + px + 1;
+    unsigned* sums = cursor + px;
+    RVH_CUDA(cudaMemsetAsync(counts, 0, size_t(px) * 4, s));
+    if (n_seg > 0) k_blend_count<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, counts);
+    k_scan_tiles<<<unsigned(tiles), kShadeThreads, 0, s>>>(counts, px, offs, sums);
+    k_scan_sums<<<1, kShadeThreads, 0, s>>>(sums, int(tiles));
+    k_scan_add<<<grid_for(px, sms), kShadeThreads, 0, s>>>(counts, px, sums, offs, cursor);
+    RVH_CUDA(cudaGetLastError());
+    unsigned total = 0;
+    RVH_CUDA(cudaMemcpyAsync(&total, offs + px, 4, cudaMemcpyDeviceToHost, s));
+    RVH_CUDA(cudaStreamSynchronize(s));
+    const size_t need_f = size_t(std::max(total, 1u)) * 8;
+    if (a->raster_frags.bytes < need_f) {
+        a->ctx->free(a->raster_frags);
+        rvh_status st = a->ctx->alloc(a->raster_frags, need_f + need_f / 4);   // room to grow
+        if (st != RVH_OK) return st;
+    }
+    auto* frags = static_cast<unsigned long long*>(a->raster_frags.ptr);
+    if (n_seg > 0)
+        k_blend_scatter<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, cursor, frags,
+                                                                        (unsigned long long)total);
+    const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
+    k_blend_resolve<<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids);
+    RVH_CUDA(cudaGetLastError());
+    return RVH_OK;
+}
+
 
 bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
 
@@ -1115,6 +1357,7 @@ rvh_status rvh_shade_desc_reference(rvh_shade_desc* d) {
     d->map_width = 1080;                                          // SHADOWMAP_WIDTH x HEIGHT, src/Renderer.cpp:9-10
     d->map_height = 720;
     d->map_mode = RVH_SHADE_MAPS_QUADS;                           // the passes draw hair.geom's quads
+    d->image_mode = RVH_IMAGE_BLEND;                              // the hair pipeline blends (Renderer.cpp:1672-1677)
     return RVH_OK;
 }
 
@@ -1225,6 +1468,7 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
     const long long px = (long long)width * height;
     const int sms = a->ctx->sm_count;
     auto* img = static_cast<float4*>(image);
+    if (sd->image_mode == RVH_IMAGE_BLEND) return render_blend(a, T, R, M, n_seg, px, img, static_cast<unsigned*>(fragment_ids), s);
     k_image_clear<<<grid_for(px, sms), kShadeThreads, 0, s>>>(px, img);
     if (n_seg > 0) k_hair_raster<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, img);
     k_hair_resolve<<<grid_for(px, sms), kShadeThreads, 0, s>>>(T, R, M, px, img, static_cast<unsigned*>(fragment_ids));

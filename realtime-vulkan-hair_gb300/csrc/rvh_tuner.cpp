@@ -108,12 +108,12 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
     rvh_tune_result r{};
     r.best_ms = 1e30f;
     const int lanes_c[5] = {1, 4, 8, 16, 32};
-    const int tile_c[3] = {1, 2, 4};
+    const int tile_c[4] = {0, 1, 2, 4};   // rounds per phase-A item; 0: whole groups near 4,096 points
     rvh_status st = RVH_OK;
     for (int res : res_list) {
         for (int i = 0; i < n && st == RVH_OK; ++i) st = set_grid_res(assets[i], res, orig[i]);
         for (int li = 0; li < 5 && st == RVH_OK; ++li)
-            for (int ti = 0; ti < 3 && st == RVH_OK; ++ti) {
+            for (int ti = 0; ti < 4 && st == RVH_OK; ++ti) {
                 const int lanes = lanes_c[li];
                 const int tile = tile_c[ti] * kWarps * (32 / lanes);
                 rvh_batch_desc bd{lanes, tile, 0, 1, 0, 0};

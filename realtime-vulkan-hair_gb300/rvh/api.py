@@ -508,11 +508,13 @@ def tess_desc_reference(**kw):
 class ShadeDesc(C.Structure):
     _fields_ = [("camera_view", C.c_float * 16), ("camera_proj", C.c_float * 16), ("light_view", C.c_float * 16),
                 ("light_proj", C.c_float * 16), ("map_width", C.c_int32), ("map_height", C.c_int32),
-                ("map_mode", C.c_int32), ("reserved", C.c_int32)]
+                ("map_mode", C.c_int32), ("image_mode", C.c_int32)]
 
 
 SHADE_MAPS_VERTICES = 0
 SHADE_MAPS_QUADS = 1
+IMAGE_NEAREST = 0
+IMAGE_BLEND = 1
 
 
 def shade_desc_reference(**kw):

@@ -238,3 +238,28 @@ def test_batched_finish_equals_plain(gpu_ctx, gpu_ctx_fast, exact):
     b.close()
     for a in plain + batched:
         a.close()
+
+
+def test_alternating_batch_groupings_equal_plain(gpu_ctx_fast):
+    """A fused step reuses the cell boxes the previous fused step left for its
+    phase-A groups only when both used the same grouping.  Fused steps of the
+    same assets alternate here between batches with different lane counts (so
+    different group boundaries); the result equals plain steps bit for bit."""
+    specs = configs.batched(n_assets=6, scale=0.05, seed=11)
+    plain = make_assets(gpu_ctx_fast, specs)
+    shared = make_assets(gpu_ctx_fast, specs)
+    batches = {lanes: api.Batch(gpu_ctx_fast, shared, lanes=lanes) for lanes in (4, 8, 16)}
+    order = [8, 8, 16, 16, 8, 4, 8, 8]
+    for k, lanes in enumerate(order):
+        for a, s in zip(plain, specs):
+            a.step(s.frame(k))
+        batches[lanes].step([s.frame(k) for s in specs])
+    for b in batches.values():
+        b.check()
+    for a, c in zip(plain, shared):
+        x, y = a.read(), c.read()
+        assert np.array_equal(x, y), "max diff %g" % np.abs(x - y).max()
+    for b in batches.values():
+        b.close()
+    for a in plain + shared:
+        a.close()

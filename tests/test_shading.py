@@ -222,24 +222,62 @@ def test_oracle_raster_image_basics(oracle):
                                            length_min=0.4, length_max=0.8, head_collider=1, n_ellipsoids=0,
                                            grid_res=0, friction=0.0, repulsion=0.0, dftl_damping=0.9)
     v, fr = oracle.tessellate(rec, 10, 12, 42, sin_mode=1, frames=True)
-    sd = api.shade_desc_reference(map_width=270, map_height=180)
+    sd = api.shade_desc_reference(map_width=270, map_height=180, image_mode=api.IMAGE_NEAREST)
     d, op = oracle.shade_maps(v, sd)
     img, ids = render_hair(v, fr, 10, 12, 42, sd, d, op, 540, 360)
     hit = ids != 0xffffffff
     assert hit.sum() > 500
     assert (img[hit][:, 3] == 0.75).all() and (img[~hit] == 0).all()
     assert ids[hit].max() < 40 * 12 * 42
+    # the reference pipeline's blending: the same nearest fragment per pixel; a pixel
+    # with one fragment is 0.75 c + 0.25 clear, an empty one keeps the clear colour
+    sd.image_mode = api.IMAGE_BLEND
+    img_b, ids_b = render_hair(v, fr, 10, 12, 42, sd, d, op, 540, 360)
+    assert np.array_equal(ids_b, ids)
+    clear = oracle.CLEAR_RGBA
+    assert (img_b[~hit] == clear).all() and (img_b[..., 3] == 1.0).all()
+    one = hit & (np.abs(img_b[..., :3] - (0.75 * img[..., :3] + 0.25 * clear[:3])).max(axis=-1) < 1e-6)
+    assert one.sum() > 0.3 * hit.sum()   # most pixels are covered by one fragment
+
+
+def test_oracle_blending_follows_primitive_order(oracle):
+    """Two quads on one line of sight: drawn far then near, both fragments blend
+    (the near one passes the LESS test after the far one); drawn near then far,
+    only the near one does.  The segment drawn first is the first in memory."""
+    from oracle.oracle_ctypes import render_hair
+    n, L, S = 2, 1, 1
+    frames = np.zeros((2, n - 1, 3, 4), np.float32)
+    frames[:, 0, 0, :3] = (1, 0, 0)
+    frames[:, 0, 1, :3] = (0, 1, 0)
+    frames[:, 0, 2, :3] = (0, 0, 1)
+    near = [[0.0, 0.5, 2.0, 0.3], [0.0, 1.5, 2.0, 0.3]]      # vertical: the quads widen along x
+    far = [[0.0, 0.5, -2.0, 0.3], [0.0, 1.5, -2.0, 0.3]]
+    sd = api.shade_desc_reference(map_width=64, map_height=64, image_mode=api.IMAGE_BLEND)
+    W, H = 360, 240
+    out = {}
+    for name, order in (("far_first", [far, near]), ("near_first", [near, far])):
+        verts = np.array([[o] for o in order], np.float32)   # (2, L, S+1, 4)
+        d, op = oracle.shade_maps(verts, sd)
+        out[name] = render_hair(verts, frames, n, L, S, sd, d, op, W, H)
+    img_ff, ids_ff = out["far_first"]
+    img_nf, ids_nf = out["near_first"]
+    both = (ids_ff == 1) & (ids_nf == 0)        # the near segment wins either way
+    assert both.sum() > 50
+    # far first: clear -> far -> near; near first: clear -> near (the far one fails the test)
+    assert not np.allclose(img_ff[both], img_nf[both], atol=1e-4)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 0])   # api.IMAGE_BLEND (the reference pipeline), api.IMAGE_NEAREST
 @pytest.mark.parametrize("n,lines,segs,w,h", [(10, 12, 42, 1080, 720), (16, 5, 17, 333, 211), (32, 8, 64, 640, 480)])
-def test_gpu_render_hair_matches_oracle(gpu_ctx, oracle, n, lines, segs, w, h):
-    """The rasterised image: the winning segment of every pixel bit for bit,
-    colours within COLOR_TOL of the oracle's."""
+def test_gpu_render_hair_matches_oracle(gpu_ctx, oracle, n, lines, segs, w, h, mode):
+    """The rasterised image: the nearest segment of every pixel bit for bit,
+    colours within COLOR_TOL of the oracle's; with blending, the fragments that
+    pass the depth test in primitive order are decided bit for bit too."""
     import torch
     a, ns = _head(gpu_ctx, seed=n + 40, n=n)
     td = api.tess_desc_reference(n_lines=lines, n_segments=segs)
-    sd = api.shade_desc_reference()
+    sd = api.shade_desc_reference(image_mode=mode)
     verts, frames, depth, opac, col, (vert_d, _) = _shade_on_gpu(gpu_ctx, a, ns, n, td, sd)
     fr_d = _dev(frames.reshape(-1))
     dep_d, opa_d = _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
