@@ -16,6 +16,10 @@ L2 (129 MB), so no flush is needed between steps.
           (rvh_batch_step_read_positions: the step kernel stages the positions).
   full_head : the 100k-strand x 32-point head alone (plain step, and a
           one-asset batch at 8, 16 and 32 lanes per strand), CUDA events.
+  error : the FP64 error of the benchmarked step: the CPU legs' sample of
+          the workload stepped 120 times through the batched launch (fast
+          math), against the FP64 oracle, beside the FP32 twin's (the
+          reference shader's arithmetic) and over the well-conditioned strands.
   --impl reference : the oracle's OpenMP C++ restatement of the reference
           shader on the host cores (the reference itself is a Vulkan shader
           and has no CPU implementation), on a bounded sample of the workload.
@@ -414,20 +418,27 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
     W, H = 1080, 720
     image = torch.empty((W * H * 4,), dtype=torch.float32, device="cuda")
 
-    def render():
-        a.render_hair(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), W, H, image.data_ptr(),
-                      tess_desc=td, shade_desc=sd, stream=st.cuda_stream)
+    ids = torch.empty((W * H,), dtype=torch.int32, device="cuda")
 
-    for _ in range(warmup):
-        render()
-    st.synchronize()
-    e0.record(st)
-    for _ in range(reps):
-        render()
-    e1.record(st)
-    e1.synchronize()
-    render_ms = e0.elapsed_time(e1) / reps
-    pixels = int((image.view(-1, 4)[:, 3] > 0).sum().item())
+    def render(desc=sd):
+        a.render_hair(vert.data_ptr(), frames.data_ptr(), depth.data_ptr(), opac.data_ptr(), W, H, image.data_ptr(),
+                      ids.data_ptr(), tess_desc=td, shade_desc=desc, stream=st.cuda_stream)
+
+    def timed_render(desc):
+        for _ in range(warmup):
+            render(desc)
+        st.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            render(desc)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # the image as the reference pipeline blends it (sd.image_mode = blend), and with the nearest fragment only
+    render_nearest_ms = timed_render(api.shade_desc_reference(image_mode=api.IMAGE_NEAREST))
+    render_ms = timed_render(sd)
+    pixels = int((ids != -1).sum().item())
     # the reference's frame: shadow + opacity passes (maps from the quads) and the hair pass (the image)
 
     def frame():
@@ -455,8 +466,10 @@ def run_shade(ctx, api, configs, warmup=3, reps=10):
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "bytes_per_launch": alg},
             "render": {"workload": "hair.geom quads of every isoline segment rasterised into 1080 x 720, "
-                                   "nearest fragment shaded by hair.frag",
-                       "segments": ns * td.n_lines * td.n_segments, "ms": render_ms, "covered_pixels": pixels},
+                                   "shaded by hair.frag",
+                       "segments": ns * td.n_lines * td.n_segments, "ms": render_ms, "covered_pixels": pixels,
+                       "image_mode": "blend in primitive order (the reference pipeline)",
+                       "ms_nearest_fragment": render_nearest_ms},
             "frame_ms": frame_ms}
 
 

@@ -23,6 +23,8 @@ struct Batch {
     std::vector<Asset*> assets;
     std::vector<int> modes;   // per asset: MODE_FUSED (loop 3 left pending), MODE_FULL, MODE_FINISH
     std::vector<int> tile_strands;   // per asset: strands per phase-A item of the current plan
+    std::vector<int> group_rounds;   // per asset: rounds per phase-A group of the current plan
+    int min_tile_points = 0;         // > 0: groups no larger than this (a request server's small launches)
     int lanes = 4;
     bool exact = false;
     bool use_graph = true;
@@ -112,6 +114,7 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     b.items.clear();
     b.need_a.assign(b.assets.size(), 0u);
     b.tile_strands.assign(b.assets.size(), 0);
+    b.group_rounds.assign(b.assets.size(), 0);
     const size_t lag = size_t(2) * size_t(std::max(1, b.n_ctas));
     struct Pending {
         int asset;
@@ -138,18 +141,24 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
             emit_b(ai);
             continue;
         }
+        // Rounds per group (the kernel's boxes span a group): at most kUnionRounds and fewer than
+        // 4e9 / scale points, as the kernel computes it; a server keeps groups within its smallest
+        // tile, so the grouping, and the boxes one step leaves the next, do not change from launch
+        // to launch.  Tiles are whole groups, the nearest to target_points.
+        const float cap = 4.0e9f / (a->params.grid_scale * float(quantum * a->n_points));
+        int U = std::max(1, std::min(kUnionRounds, int(cap)));
+        const int span = b.min_tile_points > 0 ? b.min_tile_points : target_points;   // groups fit a tile
+        U = std::max(1, std::min(U, span / (quantum * a->n_points)));
+        const int group = quantum * U;
         int ta;
         if (strands_per_tile > 0) {
             ta = std::max(quantum, (strands_per_tile + quantum - 1) / quantum * quantum);
         } else {
-            // whole groups of rounds (the kernel's boxes span a group: at most kUnionRounds rounds and
-            // fewer than 4e9 / scale points), the nearest to target_points
-            const float cap = 4.0e9f / (a->params.grid_scale * float(quantum * a->n_points));
-            const int group = quantum * std::max(1, std::min(kUnionRounds, int(cap)));
             const int want = std::max(1, target_points / a->n_points);
             ta = std::max(1, (want + group / 2) / group) * group;
         }
         b.tile_strands[ai] = ta;
+        b.group_rounds[ai] = U;
         for (int s = 0; s < a->n_strands; s += ta) {
             b.items.push_back({ITEM_A, ai, s, std::min(a->n_strands, s + ta)});
             b.need_a[ai]++;
@@ -174,11 +183,16 @@ struct GridUse {
     uint32_t box_tag = 0;
 };
 
-// The grouping of an asset's phase-A rounds in a launch: lanes per strand and
-// strands per item (groups are counted from each item's first round).  One
+// The grouping of an asset's phase-A rounds in a launch.  Groups are counted
+// from each item's first round, so with items of whole groups they start at
+// multiples of the group size whatever the tile: the grouping is (lanes per
+// strand, rounds per group); otherwise it also depends on the tile.  One
 // thread per strand (lanes 1) keeps no group boxes: 0.
-uint32_t box_layout_of(int lanes, int tile_strands) {
-    return lanes > 1 ? (uint32_t(lanes) << 24) | uint32_t(tile_strands) : 0u;
+uint32_t box_layout_of(const Batch& b, size_t i) {
+    if (b.lanes <= 1) return 0u;
+    const int quantum = kWarps * (32 / b.lanes), group = quantum * b.group_rounds[i];
+    const uint32_t key = (uint32_t(b.lanes) << 24) | (uint32_t(b.group_rounds[i]) << 20);
+    return b.tile_strands[i] % group == 0 ? key : key | (1u << 19) | uint32_t(b.tile_strands[i] & 0x7ffff);
 }
 
 rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s, DevAsset* view, GridUse* gu,
@@ -339,6 +353,7 @@ DynBatch* dyn_batch_new(Context* ctx, int lanes, rvh_status* st) {
     b.lanes = lanes;
     b.exact = ctx->math == RVH_MATH_EXACT;
     b.use_graph = false;
+    b.min_tile_points = kMinTilePoints;   // launches of any size keep one grouping per asset
     b.kernel = batch_kernel(lanes, b.exact);
     int per_sm = 0;
     if (!prepare_kernel(b.kernel) ||
@@ -406,8 +421,9 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     std::vector<GridUse> gus(assets.size());
     for (size_t i = 0; i < assets.size(); ++i) {
         rvh_status ps = prepare_asset(assets[i], modes[i], frames[i], s, &b.h_stage[slot][i], &gus[i],
-                                      box_layout_of(b.lanes, b.tile_strands[i]));
+                                      box_layout_of(b, i));
         if (ps != RVH_OK) return ps;
+        b.h_stage[slot][i].group_rounds = b.group_rounds[i];
         d->h_need[slot][i] = b.need_a[i];
     }
     std::memcpy(d->h_items[slot], b.items.data(), sizeof(WorkItem) * b.items.size());
@@ -420,7 +436,7 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     if (ls != RVH_OK) return ls;
     if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
     for (size_t i = 0; i < assets.size(); ++i)
-        commit_asset(assets[i], modes[i], gus[i], frames[i].dt, box_layout_of(b.lanes, b.tile_strands[i]));
+        commit_asset(assets[i], modes[i], gus[i], frames[i].dt, box_layout_of(b, i));
     return RVH_OK;
 }
 
@@ -499,7 +515,12 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
     }
     if (d.ctas_per_sm > 0) per_sm = std::min(per_sm, int(d.ctas_per_sm));
     b->n_ctas = std::max(1, per_sm) * ctx->sm_count;
-    plan(*b, d.strands_per_tile);
+    // phase-A items of about 4,096 points, smaller when the batch holds too few points to give
+    // every CTA about eight (one large asset alone would otherwise leave a long tail)
+    int64_t batch_pts = 0;
+    for (const Asset* a : b->assets) batch_pts += int64_t(a->n_strands) * a->n_points;
+    const int64_t per_tile = batch_pts / std::max<int64_t>(1, 8 * int64_t(b->n_ctas));
+    plan(*b, d.strands_per_tile, int(std::min<int64_t>(kTargetPointsA, std::max<int64_t>(kMinTilePoints, per_tile))));
     rvh_status s;
     auto bail = [&](rvh_status st) {
         destroy(b);
@@ -589,8 +610,9 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
     std::vector<GridUse> gus(b->assets.size());
     for (size_t i = 0; i < b->assets.size(); ++i) {
         rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i],
-                                      box_layout_of(b->lanes, b->tile_strands[i]));
+                                      box_layout_of(*b, i));
         if (ps != RVH_OK) return ps;
+        st[i].group_rounds = b->group_rounds[i];
         st[i].pos_xyz = xyz ? xyz + 3 * b->first_point[i] : nullptr;
     }
     RVH_CUDA(cudaMemcpyAsync(b->d_assets.ptr, st, sizeof(DevAsset) * b->assets.size(), cudaMemcpyHostToDevice, s));
@@ -617,7 +639,7 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
         b->ev_pairs.push_back(ev);
     }
     for (size_t i = 0; i < b->assets.size(); ++i)
-        commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt, box_layout_of(b->lanes, b->tile_strands[i]));
+        commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt, box_layout_of(*b, i));
     return RVH_OK;
 }
 

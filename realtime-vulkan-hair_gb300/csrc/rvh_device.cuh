@@ -110,6 +110,9 @@ struct DevAsset {
     int4* group_box;
     uint32_t box_tag_read;
     uint32_t box_tag_write;
+    // rounds per phase-A group (the span of one gather box and one splat box);
+    // 0: as many as keep a group's density partials exact, at most 4
+    int32_t group_rounds;
 };
 
 struct f3 {
@@ -664,6 +667,35 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
         par = head_point<M>(A.head, r0);
         if (l == 0) xn[0] = par;
     }
+    if constexpr (L > 1 && K > 1) {
+        // the chain over slot k in a rolled loop (the current slot is p[0] and xn[0],
+        // rotated after each pass, back in order after K), the L owners of a slot unrolled:
+        // a quarter of the code of a fully unrolled chain at n = 32, the same operations
+#pragma unroll 1
+        for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int o = 0; o < L; ++o) {
+                const int i = k * L + o;
+                if (i >= n) break;   // n is uniform across the warp
+                if (i == 0) continue;   // the root
+                f3 pi;
+                pi.x = __shfl_sync(FULL, p[0].x, base + o);
+                pi.y = __shfl_sync(FULL, p[0].y, base + o);
+                pi.z = __shfl_sync(FULL, p[0].z, base + o);
+                const f3 dir = v_normalize<M>(v_sub<M>(pi, par));
+                par = v_axpy<M>(par, r, dir);
+                if (l == o) xn[0] = par;
+            }
+            const f3 tp = p[0], tx = xn[0];
+#pragma unroll
+            for (int q = 0; q + 1 < K; ++q) {
+                p[q] = p[q + 1];
+                xn[q] = xn[q + 1];
+            }
+            p[K - 1] = tp;
+            xn[K - 1] = tx;
+        }
+    } else {
 #pragma unroll
     for (int i = 1; i < NMAX; ++i) {
         if (NFIX == 0 && i >= n) break;  // n is uniform across the warp
@@ -679,6 +711,7 @@ __device__ __forceinline__ unsigned strand_phase_a(const DevAsset& A, int strand
         const f3 dir = v_normalize<M>(v_sub<M>(pi, par));
         par = v_axpy<M>(par, r, dir);
         if (L == 1 || l == own) xn[k] = par;
+    }
     }
 
     // velocity, clamp and correction vector (compute.comp:195-201)

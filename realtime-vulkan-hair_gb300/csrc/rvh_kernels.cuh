@@ -511,7 +511,8 @@ __device__ __forceinline__ void tile_a(const DevAsset& A, int begin, int end, un
     const int per_round = kWarps * SPW;
     const int rounds = (end - begin + per_round - 1) / per_round;
     const float cap = 4.0e9f / (A.scale * (float)(per_round * n));   // rounds per group, density-exact
-    const int U = max(1, min(kUnionRounds, (int)cap));
+    const int Umax = max(1, min(kUnionRounds, (int)cap));
+    const int U = A.group_rounds > 0 ? min(A.group_rounds, Umax) : Umax;
     // a warp's strands are spread over the round (neighbouring strands share cells)
     auto strand_of = [&](int r) { return begin + r * per_round + g * kWarps + warp; };
     const int first_round = begin / per_round;   // tiles start on round boundaries
