@@ -412,7 +412,12 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
  * for many characters at once: each launch advances every admitted request
  * by one step; requests are admitted in arrival order as slots free up and
  * their grid scratch fits the server's HBM budget; their work shares launches
- * on the device. */
+ * on the device.  Every step is a fused step (the friction of a step is applied
+ * at the start of the next), so a character keeps its grids between requests
+ * with its last step's friction pending; when an admission waits for space,
+ * the least recently stepped idle characters have that friction applied and
+ * give their grids back, and the end of a run does the same for every
+ * character, so each asset leaves a run fully stepped. */
 typedef struct rvh_server_desc {
     int32_t max_active;           /* requests co-scheduled per launch (default 16) */
     int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (0: 8) */
@@ -442,7 +447,7 @@ typedef struct rvh_server_stats {
     double queue_ms_p50, queue_ms_p99;               /* arrival -> admission */
     double mean_batch;                               /* requests per launch */
     int64_t admission_waits;                         /* admissions deferred for lack of scratch memory */
-    uint64_t scratch_used_bytes;                     /* at the end of the run (0 when every request finished) */
+    uint64_t scratch_used_bytes;                     /* at the end of the run (0 unless the run failed) */
 } rvh_server_stats;
 rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_server** out);
 rvh_status rvh_server_destroy(rvh_server* s);

@@ -402,11 +402,12 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     b.assets = assets;
     b.modes = modes;
     // a launch carries what the requests of the moment need: tiles sized so every CTA
-    // gets about eight (small launches would otherwise leave most CTAs idle, and a
-    // few large tiles leave a tail; measured against two and four per CTA)
+    // gets about sixteen (small launches would otherwise leave most CTAs idle, and a
+    // few large tiles leave a tail; at 16 requests per launch 16 per CTA served
+    // 3 % more point-steps than 8, 14 % more than 4 and 53 % more than 2)
     int64_t launch_pts = 0;
     for (Asset* a : assets) launch_pts += int64_t(a->n_strands) * a->n_points;
-    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 8 * int64_t(b.n_ctas));
+    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 16 * int64_t(b.n_ctas));
     plan(b, 0, int(std::min<int64_t>(kTargetPointsA, std::max<int64_t>(kMinTilePoints, per_tile))));
     b.dev.n_items = int32_t(b.items.size());
     int64_t pts = 0;

@@ -80,19 +80,25 @@ struct Character {
     float dt = 1.0f / 60.0f;
     int64_t steps = 0;      // steps completed or enqueued so far
     bool busy = false;
+    // grid scratch lent from the pool; held after a request while the last fused step's
+    // friction is pending, until a later request continues it or the pool needs the space
+    bool held = false;
+    bool finishing = false; // a launch in flight applies the pending friction, then releases
+    size_t off = 0, bytes = 0;
+    int64_t last_launch = 0;
 };
 
 struct Active {
     int req;
     int remaining;          // steps still to enqueue
     int in_flight = 0;      // launches containing this request not yet completed
-    size_t off = 0, bytes = 0;
 };
 
 struct Launch {
     cudaEvent_t start, stop;
     std::vector<int> reqs;  // requests with a step in this launch
     std::vector<int> last;  // requests whose final step is in this launch
+    std::vector<int> finish;   // characters whose pending friction this launch applies
     int64_t points = 0;
 };
 
@@ -253,6 +259,16 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
     int done = 0;
     for (int i = 0; i < n; ++i)
         if (results[i].status != RVH_OK) ++done;
+    // a character's grid scratch back to the pool (its friction applied, nothing pending)
+    auto release = [&](int c) {
+        Character& ch = s->chars[c];
+        if (ch.bytes) s->pool.give(ch.off, ch.bytes);
+        ch.asset->grid[0] = ch.asset->grid[1] = ch.asset->grid[2] = DevBuf{};
+        ch.asset->pending = false;
+        ch.held = ch.finishing = false;
+        ch.off = ch.bytes = 0;
+    };
+    bool want_space = false;   // an admission waits for pool space held by idle characters
     auto complete = [&](Launch& L) {
         cudaEventSynchronize(L.stop);
         float ms = 0.f;
@@ -267,16 +283,14 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             results[r].done_s = t;
             req_ms.push_back(1e3 * (t - reqs[r].arrival_s));
             for (size_t k = 0; k < active.size(); ++k)
-                if (active[k].req == r) {
-                    if (active[k].bytes) s->pool.give(active[k].off, active[k].bytes);
-                    Asset* a = s->chars[reqs[r].character].asset;
-                    a->grid[0] = a->grid[1] = a->grid[2] = DevBuf{};
+                if (active[k].req == r) {   // the character keeps its grids and its pending friction
                     s->chars[reqs[r].character].busy = false;
                     active.erase(active.begin() + k);
                     break;
                 }
             ++done;
         }
+        for (int c : L.finish) release(c);
         for (int r : L.reqs)
             for (Active& ac : active)
                 if (ac.req == r) ac.in_flight--;
@@ -294,23 +308,25 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         for (auto it = waiting.begin(); it != waiting.end() && int(active.size()) < s->desc.max_active;) {
             const int r = *it;
             Character& ch = s->chars[reqs[r].character];
-            if (ch.busy) {
+            if (ch.busy || ch.finishing) {
                 ++it;
                 continue;
             }
             Active ac{r, reqs[r].n_steps};
             Asset* a = ch.asset;
-            if (a->params.grid_enabled) {
+            if (a->params.grid_enabled && !ch.held) {
                 const size_t gb = a->grid_bytes();
                 const size_t one = (gb + 255) & ~size_t(255);
                 size_t off = 0;
                 if (!s->pool.take(3 * one, &off)) {  // wait for memory; later requests may still fit
                     ++admission_waits;
+                    want_space = true;
                     ++it;
                     continue;
                 }
-                ac.off = off;
-                ac.bytes = 3 * one;
+                ch.held = true;
+                ch.off = off;
+                ch.bytes = 3 * one;
                 char* base = static_cast<char*>(s->slab.ptr) + off;
                 for (int g = 0; g < 3; ++g) {
                     a->grid[g] = DevBuf{base + g * one, gb, s->ctx, false};
@@ -328,9 +344,13 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         }
         max_active_seen = std::max(max_active_seen, int(active.size()));
         // launch one step of every admitted request that still has steps to enqueue
+        // Every step is fused: the last step of a request leaves its friction pending in the
+        // character's grids, and the character's next request continues from there.  When an
+        // admission waits for pool space, idle characters with grids (least recently stepped
+        // first) get their pending friction applied in this launch and release their grids.
         std::vector<Asset*> la;
         std::vector<rvh_frame> lf;
-        std::vector<int> lm;   // fused steps, except each request's last step, which is run in full
+        std::vector<int> lm;   // 0: fused step, 2: apply the pending friction only
         Launch L;
         for (Active& ac : active) {
             if (ac.remaining == 0) continue;
@@ -341,23 +361,60 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             if (ch.has_wind) rvh_wind_at(&ch.wind, ch.steps, f.t, f.wind);
             la.push_back(ch.asset);
             lf.push_back(f);
-            lm.push_back(ac.remaining == 1 ? 1 : 0);
+            lm.push_back(0);
             L.reqs.push_back(ac.req);
+            L.points += int64_t(ch.asset->n_strands) * ch.asset->n_points;
             if (ac.remaining == 1) L.last.push_back(ac.req);
+        }
+        const size_t n_steps_in_launch = la.size();
+        if (want_space && int(flight.size()) < s->desc.pipeline_depth) {
+            std::vector<int> idle;
+            for (int c = 0; c < int(s->chars.size()); ++c) {
+                const Character& ch = s->chars[c];
+                if (ch.held && !ch.busy && !ch.finishing) idle.push_back(c);
+            }
+            std::sort(idle.begin(), idle.end(),
+                      [&](int x, int y) { return s->chars[x].last_launch < s->chars[y].last_launch; });
+            // the grid triples of the waiting requests whose characters hold none, less the
+            // space that finishing launches already in flight give back
+            size_t need = 0, freed = 0;
+            for (int r : waiting) {
+                const Character& ch = s->chars[reqs[r].character];
+                if (!ch.held && ch.asset->params.grid_enabled)
+                    need += 3 * ((ch.asset->grid_bytes() + 255) & ~size_t(255));
+            }
+            for (const Character& ch : s->chars)
+                if (ch.finishing) freed += ch.bytes;
+            for (int c : idle) {
+                if (freed >= need) break;
+                Character& ch = s->chars[c];
+                freed += ch.bytes;
+                if (!ch.asset->pending) {   // nothing left to apply: the space is free now
+                    release(c);
+                    continue;
+                }
+                ch.finishing = true;
+                la.push_back(ch.asset);
+                lf.push_back(rvh_frame{ch.dt, float(double(ch.steps) * double(ch.dt)), {0.f, 0.f, 0.f}, 0});
+                lm.push_back(2);
+                L.finish.push_back(c);
+            }
+            want_space = false;
         }
         if (!la.empty() && int(flight.size()) < s->desc.pipeline_depth) {
             L.start = get_ev();
             L.stop = get_ev();
-            err = dyn_batch_launch(s->batch, la, lf, lm, stream, L.start, L.stop, &L.points);
+            err = dyn_batch_launch(s->batch, la, lf, lm, stream, L.start, L.stop, nullptr);
             if (err != RVH_OK) break;
+            for (int r : L.reqs) s->chars[reqs[r].character].last_launch = launches + 1;
             for (Active& ac : active)
                 if (ac.remaining > 0) {
                     ac.remaining--;
                     ac.in_flight++;
                     s->chars[reqs[ac.req].character].steps++;
                 }
-            steps_total += int64_t(la.size());
-            active_sum += double(la.size());
+            steps_total += int64_t(n_steps_in_launch);
+            active_sum += double(n_steps_in_launch);
             ++launches;
             flight.push_back(L);
             continue;
@@ -386,13 +443,36 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         complete(flight.front());
         flight.pop_front();
     }
-    for (Active& ac : active) {   // only after an error
-        if (ac.bytes) s->pool.give(ac.off, ac.bytes);
-        Asset* a = s->chars[reqs[ac.req].character].asset;
-        a->grid[0] = a->grid[1] = a->grid[2] = DevBuf{};
-        a->pending = false;
-        s->chars[reqs[ac.req].character].busy = false;
+    // the pending friction of every character that still holds grids, in one launch, so the
+    // run leaves every asset finished and the pool empty
+    if (err == RVH_OK) {
+        std::vector<Asset*> la;
+        std::vector<rvh_frame> lf;
+        std::vector<int> lm;
+        Launch L;
+        for (int c = 0; c < int(s->chars.size()); ++c) {
+            Character& ch = s->chars[c];
+            if (!ch.held) continue;
+            if (!ch.asset->pending) {
+                release(c);
+                continue;
+            }
+            la.push_back(ch.asset);
+            lf.push_back(rvh_frame{ch.dt, float(double(ch.steps) * double(ch.dt)), {0.f, 0.f, 0.f}, 0});
+            lm.push_back(2);
+            L.finish.push_back(c);
+        }
+        if (!la.empty()) {
+            err = dyn_batch_launch(s->batch, la, lf, lm, stream, nullptr, nullptr, nullptr);
+            if (err == RVH_OK && cudaStreamSynchronize(stream) != cudaSuccess) err = fail(RVH_ERR_CUDA, "server_run: finish");
+        }
+        if (err == RVH_OK)
+            for (int c : L.finish) release(c);
     }
+    for (Active& ac : active)   // only after an error
+        s->chars[reqs[ac.req].character].busy = false;
+    for (int c = 0; c < int(s->chars.size()); ++c)   // only after an error: drop what is left
+        if (s->chars[c].held) release(c);
     for (cudaEvent_t e : free_ev) cudaEventDestroy(e);
     const double wall = now_s();
     rvh_status chk = dyn_batch_check(s->batch);

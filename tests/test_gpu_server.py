@@ -99,6 +99,24 @@ def test_admission_respects_the_hbm_budget(gpu_ctx_fast, specs):
         a.close()
 
 
+def test_characters_give_back_their_grids_when_space_is_short(gpu_ctx_fast, specs):
+    """Room for one character's grids: the characters take turns, and before the
+    other is admitted the idle one's pending friction is applied and its grids freed."""
+    sub = [specs[0], specs[1]]
+    grids = [3 * ((32 * int(np.prod(list(s.params.grid_dims))) + 255) // 256 * 256) for s in sub]
+    srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=max(grids) + 4096)
+    assets = characters(gpu_ctx_fast, sub)
+    ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, sub)]
+    st, res, stats = srv.run([(ids[0], 2, 0.0), (ids[1], 2, 0.0), (ids[0], 3, 0.0)])
+    assert st == 0 and all(r.status == 0 for r in res)
+    assert stats.max_active == 1 and stats.admission_waits > 0 and stats.scratch_used_bytes == 0
+    assert np.array_equal(assets[0].read(), plain_reference(gpu_ctx_fast, sub[0], 5))
+    assert np.array_equal(assets[1].read(), plain_reference(gpu_ctx_fast, sub[1], 2))
+    srv.close()
+    for a in assets:
+        a.close()
+
+
 def test_bad_requests_fail_alone(gpu_ctx_fast, specs):
     srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=256 << 20)
     assets = characters(gpu_ctx_fast, specs[:1])
