@@ -513,6 +513,7 @@ struct Quad {
     float sx[4], sy[4], sz[4];
     int x0, x1, y0, y1; // covered pixel range (inclusive)
     bool ok;
+    bool near_clip;     // a corner has w <= 0: rasterised through clip_quad instead (ok is false)
 };
 
 inline Quad make_quad(const Raster& R, const float* p_k, const float* p_k1, float width_k, float rand_u) {
@@ -528,14 +529,24 @@ inline Quad make_quad(const Raster& R, const float* p_k, const float* p_k1, floa
     mul_vec4(R.vp, pb, c2);
     const float* src[4] = {c1, c1, c2, c2};
     const float off[4] = {-w1, w1, -w1, w1};
-    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    Q.near_clip = false;
+    bool behind = false, finite = true;
     for (int v = 0; v < 4; ++v) {
         Q.clip[v][0] = src[v][0] + off[v];
         Q.clip[v][1] = src[v][1];
         Q.clip[v][2] = src[v][2];
         Q.clip[v][3] = src[v][3];
+        for (int e = 0; e < 4; ++e) finite = finite && std::isfinite(Q.clip[v][e]);
+        behind = behind || !(Q.clip[v][3] > 0.f);
+    }
+    if (!finite) return Q;
+    if (behind) {   // the triangles are clipped at the near plane (clip_quad)
+        Q.near_clip = true;
+        return Q;
+    }
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    for (int v = 0; v < 4; ++v) {
         const float cw = Q.clip[v][3];
-        if (!(cw > 0.f)) return Q;
         Q.sx[v] = (Q.clip[v][0] / cw * 0.5f + 0.5f) * (float)R.width;
         Q.sy[v] = (Q.clip[v][1] / cw * 0.5f + 0.5f) * (float)R.height;
         Q.sz[v] = Q.clip[v][2] / cw;
@@ -612,47 +623,222 @@ inline int cover_quad(const Quad& Q, int px, int py, int idx[3], float l[3], flo
     return 0;
 }
 
+/* Near-plane clipping of a quad with a corner at w <= 0 (one behind the eye).
+ * Each triangle, (V0, V1, V2) and (V2, V1, V3), is clipped in clip space to the
+ * half-space z >= 0 (the near plane of a depth-zero-to-one projection, as Vulkan
+ * clips: 0 <= z <= w) by Sutherland-Hodgman, corners in triangle order: a corner
+ * with z >= 0 is kept, and an edge whose ends lie on opposite sides adds the
+ * point at s = z_a / (z_a - z_b) from its first end, its z set to 0.  The 3 or 4
+ * vertices are fanned into sub-triangles (v0, v1, v2), (v0, v2, v3), each covering
+ * pixels with the same rules as an unclipped triangle; a vertex with w <= 0 after
+ * the clip (possible only with a projection whose near plane is not z = 0) or
+ * a non-finite screen position drops its triangle.  Vertex attributes are the
+ * corners' lerped by s, interpolated perspective-correctly with the vertices' w.
+ * The pixel box is that of every kept vertex, clamped to the target, and a quad
+ * whose box exceeds 65,536 pixels is dropped as an unclipped one is.  The depth
+ * test and the [0, 1] depth range apply per fragment as before. */
+struct ClipVert {
+    float c[4];          // clip position
+    float sx, sy, sz;    // screen position and depth
+    int a, b;            // corners lerped: corner a + s (corner b - corner a)
+    float s;
+};
+struct ClipQuad {
+    ClipVert v[2][4];
+    int nv[2];           // vertices of triangle 0 and 1 after the clip (0: dropped)
+    int x0, x1, y0, y1;
+    bool ok;
+};
+
+inline int clip_triangle(const Raster& R, const Quad& Q, const int tri[3], ClipVert out[4]) {
+    int n = 0;
+    for (int e = 0; e < 3; ++e) {
+        const int a = tri[e], b = tri[(e + 1) % 3];
+        const float za = Q.clip[a][2], zb = Q.clip[b][2];
+        if (za >= 0.f) {
+            ClipVert& o = out[n++];
+            for (int q = 0; q < 4; ++q) o.c[q] = Q.clip[a][q];
+            o.a = o.b = a;
+            o.s = 0.f;
+        }
+        if ((za >= 0.f) != (zb >= 0.f)) {
+            ClipVert& o = out[n++];
+            const float t = za / (za - zb);
+            for (int q = 0; q < 4; ++q) o.c[q] = Q.clip[a][q] + t * (Q.clip[b][q] - Q.clip[a][q]);
+            o.c[2] = 0.f;
+            o.a = a;
+            o.b = b;
+            o.s = t;
+        }
+    }
+    if (n < 3) return 0;
+    for (int v = 0; v < n; ++v) {
+        ClipVert& o = out[v];
+        const float cw = o.c[3];
+        if (!(cw > 0.f)) return 0;
+        o.sx = (o.c[0] / cw * 0.5f + 0.5f) * (float)R.width;
+        o.sy = (o.c[1] / cw * 0.5f + 0.5f) * (float)R.height;
+        o.sz = o.c[2] / cw;
+        if (!std::isfinite(o.sx) || !std::isfinite(o.sy) || !std::isfinite(o.sz)) return 0;
+    }
+    return n;
+}
+
+inline ClipQuad clip_quad(const Raster& R, const Quad& Q) {
+    ClipQuad C;
+    C.ok = false;
+    const int tris[2][3] = {{0, 1, 2}, {2, 1, 3}};
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    for (int t = 0; t < 2; ++t) {
+        C.nv[t] = clip_triangle(R, Q, tris[t], C.v[t]);
+        for (int v = 0; v < C.nv[t]; ++v) {
+            xmin = std::fmin(xmin, C.v[t][v].sx);
+            xmax = std::fmax(xmax, C.v[t][v].sx);
+            ymin = std::fmin(ymin, C.v[t][v].sy);
+            ymax = std::fmax(ymax, C.v[t][v].sy);
+        }
+    }
+    if (C.nv[0] == 0 && C.nv[1] == 0) return C;
+    const float fx0 = std::ceil(xmin - 0.5f), fx1 = std::floor(xmax - 0.5f);
+    const float fy0 = std::ceil(ymin - 0.5f), fy1 = std::floor(ymax - 0.5f);
+    const float cx0 = std::fmax(fx0, 0.f), cx1 = std::fmin(fx1, (float)(R.width - 1));
+    const float cy0 = std::fmax(fy0, 0.f), cy1 = std::fmin(fy1, (float)(R.height - 1));
+    if (cx0 > cx1 || cy0 > cy1) return C;
+    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return C;
+    C.x0 = (int)cx0;
+    C.x1 = (int)cx1;
+    C.y0 = (int)cy0;
+    C.y1 = (int)cy1;
+    C.ok = true;
+    return C;
+}
+
+/* Coverage of pixel centre (px, py) by sub-triangle (i0, i1, i2) of a clipped
+ * triangle's vertices: cover_tri's arithmetic on the vertices' screen positions. */
+inline bool cover_sub(const ClipVert* V, int i0, int i1, int i2, float px, float py, int idx[3], float l[3], float& z) {
+    float area = edge_fn(V[i0].sx, V[i0].sy, V[i1].sx, V[i1].sy, V[i2].sx, V[i2].sy);
+    if (area == 0.f) return false;
+    if (area < 0.f) {
+        std::swap(i1, i2);
+        area = -area;
+    }
+    const int v[3] = {i0, i1, i2};
+    float e[3];
+    for (int t = 0; t < 3; ++t) {
+        const int a = v[(t + 1) % 3], b = v[(t + 2) % 3];
+        e[t] = edge_fn(V[a].sx, V[a].sy, V[b].sx, V[b].sy, px, py);
+        if (e[t] < 0.f || (e[t] == 0.f && !top_left(V[a].sx, V[a].sy, V[b].sx, V[b].sy))) return false;
+    }
+    for (int t = 0; t < 3; ++t) {
+        l[t] = e[t] / area;
+        idx[t] = v[t];
+    }
+    z = (l[0] * V[v[0]].sz + l[1] * V[v[1]].sz) + l[2] * V[v[2]].sz;
+    return z >= 0.f && z <= 1.f;
+}
+
+/* Coverage by clipped triangle t of C: the first of its sub-triangles that covers. */
+inline bool cover_clip_tri(const ClipQuad& C, int t, int px, int py, int idx[3], float l[3], float& z) {
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    if (C.nv[t] >= 3 && cover_sub(C.v[t], 0, 1, 2, cx, cy, idx, l, z)) return true;
+    return C.nv[t] == 4 && cover_sub(C.v[t], 0, 2, 3, cx, cy, idx, l, z);
+}
+
+/* cover_quad for a clipped quad: 0 (none), 1 or 2, the nearer triangle (ties: the first). */
+inline int cover_clip_quad(const ClipQuad& C, int px, int py, int idx[3], float l[3], float& z) {
+    int ia[3], ib[3];
+    float la[3], lb[3], za = 0.f, zb = 0.f;
+    const bool a = cover_clip_tri(C, 0, px, py, ia, la, za);
+    const bool b = cover_clip_tri(C, 1, px, py, ib, lb, zb);
+    if (a && (!b || za <= zb)) {
+        for (int t = 0; t < 3; ++t) idx[t] = ia[t], l[t] = la[t];
+        z = za;
+        return 1;
+    }
+    if (b) {
+        for (int t = 0; t < 3; ++t) idx[t] = ib[t], l[t] = lb[t];
+        z = zb;
+        return 2;
+    }
+    return 0;
+}
+
 /* hair.geom's per-isoline width factor |random(3.242551 u, u u)| + 0.5 (:46). */
 inline float geom_rand(float u, RefSin mode) { return std::fabs(frag_random(3.242551f * u, u * u, mode)) + 0.5f; }
 
+/* hair.frag's inputs at corner c of segment (s, j, k)'s quad Q (V0, V1 take
+ * vertex k's, V2, V3 vertex k + 1's). */
+inline void corner_inputs(const float* verts, const float* frames, int n, int L, int S, const Raster& R, int s, int j,
+                          int k, const Quad& Q, int c, float a[24]) {
+    const int S1 = S + 1;
+    const int kk = c < 2 ? k : k + 1;
+    const float* p = verts + 4 * ((size_t(s) * L + j) * S1 + kk);
+    const V3 pos = mk(p[0], p[1], p[2]);
+    const float u = (float)j / (float)L, v = (float)kk / (float)S;
+    const float x = v * (float)(n - 1);
+    const int sf = std::min((int)std::floor(x), n - 2);
+    const float* fr = frames + (size_t(s) * (n - 1) + sf) * 12;
+    a[0] = u;
+    a[1] = v;
+    for (int q = 0; q < 3; ++q)
+        for (int e = 0; e < 3; ++e) a[2 + 3 * q + e] = fr[4 * q + e];
+    const V3 vd = normalize(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+    const V3 ld = normalize(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+    a[11] = vd.x;
+    a[12] = vd.y;
+    a[13] = vd.z;
+    a[14] = ld.x;
+    a[15] = ld.y;
+    a[16] = ld.z;
+    mul_vec4(R.lmap, Q.clip[c], a + 17);
+    a[21] = a[22] = a[23] = 0.f;
+}
+
 /* hair.frag's outColor for the fragment of segment (s, j, k)'s quad Q at a
  * pixel, covered by the quad's triangle with corners idx[] and barycentrics
- * l[]: the corners' inputs (V0, V1 take vertex k's, V2, V3 vertex k + 1's)
- * interpolated perspective-correctly. */
+ * l[]: the corners' inputs interpolated perspective-correctly. */
 inline void segment_fragment(const float* verts, const float* frames, int n, int L, int S, const Raster& R,
                              const Maps& M, float bright, int s, int j, int k, const Quad& Q, const int idx[3],
                              const float l[3], float o[4]) {
-    const int S1 = S + 1;
-    auto vert = [&](int kk) { return verts + 4 * ((size_t(s) * L + j) * S1 + kk); };
     float attr[4][24];
-    for (int c = 0; c < 4; ++c) {
-        const int kk = c < 2 ? k : k + 1;
-        const float* p = vert(kk);
-        const V3 pos = mk(p[0], p[1], p[2]);
-        const float u = (float)j / (float)L, v = (float)kk / (float)S;
-        const float x = v * (float)(n - 1);
-        const int sf = std::min((int)std::floor(x), n - 2);
-        const float* fr = frames + (size_t(s) * (n - 1) + sf) * 12;
-        float* a = attr[c];
-        a[0] = u;
-        a[1] = v;
-        for (int q = 0; q < 3; ++q)
-            for (int e = 0; e < 3; ++e) a[2 + 3 * q + e] = fr[4 * q + e];
-        const V3 vd = normalize(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
-        const V3 ld = normalize(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
-        a[11] = vd.x;
-        a[12] = vd.y;
-        a[13] = vd.z;
-        a[14] = ld.x;
-        a[15] = ld.y;
-        a[16] = ld.z;
-        mul_vec4(R.lmap, Q.clip[c], a + 17);
-        a[21] = a[22] = a[23] = 0.f;
-    }
+    for (int c = 0; c < 4; ++c) corner_inputs(verts, frames, n, L, S, R, s, j, k, Q, c, attr[c]);
     const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
     const float qs = (q0 + q1) + q2;
     float in[24];
     for (int e = 0; e < 24; ++e) in[e] = ((q0 * attr[idx[0]][e] + q1 * attr[idx[1]][e]) + q2 * attr[idx[2]][e]) / qs;
+    in[0] = (float)j / (float)L;
+    shade_fragment_bright(in, M, bright, o);
+}
+
+/* segment_fragment for a fragment of clipped triangle t of C (vertices idx[] of
+ * C.v[t], barycentrics l[]).  A clipped vertex stands for corners a and b lerped
+ * by s, so the perspective-correct interpolation is a weighted sum of the four
+ * corners' inputs: w_c = the sum over the vertices of q_i = l_i / w_i times 1
+ * (c = a = b), 1 - s (c = a) or s (c = b), accumulated vertex by vertex; the
+ * inputs are (sum over c = 0..3 in order of w_c inputs_c) / (q_0 + q_1 + q_2). */
+inline void segment_fragment_clip(const float* verts, const float* frames, int n, int L, int S, const Raster& R,
+                                  const Maps& M, float bright, int s, int j, int k, const Quad& Q, const ClipQuad& C,
+                                  int t, const int idx[3], const float l[3], float o[4]) {
+    float attr[4][24];
+    for (int c = 0; c < 4; ++c) corner_inputs(verts, frames, n, L, S, R, s, j, k, Q, c, attr[c]);
+    float w[4] = {0.f, 0.f, 0.f, 0.f}, q[3];
+    for (int i = 0; i < 3; ++i) {
+        const ClipVert& V = C.v[t][idx[i]];
+        q[i] = l[i] / V.c[3];
+        if (V.a == V.b) {
+            w[V.a] = w[V.a] + q[i];
+        } else {
+            w[V.a] = w[V.a] + q[i] * (1.0f - V.s);
+            w[V.b] = w[V.b] + q[i] * V.s;
+        }
+    }
+    const float qs = (q[0] + q[1]) + q[2];
+    float in[24];
+    for (int e = 0; e < 24; ++e) {
+        float acc = w[0] * attr[0][e];
+        for (int c = 1; c < 4; ++c) acc = acc + w[c] * attr[c][e];
+        in[e] = acc / qs;
+    }
     in[0] = (float)j / (float)L;
     shade_fragment_bright(in, M, bright, o);
 }
@@ -686,12 +872,14 @@ inline void render_hair(const float* verts, const float* frames, int ns, int n, 
         const int j = int(line % L), s = int(line / L);
         const float* pk = vert(s, j, k);
         const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
-        if (!Q.ok) continue;
-        for (int py = Q.y0; py <= Q.y1; ++py)
-            for (int px = Q.x0; px <= Q.x1; ++px) {
+        const ClipQuad C = Q.near_clip ? clip_quad(R, Q) : ClipQuad{};
+        if (!Q.ok && !(Q.near_clip && C.ok)) continue;
+        const int x0 = Q.ok ? Q.x0 : C.x0, x1 = Q.ok ? Q.x1 : C.x1, y0 = Q.ok ? Q.y0 : C.y0, y1 = Q.ok ? Q.y1 : C.y1;
+        for (int py = y0; py <= y1; ++py)
+            for (int px = x0; px <= x1; ++px) {
                 int idx[3];
                 float l[3], z;
-                if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                if (!(Q.ok ? cover_quad(Q, px, py, idx, l, z) : cover_clip_quad(C, px, py, idx, l, z))) continue;
                 uint32_t zb;
                 std::memcpy(&zb, &z, 4);
                 const uint64_t kk = (uint64_t(zb) << 32) | uint64_t(uint32_t(id));
@@ -717,8 +905,14 @@ inline void render_hair(const float* verts, const float* frames, int ns, int n, 
             const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
             int idx[3];
             float l[3], z;
-            cover_quad(Q, px, py, idx, l, z);
-            segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, out);
+            if (Q.ok) {
+                cover_quad(Q, px, py, idx, l, z);
+                segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, out);
+            } else {
+                const ClipQuad C = clip_quad(R, Q);
+                const int t = cover_clip_quad(C, px, py, idx, l, z) - 1;
+                segment_fragment_clip(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, C, t, idx, l, out);
+            }
         }
 }
 
@@ -752,20 +946,24 @@ inline void render_hair_blend(const float* verts, const float* frames, int ns, i
         const int j = int(line % L), s = int(line / L);
         const float* pk = vert(s, j, k);
         const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
-        if (!Q.ok) continue;
+        const ClipQuad C = Q.near_clip ? clip_quad(R, Q) : ClipQuad{};
+        if (!Q.ok && !(Q.near_clip && C.ok)) continue;
+        const int x0 = Q.ok ? Q.x0 : C.x0, x1 = Q.ok ? Q.x1 : C.x1, y0 = Q.ok ? Q.y0 : C.y0, y1 = Q.ok ? Q.y1 : C.y1;
         for (int tri = 0; tri < 2; ++tri)
-            for (int py = Q.y0; py <= Q.y1; ++py)
-                for (int px = Q.x0; px <= Q.x1; ++px) {
+            for (int py = y0; py <= y1; ++py)
+                for (int px = x0; px <= x1; ++px) {
                     const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
                     int idx[3];
                     float l[3], z;
-                    const bool cov = tri == 0 ? cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z)
-                                              : cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
+                    const bool cov = !Q.ok ? cover_clip_tri(C, tri, px, py, idx, l, z)
+                                     : tri == 0 ? cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z)
+                                                : cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
                     const size_t p = size_t(py) * W + px;
                     if (!cov || !(z < depth[p])) continue;
                     depth[p] = z;
                     float c[4];
-                    segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, c);
+                    if (Q.ok) segment_fragment(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, idx, l, c);
+                    else segment_fragment_clip(verts, frames, n, L, S, R, M, bright[j], s, j, k, Q, C, tri, idx, l, c);
                     float* out = image + 4 * p;
                     const float ia = 1.0f - c[3];
                     for (int e = 0; e < 3; ++e) out[e] = c[e] * c[3] + out[e] * ia;
@@ -824,12 +1022,14 @@ inline void light_maps_quads(const float* verts, int ns, int L, int S, const Ras
             const int j = int(line % L), s = int(line / L);
             const float* pk = vert(s, j, k);
             const Quad Q = make_quad(R, pk, vert(s, j, k + 1), pk[3], rnd[j]);
-            if (!Q.ok) continue;
-            for (int py = Q.y0; py <= Q.y1; ++py)
-                for (int px = Q.x0; px <= Q.x1; ++px) {
+            const ClipQuad C = Q.near_clip ? clip_quad(R, Q) : ClipQuad{};
+            if (!Q.ok && !(Q.near_clip && C.ok)) continue;
+            const int x0 = Q.ok ? Q.x0 : C.x0, x1 = Q.ok ? Q.x1 : C.x1, y0 = Q.ok ? Q.y0 : C.y0, y1 = Q.ok ? Q.y1 : C.y1;
+            for (int py = y0; py <= y1; ++py)
+                for (int px = x0; px <= x1; ++px) {
                     int idx[3];
                     float l[3], z;
-                    if (!cover_quad(Q, px, py, idx, l, z)) continue;
+                    if (!(Q.ok ? cover_quad(Q, px, py, idx, l, z) : cover_clip_quad(C, px, py, idx, l, z))) continue;
                     const size_t t = size_t(py) * W + px;
                     if (pass == 0) {
                         if (z < depth[t]) depth[t] = z;

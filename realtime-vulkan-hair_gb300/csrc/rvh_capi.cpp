@@ -613,6 +613,7 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     c->free(a->tess_cache);
     c->free(a->raster_px);
     c->free(a->raster_frags);
+    c->free(a->raster_clip);
     delete a;
     return RVH_OK;
 }

@@ -154,8 +154,8 @@ struct Asset {
     DevBuf tess_tables;
     DevBuf tess_cache;   // per strand: root bits and the sd profiles computed from them
     // rvh_asset_render_hair's blending scratch: per-pixel counts, offsets, cursors and tile sums;
-    // the per-pixel fragment lists
-    DevBuf raster_px, raster_frags;
+    // the per-pixel fragment lists; the rasterising passes' list of near-clipped quads
+    DevBuf raster_px, raster_frags, raster_clip;
     rvh_tess_desc tess_desc{};
     size_t tess_off[6] = {0, 0, 0, 0, 0, 0};
 

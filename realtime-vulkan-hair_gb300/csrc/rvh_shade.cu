@@ -569,11 +569,12 @@ __global__ void __launch_bounds__(kShadeThreads) k_image_resolve(long long px, c
 // pixel centres at +0.5; triangles (V0, V1, V2), (V2, V1, V3) reordered to
 // positive area; covered when every edge function is > 0, or = 0 on a top-left
 // edge; depth linear in screen space, kept in [0, 1]; attributes perspective-
-// correct.  Quads with a corner at w <= 0 (no near-plane clipping), a
-// non-finite corner or a bounding box over 65,536 pixels are dropped.  The
+// correct.  A quad with a corner at w <= 0 (behind the eye) has each triangle
+// clipped at the near plane z = 0 in clip space (clip_quad); a quad with a
+// non-finite corner or a bounding box over 65,536 pixels is dropped.  The
 // nearest fragment wins (ties: the smaller segment id, then the first triangle)
-// and the pixel takes its hair.frag colour (the pipeline's order-dependent
-// alpha blending is left out).
+// and the pixel takes its hair.frag colour (RVH_IMAGE_NEAREST; RVH_IMAGE_BLEND
+// blends every passing fragment in primitive order, below).
 //   k_hair_raster   one thread per segment: the quad's pixels, depth-tested by an
 //                   atomic min of (depth bits << 32 | segment id) in the image
 //   k_hair_resolve  one thread per pixel: the winner's quad again, perspective-
@@ -603,6 +604,7 @@ struct Quad {
     float sx[4], sy[4], sz[4];
     int x0, x1, y0, y1;
     bool ok;
+    bool near_clip;   // a corner has w <= 0: rasterised through clip_quad instead (ok is false)
 };
 
 __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 pk1, float rand_u) {
@@ -616,7 +618,7 @@ __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 
     const float pa[4] = {a.x, a.y, a.z, 1.f}, pb[4] = {b.x, b.y, b.z, 1.f};
     mul_vec4(R.vp, pa, c1);
     mul_vec4(R.vp, pb, c2);
-    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    bool behind = false, finite = true;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
         const float* src = v < 2 ? c1 : c2;
@@ -624,8 +626,19 @@ __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 
         Q.clip[v][1] = src[1];
         Q.clip[v][2] = src[2];
         Q.clip[v][3] = src[3];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) finite = finite && isfinite(Q.clip[v][e]);
+        behind = behind || !(Q.clip[v][3] > 0.f);
+    }
+    if (!finite) return Q;
+    if (behind) {   // the triangles are clipped at the near plane (clip_quad)
+        Q.near_clip = true;
+        return Q;
+    }
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
         const float cw = Q.clip[v][3];
-        if (!(cw > 0.f)) return Q;
         Q.sx[v] = (Q.clip[v][0] / cw * 0.5f + 0.5f) * (float)R.width;
         Q.sy[v] = (Q.clip[v][1] / cw * 0.5f + 0.5f) * (float)R.height;
         Q.sz[v] = Q.clip[v][2] / cw;
@@ -720,6 +733,154 @@ __device__ __forceinline__ int cover_quad(const Quad& Q, int px, int py, int idx
     return 0;
 }
 
+// Near-plane clipping of a quad with a corner at w <= 0.  Each triangle,
+// (V0, V1, V2) and (V2, V1, V3), is clipped in clip space to z >= 0 (Vulkan's
+// near plane for a depth-zero-to-one projection) by Sutherland-Hodgman in
+// triangle order: a corner with z >= 0 is kept, and an edge whose ends lie on
+// opposite sides adds the point at s = z_a / (z_a - z_b) from its first end, its
+// z set to 0.  The 3 or 4 vertices fan into sub-triangles (v0, v1, v2), (v0, v2,
+// v3) that cover pixels by the unclipped rules; a vertex left at w <= 0 or at a
+// non-finite screen position drops its triangle.  A vertex's attributes are its
+// corners' lerped by s, interpolated perspective-correctly with the vertices' w.
+// The box is every kept vertex's, clamped; over 65,536 pixels the quad is dropped.
+// Such quads are rare (the eye inside the hair), so each is walked by its own lane.
+struct ClipVert {
+    float c[4];
+    float sx, sy, sz;
+    int a, b;   // corners lerped: corner a + s (corner b - corner a)
+    float s;
+};
+struct ClipQuad {
+    ClipVert v[2][4];
+    int nv[2];
+    int x0, x1, y0, y1;
+    bool ok;
+};
+
+__device__ __forceinline__ int clip_triangle(const RasterDev& R, const Quad& Q, int i0, int i1, int i2, ClipVert* out) {
+    const int tri[3] = {i0, i1, i2};
+    int n = 0;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int a = tri[e], b = tri[(e + 1) % 3];
+        const float za = Q.clip[a][2], zb = Q.clip[b][2];
+        if (za >= 0.f) {
+            ClipVert& o = out[n++];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) o.c[q] = Q.clip[a][q];
+            o.a = o.b = a;
+            o.s = 0.f;
+        }
+        if ((za >= 0.f) != (zb >= 0.f)) {
+            ClipVert& o = out[n++];
+            const float t = __fdiv_rn(za, za - zb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) o.c[q] = __fadd_rn(Q.clip[a][q], __fmul_rn(t, __fsub_rn(Q.clip[b][q], Q.clip[a][q])));
+            o.c[2] = 0.f;
+            o.a = a;
+            o.b = b;
+            o.s = t;
+        }
+    }
+    if (n < 3) return 0;
+    for (int v = 0; v < n; ++v) {
+        ClipVert& o = out[v];
+        const float cw = o.c[3];
+        if (!(cw > 0.f)) return 0;
+        o.sx = (o.c[0] / cw * 0.5f + 0.5f) * (float)R.width;
+        o.sy = (o.c[1] / cw * 0.5f + 0.5f) * (float)R.height;
+        o.sz = o.c[2] / cw;
+        if (!isfinite(o.sx) || !isfinite(o.sy) || !isfinite(o.sz)) return 0;
+    }
+    return n;
+}
+
+__device__ __noinline__ ClipQuad clip_quad(const RasterDev& R, const Quad& Q) {
+    ClipQuad C{};
+    C.ok = false;
+    C.nv[0] = clip_triangle(R, Q, 0, 1, 2, C.v[0]);
+    C.nv[1] = clip_triangle(R, Q, 2, 1, 3, C.v[1]);
+    float xmin = 3e38f, xmax = -3e38f, ymin = 3e38f, ymax = -3e38f;
+    for (int t = 0; t < 2; ++t)
+        for (int v = 0; v < C.nv[t]; ++v) {
+            xmin = fminf(xmin, C.v[t][v].sx);
+            xmax = fmaxf(xmax, C.v[t][v].sx);
+            ymin = fminf(ymin, C.v[t][v].sy);
+            ymax = fmaxf(ymax, C.v[t][v].sy);
+        }
+    if (C.nv[0] == 0 && C.nv[1] == 0) return C;
+    const float fx0 = ceilf(xmin - 0.5f), fx1 = floorf(xmax - 0.5f);
+    const float fy0 = ceilf(ymin - 0.5f), fy1 = floorf(ymax - 0.5f);
+    const float cx0 = fmaxf(fx0, 0.f), cx1 = fminf(fx1, (float)(R.width - 1));
+    const float cy0 = fmaxf(fy0, 0.f), cy1 = fminf(fy1, (float)(R.height - 1));
+    if (cx0 > cx1 || cy0 > cy1) return C;
+    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return C;
+    C.x0 = (int)cx0;
+    C.x1 = (int)cx1;
+    C.y0 = (int)cy0;
+    C.y1 = (int)cy1;
+    C.ok = true;
+    return C;
+}
+
+// cover_tri's arithmetic on sub-triangle (i0, i1, i2) of a clipped triangle's vertices.
+__device__ __forceinline__ bool cover_sub(const ClipVert* V, int i0, int i1, int i2, float px, float py, int idx[3],
+                                          float l[3], float& z) {
+    float area = edge_fn(V[i0].sx, V[i0].sy, V[i1].sx, V[i1].sy, V[i2].sx, V[i2].sy);
+    if (area == 0.f) return false;
+    if (area < 0.f) {
+        const int t = i1;
+        i1 = i2;
+        i2 = t;
+        area = -area;
+    }
+    const ClipVert &A = V[i0], &B = V[i1], &Cv = V[i2];
+    const float e0 = edge_fn(B.sx, B.sy, Cv.sx, Cv.sy, px, py);
+    if (e0 < 0.f || (e0 == 0.f && !top_left(B.sx, B.sy, Cv.sx, Cv.sy))) return false;
+    const float e1 = edge_fn(Cv.sx, Cv.sy, A.sx, A.sy, px, py);
+    if (e1 < 0.f || (e1 == 0.f && !top_left(Cv.sx, Cv.sy, A.sx, A.sy))) return false;
+    const float e2 = edge_fn(A.sx, A.sy, B.sx, B.sy, px, py);
+    if (e2 < 0.f || (e2 == 0.f && !top_left(A.sx, A.sy, B.sx, B.sy))) return false;
+    l[0] = e0 / area;
+    l[1] = e1 / area;
+    l[2] = e2 / area;
+    idx[0] = i0;
+    idx[1] = i1;
+    idx[2] = i2;
+    z = (l[0] * A.sz + l[1] * B.sz) + l[2] * Cv.sz;
+    return z >= 0.f && z <= 1.f;
+}
+
+// Coverage by clipped triangle t: the first of its sub-triangles that covers.
+__device__ __forceinline__ bool cover_clip_tri(const ClipQuad& C, int t, int px, int py, int idx[3], float l[3],
+                                               float& z) {
+    const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+    const ClipVert* V = C.v[t];
+    if (C.nv[t] >= 3 && cover_sub(V, 0, 1, 2, cx, cy, idx, l, z)) return true;
+    return C.nv[t] == 4 && cover_sub(V, 0, 2, 3, cx, cy, idx, l, z);
+}
+
+// cover_quad of a clipped quad: 0 (none), 1 or 2, the nearer triangle (ties: the first).
+__device__ __forceinline__ int cover_quad(const ClipQuad& C, int px, int py, int idx[3], float l[3], float& z) {
+    int ia[3], ib[3];
+    float la[3], lb[3], za = 0.f, zb = 0.f;
+    const bool a = cover_clip_tri(C, 0, px, py, ia, la, za);
+    const bool b = cover_clip_tri(C, 1, px, py, ib, lb, zb);
+    if (a && (!b || za <= zb)) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) idx[t] = ia[t], l[t] = la[t];
+        z = za;
+        return 1;
+    }
+    if (b) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) idx[t] = ib[t], l[t] = lb[t];
+        z = zb;
+        return 2;
+    }
+    return 0;
+}
+
 __device__ __forceinline__ void segment_of(const TessView& T, unsigned id, int& s, int& j, int& k) {
     const unsigned line = id / (unsigned)T.S;
     k = (int)(id - line * (unsigned)T.S);
@@ -749,10 +910,24 @@ __device__ __forceinline__ void shfl_quad(const Quad& src, Quad& dst, int lane) 
     }
 }
 
-// frag(Q, id, j, px, py) for every pixel of every quad of segments [0, n_seg);
-// called by all threads of the grid (whole warps).
+// Near-clipped quads found by a rasterising pass: the pass appends their
+// segment ids (append != 0), and k_clipped_quads then rasterises each with one
+// thread, so their state stays out of the common path's registers.  A later
+// pass over the same quads reuses the list (append == 0).  cap = the segment
+// count, so the list cannot overflow.
+struct ClipList {
+    unsigned* count;
+    unsigned* ids;
+    unsigned cap;
+    int append;
+};
+
+// frag(Q, id, j, px, py) for every pixel of every quad of segments [0, n_seg)
+// (near-clipped quads: appended to CL); called by all threads of the grid
+// (whole warps).
 template <class Frag>
-__device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& R, unsigned n_seg, Frag frag) {
+__device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& R, unsigned n_seg, const ClipList& CL,
+                                            Frag frag) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned warp0 = (blockIdx.x * kShadeThreads + (threadIdx.x & ~31u));
@@ -765,6 +940,10 @@ __device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& 
             segment_of(T, id, s, j, k);
             const float4* pv = vert_at(T, s, j, k);
             Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+            if (Q.near_clip && CL.append) {
+                const unsigned slot = atomicAdd(CL.count, 1u);
+                if (slot < CL.cap) CL.ids[slot] = id;
+            }
         }
         const int bw = Q.ok ? Q.x1 - Q.x0 + 1 : 0;
         const int cnt = Q.ok ? bw * (Q.y1 - Q.y0 + 1) : 0;   // <= 65,536 per quad
@@ -797,17 +976,41 @@ __device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& 
     }
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, RasterDev R, unsigned n_seg,
-                                                               float4* __restrict__ image) {
-    auto* keys = reinterpret_cast<unsigned long long*>(image);
-    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned id, int, int px, int py) {
+// frag(C, id, j, px, py) for every pixel of every listed near-clipped quad, a
+// thread per quad (the list is almost always empty).
+template <class Frag>
+__global__ void __launch_bounds__(kShadeThreads) k_clipped_quads(TessView T, RasterDev R, ClipList CL, Frag frag) {
+    const unsigned n = min(*CL.count, CL.cap);
+    for (unsigned q = blockIdx.x * kShadeThreads + threadIdx.x; q < n; q += gridDim.x * kShadeThreads) {
+        const unsigned id = CL.ids[q];
+        int s, j, k;
+        segment_of(T, id, s, j, k);
+        const float4* pv = vert_at(T, s, j, k);
+        const ClipQuad C = clip_quad(R, make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]));
+        if (!C.ok) continue;
+        for (int py = C.y0; py <= C.y1; ++py)
+            for (int px = C.x0; px <= C.x1; ++px) frag(C, id, j, px, py);
+    }
+}
+
+// Nearest fragment per pixel: an atomic min of (depth bits << 32 | segment id).
+struct NearestFrag {
+    unsigned long long* keys;   // 2 words per float4 pixel
+    int width;
+    template <class Q>
+    __device__ __forceinline__ void operator()(const Q& q, unsigned id, int, int px, int py) const {
         int idx[3];
         float l[3], z;
-        if (!cover_quad(Q, px, py, idx, l, z)) return;
+        if (!cover_quad(q, px, py, idx, l, z)) return;
         const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | id;
-        unsigned long long* slot = keys + 2 * ((size_t)py * R.width + px);
+        unsigned long long* slot = keys + 2 * ((size_t)py * width + px);
         if (key < *reinterpret_cast<volatile unsigned long long*>(slot)) atomicMin(slot, key);
-    });
+    }
+};
+
+__global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, RasterDev R, unsigned n_seg, ClipList CL,
+                                                               float4* __restrict__ image) {
+    raster_warp(T, R, n_seg, CL, NearestFrag{reinterpret_cast<unsigned long long*>(image), R.width});
 }
 
 // Light maps from hair.geom's quads, the light camera bound as the geometry
@@ -817,43 +1020,90 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_raster(TessView T, Raste
 // falls in relative to the depth map at its light-space position, which is the
 // fragment's own (lightProj * lightView * inverse(lightView) * inverse(lightProj)
 // is the identity): its pixel centre and its rasterised depth.
-__global__ void __launch_bounds__(kShadeThreads) k_light_quads_depth(TessView T, RasterDev R, unsigned n_seg,
-                                                                     unsigned* __restrict__ depth_bits) {
-    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
+struct LightDepthFrag {
+    unsigned* depth_bits;
+    int width;
+    template <class Q>
+    __device__ __forceinline__ void operator()(const Q& q, unsigned, int, int px, int py) const {
         int idx[3];
         float l[3], z;
-        if (!cover_quad(Q, px, py, idx, l, z)) return;
-        flush_min(depth_bits + (size_t)py * R.width + px, __float_as_uint(z));
-    });
-}
+        if (!cover_quad(q, px, py, idx, l, z)) return;
+        flush_min(depth_bits + (size_t)py * width + px, __float_as_uint(z));
+    }
+};
 
-__global__ void __launch_bounds__(kShadeThreads) k_light_quads_opacity(TessView T, RasterDev R, unsigned n_seg,
-                                                                       const float* __restrict__ depth,
-                                                                       uint4* __restrict__ counts) {
-    auto* words = reinterpret_cast<unsigned long long*>(counts);
-    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
+struct LightOpacityFrag {
+    const float* depth;
+    unsigned long long* words;
+    int width, height;
+    template <class Q>
+    __device__ __forceinline__ void operator()(const Q& q, unsigned, int, int px, int py) const {
         int idx[3];
         float l[3], cz;
-        if (!cover_quad(Q, px, py, idx, l, cz)) return;
+        if (!cover_quad(q, px, py, idx, l, cz)) return;
         // the fragment's light-space position: its pixel centre and rasterised depth
-        const float u = ((float)px + 0.5f) / (float)R.width, v = ((float)py + 0.5f) / (float)R.height;
-        const float z0 = tex_sample(depth, R.width, R.height, 1, u, v, 0);
+        const float u = ((float)px + 0.5f) / (float)width, v = ((float)py + 0.5f) / (float)height;
+        const float z0 = tex_sample(depth, width, height, 1, u, v, 0);
         const float d = 0.3f;
         const int layer = (cz >= z0 && cz < z0 + d) ? 1 : (cz >= z0 + d && cz < z0 + 2.f * d) ? 2
                                                           : (cz >= z0 + 2.f * d) ? 3 : 0;
         if (layer == 0) return;
-        add_counts(words + 2 * ((size_t)py * R.width + px), layer == 1, layer == 2, layer == 3);
-    });
+        add_counts(words + 2 * ((size_t)py * width + px), layer == 1, layer == 2, layer == 3);
+    }
+};
+
+__global__ void __launch_bounds__(kShadeThreads) k_light_quads_depth(TessView T, RasterDev R, unsigned n_seg,
+                                                                     ClipList CL, unsigned* __restrict__ depth_bits) {
+    raster_warp(T, R, n_seg, CL, LightDepthFrag{depth_bits, R.width});
 }
 
-// hair.frag's outColor for the fragment of segment (s, j, k)'s quad Q at
-// pixel (px, py), covered by the triangle with corners idx[] and barycentrics
-// l[]: the corners' inputs interpolated perspective-correctly.
-__device__ __forceinline__ float4 segment_fragment(const TessView& T, const RasterDev& R, const Maps& M, int s, int j,
-                                                   int k, const Quad& Q, const int idx[3], const float l[3]) {
-    float in[24];
+__global__ void __launch_bounds__(kShadeThreads) k_light_quads_opacity(TessView T, RasterDev R, unsigned n_seg,
+                                                                       ClipList CL, const float* __restrict__ depth,
+                                                                       uint4* __restrict__ counts) {
+    raster_warp(T, R, n_seg, CL,
+                LightOpacityFrag{depth, reinterpret_cast<unsigned long long*>(counts), R.width, R.height});
+}
+
+// hair.frag's inputs at corner c of segment (s, j, k)'s quad Q (V0, V1 take
+// vertex k's, V2, V3 vertex k + 1's).
+__device__ __forceinline__ void corner_inputs(const TessView& T, const RasterDev& R, int s, int j, int k, const Quad& Q,
+                                              int c, float a[24]) {
+    const int kk = c < 2 ? k : k + 1;
+    const float4 P4 = __ldg(vert_at(T, s, j, kk));
+    const V3 pos = mk(P4.x, P4.y, P4.z);
+    const float u = (float)j / (float)T.L, v = (float)kk / (float)T.S;
+    const float x = v * (float)(T.n - 1);
+    const int sf = min((int)floorf(x), T.n - 2);
+    const float4* fr = T.frames + ((size_t)s * (T.n - 1) + sf) * 3;
+    a[0] = u;
+    a[1] = v;
 #pragma unroll
-    for (int e = 0; e < 24; ++e) in[e] = 0.f;
+    for (int q = 0; q < 3; ++q) {
+        const float4 f = __ldg(fr + q);
+        a[2 + 3 * q] = f.x;
+        a[3 + 3 * q] = f.y;
+        a[4 + 3 * q] = f.z;
+    }
+    const V3 vd = nrm3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
+    const V3 ld = nrm3(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
+    a[11] = vd.x;
+    a[12] = vd.y;
+    a[13] = vd.z;
+    a[14] = ld.x;
+    a[15] = ld.y;
+    a[16] = ld.z;
+    float cl[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) cl[e] = Q.clip[c][e];
+    mul_vec4(R.lmap, cl, a + 17);
+    a[21] = a[22] = a[23] = 0.f;
+}
+
+// hair.frag's inputs for the fragment of segment (s, j, k)'s quad Q at pixel
+// (px, py), covered by the triangle with corners idx[] and barycentrics l[]:
+// the corners' inputs interpolated perspective-correctly.
+__device__ __forceinline__ void segment_inputs(const TessView& T, const RasterDev& R, int s, int j, int k,
+                                               const Quad& Q, const int idx[3], const float l[3], float in[24]) {
     const float q0 = l[0] / Q.clip[idx[0]][3], q1 = l[1] / Q.clip[idx[1]][3], q2 = l[2] / Q.clip[idx[2]][3];
     const float qs = (q0 + q1) + q2;
     const float qc[3] = {q0, q1, q2};
@@ -863,50 +1113,81 @@ __device__ __forceinline__ float4 segment_fragment(const TessView& T, const Rast
     // the corners' hair.frag inputs, accumulated in the oracle's order (q0 a0 + q1 a1) + q2 a2
 #pragma unroll
     for (int t = 0; t < 3; ++t) {
-        const int c = idx[t];
-        const int kk = c < 2 ? k : k + 1;
-        const float4 P4 = __ldg(vert_at(T, s, j, kk));
-        const V3 pos = mk(P4.x, P4.y, P4.z);
-        const float u = (float)j / (float)T.L, v = (float)kk / (float)T.S;
-        const float x = v * (float)(T.n - 1);
-        const int sf = min((int)floorf(x), T.n - 2);
-        const float4* fr = T.frames + ((size_t)s * (T.n - 1) + sf) * 3;
         float a[24];
-        a[0] = u;
-        a[1] = v;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            const float4 f = __ldg(fr + q);
-            a[2 + 3 * q] = f.x;
-            a[3 + 3 * q] = f.y;
-            a[4 + 3 * q] = f.z;
-        }
-        const V3 vd = nrm3(mk(R.cam_pos[0], R.cam_pos[1], R.cam_pos[2]) - pos);
-        const V3 ld = nrm3(mk(R.light_pos[0], R.light_pos[1], R.light_pos[2]) - pos);
-        a[11] = vd.x;
-        a[12] = vd.y;
-        a[13] = vd.z;
-        a[14] = ld.x;
-        a[15] = ld.y;
-        a[16] = ld.z;
-        float cl[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) cl[e] = Q.clip[c][e];
-        mul_vec4(R.lmap, cl, a + 17);
-        a[21] = a[22] = a[23] = 0.f;
+        corner_inputs(T, R, s, j, k, Q, idx[t], a);
 #pragma unroll
         for (int e = 0; e < 24; ++e) acc[e] = t == 0 ? qc[0] * a[e] : acc[e] + qc[t] * a[e];
     }
 #pragma unroll
     for (int e = 0; e < 24; ++e) in[e] = acc[e] / qs;
     in[0] = (float)j / (float)T.L;
-    return shade_fragment(in, M, R.bright[j]);
 }
 
+// hair.frag's inputs for the fragment of near-clipped quad Q at pixel (px, py):
+// that of triangle t (0 or 1), or with t < 0 the nearer covering triangle's.  A
+// clipped vertex stands for corners a and b lerped by s, so the perspective-
+// correct interpolation is a weighted sum of the four corners' inputs: weight
+// w_c = sum over the vertices of q_i = l_i / w_i times 1 (c = a = b), 1 - s
+// (c = a) or s (c = b), accumulated vertex by vertex; in = (sum over c in order
+// of w_c inputs_c) / (q_0 + q_1 + q_2).
+__device__ __forceinline__ void segment_inputs_clip(const TessView& T, const RasterDev& R, int s, int j, int k, int px,
+                                                 int py, int t, float* in) {
+    const float4* pv = vert_at(T, s, j, k);
+    const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+    const ClipQuad C = clip_quad(R, Q);
+    int idx[3];
+    float l[3], z;
+    if (t < 0) t = cover_quad(C, px, py, idx, l, z) - 1;
+    else cover_clip_tri(C, t, px, py, idx, l, z);
+    float w[4] = {0.f, 0.f, 0.f, 0.f}, q[3];
+    for (int i = 0; i < 3; ++i) {
+        const ClipVert& V = C.v[t][idx[i]];
+        q[i] = l[i] / V.c[3];
+        if (V.a == V.b) {
+            w[V.a] = w[V.a] + q[i];
+        } else {
+            w[V.a] = w[V.a] + q[i] * (1.0f - V.s);
+            w[V.b] = w[V.b] + q[i] * V.s;
+        }
+    }
+    const float qs = (q[0] + q[1]) + q[2];
+    float acc[24];
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        float a[24];
+        corner_inputs(T, R, s, j, k, Q, c, a);
+#pragma unroll
+        for (int e = 0; e < 24; ++e) acc[e] = c == 0 ? w[0] * a[e] : acc[e] + w[c] * a[e];
+    }
+#pragma unroll
+    for (int e = 0; e < 24; ++e) in[e] = acc[e] / qs;
+    in[0] = (float)j / (float)T.L;
+}
+
+// Pixels whose fragment comes from a near-clipped quad: the common resolve pass
+// lists them (a pixel at most once, cap = the pixel count) and leaves them to a
+// second pass compiled with the clipped path, so that path's registers stay out
+// of the common one.
+struct DeferList {
+    unsigned* count;
+    unsigned* ids;
+    unsigned cap;
+};
+
+__device__ __forceinline__ void defer_pixel(const DeferList& D, long long p) {
+    const unsigned slot = atomicAdd(D.count, 1u);
+    if (slot < D.cap) D.ids[slot] = (unsigned)p;
+}
+
+// kClipped: the listed pixels only (their winners are near-clipped quads).
+template <bool kClipped>
 __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, RasterDev R, Maps M, long long px_count,
-                                                                float4* __restrict__ image, unsigned* __restrict__ ids) {
-    for (long long p = (long long)blockIdx.x * kShadeThreads + threadIdx.x; p < px_count;
-         p += (long long)gridDim.x * kShadeThreads) {
+                                                                float4* __restrict__ image, unsigned* __restrict__ ids,
+                                                                DeferList D) {
+    const long long n = kClipped ? (long long)min(*D.count, D.cap) : px_count;
+    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kShadeThreads) {
+        const long long p = kClipped ? (long long)D.ids[i] : i;
         const unsigned long long key = reinterpret_cast<const unsigned long long*>(image)[2 * p];
         if (key == kNoVertex) {
             image[p] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -920,10 +1201,20 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, Rast
         const float4* pv = vert_at(T, s, j, k);
         const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
         const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
-        int idx[3];
-        float l[3], z;
-        cover_quad(Q, px, py, idx, l, z);
-        image[p] = segment_fragment(T, R, M, s, j, k, Q, idx, l);
+        float in[24];
+        if constexpr (kClipped) {
+            segment_inputs_clip(T, R, s, j, k, px, py, -1, in);
+        } else {
+            if (!Q.ok) {   // a near-clipped quad: the second pass shades it
+                defer_pixel(D, p);
+                continue;
+            }
+            int idx[3];
+            float l[3], z;
+            cover_quad(Q, px, py, idx, l, z);
+            segment_inputs(T, R, s, j, k, Q, idx, l, in);
+        }
+        image[p] = shade_fragment(in, M, R.bright[j]);
     }
 }
 
@@ -949,14 +1240,28 @@ __device__ __forceinline__ void for_covering_triangles(const Quad& Q, int px, in
     if (cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z)) f(0, idx, l, z);
     if (cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z)) f(1, idx, l, z);
 }
+template <class F>
+__device__ __forceinline__ void for_covering_triangles(const ClipQuad& C, int px, int py, F f) {
+    int idx[3];
+    float l[3], z;
+    if (cover_clip_tri(C, 0, px, py, idx, l, z)) f(0, idx, l, z);
+    if (cover_clip_tri(C, 1, px, py, idx, l, z)) f(1, idx, l, z);
+}
 
-__global__ void __launch_bounds__(kShadeThreads) k_blend_count(TessView T, RasterDev R, unsigned n_seg,
-                                                               unsigned* __restrict__ counts) {
-    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned, int, int px, int py) {
-        for_covering_triangles(Q, px, py, [&](int, const int*, const float*, float) {
-            atomicAdd(counts + (size_t)py * R.width + px, 1u);
+struct BlendCountFrag {
+    unsigned* counts;
+    int width;
+    template <class Q>
+    __device__ __forceinline__ void operator()(const Q& q, unsigned, int, int px, int py) const {
+        for_covering_triangles(q, px, py, [&](int, const int*, const float*, float) {
+            atomicAdd(counts + (size_t)py * width + px, 1u);
         });
-    });
+    }
+};
+
+__global__ void __launch_bounds__(kShadeThreads) k_blend_count(TessView T, RasterDev R, unsigned n_seg, ClipList CL,
+                                                               unsigned* __restrict__ counts) {
+    raster_warp(T, R, n_seg, CL, BlendCountFrag{counts, R.width});
 }
 
 // Exclusive scan of counts[0, n) into offs[0, n] (offs[n] = the total) and
@@ -1031,28 +1336,43 @@ __global__ void __launch_bounds__(kShadeThreads) k_scan_add(const unsigned* __re
     }
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, RasterDev R, unsigned n_seg,
-                                                                 unsigned* __restrict__ cursor,
-                                                                 unsigned long long* __restrict__ frags,
-                                                                 unsigned long long capacity) {
-    raster_warp(T, R, n_seg, [&](const Quad& Q, unsigned id, int, int px, int py) {
-        for_covering_triangles(Q, px, py, [&](int t, const int*, const float*, float z) {
-            const unsigned slot = atomicAdd(cursor + (size_t)py * R.width + px, 1u);
+struct BlendScatterFrag {
+    unsigned* cursor;
+    unsigned long long* frags;
+    unsigned long long capacity;
+    int width;
+    template <class Q>
+    __device__ __forceinline__ void operator()(const Q& q, unsigned id, int, int px, int py) const {
+        for_covering_triangles(q, px, py, [&](int t, const int*, const float*, float z) {
+            const unsigned slot = atomicAdd(cursor + (size_t)py * width + px, 1u);
             if (slot < capacity)   // the count pass sized the list; this never fails
                 frags[slot] = ((unsigned long long)(2u * id + (unsigned)t + 1u) << 32) | __float_as_uint(z);
         });
-    });
+    }
+};
+
+__global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, RasterDev R, unsigned n_seg, ClipList CL,
+                                                                 unsigned* __restrict__ cursor,
+                                                                 unsigned long long* __restrict__ frags,
+                                                                 unsigned long long capacity) {
+    raster_warp(T, R, n_seg, CL, BlendScatterFrag{cursor, frags, capacity, R.width});
 }
 
+// kClipped: the listed pixels only (one of their passing fragments comes from a
+// near-clipped quad; the common pass lists such a pixel and leaves it).
+template <bool kClipped>
 __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, RasterDev R, Maps M, long long px_count,
                                                                  const unsigned* __restrict__ offs,
                                                                  const unsigned long long* __restrict__ frags,
                                                                  float4 clear, float4* __restrict__ image,
-                                                                 unsigned* __restrict__ ids) {
+                                                                 unsigned* __restrict__ ids, DeferList D) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (kShadeThreads / 32);
-    for (long long p = ((long long)blockIdx.x * kShadeThreads + threadIdx.x) >> 5; p < px_count; p += warps) {
+    const long long n = kClipped ? (long long)min(*D.count, D.cap) : px_count;
+    for (long long i = ((long long)blockIdx.x * kShadeThreads + threadIdx.x) >> 5; i < n; i += warps) {
+        const long long p = kClipped ? (long long)D.ids[i] : i;
+        bool deferred = false;
         const unsigned lo = offs[p], hi = offs[p + 1];
         const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
         float3 rgb = make_float3(clear.x, clear.y, clear.z);
@@ -1091,12 +1411,21 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
                 const float4* pv = vert_at(T, s, j, k);
                 const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
                 const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
-                int idx[3];
-                float l[3], z;
-                if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
-                else cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z);
-                c = segment_fragment(T, R, M, s, j, k, Q, idx, l);
+                float in[24];
+                if (Q.ok) {
+                    int idx[3];
+                    float l[3], z;
+                    if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
+                    else cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z);
+                    segment_inputs(T, R, s, j, k, Q, idx, l, in);
+                } else if constexpr (kClipped) {
+                    segment_inputs_clip(T, R, s, j, k, px, py, (int)(key & 1u), in);
+                } else {   // a near-clipped quad: the second pass resolves this pixel
+                    deferred = true;
+                }
+                if (!deferred) c = shade_fragment(in, M, R.bright[j]);
             }
+            if (__any_sync(FULL, deferred)) break;   // warp-uniform
             for (int t = 0; t < npass; ++t) {   // SRC_ALPHA / ONE_MINUS_SRC_ALPHA, alpha ONE / ONE
                 const float cr = __shfl_sync(FULL, c.x, t), cg = __shfl_sync(FULL, c.y, t);
                 const float cb = __shfl_sync(FULL, c.z, t), ca = __shfl_sync(FULL, c.w, t);
@@ -1106,6 +1435,10 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
             }
             last = ((unsigned)(__shfl_sync(FULL, mine, npass - 1) >> 32) - 1u) >> 1;
             if (npass < 32) break;
+        }
+        if (__any_sync(FULL, deferred)) {
+            if (lane == 0) defer_pixel(D, p);
+            continue;
         }
         if (lane == 0) {
             image[p] = make_float4(rgb.x, rgb.y, rgb.z, alpha);
@@ -1200,6 +1533,32 @@ int grid_for(long long n, int sms) {
     return (int)std::max(1LL, std::min(b, (long long)sms * 8));
 }
 
+constexpr long long kMaxClipped = 1LL << 20;   // near-clipped quads drawn per rasterising pass
+
+// The asset's lists for one rasterising call over n_seg quads into px pixels
+// (grown as needed, counters zeroed): near-clipped quads (up to kMaxClipped)
+// and the pixels deferred to the clipped resolve pass (up to px).
+rvh_status raster_lists(Asset* a, long long n_seg, long long px, cudaStream_t s, ClipList* CL, DeferList* D) {
+    const long long cap = std::max(1LL, std::min(n_seg, kMaxClipped));
+    const size_t need = size_t(2 + cap + std::max(1LL, px)) * 4;
+    if (a->raster_clip.bytes < need) {
+        a->ctx->free(a->raster_clip);
+        rvh_status st = a->ctx->alloc(a->raster_clip, need);
+        if (st != RVH_OK) return st;
+    }
+    auto* p = static_cast<unsigned*>(a->raster_clip.ptr);
+    RVH_CUDA(cudaMemsetAsync(p, 0, 8, s));
+    *CL = ClipList{p, p + 2, unsigned(cap), 1};
+    if (D) *D = DeferList{p + 1, p + 2 + cap, unsigned(std::max(1LL, px))};
+    return RVH_OK;
+}
+
+// The same list, read by a later pass over the same quads.
+ClipList reuse(ClipList CL) {
+    CL.append = 0;
+    return CL;
+}
+
 // The hair pass with in-order blending: count the fragments per pixel, scan,
 // list them, resolve per pixel.  Scratch (counts, offsets, cursors, tile sums,
 // fragment list) lives in the asset, grown as needed; the fragment total is
@@ -1220,7 +1579,14 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     unsigned* cursor = offs + px + 1;
     unsigned* sums = cursor + px;
     RVH_CUDA(cudaMemsetAsync(counts, 0, size_t(px) * 4, s));
-    if (n_seg > 0) k_blend_count<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, counts);
+    ClipList CL{};
+    DeferList D{};
+    rvh_status lst = raster_lists(a, n_seg, px, s, &CL, &D);
+    if (lst != RVH_OK) return lst;
+    if (n_seg > 0) {
+        k_blend_count<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, counts);
+        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, BlendCountFrag{counts, R.width});
+    }
     k_scan_tiles<<<unsigned(tiles), kShadeThreads, 0, s>>>(counts, px, offs, sums);
     k_scan_sums<<<1, kShadeThreads, 0, s>>>(sums, int(tiles));
     k_scan_add<<<grid_for(px, sms), kShadeThreads, 0, s>>>(counts, px, sums, offs, cursor);
@@ -1235,11 +1601,15 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
         if (st != RVH_OK) return st;
     }
     auto* frags = static_cast<unsigned long long*>(a->raster_frags.ptr);
-    if (n_seg > 0)
-        k_blend_scatter<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, cursor, frags,
+    if (n_seg > 0) {
+        const BlendScatterFrag F{cursor, frags, (unsigned long long)total, R.width};
+        k_blend_scatter<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, reuse(CL), cursor, frags,
                                                                         (unsigned long long)total);
+        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
+    }
     const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
-    k_blend_resolve<<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids);
+    k_blend_resolve<false><<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids, D);
+    k_blend_resolve<true><<<sms, kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids, D);
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
 }
@@ -1416,9 +1786,16 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
         const TessView T{static_cast<const float4*>(vertices), static_cast<const float4*>(frames), a->n_points,
                          td->n_lines, td->n_segments};
         const long long n_seg = (long long)a->n_strands * td->n_lines * td->n_segments;
-        k_light_quads_depth<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, depth_bits);
-        k_light_quads_opacity<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg,
+        ClipList CL{};
+        st = raster_lists(a, n_seg, 0, s, &CL, nullptr);
+        if (st != RVH_OK) return st;
+        k_light_quads_depth<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, depth_bits);
+        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, LightDepthFrag{depth_bits, R.width});
+        const LightOpacityFrag F{static_cast<const float*>(depth_map), reinterpret_cast<unsigned long long*>(counts),
+                                 R.width, R.height};
+        k_light_quads_opacity<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, reuse(CL),
                                                                             static_cast<const float*>(depth_map), counts);
+        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
     } else if (nv > 0) {
         const VertexWalk W{static_cast<const float4*>(vertices), (long long)a->n_strands * (td->n_segments + 1),
                            td->n_lines, td->n_segments + 1};
@@ -1470,8 +1847,18 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
     auto* img = static_cast<float4*>(image);
     if (sd->image_mode == RVH_IMAGE_BLEND) return render_blend(a, T, R, M, n_seg, px, img, static_cast<unsigned*>(fragment_ids), s);
     k_image_clear<<<grid_for(px, sms), kShadeThreads, 0, s>>>(px, img);
-    if (n_seg > 0) k_hair_raster<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, img);
-    k_hair_resolve<<<grid_for(px, sms), kShadeThreads, 0, s>>>(T, R, M, px, img, static_cast<unsigned*>(fragment_ids));
+    ClipList CL{};
+    DeferList D{};
+    st = raster_lists(a, n_seg, px, s, &CL, &D);
+    if (st != RVH_OK) return st;
+    if (n_seg > 0) {
+        k_hair_raster<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, img);
+        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL,
+                                                      NearestFrag{reinterpret_cast<unsigned long long*>(img), R.width});
+    }
+    auto* fid = static_cast<unsigned*>(fragment_ids);
+    k_hair_resolve<false><<<grid_for(px, sms), kShadeThreads, 0, s>>>(T, R, M, px, img, fid, D);
+    k_hair_resolve<true><<<sms, kShadeThreads, 0, s>>>(T, R, M, px, img, fid, D);
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
 }

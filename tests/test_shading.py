@@ -341,15 +341,57 @@ def test_oracle_raster_quad_area(oracle):
     assert abs(hit - length_px * width_px) <= 2 * length_px + 4, (hit, length_px, width_px)
 
 
+def _near(sd):
+    """The near distance of a depth-zero-to-one perspective projection."""
+    m = np.array(list(sd.camera_proj), np.float64)
+    return m[14] / m[10]
+
+
+def _segment_image(oracle, a, b, sd, W=1080, H=720):
+    """The oracle's nearest-fragment ids of one segment a -> b (one isoline)."""
+    from oracle.oracle_ctypes import render_hair
+    verts = np.array([[[list(a) + [0.02], list(b) + [0.02]]]], np.float32)
+    frames = np.zeros((1, 1, 3, 4), np.float32)
+    frames[0, 0, 0, 0] = frames[0, 0, 1, 1] = frames[0, 0, 2, 2] = 1.0
+    d, op = oracle.shade_maps(verts, sd)
+    return render_hair(verts, frames, 2, 1, 1, sd, d, op, W, H)[1]
+
+
+def test_oracle_near_plane_clip_keeps_the_visible_part(oracle):
+    """A segment running from in front of the eye to behind it is clipped at the
+    near plane: it covers the pixels of the segment cut at the near plane (the
+    same quad in clip space, up to the rounding of the cut point)."""
+    sd = _desc_with_camera((0.0, 0.0, 0.0), (0.0, 0.0, -1.0))
+    sd.image_mode = api.IMAGE_NEAREST
+    near = _near(sd)
+    a, b = np.array([0.03, -0.02, -1.0]), np.array([0.05, 0.06, 1.0])   # not through the eye
+    t = (-near - a[2]) / (b[2] - a[2])   # eye-space z = -near: clip z = 0
+    cut = a + t * (b - a)
+    whole, part = _segment_image(oracle, a, b, sd) != 0xffffffff, _segment_image(oracle, a, cut, sd) != 0xffffffff
+    assert part.sum() > 200
+    assert (whole != part).sum() <= 0.02 * part.sum() + 4, ((whole != part).sum(), part.sum())
+    behind = _segment_image(oracle, b, b + np.array([0.0, 0.05, 0.5]), sd)   # wholly behind: nothing
+    assert (behind == 0xffffffff).all()
+
+
 @pytest.mark.gpu
-def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle):
-    """A camera among the strands: quads behind it (w <= 0) and near ones over
-    65,536 pixels are dropped the same way on both sides; the rest match."""
+@pytest.mark.parametrize("mode", [1, 0])   # api.IMAGE_BLEND, api.IMAGE_NEAREST
+def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle, mode):
+    """A camera among the strands: quads with a corner behind it (w <= 0) are
+    clipped at the near plane, quads over 65,536 pixels dropped, on both sides
+    the same way; ids bit for bit, colours within COLOR_TOL."""
     import torch
     a, ns = _head(gpu_ctx, seed=77, n=16)
     td = api.tess_desc_reference()
     sd = _desc_with_camera((0.0, 0.9, 0.6), (0.0, 0.2, -1.0))
+    sd.image_mode = mode
     verts, frames, depth, opac, col, (vert_d, _) = _shade_on_gpu(gpu_ctx, a, ns, 16, td, sd)
+    P = (np.array(list(sd.camera_proj), np.float64).reshape(4, 4).T @
+         np.array(list(sd.camera_view), np.float64).reshape(4, 4).T)
+    w = verts[..., :3].reshape(-1, 3).astype(np.float64) @ P[3, :3] + P[3, 3]
+    w = w.reshape(verts.shape[:3])
+    crossing = ((w[:, :, :-1] > 0) != (w[:, :, 1:] > 0)).sum()
+    assert crossing > 10, crossing   # segments that run behind the eye: the clipped path is exercised
     fr_d, dep_d, opa_d = _dev(frames.reshape(-1)), _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
     w, h = 640, 480
     img = torch.zeros((w * h * 4,), dtype=torch.float32, device="cuda")
@@ -363,6 +405,23 @@ def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle):
     assert np.array_equal(got_ids, want_ids)
     assert (got_ids != 0xffffffff).sum() > 1000
     _colors_close(img.cpu().numpy().reshape(-1, 4), want.reshape(-1, 4))
+    a.close()
+
+
+@pytest.mark.gpu
+def test_gpu_light_maps_with_the_light_inside_the_hair(gpu_ctx, oracle):
+    """Light-view quads with a corner behind the light are clipped at its near
+    plane: depth and opacity maps bit for bit with the oracle's."""
+    a, ns = _head(gpu_ctx, seed=78, n=16)
+    td = api.tess_desc_reference()
+    sd = api.shade_desc_reference(map_width=540, map_height=360, map_mode=api.SHADE_MAPS_QUADS)
+    for k, v in enumerate(_look_at((0.1, 0.8, 0.5), (0.0, 0.3, -1.0), (0.0, 1.0, 0.0))):
+        sd.light_view[k] = float(v)
+    verts, frames, depth, opac, col, _ = _shade_on_gpu(gpu_ctx, a, ns, 16, td, sd)
+    want_depth, want_opac = oracle.shade_maps(verts, sd)
+    assert _same_bits(depth, want_depth)
+    assert _same_bits(opac, want_opac)
+    assert (depth < 1).sum() > 1000
     a.close()
 
 
