@@ -271,10 +271,10 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
  * uint32, the nearest fragment's segment (s * n_lines + j) * n_segments + k (in
  * blend mode the last one written, which is the same), or 0xffffffff.  A quad
  * with a corner behind the camera has each triangle clipped at the near plane
- * (z = 0 in clip space) and the kept part drawn, as Vulkan clips (up to 2^20 such
- * quads per call; the light passes of rvh_asset_shade clip the same way); quads
- * covering more than 65,536 pixels are dropped.  Scratch: 4 B per segment up to
- * 2^20 segments and 4 B per pixel for the clipped quads. */
+ * (z = 0 in clip space) and the kept part drawn, as Vulkan clips; the light
+ * passes of rvh_asset_shade clip the same way.  Such quads and quads covering
+ * more than 65,536 pixels are drawn from a list of up to 2^20 per pass.  Scratch:
+ * 4 B per segment up to 2^20 segments and 4 B per pixel for those quads. */
 rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rvh_shade_desc* sd, const void* vertices,
                                  const void* frames, const void* depth_map, const void* opacity_map, int32_t width,
                                  int32_t height, void* image, void* fragment_ids, void* stream);

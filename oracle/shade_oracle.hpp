@@ -430,9 +430,9 @@ inline void render_image(const float* verts, const float* colors, long long nv, 
  *   each reordered to positive area; a centre is covered when every edge
  *   function is > 0, or = 0 on a top-left edge (dy < 0, or dy = 0 and dx > 0);
  *   depth interpolated linearly in screen space and kept in [0, 1]; attributes
- *   interpolated perspective-correctly (barycentrics over w).  Quads with a
- *   corner at w <= 0 (no near-plane clipping), a non-finite corner or a bounding
- *   box over 65,536 pixels are dropped.  The nearest fragment wins; ties go to
+ *   interpolated perspective-correctly (barycentrics over w).  A quad with a
+ *   corner at w <= 0 is clipped at the near plane (clip_quad); one with a
+ *   non-finite corner is dropped.  The nearest fragment wins; ties go to
  *   the smaller segment id = (s * n_lines + j) * n_segments + k, then to the
  *   first triangle.  uv.x is constant along an isoline, so the brightness hash
  *   takes the isoline's own u.
@@ -562,7 +562,6 @@ inline Quad make_quad(const Raster& R, const float* p_k, const float* p_k1, floa
     const float cx0 = std::fmax(fx0, 0.f), cx1 = std::fmin(fx1, (float)(R.width - 1));
     const float cy0 = std::fmax(fy0, 0.f), cy1 = std::fmin(fy1, (float)(R.height - 1));
     if (cx0 > cx1 || cy0 > cy1) return Q;
-    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return Q;
     Q.x0 = (int)cx0;
     Q.x1 = (int)cx1;
     Q.y0 = (int)cy0;
@@ -634,8 +633,7 @@ inline int cover_quad(const Quad& Q, int px, int py, int idx[3], float l[3], flo
  * the clip (possible only with a projection whose near plane is not z = 0) or
  * a non-finite screen position drops its triangle.  Vertex attributes are the
  * corners' lerped by s, interpolated perspective-correctly with the vertices' w.
- * The pixel box is that of every kept vertex, clamped to the target, and a quad
- * whose box exceeds 65,536 pixels is dropped as an unclipped one is.  The depth
+ * The pixel box is that of every kept vertex, clamped to the target.  The depth
  * test and the [0, 1] depth range apply per fragment as before. */
 struct ClipVert {
     float c[4];          // clip position
@@ -704,7 +702,6 @@ inline ClipQuad clip_quad(const Raster& R, const Quad& Q) {
     const float cx0 = std::fmax(fx0, 0.f), cx1 = std::fmin(fx1, (float)(R.width - 1));
     const float cy0 = std::fmax(fy0, 0.f), cy1 = std::fmin(fy1, (float)(R.height - 1));
     if (cx0 > cx1 || cy0 > cy1) return C;
-    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return C;
     C.x0 = (int)cx0;
     C.x1 = (int)cx1;
     C.y0 = (int)cy0;

@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_image_resolve(long long px, c
 // edge; depth linear in screen space, kept in [0, 1]; attributes perspective-
 // correct.  A quad with a corner at w <= 0 (behind the eye) has each triangle
 // clipped at the near plane z = 0 in clip space (clip_quad); a quad with a
-// non-finite corner or a bounding box over 65,536 pixels is dropped.  The
+// non-finite corner is dropped.  The
 // nearest fragment wins (ties: the smaller segment id, then the first triangle)
 // and the pixel takes its hair.frag colour (RVH_IMAGE_NEAREST; RVH_IMAGE_BLEND
 // blends every passing fragment in primitive order, below).
@@ -603,8 +603,9 @@ struct Quad {
     float clip[4][4];
     float sx[4], sy[4], sz[4];
     int x0, x1, y0, y1;
-    bool ok;
-    bool near_clip;   // a corner has w <= 0: rasterised through clip_quad instead (ok is false)
+    bool ok;          // drawn by the warp-cooperative passes
+    bool near_clip;   // a corner has w <= 0: drawn through clip_quad from the list (ok is false)
+    bool big;         // a box over 65,536 pixels: drawn from the list (ok is false, the box is set)
 };
 
 __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 pk1, float rand_u) {
@@ -653,12 +654,13 @@ __device__ __forceinline__ Quad make_quad(const RasterDev& R, float4 pk, float4 
     const float cx0 = fmaxf(fx0, 0.f), cx1 = fminf(fx1, (float)(R.width - 1));
     const float cy0 = fmaxf(fy0, 0.f), cy1 = fminf(fy1, (float)(R.height - 1));
     if (cx0 > cx1 || cy0 > cy1) return Q;
-    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return Q;
     Q.x0 = (int)cx0;
     Q.x1 = (int)cx1;
     Q.y0 = (int)cy0;
     Q.y1 = (int)cy1;
-    Q.ok = true;
+    // the cooperative passes' per-warp pixel counts stay below 2^21; larger quads are listed
+    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) Q.big = true;
+    else Q.ok = true;
     return Q;
 }
 
@@ -742,8 +744,8 @@ __device__ __forceinline__ int cover_quad(const Quad& Q, int px, int py, int idx
 // v3) that cover pixels by the unclipped rules; a vertex left at w <= 0 or at a
 // non-finite screen position drops its triangle.  A vertex's attributes are its
 // corners' lerped by s, interpolated perspective-correctly with the vertices' w.
-// The box is every kept vertex's, clamped; over 65,536 pixels the quad is dropped.
-// Such quads are rare (the eye inside the hair), so each is walked by its own lane.
+// The box is every kept vertex's, clamped.  Such quads are rare (the eye inside
+// the hair) and are drawn from a list.
 struct ClipVert {
     float c[4];
     float sx, sy, sz;
@@ -814,7 +816,6 @@ __device__ __noinline__ ClipQuad clip_quad(const RasterDev& R, const Quad& Q) {
     const float cx0 = fmaxf(fx0, 0.f), cx1 = fminf(fx1, (float)(R.width - 1));
     const float cy0 = fmaxf(fy0, 0.f), cy1 = fminf(fy1, (float)(R.height - 1));
     if (cx0 > cx1 || cy0 > cy1) return C;
-    if ((cx1 - cx0 + 1.f) * (cy1 - cy0 + 1.f) > 65536.f) return C;
     C.x0 = (int)cx0;
     C.x1 = (int)cx1;
     C.y0 = (int)cy0;
@@ -910,11 +911,10 @@ __device__ __forceinline__ void shfl_quad(const Quad& src, Quad& dst, int lane) 
     }
 }
 
-// Near-clipped quads found by a rasterising pass: the pass appends their
-// segment ids (append != 0), and k_clipped_quads then rasterises each with one
-// thread, so their state stays out of the common path's registers.  A later
-// pass over the same quads reuses the list (append == 0).  cap = the segment
-// count, so the list cannot overflow.
+// Near-clipped quads and quads over 65,536 pixels found by a rasterising pass:
+// the pass appends their segment ids (append != 0), and k_listed_quads then
+// rasterises each with one warp, so their state stays out of the common path's
+// registers.  A later pass over the same quads reuses the list (append == 0).
 struct ClipList {
     unsigned* count;
     unsigned* ids;
@@ -940,7 +940,7 @@ __device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& 
             segment_of(T, id, s, j, k);
             const float4* pv = vert_at(T, s, j, k);
             Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
-            if (Q.near_clip && CL.append) {
+            if ((Q.near_clip || Q.big) && CL.append) {
                 const unsigned slot = atomicAdd(CL.count, 1u);
                 if (slot < CL.cap) CL.ids[slot] = id;
             }
@@ -976,20 +976,29 @@ __device__ __forceinline__ void raster_warp(const TessView& T, const RasterDev& 
     }
 }
 
-// frag(C, id, j, px, py) for every pixel of every listed near-clipped quad, a
-// thread per quad (the list is almost always empty).
+// frag(Q or C, id, j, px, py) for every pixel of every listed quad's box (the
+// clipped quad C of a near-clipped one), a warp per quad, its lanes striding
+// over the box (the list is almost always empty).
 template <class Frag>
-__global__ void __launch_bounds__(kShadeThreads) k_clipped_quads(TessView T, RasterDev R, ClipList CL, Frag frag) {
+__global__ void __launch_bounds__(kShadeThreads) k_listed_quads(TessView T, RasterDev R, ClipList CL, Frag frag) {
     const unsigned n = min(*CL.count, CL.cap);
-    for (unsigned q = blockIdx.x * kShadeThreads + threadIdx.x; q < n; q += gridDim.x * kShadeThreads) {
+    const int lane = threadIdx.x & 31;
+    const unsigned warps = gridDim.x * (kShadeThreads / 32);
+    for (unsigned q = (blockIdx.x * kShadeThreads + threadIdx.x) >> 5; q < n; q += warps) {
         const unsigned id = CL.ids[q];
         int s, j, k;
         segment_of(T, id, s, j, k);
         const float4* pv = vert_at(T, s, j, k);
-        const ClipQuad C = clip_quad(R, make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]));
-        if (!C.ok) continue;
-        for (int py = C.y0; py <= C.y1; ++py)
-            for (int px = C.x0; px <= C.x1; ++px) frag(C, id, j, px, py);
+        const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+        if (Q.big) {
+            const int bw = Q.x1 - Q.x0 + 1, area = bw * (Q.y1 - Q.y0 + 1);   // <= 16384^2
+            for (int t = lane; t < area; t += 32) frag(Q, id, j, Q.x0 + t % bw, Q.y0 + t / bw);
+        } else if (Q.near_clip) {
+            const ClipQuad C = clip_quad(R, Q);
+            if (!C.ok) continue;
+            const int bw = C.x1 - C.x0 + 1, area = bw * (C.y1 - C.y0 + 1);
+            for (int t = lane; t < area; t += 32) frag(C, id, j, C.x0 + t % bw, C.y0 + t / bw);
+        }
     }
 }
 
@@ -1205,7 +1214,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_hair_resolve(TessView T, Rast
         if constexpr (kClipped) {
             segment_inputs_clip(T, R, s, j, k, px, py, -1, in);
         } else {
-            if (!Q.ok) {   // a near-clipped quad: the second pass shades it
+            if (Q.near_clip) {   // the second pass shades it
                 defer_pixel(D, p);
                 continue;
             }
@@ -1412,7 +1421,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
                 const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
                 const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
                 float in[24];
-                if (Q.ok) {
+                if (!Q.near_clip) {
                     int idx[3];
                     float l[3], z;
                     if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
@@ -1585,7 +1594,7 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     if (lst != RVH_OK) return lst;
     if (n_seg > 0) {
         k_blend_count<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, counts);
-        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, BlendCountFrag{counts, R.width});
+        k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, BlendCountFrag{counts, R.width});
     }
     k_scan_tiles<<<unsigned(tiles), kShadeThreads, 0, s>>>(counts, px, offs, sums);
     k_scan_sums<<<1, kShadeThreads, 0, s>>>(sums, int(tiles));
@@ -1605,7 +1614,7 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
         const BlendScatterFrag F{cursor, frags, (unsigned long long)total, R.width};
         k_blend_scatter<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, reuse(CL), cursor, frags,
                                                                         (unsigned long long)total);
-        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
+        k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
     }
     const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
     k_blend_resolve<false><<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids, D);
@@ -1790,12 +1799,12 @@ rvh_status rvh_asset_shade(rvh_asset* a, const rvh_tess_desc* td, const rvh_shad
         st = raster_lists(a, n_seg, 0, s, &CL, nullptr);
         if (st != RVH_OK) return st;
         k_light_quads_depth<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, depth_bits);
-        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, LightDepthFrag{depth_bits, R.width});
+        k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, LightDepthFrag{depth_bits, R.width});
         const LightOpacityFrag F{static_cast<const float*>(depth_map), reinterpret_cast<unsigned long long*>(counts),
                                  R.width, R.height};
         k_light_quads_opacity<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, reuse(CL),
                                                                             static_cast<const float*>(depth_map), counts);
-        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
+        k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
     } else if (nv > 0) {
         const VertexWalk W{static_cast<const float4*>(vertices), (long long)a->n_strands * (td->n_segments + 1),
                            td->n_lines, td->n_segments + 1};
@@ -1853,7 +1862,7 @@ rvh_status rvh_asset_render_hair(rvh_asset* a, const rvh_tess_desc* td, const rv
     if (st != RVH_OK) return st;
     if (n_seg > 0) {
         k_hair_raster<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, img);
-        k_clipped_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL,
+        k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL,
                                                       NearestFrag{reinterpret_cast<unsigned long long*>(img), R.width});
     }
     auto* fid = static_cast<unsigned*>(fragment_ids);

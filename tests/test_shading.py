@@ -374,12 +374,71 @@ def test_oracle_near_plane_clip_keeps_the_visible_part(oracle):
     assert (behind == 0xffffffff).all()
 
 
+def _segment_verts(a, b, width):
+    verts = np.array([[[list(a) + [width], list(b) + [width]]]], np.float32)   # (1, L = 1, S + 1 = 2, 4)
+    frames = np.zeros((1, 1, 3, 4), np.float32)
+    frames[0, 0, 0, 0] = frames[0, 0, 1, 1] = frames[0, 0, 2, 2] = 1.0
+    return verts, frames
+
+
+# one segment near the eye (0, 0, 0) looking down -z: a quad whose box is far over
+# 65,536 pixels, and one running from in front of the eye to behind it
+SEGMENTS = {"big": ((-0.05, -0.05, -0.15), (0.05, 0.05, -0.15), 1.0),
+            "crossing": ((0.03, -0.02, -1.0), (0.05, 0.06, 1.0), 0.02)}
+
+
+def test_oracle_draws_quads_over_65536_pixels(oracle):
+    """A quad whose pixel box exceeds 65,536 pixels is drawn: a diagonal ribbon
+    across most of the image."""
+    from oracle.oracle_ctypes import render_hair
+    sd = _desc_with_camera((0.0, 0.0, 0.0), (0.0, 0.0, -1.0))
+    sd.image_mode = api.IMAGE_NEAREST
+    a, b, width = SEGMENTS["big"]
+    verts, frames = _segment_verts(a, b, width)
+    d, op = oracle.shade_maps(verts, sd)
+    ids = render_hair(verts, frames, 2, 1, 1, sd, d, op, 1080, 720)[1]
+    hit = ids != 0xffffffff
+    ys, xs = np.nonzero(hit)
+    assert hit.sum() > 10000 and (xs.max() - xs.min() + 1) * (ys.max() - ys.min() + 1) > 65536
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 0])   # api.IMAGE_BLEND, api.IMAGE_NEAREST
+@pytest.mark.parametrize("case", ["big", "crossing"])
+def test_gpu_render_single_segment_matches_oracle(gpu_ctx, oracle, case, mode):
+    """The listed quads (over 65,536 pixels, or clipped at the near plane): ids
+    bit for bit, colours within COLOR_TOL of the oracle's."""
+    import torch
+    a, b, width = SEGMENTS[case]
+    verts, frames = _segment_verts(a, b, width)
+    sd = _desc_with_camera((0.0, 0.0, 0.0), (0.0, 0.0, -1.0))
+    sd.image_mode = mode
+    td = api.tess_desc_reference(n_lines=1, n_segments=1)
+    asset = api.Asset(gpu_ctx, np.zeros((1, 24), np.float32), 2, uniform_rest=0.1)
+    depth, opac = oracle.shade_maps(verts, sd)
+    W, H = 1080, 720
+    img = torch.zeros((W * H * 4,), dtype=torch.float32, device="cuda")
+    ids = torch.zeros((W * H,), dtype=torch.int32, device="cuda")
+    vd, fd = _dev(verts.reshape(-1)), _dev(frames.reshape(-1))
+    dd, od = _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
+    torch.cuda.synchronize()
+    asset.render_hair(vd.data_ptr(), fd.data_ptr(), dd.data_ptr(), od.data_ptr(), W, H, img.data_ptr(), ids.data_ptr(),
+                      tess_desc=td, shade_desc=sd)
+    gpu_ctx.synchronize()
+    got_ids = ids.cpu().numpy().view(np.uint32).reshape(H, W)
+    want, want_ids = oracle.render_hair(verts, frames, 2, 1, 1, sd, depth, opac, W, H)
+    assert np.array_equal(got_ids, want_ids)
+    assert (got_ids != 0xffffffff).sum() > 500
+    _colors_close(img.cpu().numpy().reshape(-1, 4), want.reshape(-1, 4))
+    asset.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", [1, 0])   # api.IMAGE_BLEND, api.IMAGE_NEAREST
 def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle, mode):
     """A camera among the strands: quads with a corner behind it (w <= 0) are
-    clipped at the near plane, quads over 65,536 pixels dropped, on both sides
-    the same way; ids bit for bit, colours within COLOR_TOL."""
+    clipped at the near plane, quads over 65,536 pixels drawn from the list, on
+    both sides the same way; ids bit for bit, colours within COLOR_TOL."""
     import torch
     a, ns = _head(gpu_ctx, seed=77, n=16)
     td = api.tess_desc_reference()
