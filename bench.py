@@ -211,7 +211,13 @@ def time_cpu(specs, steps, threads):
 def run_served(ctx, args, rank, lanes):
     """1,000 resident characters sized as the batched workload; Poisson arrivals
     at 20k req/s, 1-8 steps each; continuous batching at 1, 4 and 16 requests
-    per launch.  Returns {concurrency: stats}."""
+    per launch.  Returns ({concurrency: stats}, points, the batched rate of 16
+    of these characters in one graph-launched batch, i.e. a launch of the size
+    the server builds at concurrency 16).  Per concurrency: the offered load,
+    whether it was sustained (served >= 97 % of offered and no queue growth),
+    and the queue growth: the slope of each request's queueing delay against
+    its arrival time (ms of extra delay per s; about 0 when sustained)."""
+    import torch
     from rvh import api, configs
     n_chars = args.characters
     specs = configs.batched(n_assets=n_chars, seed=3)
@@ -222,6 +228,7 @@ def run_served(ctx, args, rank, lanes):
         a.set_colliders(s.colliders)
         assets.append(a)
     pts = sum(s.n_total_points for s in specs)
+    offered = 20000.0 * 4.5 * pts / n_chars
     rng = np.random.default_rng(77)
     for conc in (1, 4, 16):
         srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=2, scratch_budget_bytes=24 << 30)
@@ -231,12 +238,34 @@ def run_served(ctx, args, rank, lanes):
         st, res, stats = srv.run(reqs)
         d = stats.as_dict()
         d["status"] = st
-        d["offered_point_steps_per_s"] = 20000.0 * 4.5 * pts / n_chars
+        d["offered_point_steps_per_s"] = offered
+        delay_ms = np.array([1e3 * (r.admit_s - q[2]) for r, q in zip(res, reqs)])
+        growth = float(np.polyfit(t, delay_ms, 1)[0]) if len(t) > 1 else 0.0
+        d["queue_growth_ms_per_s"] = growth
+        d["sustained"] = bool(d["point_steps_per_s"] >= 0.97 * offered and growth < 50.0)
         out[str(conc)] = d
         srv.close()
+    # a batch of 16 of the characters, graph-launched: the batched rate at the server's launch size
+    sub = assets[:16]
+    b = api.Batch(ctx, sub, lanes=lanes)
+    frames = [specs[i].frame(0) for i in range(16)]
+    st_ = torch.cuda.Stream()
+    for k in range(5):
+        b.step(frames, stream=st_.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st_)
+    for k in range(20):
+        b.step(frames, stream=st_.cuda_stream)
+    e1.record(st_)
+    e1.synchronize()
+    b.finish(stream=st_.cuda_stream)
+    st_.synchronize()
+    sub_pts = sum(specs[i].n_total_points for i in range(16))
+    batched16 = sub_pts / (e0.elapsed_time(e1) / 20 * 1e-3)
+    b.close()
     for a in assets:
         a.close()
-    return out, pts
+    return out, pts, batched16
 
 
 def run_full_head(ctx, api, configs, warmup=5, reps=20):
@@ -761,13 +790,16 @@ def main():
     if world == 1 and not args.no_adjoint:
         adjoint = run_adjoint(ctx, api, configs)
 
-    served, served_pts = None, None
+    served, served_pts, batched16 = None, None, None
     if not args.no_served and world == 1:
         batch.close()
         for a in assets:
             a.close()
         assets, batch = [], None
-        served, served_pts = run_served(ctx, args, rank, info["lanes"])
+        served, served_pts, batched16 = run_served(ctx, args, rank, info["lanes"])
+        for d in served.values():
+            d["vs_batched"] = d["point_steps_per_s"] / value
+            d["vs_batched_16_characters"] = d["point_steps_per_s"] / batched16
 
     peak, peak_kind = load_peaks()
     achieved = alg_bytes / (step_ms * 1e-3) / 1e9
@@ -804,6 +836,7 @@ def main():
                 "workload": "%d resident characters sized as the batched workload (%d points), Poisson "
                             "arrivals 20k req/s, 1-8 steps per request, %d requests per run" % (
                                 args.characters, served_pts, args.requests),
+                "batched_16_characters_point_steps_per_s": batched16,
                 "by_concurrency": served},
         }
         print(json.dumps(line), flush=True)

@@ -1345,17 +1345,25 @@ __global__ void __launch_bounds__(kShadeThreads) k_scan_add(const unsigned* __re
     }
 }
 
+// A listed fragment: (2 * segment + triangle + 1) << 32 | depth bits, the depth's
+// sign bit (depths are in [0, 1]; -0 is stored as +0) set for a fragment of a
+// listed quad (near-clipped or over 65,536 pixels).
+constexpr unsigned kListedFrag = 0x80000000u;
+__device__ __forceinline__ float frag_depth(unsigned long long v) { return __uint_as_float((unsigned)v & 0x7fffffffu); }
+
 struct BlendScatterFrag {
     unsigned* cursor;
     unsigned long long* frags;
     unsigned long long capacity;
     int width;
+    unsigned flag;   // kListedFrag from the listed quads' pass, else 0
     template <class Q>
     __device__ __forceinline__ void operator()(const Q& q, unsigned id, int, int px, int py) const {
         for_covering_triangles(q, px, py, [&](int t, const int*, const float*, float z) {
             const unsigned slot = atomicAdd(cursor + (size_t)py * width + px, 1u);
             if (slot < capacity)   // the count pass sized the list; this never fails
-                frags[slot] = ((unsigned long long)(2u * id + (unsigned)t + 1u) << 32) | __float_as_uint(z);
+                frags[slot] = ((unsigned long long)(2u * id + (unsigned)t + 1u) << 32) |
+                              ((__float_as_uint(z) & 0x7fffffffu) | flag);
         });
     }
 };
@@ -1364,13 +1372,199 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, Ras
                                                                  unsigned* __restrict__ cursor,
                                                                  unsigned long long* __restrict__ frags,
                                                                  unsigned long long capacity) {
-    raster_warp(T, R, n_seg, CL, BlendScatterFrag{cursor, frags, capacity, R.width});
+    raster_warp(T, R, n_seg, CL, BlendScatterFrag{cursor, frags, capacity, R.width, 0u});
 }
 
-// kClipped: the listed pixels only (one of their passing fragments comes from a
-// near-clipped quad; the common pass lists such a pixel and leaves it).
-template <bool kClipped>
-__global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, RasterDev R, Maps M, long long px_count,
+constexpr int kOrderCap = 4096;                 // fragments of one pixel sorted in shared memory
+constexpr unsigned kDeferredPx = 0xffffffffu;   // pass_count of a pixel left to k_blend_resolve
+
+// Block-wide exclusive scans over kShadeThreads threads (all threads call).
+__device__ __forceinline__ float block_excl_min(float x, float* s_w) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl = fminf(incl, t);
+    }
+    if (lane == 31) s_w[warp] = incl;
+    float excl = __shfl_up_sync(FULL, incl, 1);
+    if (lane == 0) excl = 1.0f;
+    __syncthreads();
+    for (int w = 0; w < warp; ++w) excl = fminf(excl, s_w[w]);
+    return excl;
+}
+__device__ __forceinline__ unsigned block_excl_sum(unsigned x, unsigned* s_w, unsigned& total) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    unsigned before = 0;
+    total = 0;
+    for (int w = 0; w < kShadeThreads / 32; ++w) {
+        if (w < warp) before += s_w[w];
+        total += s_w[w];
+    }
+    return before + incl - x;
+}
+
+// One block per pixel (grid-stride).  A fragment passes the LESS test in
+// primitive order exactly when its depth is below 1.0 and below every
+// earlier fragment's: a failing fragment is never below the depth buffer, so
+// the buffer is the running minimum of all earlier depths.  The pixel's
+// fragments are sorted by primitive key in shared memory (bitonic; keys are
+// unique within a pixel), each thread takes a run of consecutive ones, a block
+// min-scan gives each run the minimum before it, and the passing fragments are
+// written in order to the start of the pixel's list, their number to
+// pass_count[p].  A pixel with more than kOrderCap fragments, or with one of a
+// listed quad, is listed in D instead (pass_count = kDeferredPx) and its list
+// left as it is for k_blend_resolve.
+__global__ void __launch_bounds__(kShadeThreads) k_blend_order(long long px_count, const unsigned* __restrict__ offs,
+                                                               unsigned long long* __restrict__ frags,
+                                                               unsigned* __restrict__ pass_count, DeferList D) {
+    extern __shared__ unsigned long long sk[];   // kOrderCap
+    __shared__ float s_wmin[kShadeThreads / 32];
+    __shared__ unsigned s_wcnt[kShadeThreads / 32];
+    const int tid = threadIdx.x;
+    for (long long p = blockIdx.x; p < px_count; p += gridDim.x) {
+        const unsigned lo = offs[p], F = offs[p + 1] - lo;   // block-uniform
+        if (F == 0) {
+            if (tid == 0) pass_count[p] = 0u;
+            continue;
+        }
+        if (F > (unsigned)kOrderCap) {
+            if (tid == 0) {
+                pass_count[p] = kDeferredPx;
+                defer_pixel(D, p);
+            }
+            continue;
+        }
+        unsigned N = 1;
+        while (N < F) N <<= 1;
+        bool listed = false;
+        for (unsigned i = tid; i < N; i += kShadeThreads) {
+            const unsigned long long v = i < F ? frags[lo + i] : ~0ull;
+            listed = listed || (i < F && ((unsigned)v & kListedFrag) != 0u);
+            sk[i] = v;
+        }
+        if (__syncthreads_or(listed)) {
+            if (tid == 0) {
+                pass_count[p] = kDeferredPx;
+                defer_pixel(D, p);
+            }
+            continue;
+        }
+        for (unsigned k = 2; k <= N; k <<= 1)
+            for (unsigned j = k >> 1; j > 0; j >>= 1) {
+                for (unsigned t = tid; t < N / 2; t += kShadeThreads) {
+                    const unsigned i = 2 * t - (t & (j - 1)), l = i + j;
+                    const unsigned long long a = sk[i], b = sk[l];
+                    if ((a > b) == ((i & k) == 0u)) {
+                        sk[i] = b;
+                        sk[l] = a;
+                    }
+                }
+                __syncthreads();
+            }
+        const unsigned E = (F + kShadeThreads - 1) / kShadeThreads;
+        const unsigned b0 = min(F, tid * E), b1 = min(F, b0 + E);
+        float m = 1.0f;
+        for (unsigned i = b0; i < b1; ++i) m = fminf(m, frag_depth(sk[i]));
+        const float before = block_excl_min(m, s_wmin);
+        float run = before;
+        unsigned cnt = 0;
+        for (unsigned i = b0; i < b1; ++i) {
+            const float d = frag_depth(sk[i]);
+            if (d < run) {
+                ++cnt;
+                run = d;
+            }
+        }
+        unsigned total = 0;
+        unsigned q = block_excl_sum(cnt, s_wcnt, total);
+        run = before;
+        for (unsigned i = b0; i < b1; ++i) {
+            const unsigned long long v = sk[i];
+            const float d = frag_depth(v);
+            if (d < run) {
+                frags[lo + q++] = v;
+                run = d;
+            }
+        }
+        if (tid == 0) pass_count[p] = total;
+        __syncthreads();   // sk and the scan scratch are free for the next pixel
+    }
+}
+
+// One warp per pixel: the pass_count[p] passing fragments at the start of its
+// list, shaded 32 at a time in parallel and folded in order with
+// SRC_ALPHA / ONE_MINUS_SRC_ALPHA (alpha ONE / ONE, clamped to 1) from clear.
+__global__ void __launch_bounds__(kShadeThreads) k_blend_shade(TessView T, RasterDev R, Maps M, long long px_count,
+                                                               const unsigned* __restrict__ offs,
+                                                               const unsigned long long* __restrict__ frags,
+                                                               const unsigned* __restrict__ pass_count, float4 clear,
+                                                               float4* __restrict__ image, unsigned* __restrict__ ids) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (kShadeThreads / 32);
+    for (long long p = ((long long)blockIdx.x * kShadeThreads + threadIdx.x) >> 5; p < px_count; p += warps) {
+        const unsigned P = pass_count[p];
+        if (P == kDeferredPx) continue;
+        const unsigned lo = offs[p];
+        const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
+        float3 rgb = make_float3(clear.x, clear.y, clear.z);
+        float alpha = clear.w;
+        unsigned last = 0xffffffffu;
+        for (unsigned base = 0; base < P; base += 32) {
+            const unsigned q = base + lane;
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            unsigned id = 0u;
+            if (q < P) {
+                const unsigned key = (unsigned)(__ldg(frags + lo + q) >> 32) - 1u;
+                id = key >> 1;
+                int s, j, k;
+                segment_of(T, id, s, j, k);
+                const float4* pv = vert_at(T, s, j, k);
+                const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
+                const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
+                int idx[3];
+                float l[3], z;
+                if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
+                else cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z);
+                float in[24];
+                segment_inputs(T, R, s, j, k, Q, idx, l, in);
+                c = shade_fragment(in, M, R.bright[j]);
+            }
+            const int np = (int)min(32u, P - base);
+            for (int t = 0; t < np; ++t) {
+                const float cr = __shfl_sync(FULL, c.x, t), cg = __shfl_sync(FULL, c.y, t);
+                const float cb = __shfl_sync(FULL, c.z, t), ca = __shfl_sync(FULL, c.w, t);
+                const float ia = 1.0f - ca;
+                rgb = make_float3(cr * ca + rgb.x * ia, cg * ca + rgb.y * ia, cb * ca + rgb.z * ia);
+                alpha = fminf(1.0f, ca + alpha);
+            }
+            last = __shfl_sync(FULL, id, np - 1);
+        }
+        if (lane == 0) {
+            image[p] = make_float4(rgb.x, rgb.y, rgb.z, alpha);
+            if (ids) ids[p] = last;
+        }
+    }
+}
+
+// The listed pixels of k_blend_order (a fragment of a listed quad, or too many
+// to sort), one warp per pixel over the untouched list: each pass over the
+// candidates finds the next passing fragment, the smallest key above the last
+// passing one's with a depth below it (a warp-wide min); up to 32 are shaded
+// in parallel (through the clipped path for a near-clipped quad), then folded.
+__global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, RasterDev R, Maps M,
                                                                  const unsigned* __restrict__ offs,
                                                                  const unsigned long long* __restrict__ frags,
                                                                  float4 clear, float4* __restrict__ image,
@@ -1378,10 +1572,9 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (kShadeThreads / 32);
-    const long long n = kClipped ? (long long)min(*D.count, D.cap) : px_count;
+    const long long n = (long long)min(*D.count, D.cap);
     for (long long i = ((long long)blockIdx.x * kShadeThreads + threadIdx.x) >> 5; i < n; i += warps) {
-        const long long p = kClipped ? (long long)D.ids[i] : i;
-        bool deferred = false;
+        const long long p = (long long)D.ids[i];
         const unsigned lo = offs[p], hi = offs[p + 1];
         const int py = (int)(p / R.width), px = (int)(p - (long long)py * R.width);
         float3 rgb = make_float3(clear.x, clear.y, clear.z);
@@ -1397,7 +1590,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
                 unsigned long long best = ~0ull;
                 for (unsigned f = lo + lane; f < hi; f += 32) {
                     const unsigned long long v = __ldg(frags + f);
-                    if ((unsigned)(v >> 32) > cur_key && __uint_as_float((unsigned)v) < cur_z && v < best) best = v;
+                    if ((unsigned)(v >> 32) > cur_key && frag_depth(v) < cur_z && v < best) best = v;
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -1407,7 +1600,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
                 if (best == ~0ull) break;
                 if (lane == npass) mine = best;
                 cur_key = (unsigned)(best >> 32);
-                cur_z = __uint_as_float((unsigned)best);
+                cur_z = frag_depth(best);
                 ++npass;
             }
             if (npass == 0) break;
@@ -1421,20 +1614,17 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
                 const Quad Q = make_quad(R, __ldg(pv), __ldg(pv + 1), R.rnd[j]);
                 const float cx = (float)px + 0.5f, cy = (float)py + 0.5f;
                 float in[24];
-                if (!Q.near_clip) {
+                if (Q.near_clip) {
+                    segment_inputs_clip(T, R, s, j, k, px, py, (int)(key & 1u), in);
+                } else {
                     int idx[3];
                     float l[3], z;
                     if (key & 1u) cover_tri(Q, 2, 1, 3, cx, cy, idx, l, z);
                     else cover_tri(Q, 0, 1, 2, cx, cy, idx, l, z);
                     segment_inputs(T, R, s, j, k, Q, idx, l, in);
-                } else if constexpr (kClipped) {
-                    segment_inputs_clip(T, R, s, j, k, px, py, (int)(key & 1u), in);
-                } else {   // a near-clipped quad: the second pass resolves this pixel
-                    deferred = true;
                 }
-                if (!deferred) c = shade_fragment(in, M, R.bright[j]);
+                c = shade_fragment(in, M, R.bright[j]);
             }
-            if (__any_sync(FULL, deferred)) break;   // warp-uniform
             for (int t = 0; t < npass; ++t) {   // SRC_ALPHA / ONE_MINUS_SRC_ALPHA, alpha ONE / ONE
                 const float cr = __shfl_sync(FULL, c.x, t), cg = __shfl_sync(FULL, c.y, t);
                 const float cb = __shfl_sync(FULL, c.z, t), ca = __shfl_sync(FULL, c.w, t);
@@ -1444,10 +1634,6 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_resolve(TessView T, Ras
             }
             last = ((unsigned)(__shfl_sync(FULL, mine, npass - 1) >> 32) - 1u) >> 1;
             if (npass < 32) break;
-        }
-        if (__any_sync(FULL, deferred)) {
-            if (lane == 0) defer_pixel(D, p);
-            continue;
         }
         if (lane == 0) {
             image[p] = make_float4(rgb.x, rgb.y, rgb.z, alpha);
@@ -1611,14 +1797,16 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     }
     auto* frags = static_cast<unsigned long long*>(a->raster_frags.ptr);
     if (n_seg > 0) {
-        const BlendScatterFrag F{cursor, frags, (unsigned long long)total, R.width};
+        const BlendScatterFrag F{cursor, frags, (unsigned long long)total, R.width, kListedFrag};
         k_blend_scatter<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, reuse(CL), cursor, frags,
                                                                         (unsigned long long)total);
         k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
     }
     const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
-    k_blend_resolve<false><<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids, D);
-    k_blend_resolve<true><<<sms, kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, clear, img, ids, D);
+    unsigned* pass_count = counts;   // the counts are in offs now
+    k_blend_order<<<sms * 6, kShadeThreads, kOrderCap * 8, s>>>(px, offs, frags, pass_count, D);   // 32 KB: no opt-in
+    k_blend_shade<<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, pass_count, clear, img, ids);
+    k_blend_resolve<<<sms, kShadeThreads, 0, s>>>(T, R, M, offs, frags, clear, img, ids, D);
     RVH_CUDA(cudaGetLastError());
     return RVH_OK;
 }

@@ -434,6 +434,45 @@ def test_gpu_render_single_segment_matches_oracle(gpu_ctx, oracle, case, mode):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("ns", [6000, 40])
+def test_gpu_blend_pixels_with_thousands_of_fragments(gpu_ctx, oracle, ns):
+    """Thousands of short segments crossing one spot at random depths, drawn in
+    an order unrelated to depth: pixels with more fragments than the GPU sorts
+    in shared memory (4,096) take the warp-per-pixel path; ids bit for bit,
+    colours within COLOR_TOL."""
+    import torch
+    rng = np.random.default_rng(ns)
+    z = rng.uniform(-4.0, -1.0, ns)
+    c = rng.uniform(-0.002, 0.002, (ns, 2)) * -z[:, None]   # about the same pixels at every depth
+    a_ = np.stack([c[:, 0] - 0.01 * -z, c[:, 1] - 0.01 * -z, z], 1)
+    b_ = np.stack([c[:, 0] + 0.01 * -z, c[:, 1] + 0.012 * -z, z], 1)
+    verts = np.zeros((ns, 1, 2, 4), np.float32)
+    verts[:, 0, 0, :3], verts[:, 0, 1, :3], verts[:, 0, :, 3] = a_, b_, 0.3
+    frames = np.zeros((ns, 1, 3, 4), np.float32)
+    frames[:, 0, 0, 0] = frames[:, 0, 1, 1] = frames[:, 0, 2, 2] = 1.0
+    sd = _desc_with_camera((0.0, 0.0, 0.0), (0.0, 0.0, -1.0))
+    sd.image_mode = api.IMAGE_BLEND
+    td = api.tess_desc_reference(n_lines=1, n_segments=1)
+    asset = api.Asset(gpu_ctx, np.zeros((ns, 24), np.float32), 2, uniform_rest=0.1)
+    depth, opac = oracle.shade_maps(verts, sd)
+    W, H = 320, 240
+    img = torch.zeros((W * H * 4,), dtype=torch.float32, device="cuda")
+    ids = torch.zeros((W * H,), dtype=torch.int32, device="cuda")
+    vd, fd = _dev(verts.reshape(-1)), _dev(frames.reshape(-1))
+    dd, od = _dev(depth.reshape(-1)), _dev(opac.reshape(-1))
+    torch.cuda.synchronize()
+    asset.render_hair(vd.data_ptr(), fd.data_ptr(), dd.data_ptr(), od.data_ptr(), W, H, img.data_ptr(), ids.data_ptr(),
+                      tess_desc=td, shade_desc=sd)
+    gpu_ctx.synchronize()
+    got_ids = ids.cpu().numpy().view(np.uint32).reshape(H, W)
+    want, want_ids = oracle.render_hair(verts, frames, 2, 1, 1, sd, depth, opac, W, H)
+    assert np.array_equal(got_ids, want_ids)
+    assert (got_ids != 0xffffffff).sum() > 20
+    _colors_close(img.cpu().numpy().reshape(-1, 4), want.reshape(-1, 4))
+    asset.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("mode", [1, 0])   # api.IMAGE_BLEND, api.IMAGE_NEAREST
 def test_gpu_render_hair_camera_inside_the_hair(gpu_ctx, oracle, mode):
     """A camera among the strands: quads with a corner behind it (w <= 0) are
