@@ -38,6 +38,7 @@
 #include <cstring>
 
 #include "rvh_internal.hpp"
+#include "rvh_registry.h"
 
 namespace rvh {
 namespace {
@@ -1333,15 +1334,30 @@ __global__ void __launch_bounds__(kShadeThreads) k_scan_sums(unsigned* __restric
     }
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_scan_add(const unsigned* __restrict__ counts, long long n,
+// ... and lists the pixels with fragments in active (their number in *n_active,
+// one atomic per warp), then zeroes counts (it becomes the per-pixel count of
+// passing fragments).
+__global__ void __launch_bounds__(kShadeThreads) k_scan_add(unsigned* __restrict__ counts, long long n,
                                                             const unsigned* __restrict__ sums, unsigned* __restrict__ offs,
-                                                            unsigned* __restrict__ cursor) {
-    for (long long i = (long long)blockIdx.x * kShadeThreads + threadIdx.x; i < n;
-         i += (long long)gridDim.x * kShadeThreads) {
-        const unsigned o = offs[i] + sums[i / kScanTile];
-        offs[i] = o;
-        cursor[i] = o;
-        if (i == n - 1) offs[n] = o + counts[i];
+                                                            unsigned* __restrict__ cursor, unsigned* __restrict__ active,
+                                                            unsigned* __restrict__ n_active) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * kShadeThreads; base < n; base += (long long)gridDim.x * kShadeThreads) {
+        const long long i = base + threadIdx.x;   // the loop is uniform across each warp
+        const unsigned c = i < n ? counts[i] : 0u;
+        if (i < n) {
+            const unsigned o = offs[i] + sums[i / kScanTile];
+            offs[i] = o;
+            cursor[i] = o;
+            counts[i] = 0u;
+            if (i == n - 1) offs[n] = o + c;
+        }
+        const unsigned m = __ballot_sync(FULL, c > 0u);
+        unsigned slot = 0;
+        if (lane == 0 && m) slot = atomicAdd(n_active, (unsigned)__popc(m));
+        slot = __shfl_sync(FULL, slot, 0);
+        if (c > 0u) active[slot + __popc(m & ((1u << lane) - 1u))] = (unsigned)i;
     }
 }
 
@@ -1375,7 +1391,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, Ras
     raster_warp(T, R, n_seg, CL, BlendScatterFrag{cursor, frags, capacity, R.width, 0u});
 }
 
-constexpr int kOrderCap = 4096;                 // fragments of one pixel sorted in shared memory
+constexpr int kOrderCap = 8192;                 // fragments of one pixel sorted in shared memory (64 KB)
 constexpr unsigned kDeferredPx = 0xffffffffu;   // pass_count of a pixel left to k_blend_resolve
 
 // Block-wide exclusive scans over kShadeThreads threads (all threads call).
@@ -1425,20 +1441,21 @@ __device__ __forceinline__ unsigned block_excl_sum(unsigned x, unsigned* s_w, un
 // written in order to the start of the pixel's list, their number to
 // pass_count[p].  A pixel with more than kOrderCap fragments, or with one of a
 // listed quad, is listed in D instead (pass_count = kDeferredPx) and its list
-// left as it is for k_blend_resolve.
-__global__ void __launch_bounds__(kShadeThreads) k_blend_order(long long px_count, const unsigned* __restrict__ offs,
+// left as it is for k_blend_resolve.  Only the pixels with fragments (active)
+// are visited; the others keep pass_count 0.
+__global__ void __launch_bounds__(kShadeThreads) k_blend_order(const unsigned* __restrict__ active,
+                                                               const unsigned* __restrict__ n_active,
+                                                               const unsigned* __restrict__ offs,
                                                                unsigned long long* __restrict__ frags,
                                                                unsigned* __restrict__ pass_count, DeferList D) {
     extern __shared__ unsigned long long sk[];   // kOrderCap
     __shared__ float s_wmin[kShadeThreads / 32];
     __shared__ unsigned s_wcnt[kShadeThreads / 32];
     const int tid = threadIdx.x;
-    for (long long p = blockIdx.x; p < px_count; p += gridDim.x) {
-        const unsigned lo = offs[p], F = offs[p + 1] - lo;   // block-uniform
-        if (F == 0) {
-            if (tid == 0) pass_count[p] = 0u;
-            continue;
-        }
+    const unsigned n = *n_active;
+    for (unsigned a = blockIdx.x; a < n; a += gridDim.x) {
+        const long long p = active[a];
+        const unsigned lo = offs[p], F = offs[p + 1] - lo;   // block-uniform, > 0
         if (F > (unsigned)kOrderCap) {
             if (tid == 0) {
                 pass_count[p] = kDeferredPx;
@@ -1763,7 +1780,8 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     if (n_seg >= (1LL << 31)) return fail(RVH_ERR_INVALID_ARG, "asset_render_hair: blending needs fewer than 2^31 segments");
     const int sms = a->ctx->sm_count;
     const long long tiles = (px + kScanTile - 1) / kScanTile;
-    const size_t need_px = size_t(px) * 4 * 3 + 4 + size_t(tiles) * 4;   // counts, offs (+1), cursor, tile sums
+    // counts, offs (+1), cursor, tile sums, the active pixels and their number
+    const size_t need_px = size_t(px) * 4 * 4 + 8 + size_t(tiles) * 4;
     if (a->raster_px.bytes < need_px) {
         a->ctx->free(a->raster_px);
         rvh_status st = a->ctx->alloc(a->raster_px, need_px);
@@ -1773,7 +1791,10 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     unsigned* offs = counts + px;
     unsigned* cursor = offs + px + 1;
     unsigned* sums = cursor + px;
+    unsigned* active = sums + tiles;
+    unsigned* n_active = active + px;
     RVH_CUDA(cudaMemsetAsync(counts, 0, size_t(px) * 4, s));
+    RVH_CUDA(cudaMemsetAsync(n_active, 0, 4, s));
     ClipList CL{};
     DeferList D{};
     rvh_status lst = raster_lists(a, n_seg, px, s, &CL, &D);
@@ -1784,7 +1805,7 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     }
     k_scan_tiles<<<unsigned(tiles), kShadeThreads, 0, s>>>(counts, px, offs, sums);
     k_scan_sums<<<1, kShadeThreads, 0, s>>>(sums, int(tiles));
-    k_scan_add<<<grid_for(px, sms), kShadeThreads, 0, s>>>(counts, px, sums, offs, cursor);
+    k_scan_add<<<grid_for(px, sms), kShadeThreads, 0, s>>>(counts, px, sums, offs, cursor, active, n_active);
     RVH_CUDA(cudaGetLastError());
     unsigned total = 0;
     RVH_CUDA(cudaMemcpyAsync(&total, offs + px, 4, cudaMemcpyDeviceToHost, s));
@@ -1803,8 +1824,10 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
         k_listed_quads<<<sms, kShadeThreads, 0, s>>>(T, R, CL, F);
     }
     const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
-    unsigned* pass_count = counts;   // the counts are in offs now
-    k_blend_order<<<sms * 6, kShadeThreads, kOrderCap * 8, s>>>(px, offs, frags, pass_count, D);   // 32 KB: no opt-in
+    unsigned* pass_count = counts;   // zeroed by k_scan_add (the counts are in offs)
+    if (!prepare_kernel(reinterpret_cast<const void*>(k_blend_order)))
+        return fail(RVH_ERR_CUDA, "asset_render_hair: shared memory opt-in of the ordering kernel");
+    k_blend_order<<<sms * 3, kShadeThreads, kOrderCap * 8, s>>>(active, n_active, offs, frags, pass_count, D);
     k_blend_shade<<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, pass_count, clear, img, ids);
     k_blend_resolve<<<sms, kShadeThreads, 0, s>>>(T, R, M, offs, frags, clear, img, ids, D);
     RVH_CUDA(cudaGetLastError());
