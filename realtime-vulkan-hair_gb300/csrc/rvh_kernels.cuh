@@ -450,9 +450,21 @@ struct GatherBox {
         }
         __syncthreads();
     }
+    // Whether the box holds every cell the gather reads for corners C (those of
+    // each axis: lo .. lo + cnt - 1).  A box computed from the points always
+    // does; one stored by the previous step does only while the records are
+    // the ones that step wrote, so a point that left it (records rewritten
+    // through the device pointer, say) reads the grid directly instead.
+    __device__ __forceinline__ bool holds(const BoxGeom& G, const Corners& C) const {
+        bool ok = true;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+            ok = ok && (C.cnt[ax] <= 0 || (C.lo[ax] >= G.lo[ax] && C.lo[ax] + C.cnt[ax] <= G.lo[ax] + G.ext[ax]));
+        return ok;
+    }
     __device__ __forceinline__ f3 gather(f3 x, f3 v, float dt) const {
         const Corners C = corners_of<M>(A, x);
-        if (GS.use) {
+        if (GS.use && holds(GS.G, C)) {
             const float4* bf = reinterpret_cast<const float4*>(smem);
             const BoxGeom& G = GS.G;
             if constexpr (M::kExact) {

@@ -79,6 +79,11 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
         }
     }
     RVH_DEVICE(ctx->device);
+    // pending friction first, so that the snapshot is a finished state
+    for (int i = 0; i < n; ++i) {
+        rvh_status fs = finish_pending(assets[i], ctx->stream);
+        if (fs != RVH_OK) return fs;
+    }
     RVH_CUDA(cudaDeviceSynchronize());
     // snapshot the records of every asset
     std::vector<DevBuf> snap(n);
@@ -96,11 +101,19 @@ rvh_status rvh_tune_batch(rvh_context* ctx, rvh_asset* const* assets, int32_t n,
         if (assets[i]->record_bytes())
             RVH_CUDA(cudaMemcpy(snap[i].ptr, assets[i]->strands.ptr, assets[i]->record_bytes(), cudaMemcpyDeviceToDevice));
     }
+    // the snapshot back, with no pending friction, no stored group boxes and grids to be
+    // cleared before their next use (a trial's grids and boxes describe its own last step)
     auto restore = [&]() -> rvh_status {
-        for (int i = 0; i < n; ++i)
-            if (assets[i]->record_bytes())
-                RVH_CUDA(cudaMemcpy(assets[i]->strands.ptr, snap[i].ptr, assets[i]->record_bytes(),
-                                    cudaMemcpyDeviceToDevice));
+        RVH_CUDA(cudaDeviceSynchronize());
+        for (int i = 0; i < n; ++i) {
+            Asset* a = assets[i];
+            if (a->record_bytes())
+                RVH_CUDA(cudaMemcpy(a->strands.ptr, snap[i].ptr, a->record_bytes(), cudaMemcpyDeviceToDevice));
+            a->pending = false;
+            a->box_layout = 0u;
+            a->last_grid = -1;
+            for (int g = 0; g < 3; ++g) a->grid_dirty[g] = true;
+        }
         return RVH_OK;
     };
     std::vector<int> res_list = {0};
