@@ -121,6 +121,7 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
         size_t last;
     };
     std::deque<Pending> pending;
+    std::vector<WorkItem> clears;
     auto emit_b = [&](int ai) {
         const Asset* a = b.assets[ai];
         if (!a->params.grid_enabled) return;
@@ -168,11 +169,35 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
         if (a->params.grid_enabled) {
             const int chunks = int(a->grid_bytes() / 16);
             for (int c = 0; c < chunks; c += kClearChunk)
-                b.items.push_back({ITEM_CLEAR, ai, c, std::min(chunks, c + kClearChunk)});
+                clears.push_back({ITEM_CLEAR, ai, c, std::min(chunks, c + kClearChunk)});
         }
         if (mode == MODE_FULL) pending.push_back({ai, last});
     }
     flush(true);
+    // The clears (of grids this launch does not read) spread evenly through the queue:
+    // memory-bound work beside the compute, and none left for a tail at the end (one
+    // large asset's clears after its last tile kept a few CTAs busy after the rest).
+    if (!clears.empty()) {
+        std::vector<WorkItem> merged;
+        merged.reserve(b.items.size() + clears.size());
+        const size_t nw = b.items.size(), nc = clears.size();
+        size_t wi = 0;
+        for (size_t c = 0; c < nc; ++c) {
+            const size_t upto = (c * nw) / nc;   // clear c goes before work item upto
+            while (wi < upto) merged.push_back(b.items[wi++]);
+            merged.push_back(clears[c]);
+        }
+        while (wi < nw) merged.push_back(b.items[wi++]);
+        b.items.swap(merged);
+    }
+    // the L2 prefetch of the next item pays for items of about 2,048 points and more
+    int64_t a_items = 0, a_points = 0;
+    for (const WorkItem& w : b.items)
+        if (w.kind == ITEM_A) {
+            ++a_items;
+            a_points += int64_t(w.end - w.begin) * b.assets[w.asset]->n_points;
+        }
+    b.dev.prefetch = a_items > 0 && a_points >= 2048 * a_items ? 1 : 0;
 }
 
 // Grid choice of one asset for one batched step: gather the pending friction from
