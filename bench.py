@@ -52,8 +52,10 @@ BYTES_PER_CELL = 16         # one clear/flush pass per grid cell-step
 # DRAM bytes per algorithmic byte of k_batch, from one ncu capture of the fused
 # step on the first 32 heads of the workload (dram__bytes_read.sum +
 # dram__bytes_write.sum over 80 B/point + 16 B/cell); traffic grows with points
-# and cells, so the full launch's traffic is this ratio times its bytes
-TRAFFIC_PER_ALG_BYTE = 1001.8 / 833.0
+# and cells, so the full launch's traffic is this ratio times its bytes.  Reads
+# are 652.2 MB (the L2 prefetch of each CTA's next item adds about 220 MB of
+# reads for a 2 % shorter step), writes 586.1 MB.
+TRAFFIC_PER_ALG_BYTE = (652.2 + 586.1) / 833.0
 
 
 def load_peaks():
