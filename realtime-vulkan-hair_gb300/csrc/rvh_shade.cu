@@ -1391,44 +1391,45 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_scatter(TessView T, Ras
     raster_warp(T, R, n_seg, CL, BlendScatterFrag{cursor, frags, capacity, R.width, 0u});
 }
 
-constexpr int kOrderCap = 8192;                 // fragments of one pixel sorted in shared memory (64 KB)
+constexpr int kOrderCap = 8192;                 // most fragments of one pixel sorted in shared memory (68 KB)
+constexpr int kOrderCapSmall = 2048;            // the first pass's cap (17 KB, 5 CTAs per SM; 9 in 10 pixels)
 constexpr unsigned kDeferredPx = 0xffffffffu;   // pass_count of a pixel left to k_blend_resolve
 
-// Block-wide exclusive scans over kShadeThreads threads (all threads call).
-__device__ __forceinline__ float block_excl_min(float x, float* s_w) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float incl = x;
+// Shared-memory slot of sorted-list element e: one 8-byte pad after every 16
+// elements, so that a warp's 64-bit accesses at any power-of-two stride of the
+// sort passes spread over the banks (two wavefronts per instruction, the least
+// for 32 x 8 bytes) instead of piling onto two of them.
+__device__ __forceinline__ unsigned sx(unsigned e) { return e + (e >> 4); }
+constexpr int order_smem_bytes(int cap) { return (cap + cap / 16) * 8; }
+
+// NST consecutive bitonic stages (strides low << (NST - 1) down to low) of the
+// ascending/descending network for merge size k over sk[0, N): the elements of a
+// group differ only in the NST index bits from position p0 up, so all of a
+// group's compare-exchanges of these stages stay in registers.
+template <int NST>
+__device__ __forceinline__ void sort_group(unsigned long long* sk, unsigned N, unsigned k, unsigned low, int p0,
+                                           int tid) {
+    constexpr int G = 1 << NST;
+    const unsigned below = (1u << p0) - 1u;
+    for (unsigned g = tid; g < (N >> NST); g += kShadeThreads) {
+        const unsigned base = ((g & ~below) << NST) | (g & below);
+        const bool up = (base & k) == 0u;   // every member shares the bits above p0 + NST - 1
+        unsigned long long v[G];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const float t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl = fminf(incl, t);
-    }
-    if (lane == 31) s_w[warp] = incl;
-    float excl = __shfl_up_sync(FULL, incl, 1);
-    if (lane == 0) excl = 1.0f;
-    __syncthreads();
-    for (int w = 0; w < warp; ++w) excl = fminf(excl, s_w[w]);
-    return excl;
-}
-__device__ __forceinline__ unsigned block_excl_sum(unsigned x, unsigned* s_w, unsigned& total) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned incl = x;
+        for (int m = 0; m < G; ++m) v[m] = sk[sx(base + m * low)];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
+        for (int st = NST - 1; st >= 0; --st)   // stride low << st: member bit st
+#pragma unroll
+            for (int m = 0; m < G; ++m)
+                if (!(m & (1 << st))) {
+                    const unsigned long long a = v[m], b = v[m | (1 << st)];
+                    const bool swap = (a > b) == up;
+                    v[m] = swap ? b : a;
+                    v[m | (1 << st)] = swap ? a : b;
+                }
+#pragma unroll
+        for (int m = 0; m < G; ++m) sk[sx(base + m * low)] = v[m];
     }
-    if (lane == 31) s_w[warp] = incl;
-    __syncthreads();
-    unsigned before = 0;
-    total = 0;
-    for (int w = 0; w < kShadeThreads / 32; ++w) {
-        if (w < warp) before += s_w[w];
-        total += s_w[w];
-    }
-    return before + incl - x;
 }
 
 // One block per pixel (grid-stride).  A fragment passes the LESS test in
@@ -1436,30 +1437,40 @@ __device__ __forceinline__ unsigned block_excl_sum(unsigned x, unsigned* s_w, un
 // earlier fragment's: a failing fragment is never below the depth buffer, so
 // the buffer is the running minimum of all earlier depths.  The pixel's
 // fragments are sorted by primitive key in shared memory (bitonic; keys are
-// unique within a pixel), each thread takes a run of consecutive ones, a block
-// min-scan gives each run the minimum before it, and the passing fragments are
-// written in order to the start of the pixel's list, their number to
-// pass_count[p].  A pixel with more than kOrderCap fragments, or with one of a
+// unique within a pixel), each warp takes a segment of the sorted list (the
+// minimum of the segments before it from the warps' minima) and finds its
+// passing fragments 32 at a time with warp min-scans, and the passing
+// fragments are written in order to the start of the pixel's list, their
+// number to pass_count[p].  A first pass with a small cap (more CTAs per SM, so
+// more pixels in flight) lists the larger pixels in Over for a second pass with
+// the full cap.  A pixel with more than kOrderCap fragments, or with one of a
 // listed quad, is listed in D instead (pass_count = kDeferredPx) and its list
 // left as it is for k_blend_resolve.  Only the pixels with fragments (active)
 // are visited; the others keep pass_count 0.
+template <int kCap>
 __global__ void __launch_bounds__(kShadeThreads) k_blend_order(const unsigned* __restrict__ active,
                                                                const unsigned* __restrict__ n_active,
                                                                const unsigned* __restrict__ offs,
                                                                unsigned long long* __restrict__ frags,
-                                                               unsigned* __restrict__ pass_count, DeferList D) {
-    extern __shared__ unsigned long long sk[];   // kOrderCap
+                                                               unsigned* __restrict__ pass_count, DeferList D,
+                                                               DeferList Over) {
+    extern __shared__ unsigned long long sk[];   // order_smem_bytes(kCap)
     __shared__ float s_wmin[kShadeThreads / 32];
     __shared__ unsigned s_wcnt[kShadeThreads / 32];
-    const int tid = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned n = *n_active;
     for (unsigned a = blockIdx.x; a < n; a += gridDim.x) {
         const long long p = active[a];
         const unsigned lo = offs[p], F = offs[p + 1] - lo;   // block-uniform, > 0
-        if (F > (unsigned)kOrderCap) {
+        if (F > (unsigned)kCap) {
             if (tid == 0) {
-                pass_count[p] = kDeferredPx;
-                defer_pixel(D, p);
+                if (Over.count) {   // to the pass with the larger cap
+                    defer_pixel(Over, p);
+                } else {
+                    pass_count[p] = kDeferredPx;
+                    defer_pixel(D, p);
+                }
             }
             continue;
         }
@@ -1469,7 +1480,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_order(const unsigned* _
         for (unsigned i = tid; i < N; i += kShadeThreads) {
             const unsigned long long v = i < F ? frags[lo + i] : ~0ull;
             listed = listed || (i < F && ((unsigned)v & kListedFrag) != 0u);
-            sk[i] = v;
+            sk[sx(i)] = v;
         }
         if (__syncthreads_or(listed)) {
             if (tid == 0) {
@@ -1478,42 +1489,73 @@ __global__ void __launch_bounds__(kShadeThreads) k_blend_order(const unsigned* _
             }
             continue;
         }
+        // bitonic sort, up to three stages (j, j/2, j/4) per pass over shared memory: each
+        // thread takes groups of 2^nst elements whose indices differ only in those bits,
+        // runs the stages in registers and stores the group back (a third of the passes,
+        // barriers and shared-memory traffic of one stage per pass)
         for (unsigned k = 2; k <= N; k <<= 1)
-            for (unsigned j = k >> 1; j > 0; j >>= 1) {
-                for (unsigned t = tid; t < N / 2; t += kShadeThreads) {
-                    const unsigned i = 2 * t - (t & (j - 1)), l = i + j;
-                    const unsigned long long a = sk[i], b = sk[l];
-                    if ((a > b) == ((i & k) == 0u)) {
-                        sk[i] = b;
-                        sk[l] = a;
-                    }
-                }
+            for (unsigned j = k >> 1; j > 0;) {
+                const int lj = 31 - __clz(j);
+                const int nst = lj >= 2 ? 3 : lj + 1;   // stages in this pass
+                const unsigned low = j >> (nst - 1);     // the smallest stride of the group
+                const int p0 = lj - nst + 1;             // its bit position
+                if (nst == 3) sort_group<3>(sk, N, k, low, p0, tid);
+                else if (nst == 2) sort_group<2>(sk, N, k, low, p0, tid);
+                else sort_group<1>(sk, N, k, low, p0, tid);
                 __syncthreads();
+                j >>= nst;
             }
-        const unsigned E = (F + kShadeThreads - 1) / kShadeThreads;
-        const unsigned b0 = min(F, tid * E), b1 = min(F, b0 + E);
+        // each warp takes a segment of the sorted list and walks it 32 fragments at a time
+        // (lane i reads element i of the chunk: no bank conflicts), with warp min-scans
+        constexpr unsigned kW = kShadeThreads / 32;
+        const unsigned seg = (F + 32 * kW - 1) / (32 * kW) * 32;
+        const unsigned w0 = min(F, warp * seg), w1 = min(F, w0 + seg);
         float m = 1.0f;
-        for (unsigned i = b0; i < b1; ++i) m = fminf(m, frag_depth(sk[i]));
-        const float before = block_excl_min(m, s_wmin);
-        float run = before;
+        for (unsigned i = w0 + lane; i < w1; i += 32) m = fminf(m, frag_depth(sk[sx(i)]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, o));
+        if (lane == 0) s_wmin[warp] = m;
+        __syncthreads();
+        float before = 1.0f;   // the minimum depth of every fragment before this segment
+        for (unsigned w = 0; w < (unsigned)warp; ++w) before = fminf(before, s_wmin[w]);
+        // one chunk: which of its fragments pass, given the running minimum r before it
+        auto chunk = [&](unsigned c, float& r, float& d, bool& pass) {
+            const unsigned i = c + lane;
+            d = i < w1 ? frag_depth(sk[sx(i)]) : 2.0f;   // 2.0 never passes
+            float incl = d;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl = fminf(incl, t);
+            }
+            float ex = __shfl_up_sync(FULL, incl, 1);
+            ex = lane == 0 ? r : fminf(ex, r);
+            pass = d < ex;
+            r = fminf(r, __shfl_sync(FULL, incl, 31));
+        };
         unsigned cnt = 0;
-        for (unsigned i = b0; i < b1; ++i) {
-            const float d = frag_depth(sk[i]);
-            if (d < run) {
-                ++cnt;
-                run = d;
-            }
+        float r = before;
+        for (unsigned c = w0; c < w1; c += 32) {   // warp-uniform
+            float d;
+            bool pass;
+            chunk(c, r, d, pass);
+            cnt += __popc(__ballot_sync(FULL, pass));
         }
-        unsigned total = 0;
-        unsigned q = block_excl_sum(cnt, s_wcnt, total);
-        run = before;
-        for (unsigned i = b0; i < b1; ++i) {
-            const unsigned long long v = sk[i];
-            const float d = frag_depth(v);
-            if (d < run) {
-                frags[lo + q++] = v;
-                run = d;
-            }
+        if (lane == 0) s_wcnt[warp] = cnt;
+        __syncthreads();
+        unsigned q = 0, total = 0;
+        for (unsigned w = 0; w < kW; ++w) {
+            if (w < (unsigned)warp) q += s_wcnt[w];
+            total += s_wcnt[w];
+        }
+        r = before;
+        for (unsigned c = w0; c < w1; c += 32) {
+            float d;
+            bool pass;
+            chunk(c, r, d, pass);
+            const unsigned mask = __ballot_sync(FULL, pass);
+            if (pass) frags[lo + q + __popc(mask & ((1u << lane) - 1u))] = sk[sx(c + lane)];
+            q += __popc(mask);
         }
         if (tid == 0) pass_count[p] = total;
         __syncthreads();   // sk and the scan scratch are free for the next pixel
@@ -1748,20 +1790,24 @@ int grid_for(long long n, int sms) {
 constexpr long long kMaxClipped = 1LL << 20;   // near-clipped quads drawn per rasterising pass
 
 // The asset's lists for one rasterising call over n_seg quads into px pixels
-// (grown as needed, counters zeroed): near-clipped quads (up to kMaxClipped)
-// and the pixels deferred to the clipped resolve pass (up to px).
-rvh_status raster_lists(Asset* a, long long n_seg, long long px, cudaStream_t s, ClipList* CL, DeferList* D) {
+// (grown as needed, counters zeroed): near-clipped quads (up to kMaxClipped),
+// the pixels deferred to the search resolve (up to px) and the pixels the first
+// ordering pass leaves to the second (up to px).
+rvh_status raster_lists(Asset* a, long long n_seg, long long px, cudaStream_t s, ClipList* CL, DeferList* D,
+                        DeferList* Over = nullptr) {
     const long long cap = std::max(1LL, std::min(n_seg, kMaxClipped));
-    const size_t need = size_t(2 + cap + std::max(1LL, px)) * 4;
+    const long long npx = std::max(1LL, px);
+    const size_t need = size_t(3 + cap + 2 * npx) * 4;
     if (a->raster_clip.bytes < need) {
         a->ctx->free(a->raster_clip);
         rvh_status st = a->ctx->alloc(a->raster_clip, need);
         if (st != RVH_OK) return st;
     }
     auto* p = static_cast<unsigned*>(a->raster_clip.ptr);
-    RVH_CUDA(cudaMemsetAsync(p, 0, 8, s));
-    *CL = ClipList{p, p + 2, unsigned(cap), 1};
-    if (D) *D = DeferList{p + 1, p + 2 + cap, unsigned(std::max(1LL, px))};
+    RVH_CUDA(cudaMemsetAsync(p, 0, 12, s));
+    *CL = ClipList{p, p + 3, unsigned(cap), 1};
+    if (D) *D = DeferList{p + 1, p + 3 + cap, unsigned(npx)};
+    if (Over) *Over = DeferList{p + 2, p + 3 + cap + npx, unsigned(npx)};
     return RVH_OK;
 }
 
@@ -1796,8 +1842,8 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     RVH_CUDA(cudaMemsetAsync(counts, 0, size_t(px) * 4, s));
     RVH_CUDA(cudaMemsetAsync(n_active, 0, 4, s));
     ClipList CL{};
-    DeferList D{};
-    rvh_status lst = raster_lists(a, n_seg, px, s, &CL, &D);
+    DeferList D{}, Over{};
+    rvh_status lst = raster_lists(a, n_seg, px, s, &CL, &D, &Over);
     if (lst != RVH_OK) return lst;
     if (n_seg > 0) {
         k_blend_count<<<grid_for(n_seg, sms), kShadeThreads, 0, s>>>(T, R, (unsigned)n_seg, CL, counts);
@@ -1825,9 +1871,12 @@ rvh_status render_blend(Asset* a, const TessView& T, const RasterDev& R, const M
     }
     const float4 clear = make_float4(101.f / 255.f, 129.f / 255.f, 140.f / 255.f, 1.0f);   // Renderer.cpp:2235
     unsigned* pass_count = counts;   // zeroed by k_scan_add (the counts are in offs)
-    if (!prepare_kernel(reinterpret_cast<const void*>(k_blend_order)))
+    if (!prepare_kernel(reinterpret_cast<const void*>(k_blend_order<kOrderCap>)))
         return fail(RVH_ERR_CUDA, "asset_render_hair: shared memory opt-in of the ordering kernel");
-    k_blend_order<<<sms * 3, kShadeThreads, kOrderCap * 8, s>>>(active, n_active, offs, frags, pass_count, D);
+    k_blend_order<kOrderCapSmall><<<sms * 5, kShadeThreads, order_smem_bytes(kOrderCapSmall), s>>>(
+        active, n_active, offs, frags, pass_count, D, Over);
+    k_blend_order<kOrderCap><<<sms * 3, kShadeThreads, order_smem_bytes(kOrderCap), s>>>(Over.ids, Over.count, offs,
+                                                                                        frags, pass_count, D, DeferList{});
     k_blend_shade<<<grid_for(px * 32, sms), kShadeThreads, 0, s>>>(T, R, M, px, offs, frags, pass_count, clear, img, ids);
     k_blend_resolve<<<sms, kShadeThreads, 0, s>>>(T, R, M, offs, frags, clear, img, ids, D);
     RVH_CUDA(cudaGetLastError());

@@ -434,7 +434,7 @@ def test_gpu_render_single_segment_matches_oracle(gpu_ctx, oracle, case, mode):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("ns", [9000, 40])
+@pytest.mark.parametrize("ns", [9000, 6000, 40])
 def test_gpu_blend_pixels_with_thousands_of_fragments(gpu_ctx, oracle, ns):
     """Thousands of short segments crossing one spot at random depths, drawn in
     an order unrelated to depth: pixels with more fragments than the GPU sorts
