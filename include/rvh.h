@@ -98,6 +98,21 @@ rvh_status rvh_asset_destroy(rvh_asset* a);
 /* Time/Collider/Grid uniforms of sets 1-3 (compute.comp:20-42, Scene.cpp:4-20). */
 rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p);
 rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t n);
+/* Grid groups: the reference clears ONE Scene-owned grid and dispatches every
+ * hair into it (src/Renderer.cpp:2063-2071, src/Scene.h:75-77), so hair-hair
+ * friction couples the hairs of a frame.  rvh_asset_share_grid(a, owner) makes
+ * `a` splat into and gather from owner's grid: both need the grid enabled with
+ * the same dims, origin, cell size, scale and wrap mode; `a` must share no grid
+ * yet and `owner` must not share another asset's.  `a`'s pending friction is
+ * applied and its own grids are released.  A group is stepped by a batch that
+ * holds all of its assets, in fused steps: every member's loops 1-2 and splat
+ * come before any member's loop 3 (the reference orders nothing between its
+ * dispatches).  rvh_step, full-step batches and request servers refuse group
+ * members (RVH_ERR_STATE / RVH_ERR_UNSUPPORTED), and set_params may not change
+ * a member's grid geometry.  owner = NULL takes `a` out of its group (friction
+ * applied, grids of its own again); an owner leaves only after its members.
+ * Destroying an owner gives its members grids of their own. */
+rvh_status rvh_asset_share_grid(rvh_asset* a, rvh_asset* owner);
 /* Kinematic head: the pose m (column-major 4x4 affine) of the asset's head for
  * the following steps, relative to its pose when head motion was first set.
  * Each step then places every strand's root at m * root_rest (root_rest = the

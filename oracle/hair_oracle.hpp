@@ -305,4 +305,46 @@ void step_asset(T* state, int ns, int n, const float* rest, const float* strand_
     }
 }
 
+/*
+ * One step of a group of assets sharing one grid (the reference clears one
+ * Scene-owned grid and dispatches every hair into it, src/Renderer.cpp:2063-2071,
+ * src/Scene.h:75-77).  The reference orders nothing between the dispatches; here
+ * every member's loops 1-2 and splat come before any member's loop 3, as within
+ * one asset (step_asset).  The grid geometry is the first member's (the members
+ * share it); each member gathers with its own friction and repulsion.
+ */
+template <class T>
+struct GroupMember {
+    T* state;
+    int ns, n;
+    const float* rest;
+    const rvh_sim_params* P;
+};
+
+template <class T>
+void step_group(GroupMember<T>* m, int nm, const rvh_frame& F, const rvh_collider* cols, int ncol, Grid& G) {
+    if (nm < 1) return;
+    const T dt = T(F.dt);
+    G.reset(*m[0].P);
+    for (int k = 0; k < nm; ++k) {
+        const size_t stride = size_t(12) * m[k].n;
+        for (int s = 0; s < m[k].ns; ++s) {
+            T* rec = m[k].state + stride * s;
+            strand_predict<T>(rec, m[k].n, T(m[k].rest[s]), base_force<T>(*m[k].P, F, nullptr, s), cols, ncol,
+                              *m[k].P, dt);
+            for (int i = 1; i < m[k].n; ++i) splat_point<T, false>(G, *m[k].P, ld(rec + 4 * i), ld(rec + 4 * m[k].n + 4 * i));
+        }
+    }
+    for (int k = 0; k < nm; ++k) {
+        const size_t stride = size_t(12) * m[k].n;
+        for (int s = 0; s < m[k].ns; ++s) {
+            T* rec = m[k].state + stride * s;
+            for (int i = 1; i < m[k].n; ++i) {
+                const v3<T> v = gather_point<T>(G, *m[k].P, ld(rec + 4 * i), ld(rec + 4 * m[k].n + 4 * i), dt);
+                st(rec + 4 * m[k].n + 4 * i, v, T(0));
+            }
+        }
+    }
+}
+
 }  // namespace oracle

@@ -35,9 +35,46 @@ int run(T* state, int ns, int n, const float* rest, const float* strand_wind, co
     return 0;
 }
 
+template <class T>
+int run_group(int nm, T** states, const int* ns, const int* n, const float** rest, const rvh_sim_params* P,
+              const rvh_frame* frames, const rvh_collider* cols, int ncol, int n_steps) {
+    if (nm < 1 || !states || !ns || !n || !rest || !P || !frames || ncol < 0 || ncol > RVH_MAX_COLLIDERS ||
+        n_steps < 0 || (ncol > 0 && !cols))
+        return 1;
+    std::vector<oracle::GroupMember<T>> m(nm);
+    for (int k = 0; k < nm; ++k) {
+        if (!states[k] || !rest[k] || ns[k] < 0 || n[k] < RVH_MIN_POINTS || n[k] > RVH_MAX_POINTS ||
+            !P[k].grid_enabled || P[k].grid_dims[0] != P[0].grid_dims[0] || P[k].grid_dims[1] != P[0].grid_dims[1] ||
+            P[k].grid_dims[2] != P[0].grid_dims[2] || P[k].grid_h != P[0].grid_h ||
+            P[k].grid_scale != P[0].grid_scale || P[k].grid_wrap32 != P[0].grid_wrap32 ||
+            P[k].grid_origin[0] != P[0].grid_origin[0] || P[k].grid_origin[1] != P[0].grid_origin[1] ||
+            P[k].grid_origin[2] != P[0].grid_origin[2])
+            return 1;
+        m[k] = oracle::GroupMember<T>{states[k], ns[k], n[k], rest[k], &P[k]};
+    }
+    oracle::Grid G;
+    for (int s = 0; s < n_steps; ++s)
+        oracle::step_group<T>(m.data(), nm, frames[s], cols + size_t(s) * ncol, ncol, G);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+/* Steps of a group of nm assets sharing one grid (hair_oracle.hpp step_group):
+ * per member a state (ns[k] * 12 * n[k] scalars), rest lengths and params (the
+ * same grid geometry); frames and colliders (n_steps * ncol) shared. */
+int oracle_run_group_f64(int nm, double** states, const int* ns, const int* n, const float** rest,
+                         const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                         int n_steps) {
+    return run_group<double>(nm, states, ns, n, rest, P, frames, cols, ncol, n_steps);
+}
+int oracle_run_group_f32(int nm, float** states, const int* ns, const int* n, const float** rest,
+                         const rvh_sim_params* P, const rvh_frame* frames, const rvh_collider* cols, int ncol,
+                         int n_steps) {
+    return run_group<float>(nm, states, ns, n, rest, P, frames, cols, ncol, n_steps);
+}
 
 /* Advance n_steps steps in FP64.  state = ns*12*n doubles (Strand records);
  * cols = n_steps*ncol colliders (one set per step); grid_out (nullable) gets the

@@ -133,6 +133,29 @@ def run(state, n_points, rest, params, frames, colliders, n_steps, strand_wind=N
     return grid
 
 
+def run_group(states, n_points, rests, params, frames, colliders, n_steps):
+    """Advance a group of assets sharing one grid in place (hair_oracle.hpp
+    step_group): states (all float64 -> FP64 oracle, all float32 -> FP32 twin),
+    each (ns_k, 3*n_k, 4); n_points, rests and params per member; frames and
+    colliders shared."""
+    nm = len(states)
+    dt = states[0].dtype
+    assert all(st.dtype == dt and st.flags.c_contiguous for st in states)
+    ct = C.c_double if dt == np.float64 else C.c_float
+    rests = [np.ascontiguousarray(r, np.float32) for r in rests]
+    sp = (_P(ct) * nm)(*[st.ctypes.data_as(_P(ct)) for st in states])
+    ns = (C.c_int * nm)(*[st.shape[0] for st in states])
+    nn = (C.c_int * nm)(*n_points)
+    rp = (_P(C.c_float) * nm)(*[r.ctypes.data_as(_P(C.c_float)) for r in rests])
+    pa = (T.SimParams * nm)(*params)
+    fr = _frames(frames, n_steps)
+    cols, ncol = _cols(colliders, n_steps)
+    fn = lib().oracle_run_group_f64 if dt == np.float64 else lib().oracle_run_group_f32
+    rc = fn(nm, sp, ns, nn, rp, pa, fr, cols, ncol, n_steps)
+    if rc != 0:
+        raise RuntimeError("oracle_run_group failed: %d" % rc)
+
+
 def adjoint(state0, n_points, rest, params, frames, colliders, n_steps, targets, strand_wind=None, threads=1):
     """FP64 adjoint: returns (loss, d_wind (ns,3), d_rest (ns,), d_v0 (ns,n,3))."""
     ns = state0.shape[0]

@@ -51,6 +51,9 @@ struct Batch {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
     DynBatch* finisher = nullptr;   // one launch of gather-only items for rvh_batch_finish
     std::vector<int64_t> first_point;   // per asset: its first point in the batch's position order
+    // grid groups: per asset the batch index of its grid owner (itself for an owner with
+    // members, -1 for an asset with a grid of its own)
+    std::vector<int> grid_root;
 };
 
 // Packs the curvePoints of every asset of a batch into one contiguous float4
@@ -136,7 +139,8 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     };
     for (int ai : order) {
         const Asset* a = b.assets[ai];
-        if (a->n_strands == 0) continue;
+        const bool owner = !b.grid_root.empty() && b.grid_root[ai] == ai;   // clears its group's grid
+        if (a->n_strands == 0 && !owner) continue;
         const int mode = b.modes.empty() ? MODE_FUSED : b.modes[ai];
         if (mode == MODE_FINISH) {  // gather-only items of an earlier step: nothing to wait for
             emit_b(ai);
@@ -166,7 +170,8 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
             flush(false);
         }
         const size_t last = b.items.size();
-        if (a->params.grid_enabled) {
+        const bool member = !b.grid_root.empty() && b.grid_root[ai] >= 0 && b.grid_root[ai] != ai;
+        if (a->params.grid_enabled && !member) {   // a group's grid is cleared once, by its owner
             const int chunks = int(a->grid_bytes() / 16);
             for (int c = 0; c < chunks; c += kClearChunk)
                 clears.push_back({ITEM_CLEAR, ai, c, std::min(chunks, c + kClearChunk)});
@@ -220,8 +225,26 @@ uint32_t box_layout_of(const Batch& b, size_t i) {
     return b.tile_strands[i] % group == 0 ? key : key | (1u << 19) | uint32_t(b.tile_strands[i] & 0x7ffff);
 }
 
+// The asset's stored group boxes for this step's view (optional: without a record buffer every
+// fused step recomputes its gather boxes).
+void attach_group_boxes(Asset* a, DevAsset* view, GridUse* gu, uint32_t layout) {
+    // one record pair per round of 8 strands at most (32 lanes per strand)
+    if (layout && !a->group_boxes.ptr && a->n_strands > 0) {
+        const size_t groups = (size_t(a->n_strands) + 7) / 8;
+        if (a->ctx->alloc(a->group_boxes, groups * 2 * sizeof(int4)) != RVH_OK) set_error("");
+    }
+    if (layout && a->group_boxes.ptr) {
+        view->group_box = static_cast<int4*>(a->group_boxes.ptr);
+        view->box_tag_read = (a->pending && a->box_layout == layout) ? a->box_tag : 0u;
+        gu->box_tag = a->box_tag + 1u ? a->box_tag + 1u : 1u;
+        view->box_tag_write = gu->box_tag;
+    }
+}
+
+// group_pending (an owner of a grid group): whether any asset of the group has friction
+// pending in grid[pend]; -1 uses the asset's own state.
 rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s, DevAsset* view, GridUse* gu,
-                         uint32_t layout) {
+                         uint32_t layout, int group_pending = -1) {
     *gu = GridUse{};
     if (!a->params.grid_enabled) {
         *view = a->device_view(f, -1);
@@ -236,28 +259,38 @@ rvh_status prepare_asset(Asset* a, int mode, const rvh_frame& f, cudaStream_t s,
         gu->prev = a->pend;
         return RVH_OK;
     }
-    gu->prev = a->pending ? a->pend : -1;
+    const bool held = group_pending < 0 ? a->pending : group_pending != 0;   // grid[pend] still needed
+    gu->prev = held ? a->pend : -1;
     gu->t = a->pick_grid(gu->prev, -1);
     if (a->grid_dirty[gu->t]) RVH_CUDA(cudaMemsetAsync(a->grid[gu->t].ptr, 0, a->grid_bytes(), s));
     gu->u = a->pick_grid(gu->prev, gu->t);
-    *view = a->device_view(f, gu->t, gu->prev, gu->u);
-    // group boxes: one record pair per round of 8 strands at most (32 lanes per strand)
-    if (layout && !a->group_boxes.ptr && a->n_strands > 0) {
-        const size_t groups = (size_t(a->n_strands) + 7) / 8;
-        // optional: without it every fused step recomputes its gather boxes
-        if (a->ctx->alloc(a->group_boxes, groups * 2 * sizeof(int4)) != RVH_OK) set_error("");
-    }
-    if (layout && a->group_boxes.ptr) {
-        view->group_box = static_cast<int4*>(a->group_boxes.ptr);
-        view->box_tag_read = (a->pending && a->box_layout == layout) ? a->box_tag : 0u;
-        gu->box_tag = a->box_tag + 1u ? a->box_tag + 1u : 1u;
-        view->box_tag_write = gu->box_tag;
-    }
+    *view = a->device_view(f, gu->t, a->pending ? gu->prev : -1, gu->u);
+    attach_group_boxes(a, view, gu, layout);
     return RVH_OK;
 }
 
-void commit_asset(Asset* a, int mode, const GridUse& gu, float dt, uint32_t layout) {
+// A grid group's member: the owner's choice of grids (og), its own pending friction.
+rvh_status prepare_member(Asset* a, const GridUse& og, const rvh_frame& f, DevAsset* view, GridUse* gu,
+                          uint32_t layout) {
+    *gu = og;
+    gu->box_tag = 0;
+    if (a->pending && a->pend != og.prev) return fail(RVH_ERR_STATE, "batch: a grid group's pending grids disagree");
+    *view = a->device_view(f, og.t, a->pending ? og.prev : -1, og.u);
+    attach_group_boxes(a, view, gu, layout);
+    return RVH_OK;
+}
+
+void commit_asset(Asset* a, int mode, const GridUse& gu, float dt, uint32_t layout, bool member = false) {
     if (!a->params.grid_enabled) return;
+    if (member && mode != MODE_FINISH) {   // the owner's commit keeps the group's grid flags
+        a->last_grid = gu.t;
+        a->pending = mode == MODE_FUSED;
+        a->pend = gu.t;
+        a->dt_prev = dt;
+        a->box_tag = gu.box_tag ? gu.box_tag : a->box_tag;
+        a->box_layout = gu.box_tag ? layout : 0u;
+        return;
+    }
     if (mode == MODE_FINISH) {
         a->pending = false;
         a->grid_dirty[gu.prev] = true;
@@ -528,6 +561,29 @@ rvh_status rvh_batch_create(rvh_context* ctx, rvh_asset* const* assets, int32_t 
         b->first_point.push_back(b->n_points);
         b->n_points += int64_t(assets[i]->n_strands) * assets[i]->n_points;
     }
+    // grid groups: every asset of a group in the batch, fused steps only (a full step's gather
+    // would wait for the phase A of every member, not of its own asset)
+    b->grid_root.assign(b->assets.size(), -1);
+    for (size_t i = 0; i < b->assets.size(); ++i) {
+        const Asset* a = b->assets[i];
+        if (!a->grid_grouped() || !a->params.grid_enabled) continue;
+        const Asset* owner = a->grid_owner ? a->grid_owner : a;
+        size_t members_here = 0;
+        int root = -1;
+        for (size_t j = 0; j < b->assets.size(); ++j) {
+            if (b->assets[j] == owner) root = int(j);
+            if (b->assets[j]->grid_owner == owner) ++members_here;
+        }
+        if (root < 0 || members_here != owner->grid_members.size()) {
+            destroy(b);
+            return fail(RVH_ERR_INVALID_ARG, "batch_create: a grid group's assets must all be in the batch");
+        }
+        if (d.full_steps) {
+            destroy(b);
+            return fail(RVH_ERR_UNSUPPORTED, "batch_create: assets sharing a grid take fused steps only");
+        }
+        b->grid_root[i] = root;
+    }
     b->kernel = batch_kernel(lanes, b->exact);
     if (!prepare_kernel(b->kernel)) {
         destroy(b);
@@ -634,13 +690,30 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
     RVH_CUDA(cudaEventSynchronize(b->staged[slot]));  // the copy that last read this staging buffer is done
     DevAsset* st = b->h_stage[slot];
     std::vector<GridUse> gus(b->assets.size());
-    for (size_t i = 0; i < b->assets.size(); ++i) {
-        rvh_status ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i],
-                                      box_layout_of(*b, i));
-        if (ps != RVH_OK) return ps;
-        st[i].group_rounds = b->group_rounds[i];
-        st[i].pos_xyz = xyz ? xyz + 3 * b->first_point[i] : nullptr;
-    }
+    const size_t na = b->assets.size();
+    // owners and assets with grids of their own first, then the members of grid groups
+    for (int pass = 0; pass < 2; ++pass)
+        for (size_t i = 0; i < na; ++i) {
+            const int root = b->grid_root.empty() ? -1 : b->grid_root[i];
+            const bool member = root >= 0 && root != int(i);
+            if (member != (pass == 1)) continue;
+            rvh_status ps;
+            if (member) {
+                ps = prepare_member(b->assets[i], gus[root], frames[i], &st[i], &gus[i], box_layout_of(*b, i));
+            } else {
+                int group_pending = -1;
+                if (root == int(i)) {
+                    const Asset* o = b->assets[i];
+                    group_pending = o->pending ? 1 : 0;
+                    for (const Asset* m : o->grid_members) group_pending |= m->pending ? 1 : 0;
+                }
+                ps = prepare_asset(b->assets[i], b->modes[i], frames[i], s, &st[i], &gus[i], box_layout_of(*b, i),
+                                   group_pending);
+            }
+            if (ps != RVH_OK) return ps;
+            st[i].group_rounds = b->group_rounds[i];
+            st[i].pos_xyz = xyz ? xyz + 3 * b->first_point[i] : nullptr;
+        }
     RVH_CUDA(cudaMemcpyAsync(b->d_assets.ptr, st, sizeof(DevAsset) * b->assets.size(), cudaMemcpyHostToDevice, s));
     RVH_CUDA(cudaEventRecord(b->staged[slot], s));
     std::pair<cudaEvent_t, cudaEvent_t> ev{nullptr, nullptr};
@@ -664,8 +737,10 @@ rvh_status batch_step(rvh_batch* b, const rvh_frame* frames, cudaStream_t s, flo
         RVH_CUDA(cudaEventRecord(ev.second, s));
         b->ev_pairs.push_back(ev);
     }
-    for (size_t i = 0; i < b->assets.size(); ++i)
-        commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt, box_layout_of(*b, i));
+    for (size_t i = 0; i < na; ++i) {
+        const int root = b->grid_root.empty() ? -1 : b->grid_root[i];
+        commit_asset(b->assets[i], b->modes[i], gus[i], frames[i].dt, box_layout_of(*b, i), root >= 0 && root != int(i));
+    }
     return RVH_OK;
 }
 

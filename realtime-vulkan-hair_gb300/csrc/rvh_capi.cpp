@@ -234,6 +234,8 @@ rvh_status finish_pending(Asset* a, cudaStream_t s) {
 }
 
 rvh_status launch_plain(Asset* a, const rvh_frame& f, cudaStream_t s) {
+    if (a->params.grid_enabled && a->grid_grouped())
+        return fail(RVH_ERR_STATE, "step: the asset shares its grid with other assets; step the group in one batch");
     if (a->params.grid_enabled && (!a->grid[0].ptr || !a->grid[1].ptr || !a->grid[2].ptr))
         return fail(RVH_ERR_STATE, "step: the asset's grid is held by a request server and no request is active");
     const bool exact = a->ctx->math == RVH_MATH_EXACT;
@@ -602,6 +604,23 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     DeviceGuard g(a->ctx->device);   // releases even if the switch fails
     cudaStreamSynchronize(a->ctx->stream);
     Context* c = a->ctx;
+    // a grid group outlives neither side: a member leaves its owner; an owner's members get
+    // grids of their own back (empty, and stepping then fails, if that allocation fails)
+    if (a->grid_owner) {
+        auto& m = a->grid_owner->grid_members;
+        m.erase(std::remove(m.begin(), m.end(), static_cast<Asset*>(a)), m.end());
+        for (int i = 0; i < 3; ++i) a->grid[i] = DevBuf{};
+    }
+    for (Asset* m : a->grid_members) {
+        m->grid_owner = nullptr;
+        for (int i = 0; i < 3; ++i) m->grid[i] = DevBuf{};
+        m->grid_cells = 0;
+        m->pending = false;
+        m->box_layout = 0u;
+        m->last_grid = -1;
+        if (ensure_grid(m) != RVH_OK) set_error("");
+    }
+    a->grid_members.clear();
     c->free(a->strands);
     c->free(a->rest);
     c->free(a->wind);
@@ -618,15 +637,73 @@ rvh_status rvh_asset_destroy(rvh_asset* a) {
     return RVH_OK;
 }
 
+// Same grid geometry (what a grid group shares).
+static bool same_grid(const rvh_sim_params& x, const rvh_sim_params& y) {
+    return x.grid_enabled == y.grid_enabled && x.grid_dims[0] == y.grid_dims[0] && x.grid_dims[1] == y.grid_dims[1] &&
+           x.grid_dims[2] == y.grid_dims[2] && x.grid_h == y.grid_h && x.grid_origin[0] == y.grid_origin[0] &&
+           x.grid_origin[1] == y.grid_origin[1] && x.grid_origin[2] == y.grid_origin[2] &&
+           x.grid_scale == y.grid_scale && x.grid_wrap32 == y.grid_wrap32;
+}
+
 rvh_status rvh_asset_set_params(rvh_asset* a, const rvh_sim_params* p) {
     if (!a || !p) return fail(RVH_ERR_INVALID_ARG, "set_params: NULL argument");
     rvh_status s = validate_params(*p);
     if (s != RVH_OK) return s;
+    if (a->grid_grouped() && !same_grid(a->params, *p))
+        return fail(RVH_ERR_STATE, "set_params: the asset shares its grid; leave the group to change the grid");
     RVH_DEVICE(a->ctx->device);
     s = finish_pending(a, a->ctx->stream);  // the pending gather uses the old grid geometry
     if (s != RVH_OK) return s;
     a->params = *p;
     return ensure_grid(a);
+}
+
+rvh_status rvh_asset_share_grid(rvh_asset* a, rvh_asset* owner) {
+    if (!a) return fail(RVH_ERR_INVALID_ARG, "share_grid: NULL asset");
+    RVH_DEVICE(a->ctx->device);
+    if (!owner) {   // leave the group: the pending friction first, then grids of its own
+        if (!a->grid_owner) {
+            if (!a->grid_members.empty()) return fail(RVH_ERR_STATE, "share_grid: other assets share this asset's grid");
+            return RVH_OK;
+        }
+        rvh_status fs = finish_pending(a, a->ctx->stream);
+        if (fs != RVH_OK) return fs;
+        RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
+        auto& m = a->grid_owner->grid_members;
+        m.erase(std::remove(m.begin(), m.end(), static_cast<Asset*>(a)), m.end());
+        a->grid_owner = nullptr;
+        for (int i = 0; i < 3; ++i) a->grid[i] = DevBuf{};
+        a->grid_cells = 0;
+        a->pending = false;
+        a->box_layout = 0u;
+        a->last_grid = -1;
+        return ensure_grid(a);
+    }
+    if (a == owner || a->ctx != owner->ctx) return fail(RVH_ERR_INVALID_ARG, "share_grid: another asset of the same context");
+    if (!a->params.grid_enabled || !same_grid(a->params, owner->params))
+        return fail(RVH_ERR_INVALID_ARG, "share_grid: both assets need the grid, with the same dims, origin, cell size, "
+                                         "scale and wrap mode");
+    if (a->grid_grouped()) return fail(RVH_ERR_STATE, "share_grid: the asset already shares a grid");
+    if (owner->grid_owner) return fail(RVH_ERR_STATE, "share_grid: the owner shares another asset's grid");
+    if (a->server_managed || owner->server_managed)
+        return fail(RVH_ERR_STATE, "share_grid: an asset registered with a request server");
+    if (!owner->grid[0].ptr || !owner->grid[1].ptr || !owner->grid[2].ptr)
+        return fail(RVH_ERR_STATE, "share_grid: the owner has no grid");
+    rvh_status fs = finish_pending(a, a->ctx->stream);   // gathers from a's own grid, which goes
+    if (fs != RVH_OK) return fs;
+    RVH_CUDA(cudaStreamSynchronize(a->ctx->stream));
+    for (int i = 0; i < 3; ++i) {
+        a->ctx->free(a->grid[i]);
+        a->grid[i] = DevBuf{owner->grid[i].ptr, owner->grid[i].bytes, owner->ctx, false};
+        a->grid_dirty[i] = owner->grid_dirty[i];
+    }
+    a->grid_cells = owner->grid_cells;
+    a->grid_owner = owner;
+    owner->grid_members.push_back(a);
+    a->pending = false;
+    a->box_layout = 0u;
+    a->last_grid = -1;
+    return RVH_OK;
 }
 
 rvh_status rvh_asset_set_colliders(rvh_asset* a, const rvh_collider* c, int32_t n) {

@@ -141,6 +141,11 @@ struct Asset {
     std::vector<rvh_collider> colliders;
     bool has_wind = false;
     bool server_managed = false;  // grids are lent by a request server while a request is active
+    // grid group (rvh_asset_share_grid): a member's grid[] alias its owner's buffers (not owned);
+    // the owner keeps the group's grid state (which buffer is pending, dirty) and its members
+    Asset* grid_owner = nullptr;
+    std::vector<Asset*> grid_members;
+    bool grid_grouped() const { return grid_owner != nullptr || !grid_members.empty(); }
     // kinematic head (rvh_asset_set_head_transform): roots = head * root_rest each step
     bool head_active = false;
     float head[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};   // column-major

@@ -190,6 +190,7 @@ rvh_status rvh_server_add_character(rvh_server* s, rvh_asset* a, const rvh_wind_
         if (c.asset == a) return fail(RVH_ERR_INVALID_ARG, "server_add_character: asset already registered");
     if (a->params.grid_enabled && !s->slab.ptr)
         return fail(RVH_ERR_BUDGET, "server_add_character: the server has no scratch budget for grids");
+    if (a->grid_grouped()) return fail(RVH_ERR_UNSUPPORTED, "server_add_character: the asset shares its grid");
     RVH_DEVICE(s->ctx->device);
     RVH_CUDA(cudaStreamSynchronize(s->ctx->stream));
     // the grids become per-request scratch lent from the server's pool

@@ -38,6 +38,7 @@ PROTOTYPES = [
     ("rvh_asset_destroy", _st, [_vp]),
     ("rvh_asset_set_params", _st, [_vp, _P(T.SimParams)]),
     ("rvh_asset_set_colliders", _st, [_vp, _P(T.Collider), C.c_int32]),
+    ("rvh_asset_share_grid", _st, [_vp, _vp]),
     ("rvh_asset_set_head_transform", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_set_rest_lengths", _st, [_vp, _P(C.c_float)]),
     ("rvh_asset_set_strand_wind", _st, [_vp, _P(C.c_float)]),

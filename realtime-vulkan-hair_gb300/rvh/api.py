@@ -227,6 +227,10 @@ class Asset:
         arr = (T.Collider * max(1, len(cols)))(*cols)
         check(self.lib.rvh_asset_set_colliders(self.h, arr, len(cols)))
 
+    def share_grid(self, owner):
+        """Splat into and gather from `owner`'s grid (None: a grid of its own again)."""
+        check(self.lib.rvh_asset_share_grid(self.h, owner.h if owner is not None else None))
+
     def set_head_transform(self, m):
         """m: 4x4 head pose (numpy, row-major as written; passed column-major), or None to stop."""
         if m is None:
