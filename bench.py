@@ -233,7 +233,8 @@ def run_served(ctx, args, rank, lanes):
     offered = 20000.0 * 4.5 * pts / n_chars
     rng = np.random.default_rng(77)
     for conc in (1, 4, 16):
-        srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=2, scratch_budget_bytes=24 << 30)
+        srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=2, scratch_budget_bytes=24 << 30,
+                         steps_per_launch=args.steps_per_launch)
         ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
         t = np.cumsum(rng.exponential(1.0 / 20000.0, size=args.requests))
         reqs = [(ids[int(rng.integers(0, n_chars))], int(rng.integers(1, 9)), float(ti)) for ti in t]
@@ -245,6 +246,7 @@ def run_served(ctx, args, rank, lanes):
         growth = float(np.polyfit(t, delay_ms, 1)[0]) if len(t) > 1 else 0.0
         d["queue_growth_ms_per_s"] = growth
         d["sustained"] = bool(d["point_steps_per_s"] >= 0.97 * offered and growth < 50.0)
+        d["steps_per_launch"] = args.steps_per_launch
         out[str(conc)] = d
         srv.close()
     # a batch of 16 of the characters, graph-launched: the batched rate at the server's launch size
@@ -636,6 +638,7 @@ def main():
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--characters", type=int, default=1000)
     ap.add_argument("--requests", type=int, default=3000)
+    ap.add_argument("--steps-per-launch", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world = dist_init()

@@ -429,7 +429,8 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
 /* ---- serving: continuous batching of step requests for resident characters ----
  * The server replays the reference's per-frame loop (src/main.cpp:257-285)
  * for many characters at once: each launch advances every admitted request
- * by one step; requests are admitted in arrival order as slots free up and
+ * by up to steps_per_launch steps (one persistent launch; a request's later
+ * steps wait on the device for its earlier ones); requests are admitted in arrival order as slots free up and
  * their grid scratch fits the server's HBM budget; their work shares launches
  * on the device.  Every step is a fused step (the friction of a step is applied
  * at the start of the next), so a character keeps its grids between requests
@@ -441,7 +442,8 @@ typedef struct rvh_server_desc {
     int32_t max_active;           /* requests co-scheduled per launch (default 16) */
     int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (0: 8) */
     int32_t pipeline_depth;       /* launches in flight (default 2) */
-    int32_t reserved;
+    int32_t steps_per_launch;     /* consecutive steps of a request per launch (0: 1; at most 16):
+                                     later steps wait on the device for the earlier one */
     uint64_t scratch_budget_bytes;/* HBM for the grids of admitted requests; charged to the context */
 } rvh_server_desc;
 typedef struct rvh_request {

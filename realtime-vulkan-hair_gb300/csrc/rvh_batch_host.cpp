@@ -54,6 +54,9 @@ struct Batch {
     // grid groups: per asset the batch index of its grid owner (itself for an owner with
     // members, -1 for an asset with a grid of its own)
     std::vector<int> grid_root;
+    // several steps per launch (a request server's launches): per entry of `assets` the step
+    // it is of its asset (empty: one step each); a step's entries form one segment of the queue
+    std::vector<int> entry_step;
 };
 
 // Packs the curvePoints of every asset of a batch into one contiguous float4
@@ -108,7 +111,11 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
     // grouped by points per strand (CTAs then mostly run one unrolled code path at a time),
     // largest assets first inside a group
+    // (several steps per launch: step by step, each step's entries in that order)
+    const bool multi = !b.entry_step.empty();
+    auto step_of = [&](int i) { return multi ? b.entry_step[i] : 0; };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        if (step_of(x) != step_of(y)) return step_of(x) < step_of(y);
         const Asset* ax = b.assets[x];
         const Asset* ay = b.assets[y];
         if (ax->n_points != ay->n_points) return ax->n_points > ay->n_points;
@@ -125,6 +132,7 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     };
     std::deque<Pending> pending;
     std::vector<WorkItem> clears;
+    std::vector<size_t> seg_items, seg_clears;   // per step: where its work items and clears start
     auto emit_b = [&](int ai) {
         const Asset* a = b.assets[ai];
         if (!a->params.grid_enabled) return;
@@ -139,6 +147,10 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     };
     for (int ai : order) {
         const Asset* a = b.assets[ai];
+        while (int(seg_items.size()) <= step_of(ai)) {
+            seg_items.push_back(b.items.size());
+            seg_clears.push_back(clears.size());
+        }
         const bool owner = !b.grid_root.empty() && b.grid_root[ai] == ai;   // clears its group's grid
         if (a->n_strands == 0 && !owner) continue;
         const int mode = b.modes.empty() ? MODE_FUSED : b.modes[ai];
@@ -173,8 +185,10 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
         const bool member = !b.grid_root.empty() && b.grid_root[ai] >= 0 && b.grid_root[ai] != ai;
         if (a->params.grid_enabled && !member) {   // a group's grid is cleared once, by its owner
             const int chunks = int(a->grid_bytes() / 16);
-            for (int c = 0; c < chunks; c += kClearChunk)
+            for (int c = 0; c < chunks; c += kClearChunk) {
                 clears.push_back({ITEM_CLEAR, ai, c, std::min(chunks, c + kClearChunk)});
+                if (multi) b.need_a[ai]++;   // the asset's next step waits for its clears too
+            }
         }
         if (mode == MODE_FULL) pending.push_back({ai, last});
     }
@@ -182,17 +196,24 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     // The clears (of grids this launch does not read) spread evenly through the queue:
     // memory-bound work beside the compute, and none left for a tail at the end (one
     // large asset's clears after its last tile kept a few CTAs busy after the rest).
+    // With several steps per launch each step's clears stay within its own segment, ahead
+    // of every item of the next step (whose waits are then all on earlier items).
     if (!clears.empty()) {
         std::vector<WorkItem> merged;
         merged.reserve(b.items.size() + clears.size());
-        const size_t nw = b.items.size(), nc = clears.size();
-        size_t wi = 0;
-        for (size_t c = 0; c < nc; ++c) {
-            const size_t upto = (c * nw) / nc;   // clear c goes before work item upto
-            while (wi < upto) merged.push_back(b.items[wi++]);
-            merged.push_back(clears[c]);
+        seg_items.push_back(b.items.size());
+        seg_clears.push_back(clears.size());
+        for (size_t g = 0; g + 1 < seg_items.size(); ++g) {
+            const size_t w0 = seg_items[g], nw = seg_items[g + 1] - w0;
+            const size_t c0 = seg_clears[g], nc = seg_clears[g + 1] - c0;
+            size_t wi = 0;
+            for (size_t c = 0; c < nc; ++c) {
+                const size_t upto = (c * nw) / nc;   // clear c goes before work item upto
+                while (wi < upto) merged.push_back(b.items[w0 + wi++]);
+                merged.push_back(clears[c0 + c]);
+            }
+            while (wi < nw) merged.push_back(b.items[w0 + wi++]);
         }
-        while (wi < nw) merged.push_back(b.items[wi++]);
         b.items.swap(merged);
     }
     // the L2 prefetch of the next item pays for items of about 2,048 points and more
@@ -203,6 +224,7 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
             a_points += int64_t(w.end - w.begin) * b.assets[w.asset]->n_points;
         }
     b.dev.prefetch = a_items > 0 && a_points >= 2048 * a_items ? 1 : 0;
+    b.dev.count_clears = multi ? 1 : 0;
 }
 
 // Grid choice of one asset for one batched step: gather the pending friction from
@@ -459,6 +481,7 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     Batch& b = d->b;
     b.assets = assets;
     b.modes = modes;
+    b.entry_step.clear();
     // a launch carries what the requests of the moment need: tiles sized so every CTA
     // gets about sixteen (small launches would otherwise leave most CTAs idle, and a
     // few large tiles leave a tail; at 16 requests per launch 16 per CTA served
@@ -496,6 +519,147 @@ rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, cons
     if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
     for (size_t i = 0; i < assets.size(); ++i)
         commit_asset(assets[i], modes[i], gus[i], frames[i].dt, box_layout_of(b, i));
+    return RVH_OK;
+}
+
+// Several fused steps of each asset in ONE persistent launch: the entries of an
+// asset's step s + 1 wait (on the device, bounded) for every phase-A item and
+// clear of its step s, whose positions they read, whose splat grid they gather
+// from and whose cleared grid they splat into.  The three grids rotate from
+// step to step: (pending, target, to clear) -> (target, to clear, pending).
+// modes: MODE_FUSED (steps[i] >= 1) or MODE_FINISH (steps[i] == 1); frames:
+// per asset, its steps' frames in order.
+rvh_status dyn_batch_launch_steps(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<int>& steps,
+                                  const std::vector<int>& modes, const std::vector<rvh_frame>& frames, cudaStream_t s,
+                                  cudaEvent_t ev_start, cudaEvent_t ev_stop) {
+    Batch& b = d->b;
+    const size_t na = assets.size();
+    std::vector<size_t> first(na), first_frame(na);
+    std::vector<Asset*> ents;
+    std::vector<int> emode, estep;
+    size_t nf = 0;
+    for (size_t i = 0; i < na; ++i) {
+        if (steps[i] < 1 || (modes[i] != MODE_FUSED && (modes[i] != MODE_FINISH || steps[i] != 1)))
+            return fail(RVH_ERR_INVALID_ARG, "server launch: bad steps or mode");
+        first[i] = ents.size();
+        first_frame[i] = nf;
+        nf += size_t(steps[i]);
+        for (int k = 0; k < steps[i]; ++k) {
+            ents.push_back(assets[i]);
+            emode.push_back(modes[i]);
+            estep.push_back(k);
+        }
+    }
+    if (frames.size() != nf) return fail(RVH_ERR_INVALID_ARG, "server launch: one frame per step");
+    b.assets = ents;
+    b.modes = emode;
+    b.entry_step = estep;
+    int64_t launch_pts = 0;
+    for (Asset* a : ents) launch_pts += int64_t(a->n_strands) * a->n_points;
+    const int64_t per_tile = launch_pts / std::max<int64_t>(1, 16 * int64_t(b.n_ctas));
+    plan(b, 0, int(std::min<int64_t>(kTargetPointsA, std::max<int64_t>(kMinTilePoints, per_tile))));
+    b.dev.n_items = int32_t(b.items.size());
+    if (b.items.empty()) return RVH_OK;
+    rvh_status st = dyn_reserve(d, ents.size(), b.items.size());
+    if (st != RVH_OK) return st;
+    const int slot = b.slot;
+    b.slot ^= 1;
+    RVH_CUDA(cudaEventSynchronize(b.staged[slot]));
+    DevAsset* stage = b.h_stage[slot];
+    struct After {   // what each asset's state becomes once the launch is enqueued
+        GridUse gu;
+        int t = -1, u = -1, third = -1;
+        bool third_dirty = false;
+        uint32_t tag = 0;
+        float dt = 0.f;
+    };
+    std::vector<After> after(na);
+    for (size_t i = 0; i < na; ++i) {
+        Asset* a = assets[i];
+        const size_t e0 = first[i];
+        const rvh_frame* fr = frames.data() + first_frame[i];
+        const uint32_t layout = box_layout_of(b, e0);
+        After& af = after[i];
+        af.dt = fr[steps[i] - 1].dt;
+        if (modes[i] == MODE_FINISH || !a->params.grid_enabled) {
+            if (modes[i] == MODE_FINISH) {
+                rvh_status ps = prepare_asset(a, MODE_FINISH, fr[0], s, &stage[e0], &af.gu, layout);
+                if (ps != RVH_OK) return ps;
+            } else {
+                for (int k = 0; k < steps[i]; ++k) {
+                    stage[e0 + k] = a->device_view(fr[k], -1);
+                    stage[e0 + k].wait_entry = k > 0 ? int32_t(e0 + k - 1) : -1;
+                }
+            }
+        } else {
+            if (!a->grid[0].ptr || !a->grid[1].ptr || !a->grid[2].ptr)
+                return fail(RVH_ERR_STATE, "server launch: an asset has no grids");
+            int prev = a->pending ? a->pend : -1;
+            int t = a->pick_grid(prev, -1);
+            if (a->grid_dirty[t]) RVH_CUDA(cudaMemsetAsync(a->grid[t].ptr, 0, a->grid_bytes(), s));
+            int u = a->pick_grid(prev, t);
+            af.third_dirty = steps[i] > 1 || prev >= 0;
+            if (layout && !a->group_boxes.ptr && a->n_strands > 0) {
+                const size_t groups = (size_t(a->n_strands) + 7) / 8;
+                if (a->ctx->alloc(a->group_boxes, groups * 2 * sizeof(int4)) != RVH_OK) set_error("");
+            }
+            const bool tags = layout && a->group_boxes.ptr;
+            uint32_t tag = a->box_tag;
+            for (int k = 0; k < steps[i]; ++k) {
+                const int gather = k == 0 ? (a->pending ? prev : -1) : prev;
+                DevAsset& v = stage[e0 + k];
+                v = a->device_view(fr[k], t, gather, u);
+                if (k > 0) v.dt_prev = fr[k - 1].dt;
+                v.wait_entry = k > 0 ? int32_t(e0 + k - 1) : -1;
+                if (tags) {
+                    v.group_box = static_cast<int4*>(a->group_boxes.ptr);
+                    v.box_tag_read = k > 0 ? tag : ((a->pending && a->box_layout == layout) ? a->box_tag : 0u);
+                    tag = tag + 1u ? tag + 1u : 1u;
+                    v.box_tag_write = tag;
+                }
+                const int third = 3 - t - u;   // (gathered, target, cleared) -> (target, cleared, gathered)
+                if (k + 1 < steps[i]) {
+                    prev = t;
+                    t = u;
+                    u = third;
+                } else {
+                    af.t = t;
+                    af.u = u;
+                    af.third = third;
+                }
+            }
+            af.tag = tags ? tag : 0u;
+        }
+        for (int k = 0; k < steps[i]; ++k) stage[e0 + k].group_rounds = b.group_rounds[e0 + k];
+    }
+    for (size_t e = 0; e < ents.size(); ++e) d->h_need[slot][e] = b.need_a[e];
+    std::memcpy(d->h_items[slot], b.items.data(), sizeof(WorkItem) * b.items.size());
+    RVH_CUDA(cudaMemcpyAsync(b.d_assets.ptr, stage, sizeof(DevAsset) * ents.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaMemcpyAsync(b.d_items.ptr, d->h_items[slot], sizeof(WorkItem) * b.items.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaMemcpyAsync(b.d_need.ptr, d->h_need[slot], sizeof(unsigned) * ents.size(), cudaMemcpyHostToDevice, s));
+    RVH_CUDA(cudaEventRecord(b.staged[slot], s));
+    if (ev_start) RVH_CUDA(cudaEventRecord(ev_start, s));
+    rvh_status ls = enqueue_launch(&b, s);
+    if (ls != RVH_OK) return ls;
+    if (ev_stop) RVH_CUDA(cudaEventRecord(ev_stop, s));
+    for (size_t i = 0; i < na; ++i) {
+        Asset* a = assets[i];
+        const After& af = after[i];
+        if (modes[i] == MODE_FINISH) {
+            commit_asset(a, MODE_FINISH, af.gu, af.dt, 0u);
+            continue;
+        }
+        if (!a->params.grid_enabled) continue;
+        a->grid_dirty[af.t] = true;
+        a->grid_dirty[af.u] = false;   // the last step's clear items zero it
+        if (af.third_dirty) a->grid_dirty[af.third] = true;
+        a->last_grid = af.t;
+        a->pending = true;
+        a->pend = af.t;
+        a->dt_prev = af.dt;
+        a->box_tag = af.tag ? af.tag : a->box_tag;
+        a->box_layout = af.tag ? box_layout_of(b, first[i]) : 0u;
+    }
     return RVH_OK;
 }
 

@@ -150,6 +150,7 @@ DevAsset Asset::device_view(const rvh_frame& f, int g, int prev, int next) const
     A.grid_next = gp(next);
     A.grid_prev = gp(prev);
     A.dt_prev = dt_prev;
+    A.wait_entry = -1;
     A.draw = static_cast<rvh_draw_indirect*>(draw.ptr);
     A.n_strands = n_strands;
     A.n_points = n_points;

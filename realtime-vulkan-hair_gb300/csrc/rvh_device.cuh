@@ -113,6 +113,10 @@ struct DevAsset {
     // rounds per phase-A group (the span of one gather box and one splat box);
     // 0: as many as keep a group's density partials exact, at most 4
     int32_t group_rounds;
+    // a later step of the same asset in one launch: its phase-A and clear items
+    // start only once every phase-A and clear item of entry wait_entry (the
+    // asset's previous step) is done; -1: none
+    int32_t wait_entry;
 };
 
 struct f3 {

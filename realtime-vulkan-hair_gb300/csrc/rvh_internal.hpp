@@ -192,6 +192,11 @@ void dyn_batch_free(DynBatch* d);
 rvh_status dyn_batch_launch(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<rvh_frame>& frames,
                             const std::vector<int>& modes, cudaStream_t s, cudaEvent_t ev_start, cudaEvent_t ev_stop,
                             int64_t* points);
+// Several fused steps per asset in one launch (steps[i]; frames: per asset its steps' frames);
+// mode 2 (finish) entries take one step.
+rvh_status dyn_batch_launch_steps(DynBatch* d, const std::vector<Asset*>& assets, const std::vector<int>& steps,
+                                  const std::vector<int>& modes, const std::vector<rvh_frame>& frames, cudaStream_t s,
+                                  cudaEvent_t ev_start, cudaEvent_t ev_stop);
 rvh_status dyn_batch_check(DynBatch* d);
 int dyn_batch_ctas(const DynBatch* d);
 

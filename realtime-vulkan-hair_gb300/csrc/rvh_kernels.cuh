@@ -43,9 +43,13 @@ struct BatchDev {
     int32_t n_items;
     uint32_t spin_limit;        // bounded wait of a phase-B tile (iterations of ~256 ns)
     int32_t prefetch;           // nonzero: ask L2 for the next phase-A item's strands (large items)
+    int32_t count_clears;       // nonzero (several steps per launch): clears count in done_a; otherwise
+                                // they do not, as a phase-B tile's wait counts phase-A tiles only
     unsigned* head;             // next item (reset to 0 before every launch)
-    unsigned* done_a;           // per asset: finished phase-A tiles (reset before every launch)
-    const unsigned* need_a;     // per asset: phase-A tiles in this launch
+    unsigned* done_a;           // per entry: finished phase-A tiles (and clears, with count_clears;
+                                // reset before every launch)
+    const unsigned* need_a;     // per entry: phase-A tiles in this launch (plus its clears when a
+                                // later step of the asset waits on them)
     int* error;                 // nonzero: a wait gave up (RVH_ERR_TIMEOUT)
     unsigned* stats;            // [0] phase-A rounds splatted through the shared box, [1] directly;
                                 // [2] phase-B tiles gathered from the box, [3] directly
@@ -859,6 +863,20 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_
             __syncthreads();
             if (threadIdx.x == 0) s_asset = w.asset;
         }
+        if (w.kind != ITEM_B && A.wait_entry >= 0) {   // a later step of the same asset
+            if (threadIdx.x == 0) {
+                const unsigned need = B.need_a[A.wait_entry];
+                uint32_t spins = 0;
+                while (ld_acquire_gpu(B.done_a + A.wait_entry) < need) {
+                    if (++spins > B.spin_limit) {
+                        atomicExch(B.error, RVH_ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+            }
+            __syncthreads();
+        }
         if (w.kind == ITEM_A) {
             if constexpr (L == 1) tile_a_stream<M>(A, w.begin, w.end, dsm, S, B.stats);
             else tile_a_any<L, M>(A, w.begin, w.end, dsm, S, B.stats);
@@ -886,6 +904,11 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_
         } else {
             uint4* g = reinterpret_cast<uint4*>(A.grid_next);
             for (int c = w.begin + threadIdx.x; c < w.end; c += kThreads) g[c] = make_uint4(0u, 0u, 0u, 0u);
+            __syncthreads();
+            if (B.count_clears && threadIdx.x == 0) {   // a later step of this asset splats here
+                __threadfence();
+                atomicAdd(B.done_a + w.asset, 1u);
+            }
         }
     }
 }

@@ -96,7 +96,8 @@ struct Active {
 
 struct Launch {
     cudaEvent_t start, stop;
-    std::vector<int> reqs;  // requests with a step in this launch
+    std::vector<int> reqs;  // requests with steps in this launch
+    std::vector<int> nsteps;   // how many of each
     std::vector<int> last;  // requests whose final step is in this launch
     std::vector<int> finish;   // characters whose pending friction this launch applies
     int64_t points = 0;
@@ -140,6 +141,9 @@ rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_
     if (desc) d = *desc;
     if (d.max_active < 1 || d.max_active > 4096) return fail(RVH_ERR_INVALID_ARG, "server: max_active in [1, 4096]");
     if (d.pipeline_depth < 1 || d.pipeline_depth > 8) return fail(RVH_ERR_INVALID_ARG, "server: pipeline_depth in [1, 8]");
+    if (d.steps_per_launch == 0) d.steps_per_launch = 1;
+    if (d.steps_per_launch < 1 || d.steps_per_launch > 16)
+        return fail(RVH_ERR_INVALID_ARG, "server: steps_per_launch in [1, 16]");
     if (!d.lanes_per_strand) d.lanes_per_strand = 8;
     RVH_DEVICE(ctx->device);
     rvh_server* s = new (std::nothrow) rvh_server();
@@ -275,9 +279,10 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         float ms = 0.f;
         cudaEventElapsedTime(&ms, L.start, L.stop);
         const double t = now_s();
-        for (int r : L.reqs) {
-            step_ms.push_back(ms);
-            results[r].steps_done++;
+        for (size_t q = 0; q < L.reqs.size(); ++q) {   // each step's latency: its launch's time
+            const int r = L.reqs[q];
+            for (int k = 0; k < L.nsteps[q]; ++k) step_ms.push_back(ms);
+            results[r].steps_done += L.nsteps[q];
             results[r].max_step_ms = std::max(results[r].max_step_ms, ms);
         }
         for (int r : L.last) {
@@ -350,22 +355,28 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         // admission waits for pool space, idle characters with grids (least recently stepped
         // first) get their pending friction applied in this launch and release their grids.
         std::vector<Asset*> la;
-        std::vector<rvh_frame> lf;
-        std::vector<int> lm;   // 0: fused step, 2: apply the pending friction only
+        std::vector<rvh_frame> lf;   // per asset, its steps' frames
+        std::vector<int> lm;   // 0: fused steps, 2: apply the pending friction only
+        std::vector<int> lsteps;
         Launch L;
         for (Active& ac : active) {
             if (ac.remaining == 0) continue;
             Character& ch = s->chars[reqs[ac.req].character];
-            rvh_frame f{};
-            f.dt = ch.dt;
-            f.t = float(double(ch.steps + 1) * double(ch.dt));
-            if (ch.has_wind) rvh_wind_at(&ch.wind, ch.steps, f.t, f.wind);
+            const int n_st = std::min(ac.remaining, s->desc.steps_per_launch);
+            for (int k = 0; k < n_st; ++k) {
+                rvh_frame f{};
+                f.dt = ch.dt;
+                f.t = float(double(ch.steps + k + 1) * double(ch.dt));
+                if (ch.has_wind) rvh_wind_at(&ch.wind, ch.steps + k, f.t, f.wind);
+                lf.push_back(f);
+            }
             la.push_back(ch.asset);
-            lf.push_back(f);
             lm.push_back(0);
+            lsteps.push_back(n_st);
             L.reqs.push_back(ac.req);
-            L.points += int64_t(ch.asset->n_strands) * ch.asset->n_points;
-            if (ac.remaining == 1) L.last.push_back(ac.req);
+            L.nsteps.push_back(n_st);
+            L.points += int64_t(n_st) * ch.asset->n_strands * ch.asset->n_points;
+            if (ac.remaining == n_st) L.last.push_back(ac.req);
         }
         const size_t n_steps_in_launch = la.size();
         if (want_space && int(flight.size()) < s->desc.pipeline_depth) {
@@ -398,6 +409,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
                 la.push_back(ch.asset);
                 lf.push_back(rvh_frame{ch.dt, float(double(ch.steps) * double(ch.dt)), {0.f, 0.f, 0.f}, 0});
                 lm.push_back(2);
+                lsteps.push_back(1);
                 L.finish.push_back(c);
             }
             want_space = false;
@@ -405,16 +417,17 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         if (!la.empty() && int(flight.size()) < s->desc.pipeline_depth) {
             L.start = get_ev();
             L.stop = get_ev();
-            err = dyn_batch_launch(s->batch, la, lf, lm, stream, L.start, L.stop, nullptr);
+            err = dyn_batch_launch_steps(s->batch, la, lsteps, lm, lf, stream, L.start, L.stop);
             if (err != RVH_OK) break;
             for (int r : L.reqs) s->chars[reqs[r].character].last_launch = launches + 1;
-            for (Active& ac : active)
-                if (ac.remaining > 0) {
-                    ac.remaining--;
-                    ac.in_flight++;
-                    s->chars[reqs[ac.req].character].steps++;
-                }
-            steps_total += int64_t(n_steps_in_launch);
+            for (size_t q = 0; q < L.reqs.size(); ++q)
+                for (Active& ac : active)
+                    if (ac.req == L.reqs[q]) {
+                        ac.remaining -= L.nsteps[q];
+                        ac.in_flight++;
+                        s->chars[reqs[ac.req].character].steps += L.nsteps[q];
+                    }
+            for (int n_st : L.nsteps) steps_total += n_st;
             active_sum += double(n_steps_in_launch);
             ++launches;
             flight.push_back(L);

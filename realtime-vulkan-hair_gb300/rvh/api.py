@@ -80,7 +80,7 @@ class Orbit(C.Structure):
 
 class ServerDesc(C.Structure):
     _fields_ = [("max_active", C.c_int32), ("lanes_per_strand", C.c_int32), ("pipeline_depth", C.c_int32),
-                ("reserved", C.c_int32), ("scratch_budget_bytes", C.c_uint64)]
+                ("steps_per_launch", C.c_int32), ("scratch_budget_bytes", C.c_uint64)]
 
 
 class Request(C.Structure):
@@ -394,10 +394,11 @@ class Batch:
 class Server:
     """Continuous-batching request loop over resident characters (C++)."""
 
-    def __init__(self, ctx, max_active=16, lanes=8, pipeline_depth=2, scratch_budget_bytes=1 << 30):
+    def __init__(self, ctx, max_active=16, lanes=8, pipeline_depth=2, scratch_budget_bytes=1 << 30,
+                 steps_per_launch=1):
         self.ctx = ctx
         self.lib = ctx.lib
-        d = ServerDesc(max_active, lanes, pipeline_depth, 0, scratch_budget_bytes)
+        d = ServerDesc(max_active, lanes, pipeline_depth, steps_per_launch, scratch_budget_bytes)
         h = C.c_void_p()
         check(self.lib.rvh_server_create(ctx.h, C.byref(d), C.byref(h)))
         self.h = h

@@ -37,10 +37,11 @@ def specs():
     return configs.batched(n_assets=6, scale=0.01, seed=21)
 
 
-def test_served_result_is_the_same_alone_and_in_the_mix(gpu_ctx_fast, specs):
+@pytest.mark.parametrize("spl", [1, 3, 8])   # steps of a request per launch
+def test_served_result_is_the_same_alone_and_in_the_mix(gpu_ctx_fast, specs, spl):
     steps = [5, 3, 7, 2, 6, 4]
     # alone: one request for character 0
-    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=256 << 20)
+    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=256 << 20, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, specs)
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
     st, res, stats = srv.run([(ids[0], steps[0], 0.0)])
@@ -50,7 +51,7 @@ def test_served_result_is_the_same_alone_and_in_the_mix(gpu_ctx_fast, specs):
     for a in assets:
         a.close()
     # in the mix: all six characters, arrivals spread over a few milliseconds
-    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=256 << 20)
+    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=256 << 20, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, specs)
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
     reqs = [(ids[i], steps[i], 0.002 * (i % 3)) for i in range(6)]
@@ -69,8 +70,9 @@ def test_served_result_is_the_same_alone_and_in_the_mix(gpu_ctx_fast, specs):
         a.close()
 
 
-def test_consecutive_requests_for_one_character_continue_its_state(gpu_ctx_fast, specs):
-    srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=256 << 20)
+@pytest.mark.parametrize("spl", [1, 2])
+def test_consecutive_requests_for_one_character_continue_its_state(gpu_ctx_fast, specs, spl):
+    srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=256 << 20, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, specs[:2])
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs[:2])]
     st, res, _ = srv.run([(ids[0], 2, 0.0), (ids[0], 3, 0.0), (ids[1], 4, 0.0)])
@@ -82,10 +84,11 @@ def test_consecutive_requests_for_one_character_continue_its_state(gpu_ctx_fast,
         a.close()
 
 
-def test_admission_respects_the_hbm_budget(gpu_ctx_fast, specs):
+@pytest.mark.parametrize("spl", [1, 2])
+def test_admission_respects_the_hbm_budget(gpu_ctx_fast, specs, spl):
     grid_pair = [2 * 32 * int(np.prod(list(s.params.grid_dims))) for s in specs]
     budget = 2 * max(grid_pair) + 4096
-    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=budget)
+    srv = api.Server(gpu_ctx_fast, max_active=16, scratch_budget_bytes=budget, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, specs)
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
     st, res, stats = srv.run([(i, 3, 0.0) for i in ids])
@@ -128,9 +131,10 @@ def test_bad_requests_fail_alone(gpu_ctx_fast, specs):
     assets[0].close()
 
 
-def test_poisson_trace_reports_latency(gpu_ctx_fast):
+@pytest.mark.parametrize("spl", [1, 4])
+def test_poisson_trace_reports_latency(gpu_ctx_fast, spl):
     specs = configs.batched(n_assets=24, scale=0.05, seed=31)
-    srv = api.Server(gpu_ctx_fast, max_active=8, scratch_budget_bytes=1 << 30)
+    srv = api.Server(gpu_ctx_fast, max_active=8, scratch_budget_bytes=1 << 30, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, specs)
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
     rng = np.random.default_rng(5)
