@@ -100,6 +100,7 @@ constexpr int kTargetPointsA = 4096;   // points per phase-A item
 constexpr int kMinTilePoints = 512;   // smallest phase-A item of a request-server launch
 constexpr int kTargetPointsB = kTileB;  // points per phase-B item (one shared-memory box)
 constexpr int kClearChunk = 1 << 16;   // 16-B units per clear item (1 MiB)
+constexpr int kSparseCellsPerStrand = 50;   // grid cells per strand from which an asset's items go first
 constexpr uint32_t kSpinLimit = 1u << 22;  // ~1 s of 256-ns sleeps before a wait gives up
 
 // strands_per_tile > 0 fixes the phase-A tile; else a tile holds about
@@ -109,17 +110,27 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
     const int quantum = kWarps * S;
     std::vector<int> order(b.assets.size());
     for (size_t i = 0; i < order.size(); ++i) order[i] = int(i);
-    // grouped by points per strand (CTAs then mostly run one unrolled code path at a time),
-    // largest assets first inside a group
-    // (several steps per launch: step by step, each step's entries in that order)
+    // Sparse assets first: few strands over a large grid give every round a large, mostly
+    // empty splat box (many shared-memory slabs), so their items take several times as long
+    // per point (about 90 ns against 30 at 50+ cells per strand on the 256-head workload);
+    // started last they were the launch's tail.  Then the rest grouped by points per strand
+    // (CTAs then mostly run one unrolled code path at a time; mixing them cost 10 %), smallest
+    // assets first inside a group, which leaves the short items of dense assets for the end.
+    // (Several steps per launch: step by step, each step's entries in that order.)
     const bool multi = !b.entry_step.empty();
     auto step_of = [&](int i) { return multi ? b.entry_step[i] : 0; };
+    auto sparse = [&](const Asset* a) {
+        return a->params.grid_enabled && a->n_strands > 0 &&
+               a->grid_cells >= size_t(kSparseCellsPerStrand) * size_t(a->n_strands);
+    };
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
         if (step_of(x) != step_of(y)) return step_of(x) < step_of(y);
         const Asset* ax = b.assets[x];
         const Asset* ay = b.assets[y];
+        const bool sx = sparse(ax), sy = sparse(ay);
+        if (sx != sy) return sx;
         if (ax->n_points != ay->n_points) return ax->n_points > ay->n_points;
-        return int64_t(ax->n_strands) * ax->n_points > int64_t(ay->n_strands) * ay->n_points;
+        return int64_t(ax->n_strands) * ax->n_points < int64_t(ay->n_strands) * ay->n_points;
     });
     b.items.clear();
     b.need_a.assign(b.assets.size(), 0u);
