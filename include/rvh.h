@@ -469,6 +469,8 @@ typedef struct rvh_server_stats {
     double mean_batch;                               /* requests per launch */
     int64_t admission_waits;                         /* admissions deferred for lack of scratch memory */
     uint64_t scratch_used_bytes;                     /* at the end of the run (0 unless the run failed) */
+    double gpu_busy_frac;                            /* sum of the launches' device times / wall time */
+    double host_ms_per_launch;                       /* mean host time to plan, upload and enqueue a launch */
 } rvh_server_stats;
 rvh_status rvh_server_create(rvh_context* ctx, const rvh_server_desc* desc, rvh_server** out);
 rvh_status rvh_server_destroy(rvh_server* s);

@@ -258,6 +258,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
     int64_t point_steps = 0, steps_total = 0, admission_waits = 0;
     int launches = 0, max_active_seen = 0;
     double active_sum = 0.0;
+    double busy_ms = 0.0, host_s = 0.0;   // launches' device time; host time spent enqueuing them
     rvh_status err = RVH_OK;
     const auto t0 = clk::now();
     auto now_s = [&]() { return std::chrono::duration<double>(clk::now() - t0).count(); };
@@ -278,6 +279,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         cudaEventSynchronize(L.stop);
         float ms = 0.f;
         cudaEventElapsedTime(&ms, L.start, L.stop);
+        busy_ms += ms;
         const double t = now_s();
         for (size_t q = 0; q < L.reqs.size(); ++q) {   // each step's latency: its launch's time
             const int r = L.reqs[q];
@@ -417,7 +419,9 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         if (!la.empty() && int(flight.size()) < s->desc.pipeline_depth) {
             L.start = get_ev();
             L.stop = get_ev();
+            const double h0 = now_s();
             err = dyn_batch_launch_steps(s->batch, la, lsteps, lm, lf, stream, L.start, L.stop);
+            host_s += now_s() - h0;
             if (err != RVH_OK) break;
             for (int r : L.reqs) s->chars[reqs[r].character].last_launch = launches + 1;
             for (size_t q = 0; q < L.reqs.size(); ++q)
@@ -510,6 +514,8 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
         stats->max_active = max_active_seen;
         stats->admission_waits = admission_waits;
         stats->scratch_used_bytes = s->pool.used();
+        stats->gpu_busy_frac = wall > 0 ? 1e-3 * busy_ms / wall : 0.0;
+        stats->host_ms_per_launch = launches ? 1e3 * host_s / launches : 0.0;
     }
     return err;
 }

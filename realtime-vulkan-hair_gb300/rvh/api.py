@@ -98,7 +98,7 @@ class ServerStats(C.Structure):
                 ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double), ("step_ms_p999", C.c_double),
                 ("request_ms_p50", C.c_double), ("request_ms_p99", C.c_double), ("queue_ms_p50", C.c_double),
                 ("queue_ms_p99", C.c_double), ("mean_batch", C.c_double), ("admission_waits", C.c_int64),
-                ("scratch_used_bytes", C.c_uint64)]
+                ("scratch_used_bytes", C.c_uint64), ("gpu_busy_frac", C.c_double), ("host_ms_per_launch", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
