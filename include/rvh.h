@@ -439,7 +439,8 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
  * give their grids back, and the end of a run does the same for every
  * character, so each asset leaves a run fully stepped. */
 typedef struct rvh_server_desc {
-    int32_t max_active;           /* requests co-scheduled per launch (default 16) */
+    int32_t max_active;           /* requests co-scheduled per launch (default 16): a request holds a
+                                     slot from admission until its last step is enqueued */
     int32_t lanes_per_strand;     /* batch kernel shape: 1, 4, 8, 16, 32 (0: 8) */
     int32_t pipeline_depth;       /* launches in flight (default 2) */
     int32_t steps_per_launch;     /* consecutive steps of a request per launch (0: 1; at most 16):

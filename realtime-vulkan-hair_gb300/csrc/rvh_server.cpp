@@ -3,11 +3,13 @@
 // UpdateTime -> Frame -> translateSphere loop, src/main.cpp:257-285).
 //
 // Every character's Strand records stay in HBM.  A request asks for k steps of
-// one character.  Each launch advances every ADMITTED request by one step in
-// one persistent batch launch; a request holds its slot (and its grid scratch)
-// from admission until its last step completes.  Requests are admitted in
-// arrival order as soon as (a) a slot is free, (b) its character has no other
-// request in flight, and (c) the grid scratch fits the server's HBM budget.
+// one character.  Each launch advances every ADMITTED request by up to
+// steps_per_launch steps in one persistent batch launch; a request holds its
+// slot from admission until its last step is enqueued (so a launch carries at
+// most max_active requests), its character until that step completes.
+// Requests are admitted in arrival order as soon as (a) a slot is free, (b) its
+// character has no other request in flight, and (c) the character's grid
+// scratch fits the server's HBM budget (or the character still holds its grids).
 // Up to `pipeline_depth` launches are in flight, so new arrivals join the next
 // launch while earlier ones still run on the device.
 #include <algorithm>
@@ -312,8 +314,13 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             if (results[order[next]].status == RVH_OK) waiting.push_back(order[next]);
             ++next;
         }
-        // admission: arrival order, skipping requests whose character is busy
-        for (auto it = waiting.begin(); it != waiting.end() && int(active.size()) < s->desc.max_active;) {
+        // admission: arrival order, skipping requests whose character is busy.  A request takes
+        // a slot until its last step is enqueued: launches run in stream order, so no launch
+        // steps more than max_active requests, and the next launch can be full while the
+        // current one (carrying the last steps of some requests) still runs.
+        int stepping = 0;
+        for (const Active& ac : active) stepping += ac.remaining > 0 ? 1 : 0;
+        for (auto it = waiting.begin(); it != waiting.end() && stepping < s->desc.max_active;) {
             const int r = *it;
             Character& ch = s->chars[reqs[r].character];
             if (ch.busy || ch.finishing) {
@@ -348,9 +355,10 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             results[r].admit_s = t;
             queue_ms.push_back(1e3 * (t - reqs[r].arrival_s));
             active.push_back(ac);
+            ++stepping;
             it = waiting.erase(it);
         }
-        max_active_seen = std::max(max_active_seen, int(active.size()));
+        max_active_seen = std::max(max_active_seen, stepping);
         // launch one step of every admitted request that still has steps to enqueue
         // Every step is fused: the last step of a request leaves its friction pending in the
         // character's grids, and the character's next request continues from there.  When an
