@@ -430,9 +430,10 @@ rvh_status rvh_tune_lookup(rvh_asset* const* assets, int32_t n, int32_t tuned_gr
  * The server replays the reference's per-frame loop (src/main.cpp:257-285)
  * for many characters at once: each launch advances every admitted request
  * by up to steps_per_launch steps (one persistent launch; a request's later
- * steps wait on the device for its earlier ones); requests are admitted in arrival order as slots free up and
- * their grid scratch fits the server's HBM budget; their work shares launches
- * on the device.  Every step is a fused step (the friction of a step is applied
+ * steps wait on the device for its earlier ones).  Requests are admitted in
+ * arrival order as slots free up (a slot frees when a request's last step is
+ * enqueued), their character has no request in flight, and their grid scratch
+ * fits the server's HBM budget; their work shares launches on the device.  Every step is a fused step (the friction of a step is applied
  * at the start of the next), so a character keeps its grids between requests
  * with its last step's friction pending; when an admission waits for space,
  * the least recently stepped idle characters have that friction applied and
