@@ -156,6 +156,16 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
             pending.pop_front();
         }
     };
+    // The last two waves of phase-A work (about 2 x 1,024 points per CTA) go out in items of
+    // one group: CTAs then finish within a short item of one another (with the launch's
+    // own tiles of up to 4,096 points the 64-character launch's CTAs ended 200 us apart).
+    int64_t a_left = 0;
+    for (int ai : order) {
+        const Asset* a = b.assets[ai];
+        const int mode = b.modes.empty() ? MODE_FUSED : b.modes[ai];
+        if (mode != MODE_FINISH) a_left += int64_t(a->n_strands) * a->n_points;
+    }
+    const int64_t taper = int64_t(2) * std::max(1, b.n_ctas) * (kTargetPointsA / 4);
     for (int ai : order) {
         const Asset* a = b.assets[ai];
         while (int(seg_items.size()) <= step_of(ai)) {
@@ -187,9 +197,12 @@ void plan(Batch& b, int strands_per_tile, int target_points = kTargetPointsA) {
         }
         b.tile_strands[ai] = ta;
         b.group_rounds[ai] = U;
-        for (int s = 0; s < a->n_strands; s += ta) {
-            b.items.push_back({ITEM_A, ai, s, std::min(a->n_strands, s + ta)});
+        for (int s = 0; s < a->n_strands;) {
+            const int e = std::min(a->n_strands, s + (a_left <= taper ? std::min(ta, group) : ta));
+            b.items.push_back({ITEM_A, ai, s, e});
             b.need_a[ai]++;
+            a_left -= int64_t(e - s) * a->n_points;
+            s = e;
             flush(false);
         }
         const size_t last = b.items.size();
