@@ -7,6 +7,7 @@ import pytest
 
 from rvh import api, configs
 from rvh import types as T
+from rvh._lib import RvhError
 
 pytestmark = pytest.mark.gpu
 
@@ -102,12 +103,13 @@ def test_admission_respects_the_hbm_budget(gpu_ctx_fast, specs, spl):
         a.close()
 
 
-def test_characters_give_back_their_grids_when_space_is_short(gpu_ctx_fast, specs):
+@pytest.mark.parametrize("spl", [1, 3])
+def test_characters_give_back_their_grids_when_space_is_short(gpu_ctx_fast, specs, spl):
     """Room for one character's grids: the characters take turns, and before the
     other is admitted the idle one's pending friction is applied and its grids freed."""
     sub = [specs[0], specs[1]]
     grids = [3 * ((32 * int(np.prod(list(s.params.grid_dims))) + 255) // 256 * 256) for s in sub]
-    srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=max(grids) + 4096)
+    srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=max(grids) + 4096, steps_per_launch=spl)
     assets = characters(gpu_ctx_fast, sub)
     ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, sub)]
     st, res, stats = srv.run([(ids[0], 2, 0.0), (ids[1], 2, 0.0), (ids[0], 3, 0.0)])
@@ -121,6 +123,9 @@ def test_characters_give_back_their_grids_when_space_is_short(gpu_ctx_fast, spec
 
 
 def test_bad_requests_fail_alone(gpu_ctx_fast, specs):
+    for bad in (-1, 17):   # steps per launch: 0 means 1, at most 16
+        with pytest.raises(RvhError):
+            api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=256 << 20, steps_per_launch=bad)
     srv = api.Server(gpu_ctx_fast, max_active=4, scratch_budget_bytes=256 << 20)
     assets = characters(gpu_ctx_fast, specs[:1])
     cid = srv.add_character(assets[0], wind=specs[0].wind)
