@@ -150,10 +150,12 @@ def test_batch_positions_read_back(gpu_ctx_fast, xyz):
 
 @pytest.mark.parametrize("exact", [True, False])
 @pytest.mark.parametrize("lanes", [1, 4, 8, 16, 32])
-def test_step_read_positions(gpu_ctx, gpu_ctx_fast, exact, lanes):
+@pytest.mark.parametrize("pinned", [True, False])
+def test_step_read_positions(gpu_ctx, gpu_ctx_fast, exact, lanes, pinned):
     """rvh_batch_step_read_positions: the step kernel's own xyz copy of every
     point (a moving head's roots included) equals the assets' reads, and the
-    records equal those of a twin batch stepped without the copy."""
+    records equal those of a twin batch stepped without the copy, into page-locked
+    and into pageable host memory."""
     ctx = gpu_ctx if exact else gpu_ctx_fast
     specs = configs.batched(n_assets=4, scale=0.02, seed=23)
     twin = make_assets(ctx, specs)
@@ -165,21 +167,27 @@ def test_step_read_positions(gpu_ctx, gpu_ctx_fast, exact, lanes):
     b = api.Batch(ctx, assets, lanes=lanes)
     bt = api.Batch(ctx, twin, lanes=lanes)
     pts = b.info()["points"]
-    bufs = [api.PinnedBuffer(pts * 12) for _ in range(2)]
+    if pinned:
+        bufs = [api.PinnedBuffer(pts * 12) for _ in range(2)]
+        ptrs = [p_.ptr for p_ in bufs]
+    else:
+        pageable = [np.zeros((pts, 3), np.float32) for _ in range(2)]
+        ptrs = [a_.ctypes.data for a_ in pageable]
     for k in range(3):
-        b.step_read_positions([s.frame(k) for s in specs], bufs[k % 2].ptr, pts * 12)
+        b.step_read_positions([s.frame(k) for s in specs], ptrs[k % 2], pts * 12)
         bt.step([s.frame(k) for s in specs])
     b.positions_wait()
-    got = bufs[0].array((pts, 3)).copy()   # the last step went to slot 0
+    got = (bufs[0].array((pts, 3)) if pinned else pageable[0]).copy()   # the last step went to buffer 0
     want = np.concatenate([a.read()[:, :s.n_points, :3].reshape(-1, 3) for a, s in zip(assets, specs)])
     assert np.array_equal(got, want)
     for a, t in zip(assets, twin):
         assert np.array_equal(a.read(), t.read())
     from rvh._lib import RvhError
     with pytest.raises(RvhError):
-        b.step_read_positions([s.frame(3) for s in specs], bufs[0].ptr, pts * 16)   # xyz only
-    for p_ in bufs:
-        p_.close()
+        b.step_read_positions([s.frame(3) for s in specs], ptrs[0], pts * 16)   # xyz only
+    if pinned:
+        for p_ in bufs:
+            p_.close()
     b.close()
     bt.close()
 
