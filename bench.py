@@ -233,7 +233,7 @@ def run_served(ctx, args, rank, lanes):
     offered = 20000.0 * 4.5 * pts / n_chars
     rng = np.random.default_rng(77)
     for conc in (1, 4, 16):
-        srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=3, scratch_budget_bytes=24 << 30,
+        srv = api.Server(ctx, max_active=conc, lanes=lanes, pipeline_depth=4, scratch_budget_bytes=24 << 30,
                          steps_per_launch=args.steps_per_launch)
         ids = [srv.add_character(a, wind=s.wind) for a, s in zip(assets, specs)]
         t = np.cumsum(rng.exponential(1.0 / 20000.0, size=args.requests))
@@ -247,7 +247,7 @@ def run_served(ctx, args, rank, lanes):
         d["queue_growth_ms_per_s"] = growth
         d["sustained"] = bool(d["point_steps_per_s"] >= 0.97 * offered and growth < 50.0)
         d["steps_per_launch"] = args.steps_per_launch
-        d["pipeline_depth"] = 3
+        d["pipeline_depth"] = 4
         out[str(conc)] = d
         srv.close()
     # a batch of 16 of the characters, graph-launched: the batched rate at the server's launch size
