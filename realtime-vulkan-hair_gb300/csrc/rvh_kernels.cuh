@@ -735,6 +735,15 @@ __device__ __forceinline__ void tile_a_stream(const DevAsset& A, int begin, int 
     }
 }
 
+// The generic point count, called out of line from the batch kernel: it is rare, and
+// inlined its registers pushed the common paths into spills (k_batch<8, FastMath>: 692 B
+// of spill stores with it and the phase-B tiles inline, 320 B without).
+template <int L, class M>
+__device__ __noinline__ void tile_a_generic(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
+                                            unsigned* stats) {
+    tile_a<0, L, M>(A, begin, end, smem, S, stats);
+}
+
 template <int L, class M>
 __device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end, unsigned char* smem, BoxShared& S,
                                            unsigned* stats) {
@@ -743,7 +752,7 @@ __device__ __forceinline__ void tile_a_any(const DevAsset& A, int begin, int end
         case 16: tile_a<16, L, M>(A, begin, end, smem, S, stats); break;
         case 24: tile_a<24, L, M>(A, begin, end, smem, S, stats); break;
         case 32: tile_a<32, L, M>(A, begin, end, smem, S, stats); break;
-        default: tile_a<0, L, M>(A, begin, end, smem, S, stats); break;
+        default: tile_a_generic<L, M>(A, begin, end, smem, S, stats); break;
     }
 }
 
@@ -819,6 +828,13 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_plain_b(const __gri
 }
 
 // ---- batched persistent path -----------------------------------------------
+// Phase-B tiles, called out of line from the batch kernel for the same reason (only the
+// full-step and finishing modes queue them).
+template <class M>
+__device__ __noinline__ void tile_b_out(const DevAsset& A, int s0, int s1, unsigned char* smem, BoxShared& S,
+                                        unsigned* stats) {
+    tile_b<M>(A, s0, s1, smem, S, stats);
+}
 
 template <int L, class M>
 __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_constant__ BatchDev B) {
@@ -899,7 +915,7 @@ __global__ void __launch_bounds__(kThreads, kMinCtasPerSm) k_batch(const __grid_
                 }
             }
             __syncthreads();
-            tile_b<M>(A, w.begin, w.end, dsm, S, B.stats);
+            tile_b_out<M>(A, w.begin, w.end, dsm, S, B.stats);
             if (w.begin == 0 && threadIdx.x == 0) write_draw(A);
         } else {
             uint4* g = reinterpret_cast<uint4*>(A.grid_next);
