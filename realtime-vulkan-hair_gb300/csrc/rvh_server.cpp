@@ -388,7 +388,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
             L.points += int64_t(n_st) * ch.asset->n_strands * ch.asset->n_points;
             if (ac.remaining == n_st) L.last.push_back(ac.req);
         }
-        const size_t n_steps_in_launch = la.size();
+        const size_t n_requests_in_launch = la.size();   // before any finishing characters join
         if (want_space && int(flight.size()) < s->desc.pipeline_depth) {
             std::vector<int> idle;
             for (int c = 0; c < int(s->chars.size()); ++c) {
@@ -440,7 +440,7 @@ rvh_status rvh_server_run(rvh_server* s, const rvh_request* reqs, int32_t n, rvh
                         s->chars[reqs[ac.req].character].steps += L.nsteps[q];
                     }
             for (int n_st : L.nsteps) steps_total += n_st;
-            active_sum += double(n_steps_in_launch);
+            active_sum += double(n_requests_in_launch);
             ++launches;
             flight.push_back(L);
             continue;
